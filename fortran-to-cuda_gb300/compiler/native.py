@@ -1,0 +1,172 @@
+"""Build and load the native library ``libf2c_gb300.so`` (sm_103a kernels + residency runtime).
+
+The library is compiled in-tree with nvcc for ``sm_103a`` only, under the
+reference's strict numerical contract (``--fmad=false --ftz=false
+--prec-div=true --prec-sqrt=true`` and ``-ffp-contract=off`` for host code,
+compiler/emission/numerical_contract.py:13-15), so the kernels round exactly
+like the Fortran control. There is no CPU fallback: loading fails loudly when
+the library cannot be built or found.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import hashlib
+import os
+import shutil
+import subprocess
+from concurrent.futures import ThreadPoolExecutor
+from functools import lru_cache
+from pathlib import Path
+
+PACKAGE_ROOT = Path(__file__).resolve().parent.parent
+CSRC = PACKAGE_ROOT / "csrc"
+REPO_ROOT = PACKAGE_ROOT.parent
+INCLUDE = REPO_ROOT / "include"
+BUILD_DIR = PACKAGE_ROOT / "_build"
+LIBRARY = BUILD_DIR / "libf2c_gb300.so"
+
+ARCH = ("-gencode", "arch=compute_103a,code=sm_103a")
+STRICT_CUDA = ("--fmad=false", "--ftz=false", "--prec-div=true", "--prec-sqrt=true")
+HOST_OPTIONS = ("-fPIC", "-ffp-contract=off", "-fopenmp")
+NVCC_FLAGS = ("-O3", "-std=c++17", "-lineinfo", *ARCH, *STRICT_CUDA, "-Xcompiler", ",".join(HOST_OPTIONS),
+              f"-I{INCLUDE}", f"-I{CSRC}")
+
+
+def nvcc() -> str:
+    found = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not Path(found).exists():
+        raise RuntimeError("nvcc not found: the GB300 library cannot be built")
+    return found
+
+
+def sources() -> list[Path]:
+    """Every translation unit of the library (kernels, runtime, generated entries)."""
+    found = sorted(CSRC.rglob("*.cu")) + sorted(CSRC.rglob("*.cpp"))
+    return [p for p in found if "_build" not in p.parts]
+
+
+def _headers() -> list[Path]:
+    return sorted(CSRC.rglob("*.cuh")) + sorted(CSRC.rglob("*.hpp")) + sorted(CSRC.rglob("*.h")) + \
+        sorted(INCLUDE.glob("*.h"))
+
+
+def _fingerprint(files) -> str:
+    digest = hashlib.sha256()
+    for flag in NVCC_FLAGS:
+        digest.update(flag.encode())
+    for path in files:
+        digest.update(str(path.relative_to(REPO_ROOT)).encode())
+        digest.update(path.read_bytes())
+    return digest.hexdigest()
+
+
+def build(force: bool = False, verbose: bool = False) -> Path:
+    """Compile every source in parallel and link ``libf2c_gb300.so``; skip when up to date."""
+    from . import emission  # the generated entries are part of the library
+
+    emission.write_entries()
+    srcs = sources()
+    stamp = BUILD_DIR / "fingerprint"
+    fingerprint = _fingerprint([*srcs, *_headers()])
+    if not force and LIBRARY.exists() and stamp.exists() and stamp.read_text() == fingerprint:
+        return LIBRARY
+    BUILD_DIR.mkdir(exist_ok=True)
+    compiler = nvcc()
+
+    def compile_one(src: Path) -> Path:
+        rel = src.relative_to(CSRC)
+        obj = BUILD_DIR / (str(rel).replace(os.sep, "__") + ".o")
+        cmd = [compiler, *NVCC_FLAGS, "-c", str(src), "-o", str(obj)]
+        if src.suffix == ".cpp":
+            cmd[1:1] = ["-x", "cu"]
+        result = subprocess.run(cmd, capture_output=True, text=True)
+        if result.returncode != 0:
+            raise RuntimeError(f"nvcc failed on {rel}:\n{result.stdout}\n{result.stderr}")
+        if verbose and result.stderr:
+            print(result.stderr)
+        return obj
+
+    with ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 4)) as pool:
+        objects = list(pool.map(compile_one, srcs))
+    tmp = LIBRARY.with_suffix(f".{os.getpid()}.tmp")
+    link = [compiler, *ARCH, "-shared", "-Xcompiler", "-fopenmp", *map(str, objects), "-o", str(tmp), "-lcudart"]
+    result = subprocess.run(link, capture_output=True, text=True)
+    if result.returncode != 0:
+        raise RuntimeError(f"link failed:\n{result.stdout}\n{result.stderr}")
+    os.replace(tmp, LIBRARY)
+    stamp.write_text(fingerprint)
+    return LIBRARY
+
+
+# --- ctypes mirrors of include/f2c_advection.h -------------------------------------------------
+
+MAX_SCALARS = 4
+
+
+class Grid(ctypes.Structure):
+    _fields_ = [("nx", ctypes.c_int64), ("ny", ctypes.c_int64), ("nz", ctypes.c_int64),
+                ("halo", ctypes.c_int64), ("sx", ctypes.c_int64), ("sy", ctypes.c_int64),
+                ("dx", ctypes.c_double), ("dy", ctypes.c_double), ("dz", ctypes.c_double)]
+
+
+class Fields(ctypes.Structure):
+    _fields_ = [("u", ctypes.c_void_p), ("v", ctypes.c_void_p), ("w", ctypes.c_void_p),
+                ("ut", ctypes.c_void_p), ("vt", ctypes.c_void_p), ("wt", ctypes.c_void_p),
+                ("nscalar", ctypes.c_int32), ("mode", ctypes.c_int32), ("dt", ctypes.c_double),
+                ("s", ctypes.c_void_p * MAX_SCALARS), ("st", ctypes.c_void_p * MAX_SCALARS)]
+
+
+TENDENCY, ADVANCE = 0, 1
+
+
+@lru_cache(maxsize=1)
+def load() -> ctypes.CDLL:
+    """Load the native library (building it first if needed). Raises if it cannot be had."""
+    path = LIBRARY if LIBRARY.exists() else build()
+    lib = ctypes.CDLL(str(path), mode=ctypes.RTLD_GLOBAL)
+    lib.f2c_advection_abi_version.restype = ctypes.c_uint32
+    lib.f2c_last_error.restype = ctypes.c_char_p
+    lib.f2c_advection_v1.argtypes = [ctypes.POINTER(Grid), ctypes.POINTER(Fields), ctypes.c_void_p]
+    lib.f2c_advection_v1.restype = ctypes.c_int
+    lib.f2c_halo_fill_v1.argtypes = [ctypes.POINTER(Grid), ctypes.POINTER(ctypes.c_void_p),
+                                     ctypes.POINTER(ctypes.c_int32), ctypes.c_int32, ctypes.c_void_p]
+    lib.f2c_halo_fill_v1.restype = ctypes.c_int
+    return lib
+
+
+class NativeError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"status {status}: {message}")
+        self.status = status
+
+
+def check(status: int) -> None:
+    if status != 0:
+        raise NativeError(status, load().f2c_last_error().decode(errors="replace"))
+
+
+def make_grid(nx, ny, nz, halo, dx, dy, dz, sx=None, sy=None) -> Grid:
+    return Grid(nx, ny, nz, halo, sx or nx + 2 * halo, sy or ny + 2 * halo, dx, dy, dz)
+
+
+def advection(grid: Grid, u, v, w, ut=None, vt=None, wt=None, scalars=(), scalar_out=(), mode=TENDENCY,
+              dt=0.0, stream=0) -> None:
+    """Enqueue the fused advection launch on device pointers (ints)."""
+    fields = Fields()
+    fields.u, fields.v, fields.w = u, v, w
+    fields.ut, fields.vt, fields.wt = ut, vt, wt
+    fields.nscalar = len(scalars)
+    fields.mode = mode
+    fields.dt = dt
+    for n, (s, st) in enumerate(zip(scalars, scalar_out, strict=True)):
+        fields.s[n] = s
+        fields.st[n] = st
+    check(load().f2c_advection_v1(ctypes.byref(grid), ctypes.byref(fields), ctypes.c_void_p(stream)))
+
+
+def halo_fill(grid: Grid, pointers, kinds, stream=0) -> None:
+    n = len(pointers)
+    ptrs = (ctypes.c_void_p * n)(*pointers)
+    ks = (ctypes.c_int32 * n)(*kinds)
+    check(load().f2c_halo_fill_v1(ctypes.byref(grid), ptrs, ks, n, ctypes.c_void_p(stream)))

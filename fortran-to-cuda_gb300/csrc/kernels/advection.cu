@@ -1,0 +1,113 @@
+// Fused advection templates for sm_103a and their kernel-level C ABI
+// (include/f2c_advection.h).
+//
+// One launch computes the U, V, W momentum tendencies of the reference's CDU,
+// CDV and CDW procedures (benchmarks/cdu/src/cdu.f90:113-133,
+// compiler/tests/fixtures/stencils/{cvd,cdw}.f90:105-125) and up to four
+// passive-scalar tendencies, replacing the reference's four grid-stride
+// launches per procedure (compiler/emission/cuda/kernels.py:37-69).
+#include "advection_kernels.cuh"
+
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+#include "../../../include/f2c_advection.h"
+
+namespace f2c {
+
+thread_local std::string g_last_error;
+
+int fail(int status, const std::string &message) {
+    g_last_error = message;
+    return status;
+}
+
+static bool aligned8(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 7u) == 0; }
+
+int check_grid(const f2c_grid_v1 *g) {
+    if (!g) return fail(1, "null grid");
+    if (g->nx < 1 || g->ny < 1 || g->nz < 1 || g->halo < 1)
+        return fail(1, "grid needs nx, ny, nz >= 1 and halo >= 1");
+    if (g->sx < g->nx + 2 * g->halo || g->sy < g->ny + 2 * g->halo)
+        return fail(1, "grid strides smaller than the padded extents");
+    if (g->nx > (1 << 24) || g->ny > (1 << 24) || g->nz > (1 << 24))
+        return fail(1, "grid extent beyond 2^24");
+    if (!(g->dx > 0.0) || !(g->dy > 0.0) || !(g->dz > 0.0)) return fail(1, "grid spacings must be positive");
+    return 0;
+}
+
+static int fill_args(const f2c_grid_v1 *g, const f2c_fields_v1 *f, AdvArgs &a) {
+    if (int s = check_grid(g)) return s;
+    if (!f) return fail(1, "null field record");
+    if (!f->u || !f->v || !f->w) return fail(1, "U, V and W are required");
+    if (f->nscalar < 0 || f->nscalar > F2C_MAX_SCALARS) return fail(1, "scalar count out of range");
+    if (f->mode != F2C_TENDENCY && f->mode != F2C_ADVANCE) return fail(1, "unknown output mode");
+    std::memset(&a, 0, sizeof a);
+    a.u = f->u; a.v = f->v; a.w = f->w;
+    a.out[0] = f->ut; a.out[1] = f->vt; a.out[2] = f->wt;
+    const double *ins[3] = {f->u, f->v, f->w};
+    for (int n = 0; n < 3; ++n) {
+        if (!aligned8(ins[n]) || !aligned8(a.out[n])) return fail(1, "field pointers must be 8-byte aligned");
+        for (int m = 0; m < 3; ++m)
+            if (a.out[n] && a.out[n] == ins[m]) return fail(3, "an output aliases a velocity input");
+    }
+    a.nscalar = f->nscalar;
+    for (int n = 0; n < f->nscalar; ++n) {
+        if (!f->s[n]) return fail(1, "null scalar input");
+        a.s[n] = f->s[n];
+        a.st[n] = f->st[n];
+        for (int m = 0; m < 3; ++m)
+            if (a.st[n] && (a.st[n] == ins[m] || a.st[n] == f->s[n])) return fail(3, "a scalar output aliases an input");
+    }
+    a.mode = f->mode;
+    a.dt = f->dt;
+    a.nx = (int)g->nx; a.ny = (int)g->ny; a.nz = (int)g->nz; a.h = (int)g->halo;
+    a.sx = g->sx;
+    a.plane = g->sx * g->sy;
+    a.c = make_coefficients(g->dx, g->dy, g->dz);
+    return 0;
+}
+
+} // namespace f2c
+
+using namespace f2c;
+
+extern "C" uint32_t f2c_advection_abi_version(void) { return F2C_ADVECTION_ABI_VERSION; }
+
+extern "C" const char *f2c_last_error(void) { return g_last_error.c_str(); }
+
+extern "C" int f2c_advection_v1(const f2c_grid_v1 *grid, const f2c_fields_v1 *fields, void *stream) {
+    AdvArgs a;
+    if (int s = fill_args(grid, fields, a)) return s;
+    const cudaError_t e = launch_advection(a, static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return fail(6, std::string("advection launch: ") + cudaGetErrorString(e));
+    return 0;
+}
+
+extern "C" int f2c_halo_fill_v1(const f2c_grid_v1 *grid, double *const *fields, const int32_t *kinds, int32_t count,
+                                void *stream) {
+    if (int s = check_grid(grid)) return s;
+    if (count < 0 || count > kMaxHaloFields) return fail(1, "halo field count out of range");
+    if (count == 0) return 0;
+    if (!fields || !kinds) return fail(1, "null halo field list");
+    HaloArgs h;
+    std::memset(&h, 0, sizeof h);
+    for (int n = 0; n < count; ++n) {
+        if (!fields[n]) return fail(1, "null halo field");
+        if (kinds[n] != 0 && kinds[n] != 1) return fail(1, "unknown halo kind");
+        h.f[n] = fields[n];
+        h.kind[n] = kinds[n];
+    }
+    if (grid->nz < grid->halo + 1 || grid->nx < grid->halo || grid->ny < grid->halo)
+        return fail(1, "halo fill needs nz > halo, nx >= halo and ny >= halo");
+    h.count = count;
+    h.nx = (int)grid->nx; h.ny = (int)grid->ny; h.nz = (int)grid->nz; h.h = (int)grid->halo;
+    h.sx = grid->sx;
+    h.plane = grid->sx * grid->sy;
+    const cudaError_t e = launch_halo(h, static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return fail(6, std::string("halo launch: ") + cudaGetErrorString(e));
+    return 0;
+}

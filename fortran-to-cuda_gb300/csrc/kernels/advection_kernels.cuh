@@ -1,0 +1,135 @@
+// Device kernels of the advection templates: the fused z-marching tendency
+// kernel and the single-pass boundary fill.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "advection_point.cuh"
+
+namespace f2c {
+
+constexpr int kMaxScalars = 4;
+constexpr int kMaxHaloFields = 16;
+
+struct AdvArgs {
+    const double *u, *v, *w;
+    double *out[3];
+    const double *s[kMaxScalars];
+    double *st[kMaxScalars];
+    int nscalar, mode;
+    double dt;
+    int nx, ny, nz, h;
+    long long sx, plane;
+    Coefficients c;
+};
+
+struct HaloArgs {
+    double *f[kMaxHaloFields];
+    int kind[kMaxHaloFields];
+    int count;
+    int nx, ny, nz, h;
+    long long sx, plane;
+};
+
+__device__ __forceinline__ void store_result(double *out, const double *in, long long p, double t, int mode,
+                                             double dt) {
+    if (mode == 0) {
+        out[p] = t;
+    } else {
+        out[p] = __ldg(in + p) + dt * t;
+    }
+}
+
+// Direct z-marching kernel: one thread per (i, j) column of a BX x BY tile,
+// marching KZ levels. Every value is read through the read-only path; the
+// per-point expressions are those of advection_point.cuh.
+template <int BX, int BY, int KZ>
+__global__ void __launch_bounds__(BX *BY) advection_direct_kernel(const AdvArgs a) {
+    const int i = blockIdx.x * BX + threadIdx.x;
+    const int j = blockIdx.y * BY + threadIdx.y;
+    if (i >= a.nx || j >= a.ny) return;
+    const int k0 = blockIdx.z * KZ;
+    const int k1 = min(k0 + KZ, a.nz);
+    const double *__restrict__ U = a.u;
+    const double *__restrict__ V = a.v;
+    const double *__restrict__ W = a.w;
+    const long long sx = a.sx, plane = a.plane;
+    long long p = (long long)(i + a.h) + sx * (long long)(j + a.h) + plane * (long long)(k0 + a.h);
+#define F2C_AT(A, di, dj, dk) __ldg((A) + p + (di) + (dj)*sx + (dk)*plane)
+    for (int k = k0; k < k1; ++k, p += plane) {
+        if (a.out[0]) store_result(a.out[0], U, p, F2C_CDU_POINT(F2C_AT, a.c), a.mode, a.dt);
+        if (a.out[1]) store_result(a.out[1], V, p, F2C_CDV_POINT(F2C_AT, a.c), a.mode, a.dt);
+        if (a.out[2]) store_result(a.out[2], W, p, F2C_CDW_POINT(F2C_AT, a.c), a.mode, a.dt);
+#pragma unroll
+        for (int n = 0; n < kMaxScalars; ++n) {
+            if (n < a.nscalar && a.st[n]) {
+                const double *__restrict__ S = a.s[n];
+                store_result(a.st[n], S, p, F2C_SCALAR_POINT(F2C_AT, S, a.c), a.mode, a.dt);
+            }
+        }
+    }
+#undef F2C_AT
+}
+
+// Boundary fill in one pass: every ghost value is read from the interior point
+// that the ordered fill (periodic x, then y over the whole x extent, then the
+// vertical walls over whole planes) would copy into it. Periodic maps compose,
+// and each vertical mirror source is an interior, non-wall level (nz > halo),
+// so no ghost reads another ghost and the pass order is free.
+__global__ void __launch_bounds__(256) halo_fill_kernel(const HaloArgs a) {
+    const int ex = a.nx + 2 * a.h, ey = a.ny + 2 * a.h, ez = a.nz + 2 * a.h;
+    const long long row = blockIdx.x;          // j + ey*k
+    const int fidx = blockIdx.y;
+    const int j = (int)(row % ey), k = (int)(row / ey);
+    if (k >= ez || fidx >= a.count) return;
+    double *__restrict__ f = a.f[fidx];
+    const int kind = a.kind[fidx];
+    const int h = a.h;
+    const bool jin = j >= h && j < h + a.ny;
+    const bool kwall = kind == 1 && (k == h - 1 || k == h + a.nz - 1);
+    const bool kin = k >= h && k < h + a.nz && !kwall;
+    const int jj = j < h ? j + a.ny : (j >= h + a.ny ? j - a.ny : j);
+    int kk = k;
+    double sign = 1.0;
+    if (kind == 0) {
+        if (k < h) kk = 2 * h - 1 - k;
+        else if (k >= h + a.nz) kk = 2 * (h + a.nz) - 1 - k;
+    } else if (!kwall) {
+        if (k < h - 1) { kk = 2 * (h - 1) - k; sign = -1.0; }
+        else if (k >= h + a.nz) { kk = 2 * (h + a.nz - 1) - k; sign = -1.0; }
+    }
+    const long long dst_row = a.sx * (long long)j + a.plane * (long long)k;
+    const long long src_row = a.sx * (long long)jj + a.plane * (long long)kk;
+    const bool row_interior = jin && kin;
+    for (int i = threadIdx.x; i < ex; i += blockDim.x) {
+        const bool iin = i >= h && i < h + a.nx;
+        if (row_interior && iin) continue;
+        if (kwall) {
+            f[dst_row + i] = 0.0;
+            continue;
+        }
+        const int ii = i < h ? i + a.nx : (i >= h + a.nx ? i - a.nx : i);
+        const double v = f[src_row + ii];
+        f[dst_row + i] = sign < 0.0 ? -v : v;
+    }
+}
+
+inline cudaError_t launch_advection(const AdvArgs &a, cudaStream_t stream) {
+    constexpr int BX = 32, BY = 8, KZ = 16;
+    const dim3 block(BX, BY, 1);
+    const dim3 grid((a.nx + BX - 1) / BX, (a.ny + BY - 1) / BY, (a.nz + KZ - 1) / KZ);
+    advection_direct_kernel<BX, BY, KZ><<<grid, block, 0, stream>>>(a);
+    return cudaGetLastError();
+}
+
+inline cudaError_t launch_halo(const HaloArgs &a, cudaStream_t stream) {
+    const long long rows = (long long)(a.ny + 2 * a.h) * (a.nz + 2 * a.h);
+    if (rows > 0x7fffffffLL) return cudaErrorInvalidValue;
+    const int ex = a.nx + 2 * a.h;
+    const int threads = ex >= 256 ? 256 : ((ex + 31) / 32) * 32;
+    halo_fill_kernel<<<dim3((unsigned)rows, (unsigned)a.count, 1), dim3(threads, 1, 1), 0, stream>>>(a);
+    return cudaGetLastError();
+}
+
+} // namespace f2c

@@ -1,0 +1,96 @@
+// Per-point arithmetic of the advection templates, grouped exactly as the
+// reference sources write it (left to right, parentheses kept). Built with
+// --fmad=false, each expression rounds like the Fortran control and the C
+// oracle, so results are bit-identical.
+//
+//   cdu_point: benchmarks/cdu/src/cdu.f90:66-71 (CDUdiv) then :96-101 (CDUadv)
+//              then * 0.5 (:39, multiply by `half` from CDU :124-132)
+//   cdv_point: compiler/tests/fixtures/stencils/cvd.f90:61-66 then :89-94, * 0.5
+//   cdw_point: compiler/tests/fixtures/stencils/cdw.f90:61-66 then :89-94, * 0.5
+//   scalar_point: this project's centred flux form (no reference source exists
+//              in the mount for scalar advection).
+#pragma once
+#include <cstdint>
+
+namespace f2c {
+
+struct Coefficients {
+    double Ax, Ay, Az;    // 0.25/d: every *div procedure
+    double Bux, Buy, Buz; // CDUadv: 0.5/dx, 0.125/dy, 0.125/dz
+    double Bvx, Bvy, Bvz; // CDVadv: 0.125/dx, 0.5/dy, 0.125/dz
+    double Bwx, Bwy, Bwz; // CDWadv: 0.125/dx, 0.125/dy, 0.5/dz
+    double Sx, Sy, Sz;    // scalar flux: 0.5/d
+};
+
+// F(a, di, dj, dk) reads array a at the point offset by (di, dj, dk).
+#define F2C_CDU_POINT(F, C)                                                                                         \
+    ([&]() -> double {                                                                                              \
+        double r = -(((C).Ax * (F(U, 1, 0, 0) + F(U, 0, 0, 0)) * (F(U, 1, 0, 0) + F(U, 0, 0, 0)) -                  \
+                      (C).Ax * (F(U, 0, 0, 0) + F(U, -1, 0, 0)) * (F(U, 0, 0, 0) + F(U, -1, 0, 0))) +               \
+                     ((C).Ay * (F(U, 0, 1, 0) + F(U, 0, 0, 0)) * (F(V, 1, 0, 0) + F(V, 0, 0, 0)) -                  \
+                      (C).Ay * (F(U, 0, 0, 0) + F(U, 0, -1, 0)) * (F(V, 1, -1, 0) + F(V, 0, -1, 0))) +              \
+                     ((C).Az * (F(U, 0, 0, 1) + F(U, 0, 0, 0)) * (F(W, 1, 0, 0) + F(W, 0, 0, 0)) -                  \
+                      (C).Az * (F(U, 0, 0, 0) + F(U, 0, 0, -1)) * (F(W, 1, 0, -1) + F(W, 0, 0, -1))));              \
+        const double Vadv = (F(V, 0, 0, 0) + F(V, 1, 0, 0) + F(V, 0, -1, 0) + F(V, 1, -1, 0));                      \
+        const double Wadv = (F(W, 0, 0, 0) + F(W, 1, 0, 0) + F(W, 0, 0, -1) + F(W, 1, 0, -1));                      \
+        r = r - ((C).Bux * (F(U, 1, 0, 0) - F(U, -1, 0, 0)) * F(U, 0, 0, 0) +                                       \
+                 (C).Buy * (F(U, 0, 1, 0) - F(U, 0, -1, 0)) * Vadv + (C).Buz * (F(U, 0, 0, 1) - F(U, 0, 0, -1)) * Wadv); \
+        return r * 0.5;                                                                                             \
+    }())
+
+#define F2C_CDV_POINT(F, C)                                                                                         \
+    ([&]() -> double {                                                                                              \
+        double r = -(((C).Ay * (F(V, 0, 1, 0) + F(V, 0, 0, 0)) * (F(V, 0, 1, 0) + F(V, 0, 0, 0)) -                  \
+                      (C).Ay * (F(V, 0, 0, 0) + F(V, 0, -1, 0)) * (F(V, 0, 0, 0) + F(V, 0, -1, 0))) +               \
+                     ((C).Ax * (F(V, 1, 0, 0) + F(V, 0, 0, 0)) * (F(U, 0, 1, 0) + F(U, 0, 0, 0)) -                  \
+                      (C).Ax * (F(V, 0, 0, 0) + F(V, -1, 0, 0)) * (F(U, -1, 1, 0) + F(U, -1, 0, 0))) +              \
+                     ((C).Az * (F(V, 0, 0, 1) + F(V, 0, 0, 0)) * (F(W, 0, 1, 0) + F(W, 0, 0, 0)) -                  \
+                      (C).Az * (F(V, 0, 0, 0) + F(V, 0, 0, -1)) * (F(W, 0, 1, -1) + F(W, 0, 0, -1))));              \
+        const double Uadv = (F(U, 0, 0, 0) + F(U, 0, 1, 0) + F(U, -1, 0, 0) + F(U, -1, 1, 0));                      \
+        const double Wadv = (F(W, 0, 0, 0) + F(W, 0, 1, 0) + F(W, 0, 0, -1) + F(W, 0, 1, -1));                      \
+        r = r - ((C).Bvx * (F(V, 1, 0, 0) - F(V, -1, 0, 0)) * Uadv +                                                \
+                 (C).Bvy * (F(V, 0, 1, 0) - F(V, 0, -1, 0)) * F(V, 0, 0, 0) +                                       \
+                 (C).Bvz * (F(V, 0, 0, 1) - F(V, 0, 0, -1)) * Wadv);                                                \
+        return r * 0.5;                                                                                             \
+    }())
+
+#define F2C_CDW_POINT(F, C)                                                                                         \
+    ([&]() -> double {                                                                                              \
+        double r = -(((C).Az * (F(W, 0, 0, 1) + F(W, 0, 0, 0)) * (F(W, 0, 0, 1) + F(W, 0, 0, 0)) -                  \
+                      (C).Az * (F(W, 0, 0, 0) + F(W, 0, 0, -1)) * (F(W, 0, 0, 0) + F(W, 0, 0, -1))) +               \
+                     ((C).Ay * (F(W, 0, 1, 0) + F(W, 0, 0, 0)) * (F(V, 0, 0, 1) + F(V, 0, 0, 0)) -                  \
+                      (C).Ay * (F(W, 0, 0, 0) + F(W, 0, -1, 0)) * (F(V, 0, -1, 0) + F(V, 0, -1, 1))) +              \
+                     ((C).Ax * (F(W, 1, 0, 0) + F(W, 0, 0, 0)) * (F(U, 0, 0, 1) + F(U, 0, 0, 0)) -                  \
+                      (C).Ax * (F(W, 0, 0, 0) + F(W, -1, 0, 0)) * (F(U, -1, 0, 1) + F(U, -1, 0, 0))));              \
+        const double Uadv = (F(U, 0, 0, 0) + F(U, 0, 0, 1) + F(U, -1, 0, 0) + F(U, -1, 0, 1));                      \
+        const double Vadv = (F(V, 0, 0, 0) + F(V, 0, 0, 1) + F(V, 0, -1, 0) + F(V, 0, -1, 1));                      \
+        r = r - ((C).Bwx * (F(W, 1, 0, 0) - F(W, -1, 0, 0)) * Uadv +                                                \
+                 (C).Bwy * (F(W, 0, 1, 0) - F(W, 0, -1, 0)) * Vadv +                                                \
+                 (C).Bwz * (F(W, 0, 0, 1) - F(W, 0, 0, -1)) * F(W, 0, 0, 0));                                       \
+        return r * 0.5;                                                                                             \
+    }())
+
+// Scalar S advected by U, V, W (face fluxes shareable between neighbours).
+#define F2C_SCALAR_POINT(F, S, C)                                                                                   \
+    ([&]() -> double {                                                                                              \
+        const double c = F(S, 0, 0, 0);                                                                             \
+        const double fe = ((C).Sx * F(U, 0, 0, 0)) * (F(S, 1, 0, 0) + c);                                           \
+        const double fw = ((C).Sx * F(U, -1, 0, 0)) * (c + F(S, -1, 0, 0));                                         \
+        const double fn = ((C).Sy * F(V, 0, 0, 0)) * (F(S, 0, 1, 0) + c);                                           \
+        const double fs = ((C).Sy * F(V, 0, -1, 0)) * (c + F(S, 0, -1, 0));                                         \
+        const double ft = ((C).Sz * F(W, 0, 0, 0)) * (F(S, 0, 0, 1) + c);                                           \
+        const double fb = ((C).Sz * F(W, 0, 0, -1)) * (c + F(S, 0, 0, -1));                                         \
+        return -(((fe - fw) + (fn - fs)) + (ft - fb));                                                              \
+    }())
+
+inline Coefficients make_coefficients(double dx, double dy, double dz) {
+    Coefficients c;
+    c.Ax = 0.25 / dx; c.Ay = 0.25 / dy; c.Az = 0.25 / dz;
+    c.Bux = 0.5 / dx; c.Buy = 0.125 / dy; c.Buz = 0.125 / dz;
+    c.Bvx = 0.125 / dx; c.Bvy = 0.5 / dy; c.Bvz = 0.125 / dz;
+    c.Bwx = 0.125 / dx; c.Bwy = 0.125 / dy; c.Bwz = 0.5 / dz;
+    c.Sx = 0.5 / dx; c.Sy = 0.5 / dy; c.Sz = 0.5 / dz;
+    return c;
+}
+
+} // namespace f2c

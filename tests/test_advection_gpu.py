@@ -1,0 +1,144 @@
+"""Parity of the fused sm_103a advection launch with the C oracle, through the kernel C ABI.
+
+Bar: bit-identical FP64 (the kernels are built with --fmad=false and keep the
+reference's expression grouping). Sizes cover the reference driver's geometry
+(one ghost layer, dx = 1/N), the restated driver's (halo 2, 10/10/5 m), odd and
+one-cell extents, pitched strides and the Euler advance mode.
+"""
+
+import numpy as np
+import pytest
+
+from compiler import native
+from compiler import workloads as wl
+from oracle import api, literal
+
+pytestmark = pytest.mark.gpu
+
+
+def _bits(a):
+    return np.ascontiguousarray(a).view(np.int64)
+
+
+def _device(torch, a, pitch=None):
+    """Copy a host array to the device, optionally into a wider (pitched) x stride."""
+    nz, ny, nx = a.shape
+    if pitch is None:
+        return torch.from_numpy(a).cuda(), nx
+    t = torch.full((nz, ny, pitch), float("nan"), dtype=torch.float64, device="cuda")
+    t[:, :, :nx] = torch.from_numpy(a).cuda()
+    return t, pitch
+
+
+def _run(torch, fields: wl.Fields, mode=native.TENDENCY, dt=0.0, pitch=None, which=("U", "V", "W")):
+    geo = fields.geometry
+    ins = [_device(torch, a, pitch)[0] for a in fields.arrays()]
+    sx = ins[0].shape[2]
+    outs = [torch.full_like(t, float("nan")) for t in ins]
+    grid = native.make_grid(geo.nx, geo.ny, geo.nz, geo.halo, geo.dx, geo.dy, geo.dz, sx=sx)
+    ptr = [t.data_ptr() for t in ins]
+    optr = [t.data_ptr() for t in outs]
+    sel = [optr[n] if name in which else None for n, name in enumerate(("U", "V", "W"))]
+    native.advection(grid, *ptr[:3], *sel, scalars=ptr[3:], scalar_out=optr[3:], mode=mode, dt=dt)
+    torch.cuda.synchronize()
+    nx = geo.nx + 2 * geo.halo
+    return [o[:, :, :nx].cpu().numpy() for o in outs]
+
+
+def _oracle(fields: wl.Fields, mode=native.TENDENCY, dt=0.0):
+    geo = fields.geometry
+    t = api.advection_step({"U": fields.U, "V": fields.V, "W": fields.W}, geo.dx, geo.dy, geo.dz, geo.halo,
+                           fields.scalars)
+    out = [t["U"], t["V"], t["W"], *[t[f"S{n}"] for n in range(len(fields.scalars))]]
+    if mode == native.ADVANCE:
+        out = [api.euler(a.copy(), o, dt, geo.halo) for a, o in zip(fields.arrays(), out)]
+    return out
+
+
+def _interior(a, geo):
+    return a[geo.interior()]
+
+
+@pytest.mark.parametrize("shape,halo,nscalar", [((3, 5, 2), 1, 0), ((1, 1, 1), 1, 1), ((12, 10, 6), 2, 3),
+                                                ((33, 9, 17), 2, 2), ((64, 64, 32), 2, 1)])
+def test_tendencies_bit_exact(cuda, shape, halo, nscalar):
+    geo = wl.Geometry(*shape, halo=halo)
+    fields = wl.advection_fields(geo, seed=0, nscalar=nscalar)
+    got = _run(cuda, fields)
+    ref = _oracle(fields)
+    for g, r in zip(got, ref):
+        assert np.array_equal(_bits(_interior(g, geo)), _bits(_interior(r, geo)))
+
+
+def test_reference_driver_geometry(cuda):
+    fields = wl.reference_driver_fields(16, 12, 10, seed=7)
+    geo = fields.geometry
+    got = _run(cuda, fields)
+    ref = _oracle(fields)
+    for g, r in zip(got, ref):
+        assert np.array_equal(_bits(_interior(g, geo)), _bits(_interior(r, geo)))
+
+
+def test_cdu_main_fixture_inputs_against_literal(cuda):
+    """The sin/cos inputs of cdu_main.f90:38-50 at 16^3, checked against the literal transcription."""
+    U, V, W, dx, dy, dz = literal.fixture_inputs(16, 16, 16)
+    geo = wl.Geometry(16, 16, 16, halo=1, dx=dx, dy=dy, dz=dz)
+    fields = wl.Fields(geo, U, V, W, [])
+    got = _run(cuda, fields)
+    for g, which, arr in zip(got, ("cdu", "cdv", "cdw"), (U, V, W)):
+        ref = literal.tendency(which, np.zeros_like(U), U, V, W, dx, dy, dz)
+        assert np.array_equal(_bits(_interior(g, geo)), _bits(_interior(ref, geo)))
+
+
+def test_pitched_rows(cuda):
+    geo = wl.Geometry(13, 7, 5, halo=2)
+    fields = wl.advection_fields(geo, seed=3, nscalar=1)
+    got = _run(cuda, fields, pitch=geo.nx + 2 * geo.halo + 5)
+    ref = _oracle(fields)
+    for g, r in zip(got, ref):
+        assert np.array_equal(_bits(_interior(g, geo)), _bits(_interior(r, geo)))
+
+
+def test_advance_mode(cuda):
+    geo = wl.Geometry(20, 18, 9, halo=2)
+    fields = wl.advection_fields(geo, seed=5, nscalar=2)
+    got = _run(cuda, fields, mode=native.ADVANCE, dt=0.1)
+    ref = _oracle(fields, mode=native.ADVANCE, dt=0.1)
+    for g, r in zip(got, ref):
+        assert np.array_equal(_bits(_interior(g, geo)), _bits(_interior(r, geo)))
+
+
+def test_subset_of_outputs_leaves_others_untouched(cuda):
+    geo = wl.Geometry(10, 8, 4, halo=1)
+    fields = wl.advection_fields(geo, seed=2)
+    got = _run(cuda, fields, which=("V",))
+    ref = _oracle(fields)
+    assert np.isnan(got[0]).all() and np.isnan(got[2]).all()
+    assert np.array_equal(_bits(_interior(got[1], geo)), _bits(_interior(ref[1], geo)))
+
+
+@pytest.mark.parametrize("shape,halo", [((12, 10, 6), 2), ((5, 4, 3), 1), ((9, 7, 4), 3)])
+def test_halo_fill_bit_exact(cuda, shape, halo):
+    geo = wl.Geometry(*shape, halo=halo)
+    rng = np.random.default_rng(11)
+    arrays = [rng.normal(size=geo.shape) for _ in range(3)]
+    kinds = [0, 1, 0]
+    dev = [cuda.from_numpy(a).cuda() for a in arrays]
+    grid = native.make_grid(geo.nx, geo.ny, geo.nz, halo, geo.dx, geo.dy, geo.dz)
+    native.halo_fill(grid, [t.data_ptr() for t in dev], kinds)
+    cuda.cuda.synchronize()
+    for a, kind, t in zip(arrays, kinds, dev):
+        ref = api.halo(a.copy(), kind, halo)
+        assert np.array_equal(_bits(t.cpu().numpy()), _bits(ref))
+
+
+def test_argument_errors(cuda):
+    geo = wl.Geometry(4, 4, 4, halo=1)
+    t = cuda.zeros(geo.shape, dtype=cuda.float64, device="cuda")
+    grid = native.make_grid(4, 4, 4, 1, 1.0, 1.0, 1.0)
+    with pytest.raises(native.NativeError) as err:
+        native.advection(grid, t.data_ptr(), t.data_ptr(), t.data_ptr(), ut=t.data_ptr())
+    assert err.value.status == 3
+    bad = native.make_grid(4, 4, 4, 1, 1.0, 1.0, 1.0, sx=3)
+    with pytest.raises(native.NativeError):
+        native.advection(bad, t.data_ptr(), t.data_ptr(), t.data_ptr())
