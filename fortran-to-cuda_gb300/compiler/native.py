@@ -129,9 +129,14 @@ def load() -> ctypes.CDLL:
     lib.f2c_last_error.restype = ctypes.c_char_p
     lib.f2c_advection_v1.argtypes = [ctypes.POINTER(Grid), ctypes.POINTER(Fields), ctypes.c_void_p]
     lib.f2c_advection_v1.restype = ctypes.c_int
+    lib.f2c_advection_variant_v1.argtypes = [ctypes.POINTER(Grid), ctypes.POINTER(Fields), ctypes.c_int,
+                                             ctypes.c_void_p]
+    lib.f2c_advection_variant_v1.restype = ctypes.c_int
     lib.f2c_halo_fill_v1.argtypes = [ctypes.POINTER(Grid), ctypes.POINTER(ctypes.c_void_p),
                                      ctypes.POINTER(ctypes.c_int32), ctypes.c_int32, ctypes.c_void_p]
     lib.f2c_halo_fill_v1.restype = ctypes.c_int
+    lib.f2c_fp64_rate_v1.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_double)]
+    lib.f2c_fp64_rate_v1.restype = ctypes.c_int
     return lib
 
 
@@ -150,9 +155,16 @@ def make_grid(nx, ny, nz, halo, dx, dy, dz, sx=None, sy=None) -> Grid:
     return Grid(nx, ny, nz, halo, sx or nx + 2 * halo, sy or ny + 2 * halo, dx, dy, dz)
 
 
+FACES, DIRECT = 0, 1
+
+
 def advection(grid: Grid, u, v, w, ut=None, vt=None, wt=None, scalars=(), scalar_out=(), mode=TENDENCY,
-              dt=0.0, stream=0) -> None:
-    """Enqueue the fused advection launch on device pointers (ints)."""
+              dt=0.0, stream=0, variant=FACES) -> None:
+    """Enqueue the fused advection launch on device pointers (ints).
+
+    ``variant`` FACES is the face-sharing kernel (the product path); DIRECT is the
+    straightforward per-point kernel kept as a cross-check.
+    """
     fields = Fields()
     fields.u, fields.v, fields.w = u, v, w
     fields.ut, fields.vt, fields.wt = ut, vt, wt
@@ -162,7 +174,8 @@ def advection(grid: Grid, u, v, w, ut=None, vt=None, wt=None, scalars=(), scalar
     for n, (s, st) in enumerate(zip(scalars, scalar_out, strict=True)):
         fields.s[n] = s
         fields.st[n] = st
-    check(load().f2c_advection_v1(ctypes.byref(grid), ctypes.byref(fields), ctypes.c_void_p(stream)))
+    check(load().f2c_advection_variant_v1(ctypes.byref(grid), ctypes.byref(fields), variant,
+                                          ctypes.c_void_p(stream)))
 
 
 def halo_fill(grid: Grid, pointers, kinds, stream=0) -> None:
@@ -170,3 +183,10 @@ def halo_fill(grid: Grid, pointers, kinds, stream=0) -> None:
     ptrs = (ctypes.c_void_p * n)(*pointers)
     ks = (ctypes.c_int32 * n)(*kinds)
     check(load().f2c_halo_fill_v1(ctypes.byref(grid), ptrs, ks, n, ctypes.c_void_p(stream)))
+
+
+def fp64_rate(op: int, scratch_ptr: int, scratch_elems: int) -> float:
+    """FP64 instructions/s of the current GPU: op 0 = add.rn.f64, op 1 = fma.rn.f64 (synchronous)."""
+    out = ctypes.c_double(0.0)
+    check(load().f2c_fp64_rate_v1(op, ctypes.c_void_p(scratch_ptr), scratch_elems, ctypes.byref(out)))
+    return out.value

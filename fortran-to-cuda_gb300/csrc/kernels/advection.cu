@@ -6,6 +6,7 @@
 // compiler/tests/fixtures/stencils/{cvd,cdw}.f90:105-125) and up to four
 // passive-scalar tendencies, replacing the reference's four grid-stride
 // launches per procedure (compiler/emission/cuda/kernels.py:37-69).
+#include "advection_faces.cuh"
 #include "advection_kernels.cuh"
 
 #include <cuda_runtime.h>
@@ -79,12 +80,48 @@ extern "C" uint32_t f2c_advection_abi_version(void) { return F2C_ADVECTION_ABI_V
 
 extern "C" const char *f2c_last_error(void) { return g_last_error.c_str(); }
 
-extern "C" int f2c_advection_v1(const f2c_grid_v1 *grid, const f2c_fields_v1 *fields, void *stream) {
+namespace f2c {
+
+// Face-sharing kernel instantiations: all three velocities with 0..4 scalars,
+// one velocity alone (the per-procedure entries CDU, CDV, CDW), scalars alone.
+template <int NS>
+static cudaError_t faces_for_mask(const AdvArgs &a, int mask, cudaStream_t s) {
+    switch (mask) {
+    case 7: return launch_faces<NS, 7>(a, s);
+    case 1: return launch_faces<NS, 1>(a, s);
+    case 2: return launch_faces<NS, 2>(a, s);
+    case 4: return launch_faces<NS, 4>(a, s);
+    case 0: return NS > 0 ? launch_faces<NS, 0>(a, s) : cudaSuccess;
+    default: return launch_faces<NS, 7>(a, s);  // two of three: compute all, store the requested ones
+    }
+}
+
+static cudaError_t launch_faces_dispatch(const AdvArgs &a, cudaStream_t s) {
+    const int mask = (a.out[0] ? 1 : 0) | (a.out[1] ? 2 : 0) | (a.out[2] ? 4 : 0);
+    switch (a.nscalar) {
+    case 0: return faces_for_mask<0>(a, mask, s);
+    case 1: return faces_for_mask<1>(a, mask, s);
+    case 2: return faces_for_mask<2>(a, mask, s);
+    case 3: return faces_for_mask<3>(a, mask, s);
+    default: return faces_for_mask<4>(a, mask, s);
+    }
+}
+
+} // namespace f2c
+
+extern "C" int f2c_advection_variant_v1(const f2c_grid_v1 *grid, const f2c_fields_v1 *fields, int variant,
+                                        void *stream) {
     AdvArgs a;
     if (int s = fill_args(grid, fields, a)) return s;
-    const cudaError_t e = launch_advection(a, static_cast<cudaStream_t>(stream));
+    if (variant != 0 && variant != 1) return fail(1, "unknown advection kernel variant");
+    const cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const cudaError_t e = variant == 0 ? launch_faces_dispatch(a, st) : launch_advection(a, st);
     if (e != cudaSuccess) return fail(6, std::string("advection launch: ") + cudaGetErrorString(e));
     return 0;
+}
+
+extern "C" int f2c_advection_v1(const f2c_grid_v1 *grid, const f2c_fields_v1 *fields, void *stream) {
+    return f2c_advection_variant_v1(grid, fields, 0, stream);
 }
 
 extern "C" int f2c_halo_fill_v1(const f2c_grid_v1 *grid, double *const *fields, const int32_t *kinds, int32_t count,

@@ -1,0 +1,303 @@
+// Face-sharing z-marching advection kernel for sm_103a.
+//
+// GB300 executes FP64 arithmetic at about 1.6 lane-operations per clock per SM
+// (measured), some 75x below its FP32 rate, so this FP64 stencil is bound by
+// the FP64 pipe long before HBM. The kernel therefore performs every distinct
+// operation of the reference's per-point expression trees exactly once per
+// grid point:
+//
+//  * Each flux on a cell face appears in the expressions of the two points
+//    that share the face, with the same operands in the same order (IEEE
+//    addition and multiplication commute exactly), so it is computed once:
+//    top faces are carried in registers up the z-march, east and north faces
+//    go through shared memory to the neighbour, and a ninth "edge" warp
+//    supplies the tile's west column and south row.
+//  * Sums shared between the CDU, CDV and CDW trees (e.g. U(j+1)+U feeds the
+//    CDU y-flux, the CDV x-flux and the CDV advective average) are computed
+//    once.
+//  * The final multiplication by 0.5 (benchmarks/cdu/src/cdu.f90:39) is an
+//    exact exponent decrement, done on the integer pipe (with the correctly
+//    rounded subnormal case handled in integer arithmetic as well).
+//
+// Every other operation follows the reference grouping (advection_point.cuh),
+// so results are bit-identical to the oracle. Operation count per point:
+// U, V, W: 9 face sums + 18 flux products + 15 flux differences + 48
+// advective-form operations = 90; scalars: 3 shared coefficient products +
+// 11 per scalar.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "advection_kernels.cuh"
+
+namespace f2c {
+
+constexpr int kFaceTX = 32;       // points per tile along x (one warp)
+constexpr int kFaceTY = 8;        // compute warps per tile (points along y)
+constexpr int kFaceKZ = 32;       // levels per z-chunk
+constexpr int kFaceThreads = kFaceTX * (kFaceTY + 1);
+
+// Exact x * 0.5 without the FP64 pipe: for normal x the exponent field drops by
+// one; for the smallest normals and subnormals the significand shifts right
+// with round-half-even, which is what the correctly rounded product does.
+// Infinities and NaNs are returned unchanged.
+__device__ __forceinline__ double exact_half(double x) {
+    const long long b = __double_as_longlong(x);
+    const unsigned e = (unsigned)((unsigned long long)b >> 52) & 0x7ffu;
+    const long long sign = b & (long long)0x8000000000000000ULL;
+    const long long m = b & 0x001fffffffffffffLL;  // significand (with the lowest exponent bit for e == 1)
+    const long long small = sign | ((m >> 1) + (m & (m >> 1) & 1));
+    long long r = b - (1LL << 52);
+    r = e < 2 ? small : r;
+    r = e == 0x7ffu ? b : r;
+    return __longlong_as_double(r);
+}
+
+template <int NS, int MASK>
+struct FaceSmem {
+    static constexpr int NF = 3 + NS;
+    // [buffer][flux][row][column]: x faces have TX+1 columns (column 0 = west edge),
+    // y faces TY+1 rows (row 0 = south edge).
+    static constexpr int XF = kFaceTY * (kFaceTX + 1);
+    static constexpr int YF = (kFaceTY + 1) * kFaceTX;
+    static constexpr size_t bytes = sizeof(double) * 2 * NF * (XF + YF);
+};
+
+template <int NS, int MASK>
+__global__ void __launch_bounds__(kFaceThreads, 1) advection_faces_kernel(const AdvArgs a) {
+    constexpr bool DO_U = MASK & 1, DO_V = MASK & 2, DO_W = MASK & 4;
+    using Smem = FaceSmem<NS, MASK>;
+    constexpr int NF = Smem::NF;
+    extern __shared__ double smem[];
+    double *xface = smem;                         // [2][NF][XF]
+    double *yface = smem + 2 * NF * Smem::XF;     // [2][NF][YF]
+
+    const int lane = threadIdx.x;
+    const int warp = threadIdx.y;
+    const bool edge = warp == kFaceTY;
+    const int i0 = blockIdx.x * kFaceTX, j0 = blockIdx.y * kFaceTY;
+    const int k0 = blockIdx.z * kFaceKZ;
+    const int k1 = min(k0 + kFaceKZ, a.nz);
+    const long long sx = a.sx, plane = a.plane;
+    const double *__restrict__ U = a.u;
+    const double *__restrict__ V = a.v;
+    const double *__restrict__ W = a.w;
+    const Coefficients c = a.c;
+
+    // Compute threads own (i, j); the edge warp's lanes own (i0+lane, j0-1) for the south row and
+    // (i0-1, j0+lane) for the west column.
+    const int i = i0 + lane, j = j0 + warp;
+    const bool active = !edge && i < a.nx && j < a.ny;
+    const bool south_lane = edge && i < a.nx;
+    const bool west_lane = edge && lane < kFaceTY && j0 + lane < a.ny;
+    const int ci = edge ? i : i, cj = edge ? j0 - 1 : j;  // column of the south-row role
+    long long p = (long long)(ci + a.h) + sx * (long long)(cj + a.h) + plane * (long long)(k0 + a.h);
+    long long pw = (long long)(i0 - 1 + a.h) + sx * (long long)(j0 + lane + a.h) + plane * (long long)(k0 + a.h);
+#define LD(A, q, di, dj, dk) __ldg((A) + (q) + (di) + (dj)*sx + (dk)*plane)
+
+    // Top-face fluxes of the level below the current one (bottom faces), carried up the march.
+    double FUzb = 0.0, FVzb = 0.0, FWzb = 0.0, ftb[NS > 0 ? NS : 1];
+    if (active) {
+        // prologue: top faces of level k0-1
+        const double Um = LD(U, p, 0, 0, -1), U0 = LD(U, p, 0, 0, 0);
+        const double Vm = LD(V, p, 0, 0, -1), V0 = LD(V, p, 0, 0, 0);
+        const double Wm = LD(W, p, 0, 0, -1), W0 = LD(W, p, 0, 0, 0);
+        if (DO_U) {
+            const double sUz = U0 + Um;
+            const double sWx = LD(W, p, 1, 0, -1) + Wm;
+            FUzb = (c.Az * sUz) * sWx;
+        }
+        if (DO_V || DO_W) {
+            const double sVz = V0 + Vm;
+            const double sWy = LD(W, p, 0, 1, -1) + Wm;
+            if (DO_V) FVzb = (c.Az * sVz) * sWy;
+        }
+        if (DO_W) {
+            const double sWz = W0 + Wm;
+            FWzb = (c.Az * sWz) * sWz;
+        }
+#pragma unroll
+        for (int n = 0; n < NS; ++n) {
+            const double *__restrict__ S = a.s[n];
+            ftb[n] = (c.Sz * Wm) * (LD(S, p, 0, 0, 0) + LD(S, p, 0, 0, -1));
+        }
+    }
+
+    int buf = 0;
+    for (int k = k0; k < k1; ++k, p += plane, pw += plane, buf ^= 1) {
+        double *xf = xface + buf * NF * Smem::XF;
+        double *yf = yface + buf * NF * Smem::YF;
+        // ---------------- phase A: own east / north / top faces, edge faces ----------------
+        double U0 = 0, Ue = 0, Un = 0, Up = 0, V0 = 0, Ve = 0, Vn = 0, Vp = 0, W0 = 0, We = 0, Wn = 0, Wp = 0;
+        double sUx = 0, sVx = 0, sWx = 0, sUy = 0, sVy = 0, sWy = 0, sUz = 0, sVz = 0, sWz = 0;
+        double FUx = 0, FVx = 0, FWx = 0, FUy = 0, FVy = 0, FWy = 0, FUz = 0, FVz = 0, FWz = 0;
+        double S0[NS > 0 ? NS : 1], fe[NS > 0 ? NS : 1], fn[NS > 0 ? NS : 1], ft[NS > 0 ? NS : 1];
+        if (active) {
+            U0 = LD(U, p, 0, 0, 0); Ue = LD(U, p, 1, 0, 0); Un = LD(U, p, 0, 1, 0); Up = LD(U, p, 0, 0, 1);
+            V0 = LD(V, p, 0, 0, 0); Ve = LD(V, p, 1, 0, 0); Vn = LD(V, p, 0, 1, 0); Vp = LD(V, p, 0, 0, 1);
+            W0 = LD(W, p, 0, 0, 0); We = LD(W, p, 1, 0, 0); Wn = LD(W, p, 0, 1, 0); Wp = LD(W, p, 0, 0, 1);
+            if (DO_U) sUx = Ue + U0;
+            if (DO_U || DO_V) sVx = Ve + V0;
+            if (DO_U || DO_W) sWx = We + W0;
+            if (DO_U || DO_V) sUy = Un + U0;
+            if (DO_V) sVy = Vn + V0;
+            if (DO_V || DO_W) sWy = Wn + W0;
+            if (DO_U || DO_W) sUz = Up + U0;
+            if (DO_V || DO_W) sVz = Vp + V0;
+            if (DO_W) sWz = Wp + W0;
+            if (DO_U) {
+                FUx = (c.Ax * sUx) * sUx;
+                FUy = (c.Ay * sUy) * sVx;
+                FUz = (c.Az * sUz) * sWx;
+            }
+            if (DO_V) {
+                FVx = (c.Ax * sVx) * sUy;
+                FVy = (c.Ay * sVy) * sVy;
+                FVz = (c.Az * sVz) * sWy;
+            }
+            if (DO_W) {
+                FWx = (c.Ax * sWx) * sUz;
+                FWy = (c.Ay * sWy) * sVz;
+                FWz = (c.Az * sWz) * sWz;
+            }
+            if (NS > 0) {
+                const double SxU = c.Sx * U0, SyV = c.Sy * V0, SzW = c.Sz * W0;
+#pragma unroll
+                for (int n = 0; n < NS; ++n) {
+                    const double *__restrict__ S = a.s[n];
+                    S0[n] = LD(S, p, 0, 0, 0);
+                    fe[n] = SxU * (LD(S, p, 1, 0, 0) + S0[n]);
+                    fn[n] = SyV * (LD(S, p, 0, 1, 0) + S0[n]);
+                    ft[n] = SzW * (LD(S, p, 0, 0, 1) + S0[n]);
+                }
+            }
+            const int xo = warp * (kFaceTX + 1) + lane + 1;
+            const int yo = (warp + 1) * kFaceTX + lane;
+            if (DO_U) { xf[0 * Smem::XF + xo] = FUx; yf[0 * Smem::YF + yo] = FUy; }
+            if (DO_V) { xf[1 * Smem::XF + xo] = FVx; yf[1 * Smem::YF + yo] = FVy; }
+            if (DO_W) { xf[2 * Smem::XF + xo] = FWx; yf[2 * Smem::YF + yo] = FWy; }
+#pragma unroll
+            for (int n = 0; n < NS; ++n) {
+                xf[(3 + n) * Smem::XF + xo] = fe[n];
+                yf[(3 + n) * Smem::YF + yo] = fn[n];
+            }
+        } else if (edge) {
+            if (south_lane) {
+                // north faces of row j0-1 (the tile's south faces)
+                const double u0 = LD(U, p, 0, 0, 0), un = LD(U, p, 0, 1, 0);
+                const double v0 = LD(V, p, 0, 0, 0), ve = LD(V, p, 1, 0, 0), vn = LD(V, p, 0, 1, 0);
+                const double vp = LD(V, p, 0, 0, 1);
+                const double w0 = LD(W, p, 0, 0, 0), wn = LD(W, p, 0, 1, 0);
+                const int yo = lane;
+                if (DO_U) {
+                    const double s_uy = un + u0, s_vx = ve + v0;
+                    yf[0 * Smem::YF + yo] = (c.Ay * s_uy) * s_vx;
+                }
+                if (DO_V) {
+                    const double s_vy = vn + v0;
+                    yf[1 * Smem::YF + yo] = (c.Ay * s_vy) * s_vy;
+                }
+                if (DO_W) {
+                    const double s_wy = wn + w0, s_vz = vp + v0;
+                    yf[2 * Smem::YF + yo] = (c.Ay * s_wy) * s_vz;
+                }
+                if (NS > 0) {
+                    const double SyV = c.Sy * v0;
+#pragma unroll
+                    for (int n = 0; n < NS; ++n) {
+                        const double *__restrict__ S = a.s[n];
+                        yf[(3 + n) * Smem::YF + yo] = SyV * (LD(S, p, 0, 1, 0) + LD(S, p, 0, 0, 0));
+                    }
+                }
+            }
+            if (west_lane) {
+                // east faces of column i0-1 (the tile's west faces), row j0+lane
+                const double u0 = LD(U, pw, 0, 0, 0), ue = LD(U, pw, 1, 0, 0), un = LD(U, pw, 0, 1, 0);
+                const double up = LD(U, pw, 0, 0, 1);
+                const double v0 = LD(V, pw, 0, 0, 0), ve = LD(V, pw, 1, 0, 0);
+                const double w0 = LD(W, pw, 0, 0, 0), we = LD(W, pw, 1, 0, 0);
+                const int xo = lane * (kFaceTX + 1);
+                if (DO_U) {
+                    const double s_ux = ue + u0;
+                    xf[0 * Smem::XF + xo] = (c.Ax * s_ux) * s_ux;
+                }
+                if (DO_V) {
+                    const double s_vx = ve + v0, s_uy = un + u0;
+                    xf[1 * Smem::XF + xo] = (c.Ax * s_vx) * s_uy;
+                }
+                if (DO_W) {
+                    const double s_wx = we + w0, s_uz = up + u0;
+                    xf[2 * Smem::XF + xo] = (c.Ax * s_wx) * s_uz;
+                }
+                if (NS > 0) {
+                    const double SxU = c.Sx * u0;
+#pragma unroll
+                    for (int n = 0; n < NS; ++n) {
+                        const double *__restrict__ S = a.s[n];
+                        xf[(3 + n) * Smem::XF + xo] = SxU * (LD(S, pw, 1, 0, 0) + LD(S, pw, 0, 0, 0));
+                    }
+                }
+            }
+        }
+        __syncthreads();
+        // ---------------- phase B: differences of fluxes and the advective forms ----------------
+        if (active) {
+            const int xw = warp * (kFaceTX + 1) + lane;
+            const int ys = warp * kFaceTX + lane;
+            const double Uw = LD(U, p, -1, 0, 0), Us = LD(U, p, 0, -1, 0), Um = LD(U, p, 0, 0, -1);
+            const double Vw = LD(V, p, -1, 0, 0), Vs = LD(V, p, 0, -1, 0), Vm = LD(V, p, 0, 0, -1);
+            const double Ww = LD(W, p, -1, 0, 0), Ws = LD(W, p, 0, -1, 0), Wm = LD(W, p, 0, 0, -1);
+            if (DO_U) {
+                const double r = -(((FUx - xf[0 * Smem::XF + xw]) + (FUy - yf[0 * Smem::YF + ys])) + (FUz - FUzb));
+                const double Vadv = (sVx + Vs) + LD(V, p, 1, -1, 0);
+                const double Wadv = (sWx + Wm) + LD(W, p, 1, 0, -1);
+                const double adv = ((c.Bux * (Ue - Uw)) * U0 + (c.Buy * (Un - Us)) * Vadv) + (c.Buz * (Up - Um)) * Wadv;
+                if (a.out[0]) store_result(a.out[0], U, p, exact_half(r - adv), a.mode, a.dt);
+                FUzb = FUz;
+            }
+            if (DO_V) {
+                const double r = -(((FVy - yf[1 * Smem::YF + ys]) + (FVx - xf[1 * Smem::XF + xw])) + (FVz - FVzb));
+                const double Uadv = (sUy + Uw) + LD(U, p, -1, 1, 0);
+                const double Wadv = (sWy + Wm) + LD(W, p, 0, 1, -1);
+                const double adv = ((c.Bvx * (Ve - Vw)) * Uadv + (c.Bvy * (Vn - Vs)) * V0) + (c.Bvz * (Vp - Vm)) * Wadv;
+                if (a.out[1]) store_result(a.out[1], V, p, exact_half(r - adv), a.mode, a.dt);
+                FVzb = FVz;
+            }
+            if (DO_W) {
+                const double r = -(((FWz - FWzb) + (FWy - yf[2 * Smem::YF + ys])) + (FWx - xf[2 * Smem::XF + xw]));
+                const double Uadv = (sUz + Uw) + LD(U, p, -1, 0, 1);
+                const double Vadv = (sVz + Vs) + LD(V, p, 0, -1, 1);
+                const double adv = ((c.Bwx * (We - Ww)) * Uadv + (c.Bwy * (Wn - Ws)) * Vadv) + (c.Bwz * (Wp - Wm)) * W0;
+                if (a.out[2]) store_result(a.out[2], W, p, exact_half(r - adv), a.mode, a.dt);
+                FWzb = FWz;
+            }
+#pragma unroll
+            for (int n = 0; n < NS; ++n) {
+                const double st = -(((fe[n] - xf[(3 + n) * Smem::XF + xw]) + (fn[n] - yf[(3 + n) * Smem::YF + ys])) +
+                                    (ft[n] - ftb[n]));
+                if (a.st[n]) store_result(a.st[n], a.s[n], p, st, a.mode, a.dt);
+                ftb[n] = ft[n];
+            }
+        }
+    }
+#undef LD
+}
+
+template <int NS, int MASK>
+cudaError_t launch_faces(const AdvArgs &a, cudaStream_t stream) {
+    using Smem = FaceSmem<NS, MASK>;
+    static bool configured = false;
+    if (!configured) {
+        const cudaError_t e = cudaFuncSetAttribute(advection_faces_kernel<NS, MASK>,
+                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Smem::bytes);
+        if (e != cudaSuccess) return e;
+        configured = true;
+    }
+    const dim3 block(kFaceTX, kFaceTY + 1, 1);
+    const dim3 grid((a.nx + kFaceTX - 1) / kFaceTX, (a.ny + kFaceTY - 1) / kFaceTY, (a.nz + kFaceKZ - 1) / kFaceKZ);
+    advection_faces_kernel<NS, MASK><<<grid, block, Smem::bytes, stream>>>(a);
+    return cudaGetLastError();
+}
+
+} // namespace f2c

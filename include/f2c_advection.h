@@ -61,6 +61,11 @@ const char *f2c_last_error(void);
  * not written. */
 int f2c_advection_v1(const f2c_grid_v1 *grid, const f2c_fields_v1 *fields, void *stream);
 
+/* The same computation by a chosen kernel: 0 = the face-sharing kernel that
+ * f2c_advection_v1 runs, 1 = a direct per-point kernel kept as a cross-check.
+ * Both are bit-identical to the oracle. */
+int f2c_advection_variant_v1(const f2c_grid_v1 *grid, const f2c_fields_v1 *fields, int variant, void *stream);
+
 /* Boundary fill of `count` fields: periodic in x and y; vertical walls by
  * kind: 0 mirrors the interior (U, V, scalars), 1 is a face-staggered W with
  * zero wall faces and sign-changed mirrors. Requires nz >= halo. One launch. */

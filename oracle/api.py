@@ -101,12 +101,17 @@ def yee2d(ez, hx, hy, ch, ce, h):
     lib().orc_yee2d(_ptr(ez), _ptr(hx), _ptr(hy), ch, ce, nx, ny, h)
 
 
-def advection_step(fields: dict, dx, dy, dz, h, scalars=()):
-    """Tendencies of one step: U2, V2, W2 and one tendency per scalar (new arrays)."""
+def advection_step(fields: dict, dx, dy, dz, h, scalars=(), out=None):
+    """Tendencies of one step: U2, V2, W2 and one tendency per scalar.
+
+    ``out`` (a dict with keys U, V, W, S0, ...) receives them when given; new
+    zero-filled arrays are made otherwise.
+    """
     U, V, W = fields["U"], fields["V"], fields["W"]
-    out = {}
+    if out is None:
+        out = {name: np.zeros_like(U) for name in ("U", "V", "W", *[f"S{n}" for n in range(len(scalars))])}
     for name, which in (("U", "cdu"), ("V", "cdv"), ("W", "cdw")):
-        out[name] = momentum(which, np.zeros_like(U), U, V, W, dx, dy, dz, h)
+        momentum(which, out[name], U, V, W, dx, dy, dz, h)
     for n, s in enumerate(scalars):
-        out[f"S{n}"] = scalar(np.zeros_like(U), s, U, V, W, dx, dy, dz, h)
+        scalar(out[f"S{n}"], s, U, V, W, dx, dy, dz, h)
     return out

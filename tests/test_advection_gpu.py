@@ -30,7 +30,8 @@ def _device(torch, a, pitch=None):
     return t, pitch
 
 
-def _run(torch, fields: wl.Fields, mode=native.TENDENCY, dt=0.0, pitch=None, which=("U", "V", "W")):
+def _run(torch, fields: wl.Fields, mode=native.TENDENCY, dt=0.0, pitch=None, which=("U", "V", "W"),
+         variant=native.FACES, scalars=True):
     geo = fields.geometry
     ins = [_device(torch, a, pitch)[0] for a in fields.arrays()]
     sx = ins[0].shape[2]
@@ -39,7 +40,8 @@ def _run(torch, fields: wl.Fields, mode=native.TENDENCY, dt=0.0, pitch=None, whi
     ptr = [t.data_ptr() for t in ins]
     optr = [t.data_ptr() for t in outs]
     sel = [optr[n] if name in which else None for n, name in enumerate(("U", "V", "W"))]
-    native.advection(grid, *ptr[:3], *sel, scalars=ptr[3:], scalar_out=optr[3:], mode=mode, dt=dt)
+    native.advection(grid, *ptr[:3], *sel, scalars=ptr[3:] if scalars else (),
+                     scalar_out=optr[3:] if scalars else (), mode=mode, dt=dt, variant=variant)
     torch.cuda.synchronize()
     nx = geo.nx + 2 * geo.halo
     return [o[:, :, :nx].cpu().numpy() for o in outs]
@@ -59,21 +61,27 @@ def _interior(a, geo):
     return a[geo.interior()]
 
 
+VARIANTS = [native.FACES, native.DIRECT]
+
+
+@pytest.mark.parametrize("variant", VARIANTS)
 @pytest.mark.parametrize("shape,halo,nscalar", [((3, 5, 2), 1, 0), ((1, 1, 1), 1, 1), ((12, 10, 6), 2, 3),
-                                                ((33, 9, 17), 2, 2), ((64, 64, 32), 2, 1)])
-def test_tendencies_bit_exact(cuda, shape, halo, nscalar):
+                                                ((33, 9, 17), 2, 2), ((64, 64, 32), 2, 1), ((40, 17, 70), 2, 4),
+                                                ((65, 24, 33), 1, 3)])
+def test_tendencies_bit_exact(cuda, shape, halo, nscalar, variant):
     geo = wl.Geometry(*shape, halo=halo)
     fields = wl.advection_fields(geo, seed=0, nscalar=nscalar)
-    got = _run(cuda, fields)
+    got = _run(cuda, fields, variant=variant)
     ref = _oracle(fields)
     for g, r in zip(got, ref):
         assert np.array_equal(_bits(_interior(g, geo)), _bits(_interior(r, geo)))
 
 
-def test_reference_driver_geometry(cuda):
+@pytest.mark.parametrize("variant", VARIANTS)
+def test_reference_driver_geometry(cuda, variant):
     fields = wl.reference_driver_fields(16, 12, 10, seed=7)
     geo = fields.geometry
-    got = _run(cuda, fields)
+    got = _run(cuda, fields, variant=variant)
     ref = _oracle(fields)
     for g, r in zip(got, ref):
         assert np.array_equal(_bits(_interior(g, geo)), _bits(_interior(r, geo)))
@@ -99,22 +107,44 @@ def test_pitched_rows(cuda):
         assert np.array_equal(_bits(_interior(g, geo)), _bits(_interior(r, geo)))
 
 
-def test_advance_mode(cuda):
+@pytest.mark.parametrize("variant", VARIANTS)
+def test_advance_mode(cuda, variant):
     geo = wl.Geometry(20, 18, 9, halo=2)
     fields = wl.advection_fields(geo, seed=5, nscalar=2)
-    got = _run(cuda, fields, mode=native.ADVANCE, dt=0.1)
+    got = _run(cuda, fields, mode=native.ADVANCE, dt=0.1, variant=variant)
     ref = _oracle(fields, mode=native.ADVANCE, dt=0.1)
     for g, r in zip(got, ref):
         assert np.array_equal(_bits(_interior(g, geo)), _bits(_interior(r, geo)))
 
 
-def test_subset_of_outputs_leaves_others_untouched(cuda):
-    geo = wl.Geometry(10, 8, 4, halo=1)
-    fields = wl.advection_fields(geo, seed=2)
-    got = _run(cuda, fields, which=("V",))
+@pytest.mark.parametrize("which", [("U",), ("V",), ("W",), ("U", "W"), ("V", "W"), ()])
+def test_subset_of_outputs_leaves_others_untouched(cuda, which):
+    geo = wl.Geometry(37, 11, 35, halo=2)
+    fields = wl.advection_fields(geo, seed=2, nscalar=2 if not which else 0)
+    got = _run(cuda, fields, which=which)
     ref = _oracle(fields)
-    assert np.isnan(got[0]).all() and np.isnan(got[2]).all()
-    assert np.array_equal(_bits(_interior(got[1], geo)), _bits(_interior(ref[1], geo)))
+    for n, name in enumerate(("U", "V", "W")):
+        if name in which:
+            assert np.array_equal(_bits(_interior(got[n], geo)), _bits(_interior(ref[n], geo)))
+        else:
+            assert np.isnan(got[n]).all()
+    for g, r in zip(got[3:], ref[3:]):
+        assert np.array_equal(_bits(_interior(g, geo)), _bits(_interior(r, geo)))
+
+
+def test_exact_half_on_small_values(cuda):
+    """Tendencies of tiny fields exercise the integer halving on subnormal and smallest-normal results."""
+    geo = wl.Geometry(9, 7, 5, halo=1, dx=1.0, dy=1.0, dz=1.0)
+    rng = np.random.default_rng(3)
+    scale = np.float64(2.0) ** -537
+    arrays = [rng.normal(size=geo.shape) * scale for _ in range(3)]
+    arrays[0][2, 3, 4] = 0.0
+    fields = wl.Fields(geo, *arrays, [])
+    got = _run(cuda, fields)
+    ref = _oracle(fields)
+    assert any((np.abs(_interior(r, geo)) < np.finfo(np.float64).tiny).any() for r in ref)
+    for g, r in zip(got, ref):
+        assert np.array_equal(_bits(_interior(g, geo)), _bits(_interior(r, geo)))
 
 
 @pytest.mark.parametrize("shape,halo", [((12, 10, 6), 2), ((5, 4, 3), 1), ((9, 7, 4), 3)])
