@@ -99,6 +99,34 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     return LIBRARY
 
 
+def runtime() -> ctypes.CDLL:
+    """The product library with the fort_scope_* signatures declared."""
+    from .runtime import abi
+
+    return abi.bind(load())
+
+
+CPU_RUNTIME = BUILD_DIR / "libf2c_runtime_cpu.so"
+RUNTIME_SOURCE = CSRC / "runtime" / "scoped_runtime.cpp"
+
+
+def build_cpu_runtime(force: bool = False) -> Path:
+    """The residency runtime built with its CPU test backend (g++, no CUDA): for ABI tests without a GPU."""
+    deps = [RUNTIME_SOURCE, *sorted((CSRC / "runtime").glob("*.hpp")), INCLUDE / "scoped_runtime.h"]
+    if not force and CPU_RUNTIME.exists() and all(CPU_RUNTIME.stat().st_mtime >= d.stat().st_mtime for d in deps):
+        return CPU_RUNTIME
+    BUILD_DIR.mkdir(exist_ok=True)
+    tmp = CPU_RUNTIME.with_suffix(f".{os.getpid()}.tmp")
+    cxx = os.environ.get("CXX", "g++")
+    cmd = [cxx, "-std=c++17", "-O2", "-Wall", "-Wextra", "-Werror", "-fPIC", "-shared", "-pthread",
+           "-DF2C_RUNTIME_CPU_BACKEND", "-x", "c++", str(RUNTIME_SOURCE), "-o", str(tmp)]
+    result = subprocess.run(cmd, capture_output=True, text=True)
+    if result.returncode != 0:
+        raise RuntimeError(f"CPU runtime build failed:\n{result.stderr}")
+    os.replace(tmp, CPU_RUNTIME)
+    return CPU_RUNTIME
+
+
 # --- ctypes mirrors of include/f2c_advection.h -------------------------------------------------
 
 MAX_SCALARS = 4

@@ -1,0 +1,272 @@
+// Device operations of the residency runtime, behind one small interface with
+// two implementations chosen at compile time:
+//
+//  * the CUDA backend (default): stream-ordered allocations (cudaMallocAsync),
+//    pitched rectangle copies, kernel launches and CUDA graphs on the
+//    context's own non-blocking stream, host arrays pinned in place;
+//  * the CPU test backend (F2C_RUNTIME_CPU_BACKEND): "device" memory is host
+//    memory and a kernel function is a host function `void f(void **args)`,
+//    so every coherence, queue and graph-cache rule can be tested on a machine
+//    without a GPU.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "regions.hpp"
+
+#ifndef F2C_RUNTIME_CPU_BACKEND
+#include <cuda_runtime.h>
+#endif
+
+namespace f2c::rt {
+
+struct LaunchSpec {
+    const void *function = nullptr;
+    unsigned grid[3] = {1, 1, 1}, block[3] = {1, 1, 1};
+    size_t shared_bytes = 0;
+    std::vector<void *> arguments; // pointers to argument values
+};
+
+// Copy geometry of one array: extents and element size; a box is copied as
+// contiguous runs (the leading dimensions the box spans fully) or as 2-D
+// pitched copies when the first dimension is partial.
+struct CopyPlan {
+    int rank;
+    size_t elem;
+    size_t extents[kMaxRank];
+};
+
+template <typename F>
+void for_each_run(const CopyPlan &plan, const Box &box, F &&f) {
+    // f(offset_elements, width_elements, rows, row_pitch_elements)
+    const int r = plan.rank;
+    int full = 0;
+    while (full < r && box.lo[full] == 0 && box.hi[full] == plan.extents[full]) ++full;
+    size_t inner = 1;
+    for (int d = 0; d < full; ++d) inner *= plan.extents[d];
+    size_t stride[kMaxRank];
+    stride[0] = 1;
+    for (int d = 1; d < r; ++d) stride[d] = stride[d - 1] * plan.extents[d - 1];
+    if (full == r) {
+        f(0, inner, 1, inner);
+        return;
+    }
+    // dimension `full` is the first partial one
+    size_t width, rows, pitch;
+    int outer_start;
+    if (full > 0) {
+        width = inner * (box.hi[full] - box.lo[full]);
+        rows = 1;
+        pitch = width;
+        outer_start = full + 1;
+    } else {
+        width = box.hi[0] - box.lo[0];
+        if (r >= 2) {
+            rows = box.hi[1] - box.lo[1];
+            pitch = plan.extents[0];
+            outer_start = 2;
+        } else {
+            rows = 1;
+            pitch = width;
+            outer_start = 1;
+        }
+    }
+    size_t idx[kMaxRank];
+    for (int d = outer_start; d < r; ++d) idx[d] = box.lo[d];
+    while (true) {
+        size_t off = 0;
+        if (full > 0) off += box.lo[full] * stride[full];
+        else {
+            off += box.lo[0];
+            if (r >= 2) off += box.lo[1] * stride[1];
+        }
+        for (int d = outer_start; d < r; ++d) off += idx[d] * stride[d];
+        f(off, width, rows, pitch);
+        int d = outer_start;
+        for (; d < r; ++d) {
+            if (++idx[d] < box.hi[d]) break;
+            idx[d] = box.lo[d];
+        }
+        if (d == r) break;
+    }
+}
+
+#ifdef F2C_RUNTIME_CPU_BACKEND
+
+using Stream = void *;
+struct Backend {
+    static constexpr bool cpu = true;
+    static std::string last_error() { return "cpu backend"; }
+    static bool select(int) { return true; }
+    static int current() { return 0; }
+    static bool make_stream(Stream *s) {
+        *s = nullptr;
+        return true;
+    }
+    static void destroy_stream(Stream) {}
+    static bool alloc(void **p, size_t bytes, Stream) {
+        if (std::getenv("F2C_TEST_FAIL_ALLOC")) return false;
+        *p = std::malloc(bytes ? bytes : 1);
+        return *p != nullptr;
+    }
+    static void free(void *p, Stream) { std::free(p); }
+    static bool copy(void *dst, const void *src, const CopyPlan &plan, const Box &box, bool, Stream) {
+        for_each_run(plan, box, [&](size_t off, size_t width, size_t rows, size_t pitch) {
+            for (size_t r = 0; r < rows; ++r)
+                std::memcpy(static_cast<char *>(dst) + (off + r * pitch) * plan.elem,
+                            static_cast<const char *>(src) + (off + r * pitch) * plan.elem, width * plan.elem);
+        });
+        return true;
+    }
+    static bool sync(Stream) { return !std::getenv("F2C_TEST_FAIL_WAIT"); }
+    static bool pin(void *, size_t) { return false; }
+    static void unpin(void *) {}
+    static bool memory_info(size_t *free_bytes, size_t *total) {
+        *total = size_t(16) << 30;
+        *free_bytes = size_t(12) << 30;
+        return true;
+    }
+    static bool launch(const LaunchSpec &k, Stream) {
+        if (std::getenv("F2C_TEST_FAIL_LAUNCH")) return false;
+        auto fn = reinterpret_cast<void (*)(void **)>(const_cast<void *>(k.function));
+        fn(const_cast<void **>(k.arguments.data()));
+        return true;
+    }
+    // Graphs: on the CPU backend a graph is the node count; the runtime's cached
+    // launch records (with their current arguments) are run in order.
+    struct Graph {
+        size_t nodes = 0;
+    };
+    static bool graph_build(Graph **g, const std::vector<LaunchSpec> &nodes) {
+        if (std::getenv("F2C_TEST_FAIL_GRAPH_CREATE")) return false;
+        *g = new Graph{nodes.size()};
+        return true;
+    }
+    static bool graph_update(Graph *, size_t, const LaunchSpec &) { return !std::getenv("F2C_TEST_FAIL_GRAPH_UPDATE"); }
+    static bool graph_launch(Graph *g, const std::vector<LaunchSpec> &specs, Stream s) {
+        if (specs.size() != g->nodes) return false;
+        for (const auto &k : specs)
+            if (!launch(k, s)) return false;
+        return true;
+    }
+    static void graph_destroy(Graph *g) { delete g; }
+};
+
+#else
+
+using Stream = cudaStream_t;
+struct Backend {
+    static constexpr bool cpu = false;
+    static thread_local std::string error;
+    static std::string last_error() { return error; }
+    static bool ok(cudaError_t e) {
+        if (e == cudaSuccess) return true;
+        error = cudaGetErrorString(e);
+        return false;
+    }
+    static bool select(int device) { return ok(cudaSetDevice(device)); }
+    static int current() {
+        int d = 0;
+        cudaGetDevice(&d);
+        return d;
+    }
+    static bool make_stream(Stream *s) { return ok(cudaStreamCreateWithFlags(s, cudaStreamNonBlocking)); }
+    static void destroy_stream(Stream s) {
+        if (s) cudaStreamDestroy(s);
+    }
+    static bool alloc(void **p, size_t bytes, Stream s) { return ok(cudaMallocAsync(p, bytes ? bytes : 256, s)); }
+    static void free(void *p, Stream s) {
+        if (p) cudaFreeAsync(p, s);
+    }
+    static bool copy(void *dst, const void *src, const CopyPlan &plan, const Box &box, bool to_device, Stream s) {
+        const cudaMemcpyKind kind = to_device ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost;
+        bool good = true;
+        for_each_run(plan, box, [&](size_t off, size_t width, size_t rows, size_t pitch) {
+            if (!good) return;
+            char *d = static_cast<char *>(dst) + off * plan.elem;
+            const char *sp = static_cast<const char *>(src) + off * plan.elem;
+            if (rows == 1)
+                good = ok(cudaMemcpyAsync(d, sp, width * plan.elem, kind, s));
+            else
+                good = ok(cudaMemcpy2DAsync(d, pitch * plan.elem, sp, pitch * plan.elem, width * plan.elem, rows, kind,
+                                            s));
+        });
+        return good;
+    }
+    static bool sync(Stream s) { return ok(cudaStreamSynchronize(s)); }
+    static bool pin(void *p, size_t bytes) {
+        const cudaError_t e = cudaHostRegister(p, bytes, cudaHostRegisterDefault);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return false;
+        }
+        return true;
+    }
+    static void unpin(void *p) {
+        if (cudaHostUnregister(p) != cudaSuccess) cudaGetLastError();
+    }
+    static bool memory_info(size_t *free_bytes, size_t *total) { return ok(cudaMemGetInfo(free_bytes, total)); }
+    static cudaKernelNodeParams params(const LaunchSpec &k) {
+        cudaKernelNodeParams p{};
+        p.func = const_cast<void *>(k.function);
+        p.gridDim = dim3(k.grid[0], k.grid[1], k.grid[2]);
+        p.blockDim = dim3(k.block[0], k.block[1], k.block[2]);
+        p.sharedMemBytes = (unsigned)k.shared_bytes;
+        p.kernelParams = const_cast<void **>(k.arguments.data());
+        p.extra = nullptr;
+        return p;
+    }
+    static bool launch(const LaunchSpec &k, Stream s) {
+        return ok(cudaLaunchKernel(k.function, dim3(k.grid[0], k.grid[1], k.grid[2]),
+                                   dim3(k.block[0], k.block[1], k.block[2]), const_cast<void **>(k.arguments.data()),
+                                   k.shared_bytes, s));
+    }
+    struct Graph {
+        cudaGraph_t graph = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        std::vector<cudaGraphNode_t> nodes;
+    };
+    static bool graph_build(Graph **out, const std::vector<LaunchSpec> &nodes) {
+        auto *g = new Graph;
+        if (!ok(cudaGraphCreate(&g->graph, 0))) {
+            delete g;
+            return false;
+        }
+        cudaGraphNode_t prev = nullptr;
+        for (const auto &k : nodes) {
+            cudaGraphNode_t node;
+            const cudaKernelNodeParams p = params(k);
+            if (!ok(cudaGraphAddKernelNode(&node, g->graph, prev ? &prev : nullptr, prev ? 1 : 0, &p))) {
+                graph_destroy(g);
+                return false;
+            }
+            g->nodes.push_back(node);
+            prev = node;
+        }
+        if (!ok(cudaGraphInstantiate(&g->exec, g->graph, 0))) {
+            graph_destroy(g);
+            return false;
+        }
+        *out = g;
+        return true;
+    }
+    static bool graph_update(Graph *g, size_t node, const LaunchSpec &k) {
+        const cudaKernelNodeParams p = params(k);
+        return ok(cudaGraphExecKernelNodeSetParams(g->exec, g->nodes[node], &p));
+    }
+    static bool graph_launch(Graph *g, const std::vector<LaunchSpec> &, Stream s) { return ok(cudaGraphLaunch(g->exec, s)); }
+    static void graph_destroy(Graph *g) {
+        if (!g) return;
+        if (g->exec) cudaGraphExecDestroy(g->exec);
+        if (g->graph) cudaGraphDestroy(g->graph);
+        delete g;
+    }
+};
+
+#endif
+
+} // namespace f2c::rt

@@ -1,0 +1,1680 @@
+// GB300 residency runtime: implementation of the fort_scope_* ABI
+// (include/scoped_runtime.h), the drop-in replacement for the reference's
+// compiler/runtime/scoped_runtime.cu.
+//
+// Design, GB300-first:
+//  * A domain owns the physical state: registered arrays, their device mirrors
+//    (stream-ordered allocations on the context stream), the budget with LRU
+//    eviction, and the statistics. A context borrows a domain and owns the
+//    execution state: one non-blocking stream, the task queue, the graph cache.
+//  * Coherence is tracked per array as three rectangle sets (regions.hpp):
+//    defined values, values current on the host, values current on the device.
+//    A device task uploads exactly the defined sections it reads (or partially
+//    writes) that the device lacks; a host access downloads exactly what the
+//    host lacks; observation publishes what only the device holds.
+//  * Accepted tasks join a queue that is submitted as one CUDA graph. A task
+//    sequence runs with direct launches the first time it is reached, is
+//    instantiated as a graph the second time, and is replayed afterwards with
+//    cudaGraphExecKernelNodeSetParams for the nodes whose arguments changed
+//    (the reference's policy, compiler/runtime/scoped_graphs.hpp:140-235).
+//  * Host arrays of 1 MiB or more are pinned in place at registration
+//    (FORT_SCOPE_PIN_HOST=0 disables it) so uploads and downloads run as DMA
+//    over NVLink-C2C without staging.
+//  * Failures after numerical work started poison the context and its domain;
+//    nothing is replayed (scoped_runtime.h:428-438 of the reference).
+#include "../../../include/scoped_runtime.h"
+
+#include <cinttypes>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <set>
+#include <string>
+#include <vector>
+
+#include "backend.hpp"
+#include "regions.hpp"
+
+namespace f2c::rt {
+
+#ifndef F2C_RUNTIME_CPU_BACKEND
+thread_local std::string Backend::error;
+#endif
+
+namespace {
+
+thread_local std::string t_error;
+std::recursive_mutex g_mutex;
+
+int fail(int status, const std::string &message) {
+    t_error = message;
+    return status;
+}
+
+struct Failure {
+    int status;
+    std::string message;
+};
+
+[[noreturn]] void raise(int status, const std::string &message) { throw Failure{status, message}; }
+
+bool env_flag(const char *name, bool fallback) {
+    const char *v = std::getenv(name);
+    if (!v || !*v) return fallback;
+    return std::strcmp(v, "0") != 0;
+}
+
+bool tracing() {
+    static const bool on = env_flag("FORT_RUNTIME_TRACE", false);
+    return on;
+}
+
+struct Context;
+struct Domain;
+
+struct Buffer {
+    uint64_t handle = 0, identity = 0, generation = 0;
+    int rank = 0;
+    uint32_t type = 0;
+    size_t elem = 0, bytes = 0;
+    void *host = nullptr;
+    size_t extents[kMaxRank] = {};
+    int64_t lower[kMaxRank] = {};
+    void *device = nullptr;
+    bool pinned_host = false;
+    Region defined, host_valid, device_valid;
+    enum { NONE, HOST, DEVICE } prepared = NONE;
+    Region prep_writes, prep_overwrites;
+    uint64_t last_use = 0;
+    int queued = 0; // accepted tasks not yet submitted that use this buffer
+
+    Box full() const { return whole(rank, extents); }
+    CopyPlan plan() const {
+        CopyPlan p;
+        p.rank = rank;
+        p.elem = elem;
+        for (int d = 0; d < rank; ++d) p.extents[d] = extents[d];
+        return p;
+    }
+};
+
+struct Task {
+    uint64_t code_key = 0;
+    LaunchSpec spec;
+    std::vector<std::vector<unsigned char>> values;
+    std::vector<uint64_t> buffers;
+    uint64_t threads = 0;
+};
+
+struct CachedGraph {
+    std::vector<const void *> functions;
+    std::vector<size_t> argument_counts;
+    std::vector<std::vector<std::vector<unsigned char>>> values; // per node, per argument
+    std::vector<LaunchSpec> specs;
+    Backend::Graph *graph = nullptr;
+    int reached = 0;
+};
+
+struct Domain {
+    uint64_t handle = 0;
+    int device = 0;
+    size_t budget = 0;
+    bool budget_set = false, budget_warned = false;
+    bool poisoned = false, owned_by_context = false;
+    Context *borrower = nullptr;
+    std::map<uint64_t, std::unique_ptr<Buffer>> buffers;
+    std::map<uint64_t, uint64_t> by_identity;
+    size_t device_bytes = 0, scratch_bytes = 0;
+    fort_scope_stats stats{};
+    fort_scope_residency_stats_v1 residency{};
+    uint64_t tick = 0;
+};
+
+struct Context {
+    uint64_t handle = 0;
+    Domain *domain = nullptr;
+    bool private_domain = false;
+    bool poisoned = false;
+    Stream stream = nullptr;
+    bool stream_ready = false;
+    bool queue_enabled = true, graphs_enabled = true;
+    uint64_t queue_work_limit = uint64_t(1) << 18;
+    std::vector<Task> pending;
+    uint64_t pending_threads = 0;
+    std::map<uint64_t, CachedGraph> graphs;
+    fort_scope_graph_stats_v1 graph_stats{};
+    fort_scope_graph_queue_stats_v1 queue_stats{};
+    fort_scope_completion_stats_v1 completion{};
+    char trace[6][65] = {};
+    // scratch arena
+    void *scratch = nullptr;
+    size_t scratch_capacity = 0, scratch_active_bytes = 0;
+    bool scratch_active = false;
+    uint64_t scratch_token = 0;
+    fort_scope_scratch_stats_v1 scratch_stats{};
+};
+
+std::map<uint64_t, std::unique_ptr<Context>> g_contexts;
+std::map<uint64_t, std::unique_ptr<Domain>> g_domains;
+uint64_t g_next_handle = 0x5c0de000ULL;
+std::set<uint64_t> g_retired;
+
+uint64_t new_handle() { return ++g_next_handle; }
+
+void trace_line(Context *c, const char *event, uint64_t buffer, uint64_t bytes) {
+    if (!tracing()) return;
+    std::fprintf(stderr,
+                 "FORT_SCOPED %s buffer=%" PRIu64 " bytes=%" PRIu64 " context=%" PRIu64
+                 " owner=%s procedure=%s implementation=%s\n",
+                 event, buffer, bytes, c ? c->handle : 0, c && c->trace[0][0] ? c->trace[0] : "unknown",
+                 c && c->trace[1][0] ? c->trace[1] : "unknown", c && c->trace[4][0] ? c->trace[4] : "unknown");
+}
+
+Context *find_context(fort_scope_t handle) {
+    auto it = g_contexts.find(handle);
+    if (it == g_contexts.end()) {
+        if (g_retired.count(handle)) raise(FORT_SCOPE_STALE, "stale scope context");
+        raise(FORT_SCOPE_ARGUMENT, "unknown scope context");
+    }
+    return it->second.get();
+}
+
+Context *live_context(fort_scope_t handle) {
+    Context *c = find_context(handle);
+    if (c->poisoned || c->domain->poisoned)
+        raise(FORT_SCOPE_EXECUTION, "context poisoned by an earlier execution failure; unsafe replay prohibited");
+    return c;
+}
+
+Domain *find_domain(fort_scope_domain_t handle) {
+    auto it = g_domains.find(handle);
+    if (it == g_domains.end()) {
+        if (g_retired.count(handle)) raise(FORT_SCOPE_STALE, "stale residency domain");
+        raise(FORT_SCOPE_ARGUMENT, "unknown residency domain");
+    }
+    return it->second.get();
+}
+
+Buffer *find_buffer(Context *c, fort_buffer_t handle) {
+    auto it = c->domain->buffers.find(handle);
+    if (it == c->domain->buffers.end()) {
+        if (g_retired.count(handle)) raise(FORT_SCOPE_STALE, "stale buffer handle");
+        raise(FORT_SCOPE_ARGUMENT, "unknown buffer handle");
+    }
+    return it->second.get();
+}
+
+void poison(Context *c, const std::string &message) {
+    c->poisoned = true;
+    c->domain->poisoned = true;
+    raise(FORT_SCOPE_EXECUTION, message + "; unsafe replay prohibited");
+}
+
+void ensure_stream(Context *c) {
+    if (c->stream_ready) return;
+    if (!Backend::select(c->domain->device)) raise(FORT_SCOPE_RESOURCE, "cannot select device: " + Backend::last_error());
+    if (!Backend::make_stream(&c->stream)) raise(FORT_SCOPE_RESOURCE, "cannot create stream: " + Backend::last_error());
+    c->stream_ready = true;
+}
+
+// ---- effects --------------------------------------------------------------------------------
+
+struct Effects {
+    Region reads, writes, overwrites; // writes include overwrites
+};
+
+Box section_box(const Buffer *b, const fort_scope_section &s) {
+    if (!s.lower || !s.upper) raise(FORT_SCOPE_ARGUMENT, "null section coordinates");
+    Box box;
+    box.rank = b->rank;
+    for (int d = 0; d < b->rank; ++d) {
+        box.lo[d] = s.lower[d];
+        box.hi[d] = s.upper[d];
+        if (box.hi[d] < box.lo[d] || box.hi[d] > b->extents[d]) raise(FORT_SCOPE_ARGUMENT, "section outside its array");
+    }
+    return box;
+}
+
+Effects effects_of(const Buffer *b, const fort_scope_access &a) {
+    if (a.flags & ~uint32_t(7)) raise(FORT_SCOPE_ARGUMENT, "unknown access flags");
+    auto list = [&](size_t count, const fort_scope_section *s, Region &into) {
+        if (count > kRegionLimit || (count && !s)) raise(FORT_SCOPE_ARGUMENT, "section list exceeds the bounded interface");
+        for (size_t n = 0; n < count; ++n) into.add(section_box(b, s[n]));
+    };
+    Effects e;
+    if (a.flags & FORT_SCOPE_READ_ALL) e.reads.add(b->full());
+    else list(a.read_count, a.reads, e.reads);
+    if (a.flags & FORT_SCOPE_WRITE_ALL) e.writes.add(b->full());
+    else list(a.write_count, a.writes, e.writes);
+    if (a.flags & FORT_SCOPE_OVERWRITE_ALL) e.overwrites.add(b->full());
+    else list(a.overwrite_count, a.overwrites, e.overwrites);
+    e.writes.add(e.overwrites);
+    return e;
+}
+
+// Values a task needs current where it runs: what it reads, and what it may
+// write without overwriting (the unwritten part keeps its old values).
+Region needed(const Buffer *b, const Effects &e) {
+    Region need = e.reads;
+    Region partial = e.writes;
+    partial.remove(e.overwrites);
+    need.add(partial);
+    return b->defined.clip(need);
+}
+
+void check_initialized(const Buffer *b, const Effects &e) {
+    for (const auto &box : e.reads.boxes)
+        if (!b->defined.covers(box))
+            raise(FORT_SCOPE_UNINITIALIZED, "a task reads array values that were never defined");
+}
+
+// ---- transfers ------------------------------------------------------------------------------
+
+void copy_region(Context *c, Buffer *b, const Region &r, bool to_device) {
+    Domain *d = c->domain;
+    const CopyPlan plan = b->plan();
+    for (const auto &box : r.boxes) {
+        const size_t bytes = box.volume() * b->elem;
+        if (!bytes) continue;
+        bool good = to_device ? Backend::copy(b->device, b->host, plan, box, true, c->stream)
+                              : Backend::copy(b->host, b->device, plan, box, false, c->stream);
+        if (!good) poison(c, std::string("transfer failed: ") + Backend::last_error());
+        if (to_device) {
+            d->stats.uploads++;
+            d->stats.upload_bytes += bytes;
+            trace_line(c, "upload", b->handle, bytes);
+        } else {
+            d->stats.downloads++;
+            d->stats.download_bytes += bytes;
+            trace_line(c, "download", b->handle, bytes);
+        }
+    }
+}
+
+void wait_stream(Context *c) {
+    if (!c->stream_ready) return;
+    c->domain->stats.waits++;
+    c->completion.stream_waits++;
+    if (!Backend::sync(c->stream)) poison(c, std::string("device work failed: ") + Backend::last_error());
+}
+
+Box bounding(const Region &r) {
+    Box box = r.boxes.front();
+    for (const auto &e : r.boxes)
+        for (int d = 0; d < box.rank; ++d) {
+            box.lo[d] = std::min(box.lo[d], e.lo[d]);
+            box.hi[d] = std::max(box.hi[d], e.hi[d]);
+        }
+    return box;
+}
+
+void flush(Context *c);
+
+// Install an array's new coherence sets. When one of them would exceed the
+// rectangle limit, reconcile instead: bring both copies up to date everywhere
+// values are defined (copying exactly what each side lacks under the new
+// sets), then track each side as the whole array. A definition set that is
+// still too fragmented is widened to its bounding box.
+void settle(Context *c, Buffer *b, Region defined, Region host, Region device) {
+    if (defined.fits() && host.fits() && device.fits()) {
+        b->defined = std::move(defined);
+        b->host_valid = std::move(host);
+        b->device_valid = std::move(device);
+        return;
+    }
+    flush(c);
+    if (b->device) {
+        ensure_stream(c);
+        Region down = defined.clip(device);
+        down.remove(host);
+        copy_region(c, b, down, false);
+        Region up = defined.clip(host);
+        up.remove(device);
+        copy_region(c, b, up, true);
+        wait_stream(c);
+        b->device_valid.clear();
+        b->device_valid.add(b->full());
+    } else {
+        b->device_valid.clear();
+    }
+    b->host_valid.clear();
+    b->host_valid.add(b->full());
+    if (!defined.fits()) {
+        const Box hull = bounding(defined);
+        defined.clear();
+        defined.add(hull);
+    }
+    b->defined = std::move(defined);
+    c->domain->stats.reconciliations++;
+}
+
+// ---- device storage and the budget ---------------------------------------------------------
+
+void publish_buffer(Context *c, Buffer *b) {
+    if (!b->device) return;
+    Region dirty = b->defined.clip(b->device_valid);
+    dirty.remove(b->host_valid);
+    if (dirty.empty()) return;
+    ensure_stream(c);
+    copy_region(c, b, dirty, false);
+    Region host = b->host_valid;
+    host.add(dirty);
+    settle(c, b, b->defined, host, b->device_valid);
+}
+
+void release_mirror(Context *c, Buffer *b) {
+    if (!b->device) return;
+    Backend::free(b->device, c->stream);
+    b->device = nullptr;
+    c->domain->device_bytes -= b->bytes;
+    b->device_valid.clear();
+}
+
+size_t claimed(const Domain *d) { return d->device_bytes + d->scratch_bytes; }
+
+// Make room for `bytes` more, evicting least recently used mirrors that are not
+// in `keep`, not prepared and not used by queued tasks.
+void make_room(Context *c, size_t bytes, const std::set<uint64_t> &keep) {
+    Domain *d = c->domain;
+    if (!d->budget_set) return;
+    if (claimed(d) + bytes <= d->budget) return;
+    // impossible even after evicting everything evictable: fail before touching anything
+    size_t evictable = 0;
+    for (auto &kv : d->buffers) {
+        Buffer *b = kv.second.get();
+        if (b->device && !keep.count(b->handle) && b->prepared == Buffer::NONE) evictable += b->bytes;
+    }
+    if (claimed(d) - evictable + bytes > d->budget) {
+        if (!d->budget_warned) {
+            d->budget_warned = true;
+            std::fprintf(stderr,
+                         "FORT_SCOPED budget_warning domain=%" PRIu64 " budget=%zu requested=%zu claimed=%zu: the "
+                         "statements run natively where their arrays do not fit\n",
+                         d->handle, d->budget, bytes, claimed(d));
+        }
+        raise(FORT_SCOPE_RESOURCE, "device budget too small for the task footprint");
+    }
+    if (!c->pending.empty()) {
+        d->residency.pressure_flushes++;
+        flush(c);
+    }
+    while (claimed(d) + bytes > d->budget) {
+        Buffer *victim = nullptr;
+        for (auto &kv : d->buffers) {
+            Buffer *b = kv.second.get();
+            if (!b->device || keep.count(b->handle) || b->prepared != Buffer::NONE || b->queued) continue;
+            if (!victim || b->last_use < victim->last_use) victim = b;
+        }
+        if (!victim) raise(FORT_SCOPE_RESOURCE, "device budget exhausted by arrays in use");
+        Region dirty = victim->defined.clip(victim->device_valid);
+        dirty.remove(victim->host_valid);
+        if (!dirty.empty()) {
+            d->residency.dirty_evictions++;
+            d->residency.dirty_download_bytes += dirty.volume() * victim->elem;
+            publish_buffer(c, victim);
+            wait_stream(c);
+        }
+        d->residency.evictions++;
+        d->residency.evicted_bytes += victim->bytes;
+        trace_line(c, "evict", victim->handle, victim->bytes);
+        release_mirror(c, victim);
+    }
+}
+
+void reserve(Context *c, const std::vector<Buffer *> &list) {
+    std::set<uint64_t> keep;
+    size_t need = 0;
+    for (Buffer *b : list) {
+        keep.insert(b->handle);
+        if (!b->device) need += b->bytes;
+    }
+    Domain *d = c->domain;
+    d->residency.reserve_batches++;
+    d->residency.requested_resources += list.size();
+    if (need) {
+        ensure_stream(c);
+        make_room(c, need, keep);
+    }
+    for (Buffer *b : list) {
+        b->last_use = ++d->tick;
+        if (b->device) {
+            d->residency.reuse_hits++;
+            continue;
+        }
+        if (!Backend::alloc(&b->device, b->bytes, c->stream)) {
+            b->device = nullptr;
+            raise(FORT_SCOPE_RESOURCE, "device allocation failed: " + Backend::last_error());
+        }
+        d->device_bytes += b->bytes;
+        d->stats.allocations++;
+        d->stats.allocated_bytes += b->bytes;
+        if (claimed(d) > d->stats.peak_device_bytes) d->stats.peak_device_bytes = claimed(d);
+        b->device_valid.clear();
+    }
+}
+
+// ---- the task queue ------------------------------------------------------------------------
+
+uint64_t fnv1a(uint64_t h, const void *data, size_t n) {
+    const unsigned char *p = static_cast<const unsigned char *>(data);
+    for (size_t i = 0; i < n; ++i) {
+        h ^= p[i];
+        h *= 1099511628211ULL;
+    }
+    return h;
+}
+
+void launch_direct(Context *c, std::vector<Task> &tasks) {
+    for (auto &t : tasks) {
+        trace_line(c, "launch", 0, 0);
+        if (!Backend::launch(t.spec, c->stream)) poison(c, std::string("kernel launch failed: ") + Backend::last_error());
+    }
+    c->queue_stats.direct_submissions++;
+    c->queue_stats.direct_kernels += tasks.size();
+}
+
+void submit(Context *c, std::vector<Task> &tasks, uint64_t key) {
+    ensure_stream(c);
+    Domain *d = c->domain;
+    d->stats.launches += tasks.size();
+    c->graph_stats.submissions++;
+    c->graph_stats.logical_kernels += tasks.size();
+    if (!c->graphs_enabled) {
+        launch_direct(c, tasks);
+        return;
+    }
+    CachedGraph &g = c->graphs[key];
+    bool same_topology = g.functions.size() == tasks.size();
+    for (size_t n = 0; same_topology && n < tasks.size(); ++n)
+        same_topology = g.functions[n] == tasks[n].spec.function && g.argument_counts[n] == tasks[n].values.size();
+    if (!same_topology) {
+        if (g.graph) {
+            Backend::graph_destroy(g.graph);
+            g.graph = nullptr;
+            c->graph_stats.rebuilds++;
+            c->graph_stats.destructions++;
+            c->graph_stats.live_graphs--;
+        }
+        g.functions.clear();
+        g.argument_counts.clear();
+        for (auto &t : tasks) {
+            g.functions.push_back(t.spec.function);
+            g.argument_counts.push_back(t.values.size());
+        }
+        g.reached = 0;
+    }
+    g.reached++;
+    if (g.reached == 1) {
+        // first reach: direct launches, as a warm-up of the sequence
+        launch_direct(c, tasks);
+        return;
+    }
+    std::vector<LaunchSpec> specs;
+    for (auto &t : tasks) specs.push_back(t.spec);
+    if (!g.graph) {
+        Backend::Graph *built = nullptr;
+        if (!Backend::graph_build(&built, specs)) {
+            c->queue_stats.graph_resource_fallbacks++;
+            g.reached = 0;
+            launch_direct(c, tasks);
+            return;
+        }
+        g.graph = built;
+        g.specs = specs;
+        g.values.clear();
+        for (auto &t : tasks) g.values.push_back(t.values);
+        c->graph_stats.creations++;
+        c->graph_stats.instantiations++;
+        c->graph_stats.live_graphs++;
+    } else {
+        for (size_t n = 0; n < tasks.size(); ++n) {
+            const LaunchSpec &k = tasks[n].spec;
+            const LaunchSpec &old = g.specs[n];
+            bool changed = std::memcmp(k.grid, old.grid, sizeof k.grid) || std::memcmp(k.block, old.block, sizeof k.block) ||
+                           k.shared_bytes != old.shared_bytes || g.values[n] != tasks[n].values;
+            if (!changed) continue;
+            if (!Backend::graph_update(g.graph, n, k)) poison(c, std::string("graph update failed: ") + Backend::last_error());
+            c->graph_stats.parameter_updates++;
+            g.values[n] = tasks[n].values;
+            g.specs[n] = k;
+        }
+        c->graph_stats.replays++;
+    }
+    // the stored specs point into g.values; rebind before launch
+    for (size_t n = 0; n < tasks.size(); ++n) {
+        g.specs[n].arguments.clear();
+        for (auto &v : g.values[n]) g.specs[n].arguments.push_back(v.data());
+    }
+    for (size_t n = 0; n < tasks.size(); ++n) trace_line(c, "graph_kernel", 0, 0);
+    if (!Backend::graph_launch(g.graph, g.specs, c->stream))
+        poison(c, std::string("graph launch failed: ") + Backend::last_error());
+}
+
+void flush(Context *c) {
+    if (c->pending.empty()) return;
+    std::vector<Task> tasks;
+    tasks.swap(c->pending);
+    c->pending_threads = 0;
+    uint64_t key = 14695981039346656037ULL;
+    for (auto &t : tasks) key = fnv1a(key, &t.code_key, sizeof t.code_key);
+    for (auto &t : tasks)
+        for (uint64_t h : t.buffers) {
+            auto it = c->domain->buffers.find(h);
+            if (it != c->domain->buffers.end()) it->second->queued--;
+        }
+    c->queue_stats.submissions++;
+    c->queue_stats.pending_tasks = 0;
+    trace_line(c, "flush", 0, tasks.size());
+    submit(c, tasks, key);
+}
+
+// Validate and apply the effects of one device task transactionally: nothing is
+// changed unless every binding passes.
+struct Bound {
+    Buffer *buffer;
+    Effects effects;
+};
+
+std::vector<Bound> bind_all(Context *c, const fort_scope_plan_binding *bindings, size_t count) {
+    if (count && !bindings) raise(FORT_SCOPE_ARGUMENT, "null bindings");
+    std::vector<Bound> out;
+    std::set<uint64_t> seen;
+    for (size_t n = 0; n < count; ++n) {
+        Buffer *b = find_buffer(c, bindings[n].buffer);
+        if (!seen.insert(b->handle).second) raise(FORT_SCOPE_ALIAS, "a task binds one array twice");
+        if (b->prepared != Buffer::NONE) raise(FORT_SCOPE_STATE, "array already has a prepared access");
+        Effects e = effects_of(b, bindings[n].access);
+        check_initialized(b, e);
+        out.push_back({b, std::move(e)});
+    }
+    return out;
+}
+
+void device_acquire(Context *c, std::vector<Bound> &bound) {
+    for (auto &x : bound) {
+        Buffer *b = x.buffer;
+        Region up = needed(b, x.effects);
+        up.remove(b->device_valid);
+        if (!up.empty()) {
+            copy_region(c, b, up, true);
+            Region device = b->device_valid;
+            device.add(up);
+            settle(c, b, b->defined, b->host_valid, device);
+        }
+    }
+}
+
+void device_commit(Context *c, Buffer *b, const Region &writes, const Region &overwrites) {
+    Region defined = b->defined, host = b->host_valid, device = b->device_valid;
+    device.add(writes);
+    host.remove(writes);
+    defined.add(overwrites);
+    settle(c, b, std::move(defined), std::move(host), std::move(device));
+    b->last_use = ++c->domain->tick;
+}
+
+void host_acquire(Context *c, std::vector<Bound> &bound) {
+    // A host access orders after every queued task (they may write what it
+    // reads) and after in-flight uploads (they read the host copy).
+    flush(c);
+    for (auto &x : bound) {
+        Region down = needed(x.buffer, x.effects);
+        down.remove(x.buffer->host_valid);
+        if (!down.empty()) {
+            ensure_stream(c);
+            copy_region(c, x.buffer, down, false);
+            Region host = x.buffer->host_valid;
+            host.add(down);
+            settle(c, x.buffer, x.buffer->defined, host, x.buffer->device_valid);
+        }
+    }
+    wait_stream(c);
+}
+
+void host_commit(Context *c, Buffer *b, const Region &writes, const Region &overwrites) {
+    Region defined = b->defined, host = b->host_valid, device = b->device_valid;
+    host.add(writes);
+    device.remove(writes);
+    defined.add(overwrites);
+    settle(c, b, std::move(defined), std::move(host), std::move(device));
+}
+
+LaunchSpec spec_of(const fort_scope_kernel_v1 &k) {
+    if (k.version != FORT_SCOPE_GRAPH_ABI_VERSION) raise(FORT_SCOPE_ARGUMENT, "unknown kernel record version");
+    if (!k.function) raise(FORT_SCOPE_ARGUMENT, "null kernel function");
+    if (k.argument_count > 384) raise(FORT_SCOPE_ARGUMENT, "too many kernel arguments");
+    if (k.argument_count && !k.arguments) raise(FORT_SCOPE_ARGUMENT, "null kernel arguments");
+    for (int d = 0; d < 3; ++d)
+        if (!k.grid[d] || !k.block[d]) raise(FORT_SCOPE_ARGUMENT, "empty launch dimension");
+    if ((uint64_t)k.block[0] * k.block[1] * k.block[2] > 1024) raise(FORT_SCOPE_ARGUMENT, "block larger than 1024 threads");
+    LaunchSpec s;
+    s.function = k.function;
+    for (int d = 0; d < 3; ++d) {
+        s.grid[d] = k.grid[d];
+        s.block[d] = k.block[d];
+    }
+    s.shared_bytes = k.shared_bytes;
+    return s;
+}
+
+Task make_task(uint64_t code_key, const fort_scope_kernel_v1 &k, const size_t *sizes) {
+    Task t;
+    t.code_key = code_key;
+    t.spec = spec_of(k);
+    if (k.argument_count && !sizes) raise(FORT_SCOPE_ARGUMENT, "argument sizes are required");
+    size_t total = 0;
+    for (size_t n = 0; n < k.argument_count; ++n) {
+        if (!sizes[n] || !k.arguments[n]) raise(FORT_SCOPE_ARGUMENT, "empty kernel argument");
+        total += sizes[n];
+        const unsigned char *v = static_cast<const unsigned char *>(k.arguments[n]);
+        t.values.emplace_back(v, v + sizes[n]);
+    }
+    if (total > 32764) raise(FORT_SCOPE_ARGUMENT, "kernel arguments exceed the launch parameter space");
+    for (auto &v : t.values) t.spec.arguments.push_back(v.data());
+    t.threads = (uint64_t)k.grid[0] * k.grid[1] * k.grid[2] * k.block[0] * k.block[1] * k.block[2];
+    return t;
+}
+
+void accept(Context *c, Task &&task, std::vector<Bound> &bound) {
+    for (auto &x : bound)
+        if (!x.buffer->device) raise(FORT_SCOPE_STATE, "task binds an array whose device storage is not reserved");
+    ensure_stream(c);
+    device_acquire(c, bound);
+    for (auto &x : bound) {
+        device_commit(c, x.buffer, x.effects.writes, x.effects.overwrites);
+        x.buffer->queued++;
+        task.buffers.push_back(x.buffer->handle);
+    }
+    size_t bytes = 0;
+    for (auto &v : task.values) bytes += v.size();
+    c->queue_stats.accepted_tasks++;
+    c->queue_stats.copied_argument_bytes += bytes;
+    c->pending_threads += task.threads;
+    c->pending.push_back(std::move(task));
+    c->queue_stats.pending_tasks = c->pending.size();
+    if (c->pending.size() > c->queue_stats.peak_pending_tasks) c->queue_stats.peak_pending_tasks = c->pending.size();
+    trace_line(c, "queue_enqueue", 0, bytes);
+    if (!c->queue_enabled || (c->queue_work_limit && c->pending_threads >= c->queue_work_limit)) flush(c);
+}
+
+Context *make_context(Domain *d, bool private_domain) {
+    auto c = std::make_unique<Context>();
+    c->handle = new_handle();
+    c->domain = d;
+    c->private_domain = private_domain;
+    c->queue_enabled = env_flag("FORT_SCOPE_GRAPH_QUEUE", true);
+    c->graphs_enabled = env_flag("FORT_SCOPE_CUDA_GRAPHS", true);
+    if (const char *w = std::getenv("FORT_SCOPE_GRAPH_QUEUE_WORK")) c->queue_work_limit = std::strtoull(w, nullptr, 10);
+    c->queue_stats.version = 1;
+    c->queue_stats.queue_enabled = c->queue_enabled;
+    c->queue_stats.graphs_enabled = c->graphs_enabled;
+    c->graph_stats.version = 1;
+    c->completion.version = 1;
+    c->scratch_stats.version = 1;
+    d->borrower = c.get();
+    Context *raw = c.get();
+    g_contexts[raw->handle] = std::move(c);
+    return raw;
+}
+
+Domain *make_domain(int device) {
+    if (device < 0) raise(FORT_SCOPE_ARGUMENT, "negative device ordinal");
+    auto d = std::make_unique<Domain>();
+    d->handle = new_handle();
+    d->device = device;
+    d->residency.version = 1;
+    Domain *raw = d.get();
+    g_domains[raw->handle] = std::move(d);
+    return raw;
+}
+
+void destroy_buffer(Context *c, Buffer *b) {
+    release_mirror(c, b);
+    if (b->pinned_host) Backend::unpin(b->host);
+    c->domain->by_identity.erase(b->identity);
+    g_retired.insert(b->handle);
+    c->domain->buffers.erase(b->handle);
+}
+
+void release_scratch(Context *c) {
+    if (c->scratch) {
+        Backend::free(c->scratch, c->stream);
+        c->domain->scratch_bytes -= c->scratch_capacity;
+        c->scratch = nullptr;
+        c->scratch_capacity = 0;
+    }
+}
+
+void detach(Context *c) {
+    if (c->stream_ready) {
+        Backend::sync(c->stream);
+        for (auto &kv : c->graphs)
+            if (kv.second.graph) Backend::graph_destroy(kv.second.graph);
+        Backend::destroy_stream(c->stream);
+    }
+    if (c->domain->borrower == c) c->domain->borrower = nullptr;
+    g_retired.insert(c->handle);
+    g_contexts.erase(c->handle);
+}
+
+// Publish and free every array of a domain through `c` (its last context).
+void close_domain_through(Context *c, bool publish) {
+    Domain *d = c->domain;
+    if (publish) {
+        flush(c);
+        for (auto &kv : d->buffers) publish_buffer(c, kv.second.get());
+        wait_stream(c);
+    }
+    std::vector<Buffer *> all;
+    for (auto &kv : d->buffers) all.push_back(kv.second.get());
+    for (Buffer *b : all) destroy_buffer(c, b);
+    release_scratch(c);
+}
+
+template <typename F>
+int guarded(F &&f) {
+    std::lock_guard<std::recursive_mutex> lock(g_mutex);
+    try {
+        return f();
+    } catch (Failure &e) {
+        return fail(e.status, e.message);
+    } catch (std::bad_alloc &) {
+        return fail(FORT_SCOPE_RESOURCE, "host memory exhausted");
+    }
+}
+
+void copy_field(char *dst, const char *src) {
+    if (!src) {
+        dst[0] = 0;
+        return;
+    }
+    size_t n = strnlen(src, 65);
+    if (n >= 65) n = 0; // invalid identity: unknown
+    std::memcpy(dst, src, n);
+    dst[n] = 0;
+}
+
+size_t parse_bytes(const char *text, bool *ok) {
+    char *end = nullptr;
+    const unsigned long long v = std::strtoull(text, &end, 10);
+    *ok = end != text;
+    unsigned long long scale = 1;
+    if (end && *end) {
+        switch (*end) {
+        case 'K': case 'k': scale = 1ULL << 10; break;
+        case 'M': case 'm': scale = 1ULL << 20; break;
+        case 'G': case 'g': scale = 1ULL << 30; break;
+        default: *ok = false;
+        }
+        if (end[1]) *ok = false;
+    }
+    return (size_t)(v * scale);
+}
+
+} // namespace
+} // namespace f2c::rt
+
+using namespace f2c::rt;
+
+extern "C" {
+
+uint32_t fort_scope_abi_version(void) { return FORT_SCOPE_ABI_VERSION; }
+
+const char *fort_scope_error(void) { return t_error.c_str(); }
+
+int fort_scope_report_error(int status, const char *message) {
+    t_error = message ? message : "";
+    return status;
+}
+
+int fort_scope_execution_error(fort_scope_t context, const char *message) {
+    std::lock_guard<std::recursive_mutex> lock(g_mutex);
+    auto it = g_contexts.find(context);
+    if (it != g_contexts.end()) {
+        it->second->poisoned = true;
+        it->second->domain->poisoned = true;
+    }
+    t_error = std::string(message ? message : "execution failure") + "; unsafe replay prohibited";
+    return FORT_SCOPE_EXECUTION;
+}
+
+void fort_scope_trace_set_v1(fort_scope_t context, uint32_t update_mask, const char *owner, const char *procedure,
+                             const char *segment, const char *operation, const char *implementation,
+                             const char *boundary, fort_scope_trace_state_v1 *previous) {
+    if (!tracing()) {
+        if (previous) previous->version = 0;
+        return;
+    }
+    std::lock_guard<std::recursive_mutex> lock(g_mutex);
+    auto it = g_contexts.find(context);
+    if (it == g_contexts.end()) {
+        if (previous) previous->version = 0;
+        return;
+    }
+    Context *c = it->second.get();
+    if (previous) {
+        previous->version = FORT_SCOPE_TRACE_ABI_VERSION;
+        previous->reserved = 0;
+        char *fields[6] = {previous->owner, previous->procedure, previous->segment, previous->operation,
+                           previous->implementation, previous->boundary};
+        for (int n = 0; n < 6; ++n) std::memcpy(fields[n], c->trace[n], 65);
+    }
+    const char *values[6] = {owner, procedure, segment, operation, implementation, boundary};
+    for (int n = 0; n < 6; ++n)
+        if (update_mask & (1u << n)) copy_field(c->trace[n], values[n]);
+}
+
+void fort_scope_trace_restore_v1(fort_scope_t context, const fort_scope_trace_state_v1 *previous) {
+    if (!tracing() || !previous || previous->version != FORT_SCOPE_TRACE_ABI_VERSION) return;
+    std::lock_guard<std::recursive_mutex> lock(g_mutex);
+    auto it = g_contexts.find(context);
+    if (it == g_contexts.end()) return;
+    const char *fields[6] = {previous->owner, previous->procedure, previous->segment, previous->operation,
+                             previous->implementation, previous->boundary};
+    for (int n = 0; n < 6; ++n) std::memcpy(it->second->trace[n], fields[n], 65);
+}
+
+// ---- contexts and domains ----
+
+int fort_scope_create(int device, fort_scope_t *context) {
+    return guarded([&] {
+        if (!context) raise(FORT_SCOPE_ARGUMENT, "null context output");
+        Domain *d = make_domain(device);
+        d->owned_by_context = true;
+        *context = make_context(d, true)->handle;
+        return FORT_SCOPE_OK;
+    });
+}
+
+int fort_scope_domain_create_v1(int device, fort_scope_domain_t *domain) {
+    return guarded([&] {
+        if (!domain) raise(FORT_SCOPE_ARGUMENT, "null domain output");
+        *domain = make_domain(device)->handle;
+        return FORT_SCOPE_OK;
+    });
+}
+
+int fort_scope_create_in_domain_v1(fort_scope_domain_t domain, fort_scope_t *context) {
+    return guarded([&] {
+        if (!context) raise(FORT_SCOPE_ARGUMENT, "null context output");
+        Domain *d = find_domain(domain);
+        if (d->poisoned) raise(FORT_SCOPE_EXECUTION, "domain poisoned by an execution failure");
+        if (d->borrower) raise(FORT_SCOPE_STATE, "domain already borrowed by a context");
+        *context = make_context(d, false)->handle;
+        return FORT_SCOPE_OK;
+    });
+}
+
+int fort_scope_domain_get_v1(fort_scope_t context, fort_scope_domain_t *domain) {
+    return guarded([&] {
+        if (!domain) raise(FORT_SCOPE_ARGUMENT, "null domain output");
+        Context *c = find_context(context);
+        *domain = c->private_domain ? 0 : c->domain->handle;
+        return FORT_SCOPE_OK;
+    });
+}
+
+int fort_scope_domain_device_get_v1(fort_scope_domain_t domain, int *device) {
+    return guarded([&] {
+        if (!device) raise(FORT_SCOPE_ARGUMENT, "null device output");
+        *device = find_domain(domain)->device;
+        return FORT_SCOPE_OK;
+    });
+}
+
+int fort_scope_domain_stats_get_v1(fort_scope_domain_t domain, fort_scope_stats *stats) {
+    return guarded([&] {
+        if (!stats) raise(FORT_SCOPE_ARGUMENT, "null stats output");
+        *stats = find_domain(domain)->stats;
+        return FORT_SCOPE_OK;
+    });
+}
+
+int fort_scope_domain_close_v1(fort_scope_domain_t domain) {
+    return guarded([&] {
+        Domain *d = find_domain(domain);
+        if (d->borrower) raise(FORT_SCOPE_STATE, "domain still borrowed by a context");
+        if (d->poisoned) raise(FORT_SCOPE_EXECUTION, "domain poisoned; abandon it instead");
+        for (auto &kv : d->buffers)
+            if (kv.second->prepared != Buffer::NONE) raise(FORT_SCOPE_STATE, "domain has a prepared access");
+        Context *c = make_context(d, false);
+        int status = FORT_SCOPE_OK;
+        try {
+            close_domain_through(c, true);
+        } catch (Failure &e) {
+            status = fail(e.status, e.message);
+        }
+        detach(c);
+        g_retired.insert(d->handle);
+        g_domains.erase(d->handle);
+        return status;
+    });
+}
+
+int fort_scope_domain_abandon_v1(fort_scope_domain_t domain) {
+    return guarded([&] {
+        Domain *d = find_domain(domain);
+        if (d->borrower) raise(FORT_SCOPE_STATE, "domain still borrowed by a context");
+        d->poisoned = false;
+        Context *c = make_context(d, false);
+        close_domain_through(c, false);
+        detach(c);
+        g_retired.insert(d->handle);
+        g_domains.erase(d->handle);
+        return FORT_SCOPE_OK;
+    });
+}
+
+int fort_scope_domain_workspace_reserve_v1(fort_scope_domain_t, size_t, uint64_t *) {
+    return fail(FORT_SCOPE_RESOURCE, "external workspace claims are not provided by the GB300 advection runtime");
+}
+int fort_scope_domain_workspace_resize_v1(fort_scope_domain_t, uint64_t, size_t) {
+    return fail(FORT_SCOPE_RESOURCE, "external workspace claims are not provided by the GB300 advection runtime");
+}
+int fort_scope_domain_workspace_release_v1(fort_scope_domain_t, uint64_t) {
+    return fail(FORT_SCOPE_RESOURCE, "external workspace claims are not provided by the GB300 advection runtime");
+}
+
+int fort_scope_set_device_budget(fort_scope_t context, size_t bytes) {
+    return guarded([&] {
+        Context *c = live_context(context);
+        c->domain->budget = bytes;
+        c->domain->budget_set = true;
+        return FORT_SCOPE_OK;
+    });
+}
+
+int fort_scope_device_budget_default_v1(int device, size_t *bytes) {
+    return guarded([&] {
+        if (!bytes) raise(FORT_SCOPE_ARGUMENT, "null budget output");
+        if (device < 0) raise(FORT_SCOPE_ARGUMENT, "negative device ordinal");
+        if (const char *text = std::getenv("FORT_RESIDENT_DEVICE_BUDGET")) {
+            bool ok = false;
+            const size_t v = parse_bytes(text, &ok);
+            if (!ok) raise(FORT_SCOPE_ARGUMENT, "FORT_RESIDENT_DEVICE_BUDGET must be bytes or a count with K, M or G");
+            *bytes = v;
+            return FORT_SCOPE_OK;
+        }
+        const int previous = Backend::current();
+        if (!Backend::select(device)) raise(FORT_SCOPE_RESOURCE, "cannot select device: " + Backend::last_error());
+        size_t free_bytes = 0, total = 0;
+        const bool ok = Backend::memory_info(&free_bytes, &total);
+        Backend::select(previous);
+        if (!ok) raise(FORT_SCOPE_RESOURCE, "cannot query device memory: " + Backend::last_error());
+        size_t reserve = total / 16;
+        if (reserve < (size_t(512) << 20)) reserve = size_t(512) << 20;
+        *bytes = free_bytes > reserve ? free_bytes - reserve : 0;
+        return FORT_SCOPE_OK;
+    });
+}
+
+int fort_scope_domain_budget_get_v1(fort_scope_domain_t domain, size_t *budget, size_t *unclaimed) {
+    return guarded([&] {
+        if (!budget || !unclaimed) raise(FORT_SCOPE_ARGUMENT, "null budget output");
+        Domain *d = find_domain(domain);
+        *budget = d->budget_set ? d->budget : SIZE_MAX;
+        const size_t used = claimed(d);
+        *unclaimed = *budget > used ? *budget - used : 0;
+        return FORT_SCOPE_OK;
+    });
+}
+
+int fort_scope_close(fort_scope_t context) {
+    return guarded([&] {
+        Context *c = find_context(context);
+        if (c->poisoned || c->domain->poisoned)
+            raise(FORT_SCOPE_EXECUTION, "context poisoned; abandon it instead of publishing");
+        if (c->scratch_active) raise(FORT_SCOPE_STATE, "context holds an active scratch lease");
+        for (auto &kv : c->domain->buffers)
+            if (kv.second->prepared != Buffer::NONE) raise(FORT_SCOPE_STATE, "context has a prepared access");
+        Domain *d = c->domain;
+        if (c->private_domain) {
+            close_domain_through(c, true);
+            detach(c);
+            g_retired.insert(d->handle);
+            g_domains.erase(d->handle);
+        } else {
+            flush(c);
+            wait_stream(c);
+            release_scratch(c);
+            detach(c);
+        }
+        return FORT_SCOPE_OK;
+    });
+}
+
+int fort_scope_abandon(fort_scope_t context) {
+    return guarded([&] {
+        Context *c = find_context(context);
+        if (!c->poisoned && !c->domain->poisoned) raise(FORT_SCOPE_STATE, "abandon is only for failed contexts");
+        c->pending.clear();
+        Domain *d = c->domain;
+        for (auto &kv : d->buffers) {
+            kv.second->prepared = Buffer::NONE;
+            kv.second->queued = 0;
+        }
+        c->scratch_active = false;
+        release_scratch(c);
+        if (c->private_domain) {
+            close_domain_through(c, false);
+            detach(c);
+            g_retired.insert(d->handle);
+            g_domains.erase(d->handle);
+        } else {
+            detach(c);
+        }
+        return FORT_SCOPE_OK;
+    });
+}
+
+int fort_scope_wait(fort_scope_t context) {
+    return guarded([&] {
+        Context *c = live_context(context);
+        flush(c);
+        wait_stream(c);
+        return FORT_SCOPE_OK;
+    });
+}
+
+// ---- registration ----
+
+static int register_impl(fort_scope_t context, uint64_t identity, uint64_t generation, const fort_scope_layout *layout,
+                         const fort_scope_section *initialized, size_t initialized_count, bool all_defined,
+                         fort_buffer_t *out) {
+    return guarded([&] {
+        if (!layout || !out) raise(FORT_SCOPE_ARGUMENT, "null registration argument");
+        Context *c = live_context(context);
+        Domain *d = c->domain;
+        if (layout->rank < 1 || layout->rank > (uint32_t)kMaxRank) raise(FORT_SCOPE_ARGUMENT, "unsupported rank");
+        if (layout->type > FORT_SCOPE_LOGICAL) raise(FORT_SCOPE_ARGUMENT, "unknown element type");
+        if (!layout->element_bytes || !layout->extents || !layout->lower_bounds)
+            raise(FORT_SCOPE_ARGUMENT, "incomplete layout");
+        const size_t expect[] = {0, 4, 8, 4, 0};
+        if (expect[layout->type] && layout->element_bytes != expect[layout->type])
+            raise(FORT_SCOPE_ARGUMENT, "element size does not match the element type");
+        size_t count = 1;
+        for (uint32_t r = 0; r < layout->rank; ++r) {
+            const size_t e = layout->extents[r];
+            if (e && count > SIZE_MAX / e) raise(FORT_SCOPE_ARGUMENT, "array size overflows");
+            count *= e;
+        }
+        if (count && count > SIZE_MAX / layout->element_bytes) raise(FORT_SCOPE_ARGUMENT, "array size overflows");
+        const size_t bytes = count * layout->element_bytes;
+        if (!bytes) raise(FORT_SCOPE_ARGUMENT, "empty arrays cannot be registered");
+        if (!layout->host) raise(FORT_SCOPE_ARGUMENT, "null host storage");
+        auto existing = d->by_identity.find(identity);
+        if (existing != d->by_identity.end()) {
+            Buffer *b = d->buffers.at(existing->second).get();
+            bool same = b->rank == (int)layout->rank && b->type == layout->type && b->elem == layout->element_bytes &&
+                        b->host == layout->host;
+            for (int r = 0; same && r < b->rank; ++r) same = b->extents[r] == layout->extents[r];
+            if (!same) raise(FORT_SCOPE_ALIAS, "identity already registered with another layout");
+            b->generation = generation;
+            for (int r = 0; r < b->rank; ++r) b->lower[r] = layout->lower_bounds[r];
+            *out = b->handle;
+            return FORT_SCOPE_OK;
+        }
+        const char *lo = static_cast<const char *>(layout->host);
+        for (auto &kv : d->buffers) {
+            const Buffer *o = kv.second.get();
+            const char *olo = static_cast<const char *>(o->host);
+            if (lo < olo + o->bytes && olo < lo + bytes)
+                raise(FORT_SCOPE_ALIAS, "host storage overlaps a registered array");
+        }
+        auto b = std::make_unique<Buffer>();
+        b->handle = new_handle();
+        b->identity = identity;
+        b->generation = generation;
+        b->rank = (int)layout->rank;
+        b->type = layout->type;
+        b->elem = layout->element_bytes;
+        b->bytes = bytes;
+        b->host = layout->host;
+        for (int r = 0; r < b->rank; ++r) {
+            b->extents[r] = layout->extents[r];
+            b->lower[r] = layout->lower_bounds[r];
+        }
+        b->host_valid.add(b->full());
+        if (all_defined) {
+            b->defined.add(b->full());
+        } else {
+            if (initialized_count > kRegionLimit || (initialized_count && !initialized))
+                raise(FORT_SCOPE_ARGUMENT, "initialized section list exceeds the bounded interface");
+            for (size_t n = 0; n < initialized_count; ++n) b->defined.add(section_box(b.get(), initialized[n]));
+        }
+        if (!Backend::cpu && bytes >= (size_t(1) << 20) && env_flag("FORT_SCOPE_PIN_HOST", true))
+            b->pinned_host = Backend::pin(b->host, bytes);
+        *out = b->handle;
+        trace_line(c, "register", b->handle, bytes);
+        d->by_identity[identity] = b->handle;
+        d->buffers[b->handle] = std::move(b);
+        return FORT_SCOPE_OK;
+    });
+}
+
+int fort_scope_register(fort_scope_t context, uint64_t identity, uint64_t generation, const fort_scope_layout *layout,
+                        int host_initialized, fort_buffer_t *buffer) {
+    return register_impl(context, identity, generation, layout, nullptr, 0, host_initialized != 0, buffer);
+}
+
+int fort_scope_register_sections(fort_scope_t context, uint64_t identity, uint64_t generation,
+                                 const fort_scope_layout *layout, const fort_scope_section *initialized,
+                                 size_t initialized_count, fort_buffer_t *buffer) {
+    return register_impl(context, identity, generation, layout, initialized, initialized_count, false, buffer);
+}
+
+int fort_scope_admit_source_reads_v1(fort_scope_t context, fort_buffer_t buffer, const fort_scope_section *sections,
+                                     size_t count) {
+    return guarded([&] {
+        Context *c = live_context(context);
+        Buffer *b = find_buffer(c, buffer);
+        if (count > kRegionLimit || (count && !sections)) raise(FORT_SCOPE_ARGUMENT, "section list exceeds the bounded interface");
+        Region add;
+        for (size_t n = 0; n < count; ++n) add.add(section_box(b, sections[n]));
+        Region fresh = b->defined.missing(b->full()).clip(add);
+        Region defined = b->defined, host = b->host_valid, device = b->device_valid;
+        defined.add(fresh);
+        host.add(fresh);
+        device.remove(fresh);
+        settle(c, b, std::move(defined), std::move(host), std::move(device));
+        return FORT_SCOPE_OK;
+    });
+}
+
+int fort_scope_identity_swap_v1(fort_scope_t context, fort_buffer_t, fort_buffer_t, const fort_scope_layout *,
+                                const fort_scope_layout *, fort_buffer_t *, fort_buffer_t *) {
+    std::lock_guard<std::recursive_mutex> lock(g_mutex);
+    auto it = g_contexts.find(context);
+    if (it != g_contexts.end()) {
+        it->second->poisoned = true;
+        it->second->domain->poisoned = true;
+    }
+    return fail(FORT_SCOPE_EXECUTION, "identity swap is not provided by the GB300 advection runtime; unsafe replay prohibited");
+}
+
+int fort_scope_forget_definition(fort_scope_t context, fort_buffer_t buffer) {
+    return guarded([&] {
+        Context *c = live_context(context);
+        Buffer *b = find_buffer(c, buffer);
+        if (b->prepared != Buffer::NONE) raise(FORT_SCOPE_STATE, "cannot forget definitions under a prepared access");
+        b->defined.clear();
+        return FORT_SCOPE_OK;
+    });
+}
+
+int fort_scope_layout_get(fort_scope_t context, fort_buffer_t buffer, fort_scope_layout *layout) {
+    return guarded([&] {
+        if (!layout) raise(FORT_SCOPE_ARGUMENT, "null layout output");
+        Context *c = live_context(context);
+        Buffer *b = find_buffer(c, buffer);
+        layout->rank = (uint32_t)b->rank;
+        layout->type = b->type;
+        layout->element_bytes = b->elem;
+        layout->host = b->host;
+        layout->extents = b->extents;
+        layout->lower_bounds = b->lower;
+        layout->generation = b->generation;
+        return FORT_SCOPE_OK;
+    });
+}
+
+int fort_scope_buffer_valid_v1(fort_scope_t context, fort_buffer_t buffer, int *valid) {
+    return guarded([&] {
+        if (!valid) raise(FORT_SCOPE_ARGUMENT, "null output");
+        Context *c = find_context(context);
+        *valid = c->domain->buffers.count(buffer) ? 1 : 0;
+        return FORT_SCOPE_OK;
+    });
+}
+
+// ---- accesses ----
+
+int fort_scope_access_begin_v1(fort_scope_t context, const fort_scope_plan_binding *bindings, size_t count, int device,
+                               void **devices) {
+    return guarded([&] {
+        Context *c = live_context(context);
+        if (device && count && !devices) raise(FORT_SCOPE_ARGUMENT, "null device pointer output");
+        std::vector<Bound> bound = bind_all(c, bindings, count);
+        if (!count) return FORT_SCOPE_OK;
+        if (device) {
+            // direct device work is ordered after every queued task
+            flush(c);
+            std::vector<Buffer *> list;
+            for (auto &x : bound) list.push_back(x.buffer);
+            reserve(c, list);
+            device_acquire(c, bound);
+        } else {
+            host_acquire(c, bound);
+        }
+        for (size_t n = 0; n < bound.size(); ++n) {
+            Buffer *b = bound[n].buffer;
+            b->prepared = device ? Buffer::DEVICE : Buffer::HOST;
+            b->prep_writes = bound[n].effects.writes;
+            b->prep_overwrites = bound[n].effects.overwrites;
+            if (device) devices[n] = b->device;
+        }
+        return FORT_SCOPE_OK;
+    });
+}
+
+int fort_scope_original_host_begin_v1(fort_scope_t context, const fort_scope_plan_binding *bindings, size_t count) {
+    return guarded([&] {
+        Context *c = live_context(context);
+        std::vector<Bound> bound;
+        if (count && !bindings) raise(FORT_SCOPE_ARGUMENT, "null bindings");
+        for (size_t n = 0; n < count; ++n) {
+            Buffer *b = find_buffer(c, bindings[n].buffer);
+            if (b->prepared != Buffer::NONE) raise(FORT_SCOPE_STATE, "array already has a prepared access");
+            bound.push_back({b, effects_of(b, bindings[n].access)});
+        }
+        host_acquire(c, bound);
+        for (auto &x : bound) {
+            x.buffer->prepared = Buffer::HOST;
+            x.buffer->prep_writes = x.effects.writes;
+            x.buffer->prep_overwrites = x.effects.overwrites;
+        }
+        return FORT_SCOPE_OK;
+    });
+}
+
+int fort_scope_host_begin(fort_scope_t context, fort_buffer_t buffer, const fort_scope_access *access) {
+    if (!access) return fail(FORT_SCOPE_ARGUMENT, "null access");
+    fort_scope_plan_binding binding{buffer, *access};
+    return fort_scope_access_begin_v1(context, &binding, 1, 0, nullptr);
+}
+
+int fort_scope_device_begin(fort_scope_t context, fort_buffer_t buffer, const fort_scope_access *access, void **device) {
+    if (!access || !device) return fail(FORT_SCOPE_ARGUMENT, "null access or device output");
+    fort_scope_plan_binding binding{buffer, *access};
+    return fort_scope_access_begin_v1(context, &binding, 1, 1, device);
+}
+
+static int end_impl(fort_scope_t context, fort_buffer_t buffer, bool device) {
+    return guarded([&] {
+        Context *c = live_context(context);
+        Buffer *b = find_buffer(c, buffer);
+        if (b->prepared != (device ? Buffer::DEVICE : Buffer::HOST))
+            raise(FORT_SCOPE_STATE, device ? "no prepared device access" : "no prepared host access");
+        if (device) {
+            device_commit(c, b, b->prep_writes, b->prep_overwrites);
+        } else {
+            host_commit(c, b, b->prep_writes, b->prep_overwrites);
+        }
+        b->prepared = Buffer::NONE;
+        b->prep_writes.clear();
+        b->prep_overwrites.clear();
+        return FORT_SCOPE_OK;
+    });
+}
+
+int fort_scope_host_end(fort_scope_t context, fort_buffer_t buffer) { return end_impl(context, buffer, false); }
+int fort_scope_device_end(fort_scope_t context, fort_buffer_t buffer) { return end_impl(context, buffer, true); }
+
+int fort_scope_cancel_access(fort_scope_t context, fort_buffer_t buffer) {
+    return guarded([&] {
+        Context *c = find_context(context);
+        Buffer *b = find_buffer(c, buffer);
+        if (b->prepared == Buffer::NONE) raise(FORT_SCOPE_STATE, "no prepared access to cancel");
+        b->prepared = Buffer::NONE;
+        b->prep_writes.clear();
+        b->prep_overwrites.clear();
+        return FORT_SCOPE_OK;
+    });
+}
+
+int fort_scope_device_reserve_v1(fort_scope_t context, fort_buffer_t buffer, void **device) {
+    return fort_scope_device_reserve_many_v1(context, &buffer, 1, device);
+}
+
+int fort_scope_device_reserve_many_v1(fort_scope_t context, const fort_buffer_t *buffers, size_t count,
+                                      void **devices) {
+    return guarded([&] {
+        Context *c = live_context(context);
+        if (count && (!buffers || !devices)) raise(FORT_SCOPE_ARGUMENT, "null reservation arrays");
+        std::vector<Buffer *> list;
+        std::set<uint64_t> seen;
+        for (size_t n = 0; n < count; ++n) {
+            Buffer *b = find_buffer(c, buffers[n]);
+            if (seen.insert(b->handle).second) list.push_back(b);
+        }
+        if (list.empty()) return FORT_SCOPE_OK;
+        reserve(c, list);
+        for (size_t n = 0; n < count; ++n) devices[n] = find_buffer(c, buffers[n])->device;
+        return FORT_SCOPE_OK;
+    });
+}
+
+// ---- publication ----
+
+int fort_scope_observe_v1(fort_scope_t context, const fort_buffer_t *buffers, size_t count) {
+    return guarded([&] {
+        Context *c = live_context(context);
+        if (count && !buffers) raise(FORT_SCOPE_ARGUMENT, "null buffer list");
+        std::vector<Buffer *> list;
+        for (size_t n = 0; n < count; ++n) {
+            Buffer *b = find_buffer(c, buffers[n]);
+            if (b->prepared != Buffer::NONE) raise(FORT_SCOPE_STATE, "cannot observe under a prepared access");
+            list.push_back(b);
+        }
+        if (list.empty()) return FORT_SCOPE_OK;
+        flush(c);
+        bool any = false;
+        for (Buffer *b : list) {
+            if (!b->device) continue;
+            Region dirty = b->defined.clip(b->device_valid);
+            dirty.remove(b->host_valid);
+            if (!dirty.empty()) any = true;
+            publish_buffer(c, b);
+        }
+        if (any || c->stream_ready) wait_stream(c);
+        return FORT_SCOPE_OK;
+    });
+}
+
+int fort_scope_observe_all_v1(fort_scope_t context) {
+    std::vector<fort_buffer_t> all;
+    {
+        std::lock_guard<std::recursive_mutex> lock(g_mutex);
+        auto it = g_contexts.find(context);
+        if (it != g_contexts.end())
+            for (auto &kv : it->second->domain->buffers) all.push_back(kv.first);
+    }
+    return fort_scope_observe_v1(context, all.data(), all.size());
+}
+
+static int drop_values(fort_scope_t context, fort_buffer_t buffer, bool recycle) {
+    return guarded([&] {
+        Context *c = live_context(context);
+        Buffer *b = find_buffer(c, buffer);
+        if (b->prepared != Buffer::NONE) raise(FORT_SCOPE_STATE, "cannot discard under a prepared access");
+        if (recycle && b->queued) return FORT_SCOPE_OK; // the new definition replaces the values
+        if (b->queued) flush(c);
+        b->defined.clear();
+        return FORT_SCOPE_OK;
+    });
+}
+
+int fort_scope_discard_v1(fort_scope_t context, fort_buffer_t buffer) { return drop_values(context, buffer, false); }
+int fort_scope_recycle_v1(fort_scope_t context, fort_buffer_t buffer) { return drop_values(context, buffer, true); }
+
+int fort_scope_retire_v1(fort_scope_t context, fort_buffer_t buffer) {
+    return guarded([&] {
+        Context *c = live_context(context);
+        Buffer *b = find_buffer(c, buffer);
+        if (b->prepared != Buffer::NONE) raise(FORT_SCOPE_STATE, "cannot retire under a prepared access");
+        if (b->queued) flush(c);
+        wait_stream(c);
+        destroy_buffer(c, b);
+        return FORT_SCOPE_OK;
+    });
+}
+
+int fort_scope_unregister(fort_scope_t context, fort_buffer_t buffer) {
+    return guarded([&] {
+        Context *c = live_context(context);
+        Buffer *b = find_buffer(c, buffer);
+        if (b->prepared != Buffer::NONE) raise(FORT_SCOPE_STATE, "cannot unregister under a prepared access");
+        flush(c);
+        publish_buffer(c, b);
+        wait_stream(c);
+        destroy_buffer(c, b);
+        return FORT_SCOPE_OK;
+    });
+}
+
+int fort_scope_stats_get(fort_scope_t context, fort_scope_stats *stats) {
+    return guarded([&] {
+        if (!stats) raise(FORT_SCOPE_ARGUMENT, "null stats output");
+        *stats = find_context(context)->domain->stats;
+        return FORT_SCOPE_OK;
+    });
+}
+
+int fort_scope_residency_stats_get_v1(fort_scope_t context, fort_scope_residency_stats_v1 *stats) {
+    return guarded([&] {
+        if (!stats) raise(FORT_SCOPE_ARGUMENT, "null stats output");
+        *stats = find_context(context)->domain->residency;
+        return FORT_SCOPE_OK;
+    });
+}
+
+int fort_scope_completion_stats_get_v1(fort_scope_t context, fort_scope_completion_stats_v1 *stats) {
+    return guarded([&] {
+        if (!stats) raise(FORT_SCOPE_ARGUMENT, "null stats output");
+        *stats = find_context(context)->completion;
+        return FORT_SCOPE_OK;
+    });
+}
+
+// ---- scratch ----
+
+int fort_scope_scratch_acquire_v1(fort_scope_t context, size_t bytes, fort_scope_scratch_lease_v1 *lease) {
+    return guarded([&] {
+        if (!lease) raise(FORT_SCOPE_ARGUMENT, "null lease output");
+        Context *c = live_context(context);
+        if (c->scratch_active) raise(FORT_SCOPE_STATE, "context already holds a scratch lease");
+        if (bytes) {
+            if (bytes > c->scratch_capacity) {
+                ensure_stream(c);
+                const size_t grow = bytes - c->scratch_capacity;
+                make_room(c, grow, {});
+                if (c->scratch) {
+                    wait_stream(c); // complete earlier uses before the old arena is retired
+                    release_scratch(c);
+                    c->scratch_stats.grows++;
+                }
+                void *p = nullptr;
+                if (!Backend::alloc(&p, bytes, c->stream)) raise(FORT_SCOPE_RESOURCE, "scratch allocation failed");
+                c->scratch = p;
+                c->scratch_capacity = bytes;
+                c->domain->scratch_bytes += bytes;
+                c->scratch_stats.allocations++;
+                if (claimed(c->domain) > c->domain->stats.peak_device_bytes)
+                    c->domain->stats.peak_device_bytes = claimed(c->domain);
+            } else {
+                c->scratch_stats.reuses++;
+            }
+        }
+        c->scratch_active = true;
+        c->scratch_active_bytes = bytes;
+        c->scratch_token = new_handle();
+        c->scratch_stats.acquisitions++;
+        if (bytes > c->scratch_stats.peak_scratch_bytes) c->scratch_stats.peak_scratch_bytes = bytes;
+        lease->version = FORT_SCOPE_SCRATCH_ABI_VERSION;
+        lease->reserved = 0;
+        lease->token = c->scratch_token;
+        lease->device = bytes ? c->scratch : nullptr;
+        lease->bytes = bytes;
+        lease->capacity = c->scratch_capacity;
+        return FORT_SCOPE_OK;
+    });
+}
+
+int fort_scope_scratch_release_v1(fort_scope_t context, uint64_t token) {
+    return guarded([&] {
+        Context *c = find_context(context);
+        if (!c->scratch_active || token != c->scratch_token) raise(FORT_SCOPE_STALE, "not the active scratch lease");
+        c->scratch_active = false;
+        c->scratch_active_bytes = 0;
+        c->scratch_stats.releases++;
+        return FORT_SCOPE_OK;
+    });
+}
+
+int fort_scope_scratch_stats_get_v1(fort_scope_t context, fort_scope_scratch_stats_v1 *stats) {
+    return guarded([&] {
+        if (!stats) raise(FORT_SCOPE_ARGUMENT, "null stats output");
+        Context *c = find_context(context);
+        *stats = c->scratch_stats;
+        stats->version = FORT_SCOPE_SCRATCH_ABI_VERSION;
+        stats->active = c->scratch_active;
+        stats->capacity_bytes = c->scratch_capacity;
+        stats->active_bytes = c->scratch_active_bytes;
+        stats->peak_total_device_bytes = c->domain->stats.peak_device_bytes;
+        return FORT_SCOPE_OK;
+    });
+}
+
+// ---- launches, queue and graphs ----
+
+int fort_scope_gpu_enter(fort_scope_t context, int *previous_device, void **stream) {
+    return guarded([&] {
+        if (!previous_device || !stream) raise(FORT_SCOPE_ARGUMENT, "null output");
+        Context *c = live_context(context);
+        *previous_device = Backend::current();
+        ensure_stream(c);
+        if (!Backend::select(c->domain->device)) raise(FORT_SCOPE_RESOURCE, "cannot select device");
+        *stream = (void *)c->stream;
+        return FORT_SCOPE_OK;
+    });
+}
+
+int fort_scope_gpu_leave(fort_scope_t context, int previous_device) {
+    return guarded([&] {
+        find_context(context);
+        Backend::select(previous_device);
+        return FORT_SCOPE_OK;
+    });
+}
+
+int fort_scope_note_launch(fort_scope_t context) {
+    return guarded([&] {
+        Context *c = live_context(context);
+        c->domain->stats.launches++;
+        trace_line(c, "launch", 0, 0);
+        return FORT_SCOPE_OK;
+    });
+}
+
+int fort_scope_graph_enqueue_v1(fort_scope_t context, uint64_t code_key, const fort_scope_graph_task_v1 *task,
+                                const size_t *argument_sizes) {
+    return guarded([&] {
+        if (!task) raise(FORT_SCOPE_ARGUMENT, "null task");
+        Context *c = live_context(context);
+        Task t = make_task(code_key, task->kernel, argument_sizes);
+        std::vector<Bound> bound = bind_all(c, task->bindings, task->binding_count);
+        accept(c, std::move(t), bound);
+        return FORT_SCOPE_OK;
+    });
+}
+
+int fort_scope_graph_enqueue_members_v1(fort_scope_t context, uint64_t code_key, const fort_scope_kernel_v1 *kernel,
+                                        const size_t *argument_sizes, const fort_scope_graph_member_v1 *members,
+                                        size_t member_count) {
+    return guarded([&] {
+        if (!kernel || (member_count && !members)) raise(FORT_SCOPE_ARGUMENT, "null merged launch");
+        Context *c = live_context(context);
+        Task t = make_task(code_key, *kernel, argument_sizes);
+        std::vector<std::vector<Bound>> each;
+        for (size_t m = 0; m < member_count; ++m) each.push_back(bind_all(c, members[m].bindings, members[m].binding_count));
+        // members must be independent on their actual sections
+        for (size_t a = 0; a < each.size(); ++a)
+            for (size_t b = a + 1; b < each.size(); ++b)
+                for (auto &x : each[a])
+                    for (auto &y : each[b]) {
+                        if (x.buffer != y.buffer) continue;
+                        Region rw_y = y.effects.reads;
+                        rw_y.add(y.effects.writes);
+                        Region rw_x = x.effects.reads;
+                        rw_x.add(x.effects.writes);
+                        if (!x.effects.writes.clip(rw_y).empty() || !y.effects.writes.clip(rw_x).empty())
+                            raise(FORT_SCOPE_BOUNDARY, "members of a merged launch touch sections another member writes");
+                    }
+        std::vector<Bound> merged;
+        for (auto &list : each)
+            for (auto &x : list) {
+                Bound *into = nullptr;
+                for (auto &m : merged)
+                    if (m.buffer == x.buffer) into = &m;
+                if (!into) {
+                    merged.push_back(x);
+                    continue;
+                }
+                into->effects.reads.add(x.effects.reads);
+                into->effects.writes.add(x.effects.writes);
+                into->effects.overwrites.add(x.effects.overwrites);
+            }
+        accept(c, std::move(t), merged);
+        return FORT_SCOPE_OK;
+    });
+}
+
+int fort_scope_graph_flush_v1(fort_scope_t context) {
+    return guarded([&] {
+        Context *c = live_context(context);
+        if (!c->pending.empty()) c->queue_stats.explicit_flushes++;
+        flush(c);
+        return FORT_SCOPE_OK;
+    });
+}
+
+int fort_scope_graph_queue_cancel_v1(fort_scope_t context) {
+    return guarded([&] {
+        Context *c = live_context(context);
+        if (!c->pending.empty())
+            raise(FORT_SCOPE_STATE, "accepted tasks already committed their effects; flush them instead");
+        return FORT_SCOPE_OK;
+    });
+}
+
+int fort_scope_graph_queue_stats_get_v1(fort_scope_t context, fort_scope_graph_queue_stats_v1 *stats) {
+    return guarded([&] {
+        if (!stats) raise(FORT_SCOPE_ARGUMENT, "null stats output");
+        *stats = find_context(context)->queue_stats;
+        return FORT_SCOPE_OK;
+    });
+}
+
+int fort_scope_graph_submit_v1(fort_scope_t context, uint64_t group_key, const fort_scope_kernel_v1 *kernels,
+                               size_t count) {
+    return guarded([&] {
+        Context *c = live_context(context);
+        if (count && !kernels) raise(FORT_SCOPE_ARGUMENT, "null kernels");
+        if (!count) return FORT_SCOPE_OK;
+        std::vector<Task> tasks;
+        for (size_t n = 0; n < count; ++n) {
+            Task t;
+            t.spec = spec_of(kernels[n]);
+            for (size_t a = 0; a < kernels[n].argument_count; ++a) t.spec.arguments.push_back(kernels[n].arguments[a]);
+            tasks.push_back(std::move(t));
+        }
+        flush(c);
+        // arguments are borrowed for this call only: launch them from caller storage
+        ensure_stream(c);
+        c->domain->stats.launches += count;
+        c->graph_stats.submissions++;
+        c->graph_stats.logical_kernels += count;
+        (void)group_key;
+        launch_direct(c, tasks);
+        return FORT_SCOPE_OK;
+    });
+}
+
+int fort_scope_graph_execute_v1(fort_scope_t, uint64_t, const fort_scope_graph_task_v1 *, size_t) {
+    return fail(FORT_SCOPE_RESOURCE, "checked graph execution is not provided; use fort_scope_graph_enqueue_v1");
+}
+
+int fort_scope_graph_stats_get_v1(fort_scope_t context, fort_scope_graph_stats_v1 *stats) {
+    return guarded([&] {
+        if (!stats) raise(FORT_SCOPE_ARGUMENT, "null stats output");
+        *stats = find_context(context)->graph_stats;
+        return FORT_SCOPE_OK;
+    });
+}
+
+int fort_scope_external_execute_v1(fort_scope_t, const fort_scope_external_call_v1 *, fort_scope_external_worker_v1,
+                                   void *, fort_scope_external_report_v1 *report) {
+    if (report) {
+        report->version = FORT_SCOPE_EXTERNAL_ABI_VERSION;
+        report->status = FORT_SCOPE_RESOURCE;
+        report->started = 0;
+        report->committed = 0;
+    }
+    return fail(FORT_SCOPE_RESOURCE, "external providers are not provided by the GB300 advection runtime");
+}
+
+} // extern "C"

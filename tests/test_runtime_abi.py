@@ -1,0 +1,539 @@
+"""Residency runtime ABI on the CPU test backend (no GPU).
+
+Each scenario drives the fort_scope_* entry points through ctypes. Scenarios
+marked ``both`` run against this repository's runtime and, where the reference
+checkout is present on this machine, against the reference's own runtime built
+with its CPU test switch (oracle/build_ref.py): both must return the same
+statuses, host values and transfer counts. The behaviours restated here are
+those the reference's runtime tests exercise (compiler/tests/test_scoped_runtime.py,
+test_scoped_graph_queue.py, test_scoped_scratch.py, test_scoped_access_batch.py).
+"""
+
+import ctypes as c
+import os
+import subprocess
+import sys
+
+import numpy as np
+import pytest
+
+from compiler import native
+from compiler.runtime import abi
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _ours():
+    return abi.bind(c.CDLL(str(native.build_cpu_runtime())))
+
+
+def _reference():
+    from oracle import build_ref
+
+    path = build_ref.build_if_available()
+    if path is None:
+        pytest.skip("reference runtime not buildable here")
+    return abi.bind(c.CDLL(str(path)))
+
+
+@pytest.fixture(scope="module")
+def ours():
+    return _ours()
+
+
+@pytest.fixture(scope="module", params=["gb300", "reference"])
+def both(request):
+    return _ours() if request.param == "gb300" else _reference()
+
+
+def _array(values):
+    a = np.ascontiguousarray(np.asarray(values, dtype=np.float64))
+    return a, a.ctypes.data
+
+
+def _dev(pointer, count):
+    return np.ctypeslib.as_array(c.cast(pointer, c.POINTER(c.c_double)), shape=(count,))
+
+
+def _device_begin(scope, handle, access):
+    out = c.c_void_p()
+    status = scope.lib.fort_scope_device_begin(scope.handle, handle, c.byref(access), c.byref(out))
+    return status, out.value
+
+
+# ------------------------------------------------------------------------------- both runtimes
+
+
+def test_read_mirror_and_duplicate_registration(both):
+    scope = abi.Scope(both)
+    host, address = _array(range(8))
+    status, h = scope.register(address, [8], lower=[-2])
+    assert status == abi.OK
+    status, again = scope.register(address, [8], lower=[-2])
+    assert (status, again) == (abi.OK, h)
+    status, dev = _device_begin(scope, h, abi.access(flags=abi.READ_ALL | abi.WRITE_ALL))
+    assert status == abi.OK
+    _dev(dev, 8)[:] += 10
+    assert both.fort_scope_device_end(scope.handle, h) == abi.OK
+    assert both.fort_scope_host_begin(scope.handle, h, c.byref(abi.access(flags=abi.READ_ALL))) == abi.OK
+    assert host.tolist() == [i + 10.0 for i in range(8)]
+    assert both.fort_scope_host_end(scope.handle, h) == abi.OK
+    status, dev = _device_begin(scope, again, abi.access(flags=abi.READ_ALL))
+    assert status == abi.OK and _dev(dev, 8)[7] == 17.0
+    assert both.fort_scope_device_end(scope.handle, again) == abi.OK
+    stats = scope.stats()
+    assert (stats.uploads, stats.downloads, stats.allocations) == (1, 1, 1)
+    assert both.fort_scope_close(scope.handle) == abi.OK
+    assert both.fort_scope_wait(scope.handle) == abi.STALE
+
+
+def test_device_interior_and_host_faces_both_survive(both):
+    """The device writes the interior of a 4x4x4 array, the host its opposite x faces; both persist."""
+    scope = abi.Scope(both)
+    host, address = _array(np.arange(64.0))
+    status, h = scope.register(address, [4, 4, 4])
+    assert status == abi.OK
+    interior = ((1, 1, 1), (3, 3, 3))
+    acc = abi.access(read=[interior], write=[interior], overwrite=[interior])
+    status, dev = _device_begin(scope, h, acc)
+    assert status == abi.OK
+    d = _dev(dev, 64).reshape(4, 4, 4)  # [k][j][i]
+    d[1:3, 1:3, 1:3] = -1.0
+    assert both.fort_scope_device_end(scope.handle, h) == abi.OK
+    faces = [((0, 0, 0), (1, 4, 4)), ((3, 0, 0), (4, 4, 4))]
+    acc = abi.access(write=faces, overwrite=faces)
+    assert both.fort_scope_host_begin(scope.handle, h, c.byref(acc)) == abi.OK
+    view = host.reshape(4, 4, 4)
+    view[:, :, 0] = 100.0
+    view[:, :, 3] = 200.0
+    assert both.fort_scope_host_end(scope.handle, h) == abi.OK
+    arr = (abi.U64 * 1)(h)
+    assert both.fort_scope_observe_v1(scope.handle, arr, 1) == abi.OK
+    expect = np.arange(64.0).reshape(4, 4, 4)
+    expect[1:3, 1:3, 1:3] = -1.0
+    expect[:, :, 0] = 100.0
+    expect[:, :, 3] = 200.0
+    assert np.array_equal(view, expect)
+    # and the device copy agrees where the device is current
+    status, dev = _device_begin(scope, h, abi.access(flags=abi.READ_ALL))
+    assert status == abi.OK
+    assert np.array_equal(_dev(dev, 64).reshape(4, 4, 4), expect)
+    assert both.fort_scope_device_end(scope.handle, h) == abi.OK
+    assert both.fort_scope_close(scope.handle) == abi.OK
+
+
+def test_undefined_reads_are_rejected(both):
+    scope = abi.Scope(both)
+    host, address = _array(np.zeros(6))
+    status, h = scope.register(address, [6], initialized=False)
+    assert status == abi.OK
+    status, _ = _device_begin(scope, h, abi.access(flags=abi.READ_ALL))
+    assert status == abi.UNINITIALIZED
+    # an overwrite defines the values; then they can be read
+    status, dev = _device_begin(scope, h, abi.access(write=[((0,), (6,))], overwrite=[((0,), (6,))]))
+    assert status == abi.OK
+    _dev(dev, 6)[:] = 4.0
+    assert both.fort_scope_device_end(scope.handle, h) == abi.OK
+    status, _ = _device_begin(scope, h, abi.access(flags=abi.READ_ALL))
+    assert status == abi.OK
+    assert both.fort_scope_device_end(scope.handle, h) == abi.OK
+    assert both.fort_scope_close(scope.handle) == abi.OK
+    assert host.tolist() == [4.0] * 6
+
+
+def test_partial_initialization(both):
+    scope = abi.Scope(both)
+    host, address = _array(np.arange(10.0))
+    status, h = scope.register(address, [10], defined=[((2,), (8,))])
+    assert status == abi.OK
+    status, _ = _device_begin(scope, h, abi.access(read=[((1,), (5,))]))
+    assert status == abi.UNINITIALIZED
+    status, dev = _device_begin(scope, h, abi.access(read=[((2,), (8,))], write=[((2,), (8,))]))
+    assert status == abi.OK
+    _dev(dev, 10)[2:8] *= 2
+    assert both.fort_scope_device_end(scope.handle, h) == abi.OK
+    assert both.fort_scope_close(scope.handle) == abi.OK
+    assert host.tolist() == [0, 1, 4, 6, 8, 10, 12, 14, 8, 9]
+
+
+def test_forget_definition_keeps_values_but_forbids_reads(both):
+    scope = abi.Scope(both)
+    host, address = _array(np.ones(4))
+    status, h = scope.register(address, [4])
+    assert status == abi.OK
+    assert both.fort_scope_forget_definition(scope.handle, h) == abi.OK
+    status, _ = _device_begin(scope, h, abi.access(flags=abi.READ_ALL))
+    assert status == abi.UNINITIALIZED
+    assert both.fort_scope_close(scope.handle) == abi.OK
+    assert host.tolist() == [1.0] * 4
+
+
+def test_prepared_access_rules(both):
+    scope = abi.Scope(both)
+    _, address = _array(np.ones(4))
+    _, h = scope.register(address, [4])
+    status, _ = _device_begin(scope, h, abi.access(flags=abi.READ_ALL))
+    assert status == abi.OK
+    # a second access on a prepared array, and definition changes under it, are refused
+    status, _ = _device_begin(scope, h, abi.access(flags=abi.READ_ALL))
+    assert status != abi.OK
+    assert both.fort_scope_forget_definition(scope.handle, h) != abi.OK
+    assert both.fort_scope_cancel_access(scope.handle, h) == abi.OK
+    assert both.fort_scope_device_end(scope.handle, h) != abi.OK
+    assert both.fort_scope_close(scope.handle) == abi.OK
+
+
+def test_alias_and_layout_errors(both):
+    scope = abi.Scope(both)
+    host, address = _array(np.zeros(16))
+    status, h = scope.register(address, [16])
+    assert status == abi.OK
+    # overlapping host storage under another identity
+    status, _ = scope.register(address + 8 * 4, [4], identity=address + 32)
+    assert status == abi.ALIAS
+    # the layout comes back as registered
+    layout = abi.Layout()
+    assert both.fort_scope_layout_get(scope.handle, h, c.byref(layout)) == abi.OK
+    assert (layout.rank, layout.type, layout.element_bytes, layout.extents[0]) == (1, abi.REAL64, 8, 16)
+    assert both.fort_scope_unregister(scope.handle, h) == abi.OK
+    assert both.fort_scope_layout_get(scope.handle, h, c.byref(layout)) == abi.STALE
+    assert both.fort_scope_close(scope.handle) == abi.OK
+
+
+def test_unregister_publishes_device_values(both):
+    scope = abi.Scope(both)
+    host, address = _array(np.zeros(5))
+    _, h = scope.register(address, [5])
+    status, dev = _device_begin(scope, h, abi.access(flags=abi.WRITE_ALL | abi.OVERWRITE_ALL))
+    assert status == abi.OK
+    _dev(dev, 5)[:] = 3.0
+    assert both.fort_scope_device_end(scope.handle, h) == abi.OK
+    assert host.tolist() == [0.0] * 5
+    assert both.fort_scope_unregister(scope.handle, h) == abi.OK
+    assert host.tolist() == [3.0] * 5
+    assert both.fort_scope_close(scope.handle) == abi.OK
+
+
+def test_budget_eviction_publishes_dirty_values(both):
+    scope = abi.Scope(both)
+    a, pa = _array(np.zeros(128))
+    b, pb = _array(np.zeros(128))
+    assert both.fort_scope_set_device_budget(scope.handle, 128 * 8 + 512) == abi.OK
+    _, ha = scope.register(pa, [128])
+    _, hb = scope.register(pb, [128])
+    status, dev = _device_begin(scope, ha, abi.access(flags=abi.WRITE_ALL | abi.OVERWRITE_ALL))
+    assert status == abi.OK
+    _dev(dev, 128)[:] = 7.0
+    assert both.fort_scope_device_end(scope.handle, ha) == abi.OK
+    status, dev = _device_begin(scope, hb, abi.access(flags=abi.READ_ALL | abi.WRITE_ALL))
+    assert status == abi.OK
+    _dev(dev, 128)[:] += 1.0
+    assert both.fort_scope_device_end(scope.handle, hb) == abi.OK
+    assert a.tolist() == [7.0] * 128  # published when it was evicted
+    assert both.fort_scope_close(scope.handle) == abi.OK
+    assert b.tolist() == [1.0] * 128
+
+
+def test_oversized_footprint_fails_before_any_change(both):
+    scope = abi.Scope(both)
+    a, pa = _array(np.zeros(64))
+    assert both.fort_scope_set_device_budget(scope.handle, 64) == abi.OK
+    _, ha = scope.register(pa, [64])
+    status, _ = _device_begin(scope, ha, abi.access(flags=abi.READ_ALL))
+    assert status == abi.RESOURCE
+    assert scope.stats().allocations == 0
+    assert both.fort_scope_close(scope.handle) == abi.OK
+
+
+def test_scratch_leases(both):
+    scope = abi.Scope(both)
+    lease = abi.ScratchLease()
+    assert both.fort_scope_scratch_acquire_v1(scope.handle, 0, c.byref(lease)) == abi.OK
+    assert lease.device is None and lease.token
+    other = abi.ScratchLease()
+    assert both.fort_scope_scratch_acquire_v1(scope.handle, 16, c.byref(other)) == abi.STATE
+    assert both.fort_scope_scratch_release_v1(scope.handle, lease.token + 1) != abi.OK
+    assert both.fort_scope_scratch_release_v1(scope.handle, lease.token) == abi.OK
+    assert both.fort_scope_scratch_acquire_v1(scope.handle, 4096, c.byref(lease)) == abi.OK
+    first = lease.device
+    assert first and lease.capacity >= 4096
+    assert both.fort_scope_scratch_release_v1(scope.handle, lease.token) == abi.OK
+    assert both.fort_scope_scratch_acquire_v1(scope.handle, 1024, c.byref(lease)) == abi.OK
+    assert lease.device == first  # reused, not regrown
+    assert both.fort_scope_close(scope.handle) == abi.STATE  # an active lease blocks close
+    assert both.fort_scope_scratch_release_v1(scope.handle, lease.token) == abi.OK
+    stats = abi.ScratchStats()
+    assert both.fort_scope_scratch_stats_get_v1(scope.handle, c.byref(stats)) == abi.OK
+    assert (stats.acquisitions, stats.releases, stats.active) == (3, 3, 0)
+    assert both.fort_scope_close(scope.handle) == abi.OK
+
+
+def test_domain_outlives_borrowing_context(both):
+    domain = abi.U64()
+    assert both.fort_scope_domain_create_v1(0, c.byref(domain)) == abi.OK
+    scope = abi.Scope(both, domain=domain.value)
+    host, address = _array(np.zeros(4))
+    _, h = scope.register(address, [4])
+    status, dev = _device_begin(scope, h, abi.access(flags=abi.WRITE_ALL | abi.OVERWRITE_ALL))
+    assert status == abi.OK
+    _dev(dev, 4)[:] = 9.0
+    assert both.fort_scope_device_end(scope.handle, h) == abi.OK
+    got = abi.U64()
+    assert both.fort_scope_domain_get_v1(scope.handle, c.byref(got)) == abi.OK and got.value == domain.value
+    assert both.fort_scope_close(scope.handle) == abi.OK
+    assert host.tolist() == [0.0] * 4  # a borrowed context does not publish
+    second = abi.Scope(both, domain=domain.value)
+    assert both.fort_scope_close(second.handle) == abi.OK
+    assert both.fort_scope_domain_close_v1(domain.value) == abi.OK
+    assert host.tolist() == [9.0] * 4  # domain close is the publication frontier
+
+
+def test_budget_default_from_environment(both, monkeypatch):
+    monkeypatch.setenv("FORT_RESIDENT_DEVICE_BUDGET", "3M")
+    out = c.c_size_t()
+    assert both.fort_scope_device_budget_default_v1(0, c.byref(out)) == abi.OK
+    assert out.value == 3 << 20
+    monkeypatch.setenv("FORT_RESIDENT_DEVICE_BUDGET", "12x")
+    assert both.fort_scope_device_budget_default_v1(0, c.byref(out)) != abi.OK
+
+
+def test_execution_error_poisons(both):
+    scope = abi.Scope(both)
+    _, address = _array(np.zeros(4))
+    _, h = scope.register(address, [4])
+    assert both.fort_scope_execution_error(scope.handle, b"kernel failed") == abi.EXECUTION
+    assert both.fort_scope_wait(scope.handle) == abi.EXECUTION
+    status, _ = _device_begin(scope, h, abi.access(flags=abi.READ_ALL))
+    assert status == abi.EXECUTION
+    assert both.fort_scope_close(scope.handle) != abi.OK
+    assert both.fort_scope_abandon(scope.handle) == abi.OK
+
+
+# ------------------------------------------------------------------------------- this runtime
+
+KERNEL = c.CFUNCTYPE(None, c.POINTER(c.c_void_p))
+
+
+def _axpy_kernel(log):
+    """A host 'kernel' for the CPU backend: x[i] = x[i] * a + b for i < n; arguments (double*, int, double, double)."""
+
+    def run(args):
+        pointer = c.cast(args[0], c.POINTER(c.c_void_p))[0]
+        n = c.cast(args[1], c.POINTER(c.c_int))[0]
+        a = c.cast(args[2], c.POINTER(c.c_double))[0]
+        b = c.cast(args[3], c.POINTER(c.c_double))[0]
+        x = _dev(pointer, n)
+        x[:] = x * a + b
+        log.append((n, a, b))
+
+    return KERNEL(run)
+
+
+def _enqueue(scope, fn, handle, n, a, b, key=7, grid=1, block=32):
+    dev = (c.c_void_p * 1)()
+    harr = (abi.U64 * 1)(handle)
+    assert scope.lib.fort_scope_device_reserve_many_v1(scope.handle, harr, 1, dev) == abi.OK
+    values = [c.c_void_p(dev[0]), c.c_int(n), c.c_double(a), c.c_double(b)]
+    argv = (c.c_void_p * 4)(*[c.cast(c.pointer(v), c.c_void_p) for v in values])
+    sizes = (c.c_size_t * 4)(8, 4, 8, 8)
+    kernel = abi.Kernel(1, 0, c.cast(fn, c.c_void_p), (c.c_uint32 * 3)(grid, 1, 1), (c.c_uint32 * 3)(block, 1, 1),
+                        0, argv, 4)
+    acc = abi.access(flags=abi.READ_ALL | abi.WRITE_ALL)
+    binding = (abi.Binding * 1)(abi.Binding(handle, acc))
+    task = abi.Task(kernel, binding, 1)
+    return scope.lib.fort_scope_graph_enqueue_v1(scope.handle, key, c.byref(task), sizes)
+
+
+def test_queue_replays_as_graph_with_parameter_updates(ours):
+    scope = abi.Scope(ours)
+    host, address = _array(np.ones(8))
+    _, h = scope.register(address, [8])
+    log = []
+    fn = _axpy_kernel(log)
+    for step in range(4):
+        assert _enqueue(scope, fn, h, 8, 2.0, float(step)) == abi.OK
+        assert ours.fort_scope_graph_flush_v1(scope.handle) == abi.OK
+    assert ours.fort_scope_wait(scope.handle) == abi.OK
+    g = abi.GraphStats()
+    assert ours.fort_scope_graph_stats_get_v1(scope.handle, c.byref(g)) == abi.OK
+    # first reach direct, second instantiates, the rest replay; b changes every step
+    assert (g.creations, g.instantiations, g.replays, g.parameter_updates) == (1, 1, 2, 2)
+    q = abi.QueueStats()
+    assert ours.fort_scope_graph_queue_stats_get_v1(scope.handle, c.byref(q)) == abi.OK
+    assert (q.accepted_tasks, q.direct_submissions, q.explicit_flushes) == (4, 1, 4)
+    assert [entry[2] for entry in log] == [0.0, 1.0, 2.0, 3.0]
+    assert ours.fort_scope_observe_v1(scope.handle, (abi.U64 * 1)(h), 1) == abi.OK
+    expect = 1.0
+    for step in range(4):
+        expect = expect * 2.0 + step
+    assert host.tolist() == [expect] * 8
+    assert ours.fort_scope_close(scope.handle) == abi.OK
+
+
+def test_queue_flushes_itself_at_the_work_threshold(monkeypatch):
+    monkeypatch.setenv("FORT_SCOPE_GRAPH_QUEUE_WORK", "64")
+    lib = _ours()
+    scope = abi.Scope(lib)
+    _, address = _array(np.zeros(4))
+    _, h = scope.register(address, [4])
+    log = []
+    fn = _axpy_kernel(log)
+    assert _enqueue(scope, fn, h, 4, 1.0, 1.0, block=32) == abi.OK
+    assert log == []  # 32 threads: still queued
+    assert _enqueue(scope, fn, h, 4, 1.0, 1.0, block=32) == abi.OK
+    assert len(log) == 2  # 64 threads: submitted
+    assert lib.fort_scope_close(scope.handle) == abi.OK
+
+
+def test_host_access_drains_queued_writers(ours):
+    scope = abi.Scope(ours)
+    host, address = _array(np.zeros(4))
+    _, h = scope.register(address, [4])
+    log = []
+    fn = _axpy_kernel(log)
+    assert _enqueue(scope, fn, h, 4, 1.0, 5.0) == abi.OK
+    assert log == []
+    assert ours.fort_scope_host_begin(scope.handle, h, c.byref(abi.access(flags=abi.READ_ALL))) == abi.OK
+    assert len(log) == 1 and host.tolist() == [5.0] * 4
+    assert ours.fort_scope_host_end(scope.handle, h) == abi.OK
+    assert ours.fort_scope_close(scope.handle) == abi.OK
+
+
+def test_queue_policies_are_captured_at_create(monkeypatch):
+    monkeypatch.setenv("FORT_SCOPE_GRAPH_QUEUE", "0")
+    monkeypatch.setenv("FORT_SCOPE_CUDA_GRAPHS", "0")
+    lib = _ours()
+    scope = abi.Scope(lib)
+    monkeypatch.delenv("FORT_SCOPE_GRAPH_QUEUE")
+    _, address = _array(np.zeros(4))
+    _, h = scope.register(address, [4])
+    log = []
+    fn = _axpy_kernel(log)
+    for _ in range(3):
+        assert _enqueue(scope, fn, h, 4, 1.0, 1.0) == abi.OK
+        assert len(log) >= 1  # submitted at once
+    q = abi.QueueStats()
+    assert lib.fort_scope_graph_queue_stats_get_v1(scope.handle, c.byref(q)) == abi.OK
+    assert (q.queue_enabled, q.graphs_enabled, q.direct_kernels) == (0, 0, 3)
+    assert lib.fort_scope_close(scope.handle) == abi.OK
+
+
+def test_enqueue_requires_reserved_storage_and_valid_arguments(ours):
+    scope = abi.Scope(ours)
+    _, address = _array(np.zeros(4))
+    _, h = scope.register(address, [4])
+    fn = _axpy_kernel([])
+    acc = abi.access(flags=abi.READ_ALL)
+    binding = (abi.Binding * 1)(abi.Binding(h, acc))
+    value = c.c_int(1)
+    argv = (c.c_void_p * 1)(c.cast(c.pointer(value), c.c_void_p))
+    kernel = abi.Kernel(1, 0, c.cast(fn, c.c_void_p), (c.c_uint32 * 3)(1, 1, 1), (c.c_uint32 * 3)(1, 1, 1), 0, argv, 1)
+    task = abi.Task(kernel, binding, 1)
+    assert ours.fort_scope_graph_enqueue_v1(scope.handle, 1, c.byref(task), (c.c_size_t * 1)(4)) == abi.STATE
+    assert ours.fort_scope_graph_enqueue_v1(scope.handle, 1, c.byref(task), None) == abi.ARGUMENT
+    kernel.block[0] = 2048
+    task = abi.Task(kernel, binding, 1)
+    assert ours.fort_scope_graph_enqueue_v1(scope.handle, 1, c.byref(task), (c.c_size_t * 1)(4)) == abi.ARGUMENT
+    assert ours.fort_scope_close(scope.handle) == abi.OK
+
+
+def test_merged_members_must_be_independent(ours):
+    scope = abi.Scope(ours)
+    _, address = _array(np.zeros(10))
+    _, h = scope.register(address, [10])
+    dev = (c.c_void_p * 1)()
+    assert ours.fort_scope_device_reserve_many_v1(scope.handle, (abi.U64 * 1)(h), 1, dev) == abi.OK
+    log = []
+    fn = _axpy_kernel(log)
+    values = [c.c_void_p(dev[0]), c.c_int(10), c.c_double(1.0), c.c_double(0.0)]
+    argv = (c.c_void_p * 4)(*[c.cast(c.pointer(v), c.c_void_p) for v in values])
+    sizes = (c.c_size_t * 4)(8, 4, 8, 8)
+    kernel = abi.Kernel(1, 0, c.cast(fn, c.c_void_p), (c.c_uint32 * 3)(1, 1, 1), (c.c_uint32 * 3)(1, 1, 1), 0, argv, 4)
+    low = abi.access(read=[((0,), (1,))], write=[((0,), (1,))], overwrite=[((0,), (1,))])
+    high = abi.access(read=[((9,), (10,))], write=[((9,), (10,))], overwrite=[((9,), (10,))])
+    m1 = (abi.Binding * 1)(abi.Binding(h, low))
+    m2 = (abi.Binding * 1)(abi.Binding(h, high))
+    members = (abi.Member * 2)(abi.Member(m1, 1), abi.Member(m2, 1))
+    assert ours.fort_scope_graph_enqueue_members_v1(scope.handle, 3, c.byref(kernel), sizes, members, 2) == abi.OK
+    clash = abi.access(read=[((0,), (2,))])
+    m2 = (abi.Binding * 1)(abi.Binding(h, clash))
+    members = (abi.Member * 2)(abi.Member(m1, 1), abi.Member(m2, 1))
+    assert ours.fort_scope_graph_enqueue_members_v1(scope.handle, 3, c.byref(kernel), sizes, members, 2) == abi.BOUNDARY
+    assert ours.fort_scope_close(scope.handle) == abi.OK
+
+
+def test_failed_launch_poisons_without_replay(monkeypatch):
+    lib = _ours()
+    scope = abi.Scope(lib)
+    host, address = _array(np.zeros(4))
+    _, h = scope.register(address, [4])
+    log = []
+    fn = _axpy_kernel(log)
+    assert _enqueue(scope, fn, h, 4, 1.0, 1.0) == abi.OK
+    monkeypatch.setenv("F2C_TEST_FAIL_LAUNCH", "1")
+    assert lib.fort_scope_graph_flush_v1(scope.handle) == abi.EXECUTION
+    monkeypatch.delenv("F2C_TEST_FAIL_LAUNCH")
+    assert "unsafe replay prohibited" in lib.fort_scope_error().decode()
+    dev = (c.c_void_p * 1)()
+    assert lib.fort_scope_device_reserve_many_v1(scope.handle, (abi.U64 * 1)(h), 1, dev) == abi.EXECUTION
+    assert lib.fort_scope_close(scope.handle) == abi.EXECUTION
+    assert lib.fort_scope_abandon(scope.handle) == abi.OK
+    assert log == [] and host.tolist() == [0.0] * 4
+
+
+def test_graph_build_failure_falls_back_to_direct_launches(monkeypatch):
+    lib = _ours()
+    scope = abi.Scope(lib)
+    host, address = _array(np.zeros(4))
+    _, h = scope.register(address, [4])
+    log = []
+    fn = _axpy_kernel(log)
+    monkeypatch.setenv("F2C_TEST_FAIL_GRAPH_CREATE", "1")
+    for _ in range(3):
+        assert _enqueue(scope, fn, h, 4, 1.0, 1.0) == abi.OK
+        assert lib.fort_scope_graph_flush_v1(scope.handle) == abi.OK
+    q = abi.QueueStats()
+    assert lib.fort_scope_graph_queue_stats_get_v1(scope.handle, c.byref(q)) == abi.OK
+    assert q.graph_resource_fallbacks >= 1 and len(log) == 3
+    assert lib.fort_scope_close(scope.handle) == abi.OK
+    assert host.tolist() == [3.0] * 4
+
+
+def test_fragmented_sections_reconcile(ours):
+    scope = abi.Scope(ours)
+    host, address = _array(np.zeros(600))
+    _, h = scope.register(address, [600])
+    for i in range(0, 600, 4):
+        box = ((i,), (i + 1,))
+        status, dev = _device_begin(scope, h, abi.access(write=[box], overwrite=[box]))
+        assert status == abi.OK
+        _dev(dev, 600)[i] = float(i)
+        assert ours.fort_scope_device_end(scope.handle, h) == abi.OK
+    assert ours.fort_scope_observe_v1(scope.handle, (abi.U64 * 1)(h), 1) == abi.OK
+    expect = np.zeros(600)
+    expect[::4] = np.arange(0, 600, 4)
+    assert np.array_equal(host, expect)
+    assert scope.stats().reconciliations >= 1
+    assert ours.fort_scope_close(scope.handle) == abi.OK
+
+
+def test_trace_lines(tmp_path):
+    script = tmp_path / "trace.py"
+    script.write_text(
+        "import sys, ctypes as c, numpy as np\n"
+        f"sys.path[:0] = [{os.path.join(ROOT, 'fortran-to-cuda_gb300')!r}]\n"
+        "from compiler import native\n"
+        "from compiler.runtime import abi\n"
+        "lib = abi.bind(c.CDLL(str(native.build_cpu_runtime())))\n"
+        "s = abi.Scope(lib)\n"
+        "a = np.zeros(4)\n"
+        "st, h = s.register(a.ctypes.data, [4])\n"
+        "d = c.c_void_p()\n"
+        "assert lib.fort_scope_device_begin(s.handle, h, c.byref(abi.access(flags=3)), c.byref(d)) == 0\n"
+        "assert lib.fort_scope_device_end(s.handle, h) == 0\n"
+        "assert lib.fort_scope_close(s.handle) == 0\n")
+    env = dict(os.environ, FORT_RUNTIME_TRACE="1")
+    out = subprocess.run([sys.executable, str(script)], capture_output=True, text=True, env=env, timeout=120)
+    assert out.returncode == 0, out.stderr
+    events = [line.split()[1] for line in out.stderr.splitlines() if line.startswith("FORT_SCOPED ")]
+    assert events.count("upload") == 1 and events.count("download") == 1 and "register" in events
