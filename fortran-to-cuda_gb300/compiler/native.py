@@ -51,8 +51,11 @@ def _headers() -> list[Path]:
         sorted(INCLUDE.glob("*.h"))
 
 
+LINK_TAG = "link:-Bsymbolic"
+
+
 def _fingerprint(files) -> str:
-    digest = hashlib.sha256()
+    digest = hashlib.sha256(LINK_TAG.encode())
     for flag in NVCC_FLAGS:
         digest.update(flag.encode())
     for path in files:
@@ -90,7 +93,8 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     with ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 4)) as pool:
         objects = list(pool.map(compile_one, srcs))
     tmp = LIBRARY.with_suffix(f".{os.getpid()}.tmp")
-    link = [compiler, *ARCH, "-shared", "-Xcompiler", "-fopenmp", *map(str, objects), "-o", str(tmp), "-lcudart"]
+    link = [compiler, *ARCH, "-shared", "-Xcompiler", "-fopenmp", "-Xlinker", "-Bsymbolic", *map(str, objects),
+            "-o", str(tmp), "-lcudart"]
     result = subprocess.run(link, capture_output=True, text=True)
     if result.returncode != 0:
         raise RuntimeError(f"link failed:\n{result.stdout}\n{result.stderr}")
@@ -119,7 +123,7 @@ def build_cpu_runtime(force: bool = False) -> Path:
     tmp = CPU_RUNTIME.with_suffix(f".{os.getpid()}.tmp")
     cxx = os.environ.get("CXX", "g++")
     cmd = [cxx, "-std=c++17", "-O2", "-Wall", "-Wextra", "-Werror", "-fPIC", "-shared", "-pthread",
-           "-DF2C_RUNTIME_CPU_BACKEND", "-x", "c++", str(RUNTIME_SOURCE), "-o", str(tmp)]
+           "-Wl,-Bsymbolic", "-DF2C_RUNTIME_CPU_BACKEND", "-x", "c++", str(RUNTIME_SOURCE), "-o", str(tmp)]
     result = subprocess.run(cmd, capture_output=True, text=True)
     if result.returncode != 0:
         raise RuntimeError(f"CPU runtime build failed:\n{result.stderr}")
@@ -152,7 +156,7 @@ TENDENCY, ADVANCE = 0, 1
 def load() -> ctypes.CDLL:
     """Load the native library (building it first if needed). Raises if it cannot be had."""
     path = LIBRARY if LIBRARY.exists() else build()
-    lib = ctypes.CDLL(str(path), mode=ctypes.RTLD_GLOBAL)
+    lib = ctypes.CDLL(str(path))
     lib.f2c_advection_abi_version.restype = ctypes.c_uint32
     lib.f2c_last_error.restype = ctypes.c_char_p
     lib.f2c_advection_v1.argtypes = [ctypes.POINTER(Grid), ctypes.POINTER(Fields), ctypes.c_void_p]

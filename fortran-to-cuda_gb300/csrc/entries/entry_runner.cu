@@ -1,0 +1,402 @@
+// Template runner behind every generated numerical entry.
+//
+// The protocol mirrors the reference's generated entries
+// (compiler/emission/cuda/scoped.py:237-512): ABI version and mode checks,
+// writable-alias check, layout check per array, loop extents, the exact
+// read/write sections of the template, storage reservation, the definition
+// change of intent(out) arrays, and one queued task through
+// fort_scope_graph_enqueue_v1 (the runtime submits the queue as a replayed
+// CUDA graph). Where the reference entry runs its generated CPU worker (native
+// mode, or device resources unavailable before any work started), this entry
+// returns FORT_SCOPE_DECLINED and performs nothing: the spliced call block
+// then publishes the domain and runs the original Fortran statements.
+#include <cuda_runtime.h>
+
+#include <array>
+#include <cstring>
+#include <deque>
+#include <vector>
+
+#include "../kernels/advection_faces.cuh"
+#include "../kernels/advection_kernels.cuh"
+#include "../kernels/procedures.cuh"
+#include "entry_runner.hpp"
+
+namespace f2c::entries {
+namespace {
+
+using Triple = std::array<size_t, 3>;
+
+// Storage-stable list of sections for one array.
+class Sections {
+public:
+    void add(const Triple &lo, const Triple &hi) {
+        lo_.push_back(lo);
+        hi_.push_back(hi);
+    }
+    const fort_scope_section *data() {
+        list_.clear();
+        for (size_t n = 0; n < lo_.size(); ++n) list_.push_back({lo_[n].data(), hi_[n].data()});
+        return list_.data();
+    }
+    size_t size() const { return lo_.size(); }
+
+private:
+    std::deque<Triple> lo_, hi_;
+    std::vector<fort_scope_section> list_;
+};
+
+struct Geometry {
+    long long n[3];
+    long long h;
+    size_t ext[3];
+    // [h+a, h+n+b) on axis d
+    size_t lo(int d, int a) const { return (size_t)(h + a); }
+    size_t hi(int d, int b) const { return (size_t)(h + n[d] + b); }
+    Triple box_lo(int ax, int ay, int az) const { return {lo(0, ax), lo(1, ay), lo(2, az)}; }
+    Triple box_hi(int bx, int by, int bz) const { return {hi(0, bx), hi(1, by), hi(2, bz)}; }
+};
+
+void add_box(Sections &s, const Geometry &g, int ax, int bx, int ay, int by, int az, int bz) {
+    s.add(g.box_lo(ax, ay, az), g.box_hi(bx, by, bz));
+}
+void add_interior(Sections &s, const Geometry &g) { add_box(s, g, 0, 0, 0, 0, 0, 0); }
+void add_cross(Sections &s, const Geometry &g) {
+    add_box(s, g, -1, 1, 0, 0, 0, 0);
+    add_box(s, g, 0, 0, -1, 1, 0, 0);
+    add_box(s, g, 0, 0, 0, 0, -1, 1);
+}
+// the non-own velocity reads of each momentum procedure
+void add_cdu_v(Sections &s, const Geometry &g) { add_box(s, g, 0, 1, -1, 0, 0, 0); }
+void add_cdu_w(Sections &s, const Geometry &g) { add_box(s, g, 0, 1, 0, 0, -1, 0); }
+void add_cdv_u(Sections &s, const Geometry &g) { add_box(s, g, -1, 0, 0, 1, 0, 0); }
+void add_cdv_w(Sections &s, const Geometry &g) { add_box(s, g, 0, 0, 0, 1, -1, 0); }
+void add_cdw_u(Sections &s, const Geometry &g) { add_box(s, g, -1, 0, 0, 0, 0, 1); }
+void add_cdw_v(Sections &s, const Geometry &g) { add_box(s, g, 0, 0, -1, 0, 0, 1); }
+
+struct Use {
+    fort_buffer_t handle;
+    bool written;
+    bool overwritten;   // every written element is written (an exact overwrite)
+    bool read;
+    bool intent_out;
+    Sections reads, writes;
+};
+
+int declined() { return FORT_SCOPE_DECLINED; }
+
+template <int NS, int MASK>
+void faces_spec(const AdvArgs &a, fort_scope_kernel_v1 &k) {
+    using Smem = FaceSmem<NS, MASK>;
+    static bool configured = false;
+    if (!configured) {
+        cudaFuncSetAttribute(advection_faces_kernel<NS, MASK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)Smem::bytes);
+        configured = true;
+    }
+    k.function = (const void *)advection_faces_kernel<NS, MASK>;
+    k.grid[0] = (a.nx + kFaceTX - 1) / kFaceTX;
+    k.grid[1] = (a.ny + kFaceTY - 1) / kFaceTY;
+    k.grid[2] = (a.nz + kFaceKZ - 1) / kFaceKZ;
+    k.block[0] = kFaceTX;
+    k.block[1] = kFaceTY + 1;
+    k.block[2] = 1;
+    k.shared_bytes = Smem::bytes;
+}
+
+template <int MASK>
+void faces_spec_ns(int ns, const AdvArgs &a, fort_scope_kernel_v1 &k) {
+    switch (ns) {
+    case 0: faces_spec<0, MASK>(a, k); break;
+    case 1: faces_spec<1, MASK>(a, k); break;
+    case 2: faces_spec<2, MASK>(a, k); break;
+    case 3: faces_spec<3, MASK>(a, k); break;
+    default: faces_spec<4, MASK>(a, k); break;
+    }
+}
+
+const void *procedure_function(Template t) {
+    switch (t) {
+    case Template::Set: return (const void *)procedure_kernel<kOpSet>;
+    case Template::Multiply: return (const void *)procedure_kernel<kOpMultiply>;
+    case Template::CduDiv: return (const void *)procedure_kernel<kOpCduDiv>;
+    case Template::CduAdv: return (const void *)procedure_kernel<kOpCduAdv>;
+    case Template::CdvDiv: return (const void *)procedure_kernel<kOpCdvDiv>;
+    case Template::CdvAdv: return (const void *)procedure_kernel<kOpCdvAdv>;
+    case Template::CdwDiv: return (const void *)procedure_kernel<kOpCdwDiv>;
+    case Template::CdwAdv: return (const void *)procedure_kernel<kOpCdwAdv>;
+    default: return nullptr;
+    }
+}
+
+int run(const EntryCall &call) {
+    if (fort_scope_abi_version() != FORT_SCOPE_ABI_VERSION)
+        return fort_scope_report_error(FORT_SCOPE_ARGUMENT, "incompatible shared runtime ABI");
+    if (call.mode < FORT_SCOPE_NATIVE || call.mode > FORT_SCOPE_GPU)
+        return fort_scope_report_error(FORT_SCOPE_ARGUMENT, "unknown shared execution mode");
+    for (int n = 0; n < call.nreals; ++n)
+        if (!call.reals[n]) return fort_scope_report_error(FORT_SCOPE_ARGUMENT, "null shared scalar argument");
+    for (int n = 0; n < call.nints; ++n)
+        if (!call.ints[n]) return fort_scope_report_error(FORT_SCOPE_ARGUMENT, "null shared scalar argument");
+    if (call.mode == FORT_SCOPE_NATIVE) return declined();
+
+    const Template t = call.kind;
+    const int ns = call.nscalar;
+    const bool step = t == Template::Step || t == Template::StepAdvance;
+    const bool halo = t == Template::Halo;
+    const bool procedure = !step && !halo;
+
+    // ---- roles of the arrays, in the declared argument order ----
+    std::deque<Use> uses(call.narrays);
+    for (int n = 0; n < call.narrays; ++n) uses[n].handle = call.arrays[n];
+    auto role = [&](int n, bool read, bool written, bool overwritten, bool intent_out) {
+        uses[n].read = read;
+        uses[n].written = written;
+        uses[n].overwritten = overwritten;
+        uses[n].intent_out = intent_out;
+    };
+    switch (t) {
+    case Template::Set: role(0, false, true, true, true); break;
+    case Template::Multiply: role(0, true, true, false, false); break;
+    case Template::CduDiv: case Template::CdvDiv: case Template::CdwDiv:
+    case Template::Cdu: case Template::Cdv: case Template::Cdw:
+        role(0, false, true, true, true);
+        for (int n = 1; n < 4; ++n) role(n, true, false, false, false);
+        break;
+    case Template::CduAdv: case Template::CdvAdv: case Template::CdwAdv:
+        role(0, true, true, false, false);
+        for (int n = 1; n < 4; ++n) role(n, true, false, false, false);
+        break;
+    case Template::Step: case Template::StepAdvance:
+        for (int n = 0; n < 3; ++n) role(n, false, true, true, true);
+        for (int n = 3; n < 6 + ns; ++n) role(n, true, false, false, false);
+        for (int n = 6 + ns; n < 6 + 2 * ns; ++n) role(n, false, true, true, true);
+        break;
+    case Template::Halo:
+        for (int n = 0; n < call.narrays; ++n) role(n, true, true, true, false);
+        break;
+    }
+    // writable arguments must not alias any other argument
+    for (int a = 0; a < call.narrays; ++a)
+        for (int b = 0; b < a; ++b)
+            if (uses[a].handle == uses[b].handle && (uses[a].written || uses[b].written))
+                return fort_scope_report_error(FORT_SCOPE_ALIAS, "writable entry arguments alias");
+
+    // ---- layouts ----
+    Geometry g{};
+    for (int n = 0; n < call.narrays; ++n) {
+        fort_scope_layout layout{};
+        if (int s = fort_scope_layout_get(call.context, uses[n].handle, &layout)) return s;
+        if (layout.rank != 3 || layout.type != FORT_SCOPE_REAL64 || layout.element_bytes != sizeof(double))
+            return fort_scope_report_error(FORT_SCOPE_ARGUMENT, "entry layout/type mismatch");
+        if (n == 0) {
+            for (int d = 0; d < 3; ++d) g.ext[d] = layout.extents[d];
+        } else {
+            for (int d = 0; d < 3; ++d)
+                if (layout.extents[d] != g.ext[d]) return declined(); // templates take one shape per call
+        }
+    }
+    // ---- loop extents and the interior offset ----
+    const int *ints[8];
+    for (int n = 0; n < call.nints; ++n) ints[n] = call.ints[n];
+    for (int d = 0; d < 3; ++d) g.n[d] = *ints[d];
+    g.h = procedure ? 1 : *ints[3];
+    if (g.n[0] < 1 || g.n[1] < 1 || g.n[2] < 1) return FORT_SCOPE_OK; // no iterations: nothing to do
+    if (g.h < 1) return fort_scope_report_error(FORT_SCOPE_ARGUMENT, "halo width must be at least one");
+    for (int d = 0; d < 3; ++d)
+        if ((size_t)(g.n[d] + 2 * g.h) > g.ext[d])
+            return fort_scope_report_error(FORT_SCOPE_ARGUMENT, "invalid physical entry footprint");
+    if (halo) {
+        for (int d = 0; d < 3; ++d)
+            if ((size_t)(g.n[d] + 2 * g.h) != g.ext[d]) return declined();
+        if (g.n[2] < g.h + 1 || g.n[0] < g.h || g.n[1] < g.h) return declined();
+    }
+
+    // ---- exact sections ----
+    auto out_sections = [&](Use &u) {
+        add_interior(u.writes, g);
+        if (u.read) add_interior(u.reads, g);
+    };
+    switch (t) {
+    case Template::Set: case Template::Multiply: out_sections(uses[0]); break;
+    case Template::CduDiv: case Template::CduAdv: case Template::Cdu:
+        out_sections(uses[0]);
+        add_cross(uses[1].reads, g);
+        add_cdu_v(uses[2].reads, g);
+        add_cdu_w(uses[3].reads, g);
+        break;
+    case Template::CdvDiv: case Template::CdvAdv: case Template::Cdv:
+        out_sections(uses[0]);
+        add_cdv_u(uses[1].reads, g);
+        add_cross(uses[2].reads, g);
+        add_cdv_w(uses[3].reads, g);
+        break;
+    case Template::CdwDiv: case Template::CdwAdv: case Template::Cdw:
+        out_sections(uses[0]);
+        add_cdw_u(uses[1].reads, g);
+        add_cdw_v(uses[2].reads, g);
+        add_cross(uses[3].reads, g);
+        break;
+    case Template::Step: case Template::StepAdvance: {
+        for (int n = 0; n < 3; ++n) out_sections(uses[n]);
+        Use &U = uses[3], &V = uses[4], &W = uses[5];
+        add_cross(U.reads, g);
+        add_cdv_u(U.reads, g);
+        add_cdw_u(U.reads, g);
+        add_cross(V.reads, g);
+        add_cdu_v(V.reads, g);
+        add_cdw_v(V.reads, g);
+        add_cross(W.reads, g);
+        add_cdu_w(W.reads, g);
+        add_cdv_w(W.reads, g);
+        for (int n = 0; n < ns; ++n) {
+            add_cross(uses[6 + n].reads, g);
+            out_sections(uses[6 + ns + n]);
+        }
+        break;
+    }
+    case Template::Halo: {
+        for (int n = 0; n < call.narrays; ++n) {
+            Use &u = uses[n];
+            add_interior(u.reads, g);
+            const size_t ex = g.ext[0], ey = g.ext[1], ez = g.ext[2], h = (size_t)g.h;
+            const size_t nx = (size_t)g.n[0], ny = (size_t)g.n[1], nz = (size_t)g.n[2];
+            u.writes.add({0, 0, 0}, {ex, ey, h});
+            u.writes.add({0, 0, h + nz}, {ex, ey, ez});
+            u.writes.add({0, 0, h}, {ex, h, h + nz});
+            u.writes.add({0, h + ny, h}, {ex, ey, h + nz});
+            u.writes.add({0, h, h}, {h, h + ny, h + nz});
+            u.writes.add({h + nx, h, h}, {ex, h + ny, h + nz});
+            if (n == 2) u.writes.add({h, h, h + nz - 1}, {h + nx, h + ny, h + nz}); // W top wall faces
+        }
+        break;
+    }
+    }
+
+    // ---- storage first, so a resource failure changes nothing ----
+    std::vector<fort_buffer_t> handles;
+    for (auto &u : uses) handles.push_back(u.handle);
+    std::vector<void *> devices(handles.size(), nullptr);
+    {
+        const int s = fort_scope_device_reserve_many_v1(call.context, handles.data(), handles.size(), devices.data());
+        if (s == FORT_SCOPE_RESOURCE) return declined();
+        if (s) return s;
+    }
+    for (auto &u : uses)
+        if (u.intent_out)
+            if (int s = fort_scope_forget_definition(call.context, u.handle)) return s;
+
+    // ---- kernel arguments ----
+    AdvArgs adv{};
+    ProcedureArgs proc{};
+    HaloArgs hal{};
+    fort_scope_kernel_v1 kernel{};
+    kernel.version = FORT_SCOPE_GRAPH_ABI_VERSION;
+    void *argument = nullptr;
+    size_t argument_size = 0;
+    const long long sx = (long long)g.ext[0], plane = (long long)(g.ext[0] * g.ext[1]);
+    auto dev = [&](int n) { return static_cast<double *>(devices[n]); };
+    if (procedure && (t == Template::Cdu || t == Template::Cdv || t == Template::Cdw)) {
+        adv.u = dev(1); adv.v = dev(2); adv.w = dev(3);
+        const int slot = t == Template::Cdu ? 0 : t == Template::Cdv ? 1 : 2;
+        adv.out[slot] = dev(0);
+        adv.nx = (int)g.n[0]; adv.ny = (int)g.n[1]; adv.nz = (int)g.n[2]; adv.h = (int)g.h;
+        adv.sx = sx; adv.plane = plane;
+        adv.c = make_coefficients(*call.reals[0], *call.reals[1], *call.reals[2]);
+        if (t == Template::Cdu) faces_spec_ns<1>(0, adv, kernel);
+        else if (t == Template::Cdv) faces_spec_ns<2>(0, adv, kernel);
+        else faces_spec_ns<4>(0, adv, kernel);
+        argument = &adv;
+        argument_size = sizeof adv;
+    } else if (procedure) {
+        proc.out = dev(0);
+        if (t != Template::Set && t != Template::Multiply) {
+            proc.u = dev(1); proc.v = dev(2); proc.w = dev(3);
+            proc.c = make_coefficients(*call.reals[0], *call.reals[1], *call.reals[2]);
+        } else {
+            proc.value = *call.reals[0];
+        }
+        proc.nx = (int)g.n[0]; proc.ny = (int)g.n[1]; proc.nz = (int)g.n[2]; proc.h = 1;
+        proc.sx = sx; proc.plane = plane;
+        kernel.function = procedure_function(t);
+        const dim3 grid = procedure_grid(proc);
+        kernel.grid[0] = grid.x; kernel.grid[1] = grid.y; kernel.grid[2] = grid.z;
+        kernel.block[0] = kProcBX; kernel.block[1] = kProcBY; kernel.block[2] = 1;
+        argument = &proc;
+        argument_size = sizeof proc;
+    } else if (step) {
+        adv.out[0] = dev(0); adv.out[1] = dev(1); adv.out[2] = dev(2);
+        adv.u = dev(3); adv.v = dev(4); adv.w = dev(5);
+        adv.nscalar = ns;
+        for (int n = 0; n < ns; ++n) {
+            adv.s[n] = dev(6 + n);
+            adv.st[n] = dev(6 + ns + n);
+        }
+        adv.mode = t == Template::StepAdvance ? 1 : 0;
+        adv.dt = t == Template::StepAdvance ? *call.reals[3] : 0.0;
+        adv.nx = (int)g.n[0]; adv.ny = (int)g.n[1]; adv.nz = (int)g.n[2]; adv.h = (int)g.h;
+        adv.sx = sx; adv.plane = plane;
+        adv.c = make_coefficients(*call.reals[0], *call.reals[1], *call.reals[2]);
+        faces_spec_ns<7>(ns, adv, kernel);
+        argument = &adv;
+        argument_size = sizeof adv;
+    } else {
+        hal.count = call.narrays;
+        for (int n = 0; n < call.narrays; ++n) {
+            hal.f[n] = dev(n);
+            hal.kind[n] = n == 2 ? 1 : 0;
+        }
+        hal.nx = (int)g.n[0]; hal.ny = (int)g.n[1]; hal.nz = (int)g.n[2]; hal.h = (int)g.h;
+        hal.sx = sx; hal.plane = plane;
+        const long long ex = g.n[0] + 2 * g.h;
+        kernel.function = (const void *)halo_fill_kernel;
+        kernel.grid[0] = (unsigned)(g.ext[1] * g.ext[2]);
+        kernel.grid[1] = (unsigned)call.narrays;
+        kernel.grid[2] = 1;
+        kernel.block[0] = ex >= 256 ? 256 : (unsigned)(((ex + 31) / 32) * 32);
+        kernel.block[1] = kernel.block[2] = 1;
+        argument = &hal;
+        argument_size = sizeof hal;
+    }
+    void *arguments[1] = {argument};
+    kernel.arguments = arguments;
+    kernel.argument_count = 1;
+
+    // ---- one queued task with the exact effects ----
+    std::vector<fort_scope_plan_binding> bindings;
+    for (auto &u : uses) {
+        fort_scope_plan_binding b{};
+        b.buffer = u.handle;
+        b.access.read_count = u.reads.size();
+        b.access.reads = u.reads.size() ? u.reads.data() : nullptr;
+        if (u.written) {
+            b.access.write_count = u.writes.size();
+            b.access.writes = u.writes.data();
+            if (u.overwritten) {
+                b.access.overwrite_count = u.writes.size();
+                b.access.overwrites = b.access.writes;
+            }
+        }
+        bindings.push_back(b);
+    }
+    fort_scope_graph_task_v1 task{};
+    task.kernel = kernel;
+    task.bindings = bindings.data();
+    task.binding_count = bindings.size();
+    const size_t sizes[1] = {argument_size};
+    const int status = fort_scope_graph_enqueue_v1(call.context, call.code_key, &task, sizes);
+    if (status == FORT_SCOPE_OK) return FORT_SCOPE_OK;
+    if (status == FORT_SCOPE_EXECUTION) return status;
+    // nothing was accepted: only definitions were forgotten, which the original statements redefine
+    return status;
+}
+
+} // namespace
+
+int run_entry(const EntryCall &call) {
+    if (call.narrays < 1 || call.narrays > kMaxEntryArrays || call.nints > 8 || call.nreals > 8)
+        return fort_scope_report_error(FORT_SCOPE_ARGUMENT, "malformed entry call");
+    return run(call);
+}
+
+} // namespace f2c::entries

@@ -77,7 +77,7 @@ __global__ void __launch_bounds__(BX *BY) advection_direct_kernel(const AdvArgs 
 // vertical walls over whole planes) would copy into it. Periodic maps compose,
 // and each vertical mirror source is an interior, non-wall level (nz > halo),
 // so no ghost reads another ghost and the pass order is free.
-__global__ void __launch_bounds__(256) halo_fill_kernel(const HaloArgs a) {
+static __global__ void __launch_bounds__(256) halo_fill_kernel(const HaloArgs a) {
     const int ex = a.nx + 2 * a.h, ey = a.ny + 2 * a.h, ez = a.nz + 2 * a.h;
     const long long row = blockIdx.x;          // j + ey*k
     const int fidx = blockIdx.y;

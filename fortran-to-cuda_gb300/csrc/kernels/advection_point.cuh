@@ -23,52 +23,64 @@ struct Coefficients {
 };
 
 // F(a, di, dj, dk) reads array a at the point offset by (di, dj, dk).
-#define F2C_CDU_POINT(F, C)                                                                                         \
+// *_DIV is the flux-form procedure (it overwrites the output), *_ADV(prev)
+// subtracts the advective form from the value `prev` (the procedure's
+// read-modify-write of the output), *_POINT is the whole procedure: DIV, then
+// ADV of it, then the multiplication by one half.
+#define F2C_CDU_DIV(F, C)                                                                                           \
+    (-(((C).Ax * (F(U, 1, 0, 0) + F(U, 0, 0, 0)) * (F(U, 1, 0, 0) + F(U, 0, 0, 0)) -                                \
+        (C).Ax * (F(U, 0, 0, 0) + F(U, -1, 0, 0)) * (F(U, 0, 0, 0) + F(U, -1, 0, 0))) +                             \
+       ((C).Ay * (F(U, 0, 1, 0) + F(U, 0, 0, 0)) * (F(V, 1, 0, 0) + F(V, 0, 0, 0)) -                                \
+        (C).Ay * (F(U, 0, 0, 0) + F(U, 0, -1, 0)) * (F(V, 1, -1, 0) + F(V, 0, -1, 0))) +                            \
+       ((C).Az * (F(U, 0, 0, 1) + F(U, 0, 0, 0)) * (F(W, 1, 0, 0) + F(W, 0, 0, 0)) -                                \
+        (C).Az * (F(U, 0, 0, 0) + F(U, 0, 0, -1)) * (F(W, 1, 0, -1) + F(W, 0, 0, -1)))))
+
+#define F2C_CDU_ADV(F, C, prev)                                                                                     \
     ([&]() -> double {                                                                                              \
-        double r = -(((C).Ax * (F(U, 1, 0, 0) + F(U, 0, 0, 0)) * (F(U, 1, 0, 0) + F(U, 0, 0, 0)) -                  \
-                      (C).Ax * (F(U, 0, 0, 0) + F(U, -1, 0, 0)) * (F(U, 0, 0, 0) + F(U, -1, 0, 0))) +               \
-                     ((C).Ay * (F(U, 0, 1, 0) + F(U, 0, 0, 0)) * (F(V, 1, 0, 0) + F(V, 0, 0, 0)) -                  \
-                      (C).Ay * (F(U, 0, 0, 0) + F(U, 0, -1, 0)) * (F(V, 1, -1, 0) + F(V, 0, -1, 0))) +              \
-                     ((C).Az * (F(U, 0, 0, 1) + F(U, 0, 0, 0)) * (F(W, 1, 0, 0) + F(W, 0, 0, 0)) -                  \
-                      (C).Az * (F(U, 0, 0, 0) + F(U, 0, 0, -1)) * (F(W, 1, 0, -1) + F(W, 0, 0, -1))));              \
         const double Vadv = (F(V, 0, 0, 0) + F(V, 1, 0, 0) + F(V, 0, -1, 0) + F(V, 1, -1, 0));                      \
         const double Wadv = (F(W, 0, 0, 0) + F(W, 1, 0, 0) + F(W, 0, 0, -1) + F(W, 1, 0, -1));                      \
-        r = r - ((C).Bux * (F(U, 1, 0, 0) - F(U, -1, 0, 0)) * F(U, 0, 0, 0) +                                       \
-                 (C).Buy * (F(U, 0, 1, 0) - F(U, 0, -1, 0)) * Vadv + (C).Buz * (F(U, 0, 0, 1) - F(U, 0, 0, -1)) * Wadv); \
-        return r * 0.5;                                                                                             \
+        return (prev) - ((C).Bux * (F(U, 1, 0, 0) - F(U, -1, 0, 0)) * F(U, 0, 0, 0) +                               \
+                         (C).Buy * (F(U, 0, 1, 0) - F(U, 0, -1, 0)) * Vadv +                                        \
+                         (C).Buz * (F(U, 0, 0, 1) - F(U, 0, 0, -1)) * Wadv);                                        \
     }())
 
-#define F2C_CDV_POINT(F, C)                                                                                         \
+#define F2C_CDV_DIV(F, C)                                                                                           \
+    (-(((C).Ay * (F(V, 0, 1, 0) + F(V, 0, 0, 0)) * (F(V, 0, 1, 0) + F(V, 0, 0, 0)) -                                \
+        (C).Ay * (F(V, 0, 0, 0) + F(V, 0, -1, 0)) * (F(V, 0, 0, 0) + F(V, 0, -1, 0))) +                             \
+       ((C).Ax * (F(V, 1, 0, 0) + F(V, 0, 0, 0)) * (F(U, 0, 1, 0) + F(U, 0, 0, 0)) -                                \
+        (C).Ax * (F(V, 0, 0, 0) + F(V, -1, 0, 0)) * (F(U, -1, 1, 0) + F(U, -1, 0, 0))) +                            \
+       ((C).Az * (F(V, 0, 0, 1) + F(V, 0, 0, 0)) * (F(W, 0, 1, 0) + F(W, 0, 0, 0)) -                                \
+        (C).Az * (F(V, 0, 0, 0) + F(V, 0, 0, -1)) * (F(W, 0, 1, -1) + F(W, 0, 0, -1)))))
+
+#define F2C_CDV_ADV(F, C, prev)                                                                                     \
     ([&]() -> double {                                                                                              \
-        double r = -(((C).Ay * (F(V, 0, 1, 0) + F(V, 0, 0, 0)) * (F(V, 0, 1, 0) + F(V, 0, 0, 0)) -                  \
-                      (C).Ay * (F(V, 0, 0, 0) + F(V, 0, -1, 0)) * (F(V, 0, 0, 0) + F(V, 0, -1, 0))) +               \
-                     ((C).Ax * (F(V, 1, 0, 0) + F(V, 0, 0, 0)) * (F(U, 0, 1, 0) + F(U, 0, 0, 0)) -                  \
-                      (C).Ax * (F(V, 0, 0, 0) + F(V, -1, 0, 0)) * (F(U, -1, 1, 0) + F(U, -1, 0, 0))) +              \
-                     ((C).Az * (F(V, 0, 0, 1) + F(V, 0, 0, 0)) * (F(W, 0, 1, 0) + F(W, 0, 0, 0)) -                  \
-                      (C).Az * (F(V, 0, 0, 0) + F(V, 0, 0, -1)) * (F(W, 0, 1, -1) + F(W, 0, 0, -1))));              \
         const double Uadv = (F(U, 0, 0, 0) + F(U, 0, 1, 0) + F(U, -1, 0, 0) + F(U, -1, 1, 0));                      \
         const double Wadv = (F(W, 0, 0, 0) + F(W, 0, 1, 0) + F(W, 0, 0, -1) + F(W, 0, 1, -1));                      \
-        r = r - ((C).Bvx * (F(V, 1, 0, 0) - F(V, -1, 0, 0)) * Uadv +                                                \
-                 (C).Bvy * (F(V, 0, 1, 0) - F(V, 0, -1, 0)) * F(V, 0, 0, 0) +                                       \
-                 (C).Bvz * (F(V, 0, 0, 1) - F(V, 0, 0, -1)) * Wadv);                                                \
-        return r * 0.5;                                                                                             \
+        return (prev) - ((C).Bvx * (F(V, 1, 0, 0) - F(V, -1, 0, 0)) * Uadv +                                        \
+                         (C).Bvy * (F(V, 0, 1, 0) - F(V, 0, -1, 0)) * F(V, 0, 0, 0) +                               \
+                         (C).Bvz * (F(V, 0, 0, 1) - F(V, 0, 0, -1)) * Wadv);                                        \
     }())
 
-#define F2C_CDW_POINT(F, C)                                                                                         \
+#define F2C_CDW_DIV(F, C)                                                                                           \
+    (-(((C).Az * (F(W, 0, 0, 1) + F(W, 0, 0, 0)) * (F(W, 0, 0, 1) + F(W, 0, 0, 0)) -                                \
+        (C).Az * (F(W, 0, 0, 0) + F(W, 0, 0, -1)) * (F(W, 0, 0, 0) + F(W, 0, 0, -1))) +                             \
+       ((C).Ay * (F(W, 0, 1, 0) + F(W, 0, 0, 0)) * (F(V, 0, 0, 1) + F(V, 0, 0, 0)) -                                \
+        (C).Ay * (F(W, 0, 0, 0) + F(W, 0, -1, 0)) * (F(V, 0, -1, 0) + F(V, 0, -1, 1))) +                            \
+       ((C).Ax * (F(W, 1, 0, 0) + F(W, 0, 0, 0)) * (F(U, 0, 0, 1) + F(U, 0, 0, 0)) -                                \
+        (C).Ax * (F(W, 0, 0, 0) + F(W, -1, 0, 0)) * (F(U, -1, 0, 1) + F(U, -1, 0, 0)))))
+
+#define F2C_CDW_ADV(F, C, prev)                                                                                     \
     ([&]() -> double {                                                                                              \
-        double r = -(((C).Az * (F(W, 0, 0, 1) + F(W, 0, 0, 0)) * (F(W, 0, 0, 1) + F(W, 0, 0, 0)) -                  \
-                      (C).Az * (F(W, 0, 0, 0) + F(W, 0, 0, -1)) * (F(W, 0, 0, 0) + F(W, 0, 0, -1))) +               \
-                     ((C).Ay * (F(W, 0, 1, 0) + F(W, 0, 0, 0)) * (F(V, 0, 0, 1) + F(V, 0, 0, 0)) -                  \
-                      (C).Ay * (F(W, 0, 0, 0) + F(W, 0, -1, 0)) * (F(V, 0, -1, 0) + F(V, 0, -1, 1))) +              \
-                     ((C).Ax * (F(W, 1, 0, 0) + F(W, 0, 0, 0)) * (F(U, 0, 0, 1) + F(U, 0, 0, 0)) -                  \
-                      (C).Ax * (F(W, 0, 0, 0) + F(W, -1, 0, 0)) * (F(U, -1, 0, 1) + F(U, -1, 0, 0))));              \
         const double Uadv = (F(U, 0, 0, 0) + F(U, 0, 0, 1) + F(U, -1, 0, 0) + F(U, -1, 0, 1));                      \
         const double Vadv = (F(V, 0, 0, 0) + F(V, 0, 0, 1) + F(V, 0, -1, 0) + F(V, 0, -1, 1));                      \
-        r = r - ((C).Bwx * (F(W, 1, 0, 0) - F(W, -1, 0, 0)) * Uadv +                                                \
-                 (C).Bwy * (F(W, 0, 1, 0) - F(W, 0, -1, 0)) * Vadv +                                                \
-                 (C).Bwz * (F(W, 0, 0, 1) - F(W, 0, 0, -1)) * F(W, 0, 0, 0));                                       \
-        return r * 0.5;                                                                                             \
+        return (prev) - ((C).Bwx * (F(W, 1, 0, 0) - F(W, -1, 0, 0)) * Uadv +                                        \
+                         (C).Bwy * (F(W, 0, 1, 0) - F(W, 0, -1, 0)) * Vadv +                                        \
+                         (C).Bwz * (F(W, 0, 0, 1) - F(W, 0, 0, -1)) * F(W, 0, 0, 0));                               \
     }())
+
+#define F2C_CDU_POINT(F, C) (F2C_CDU_ADV(F, C, F2C_CDU_DIV(F, C)) * 0.5)
+#define F2C_CDV_POINT(F, C) (F2C_CDV_ADV(F, C, F2C_CDV_DIV(F, C)) * 0.5)
+#define F2C_CDW_POINT(F, C) (F2C_CDW_ADV(F, C, F2C_CDW_DIV(F, C)) * 0.5)
 
 // Scalar S advected by U, V, W (face fluxes shareable between neighbours).
 #define F2C_SCALAR_POINT(F, S, C)                                                                                   \

@@ -1,0 +1,175 @@
+"""Generated numerical entries through the C ABI, driven like the spliced Fortran call blocks.
+
+Each test opens an epoch on a residency domain, binds host arrays, calls the
+entries (``cpp_fort_shared_<digest>``) with FORT_SCOPE_GPU exactly as the
+call block does (context, mode, handles, scalars by reference), publishes,
+and compares the host arrays with the C oracle bit for bit.
+"""
+
+import numpy as np
+import pytest
+
+from compiler import emission, native
+from compiler import workloads as wl
+from compiler.resident.domain import ResidentDomain
+from compiler.runtime import abi
+from oracle import api
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture()
+def resident(cuda):
+    lib = native.runtime()
+    dom = ResidentDomain(lib)
+    yield dom, emission.bind(lib)
+    if dom.context:
+        dom.close()
+
+
+def _bits(a):
+    return np.ascontiguousarray(a).view(np.int64)
+
+
+def _same(a, b):
+    return np.array_equal(_bits(a), _bits(b))
+
+
+def _call(fns, dom, procedure, arrays, reals=(), ints=()):
+    return emission.call(fns, procedure, dom.context, abi.GPU, arrays, reals, ints)
+
+
+@pytest.mark.parametrize("which", ["cdu", "cdv", "cdw"])
+def test_procedure_entry_matches_oracle(resident, which):
+    dom, fns = resident
+    f = wl.reference_driver_fields(24, 20, 12, seed=3)
+    geo = f.geometry
+    out = np.zeros_like(f.U)
+    dom.begin_epoch()
+    handles = [dom.bind_real64(a) for a in (out, f.U, f.V, f.W)]
+    for _ in range(3):
+        assert _call(fns, dom, f"momentumadvection::{which}", handles, [geo.dx, geo.dy, geo.dz],
+                     [geo.nx, geo.ny, geo.nz]) == abi.OK
+        assert dom.lib.fort_scope_graph_flush_v1(dom.context) == abi.OK
+    dom.end_epoch()
+    ref = api.momentum(which, np.zeros_like(f.U), f.U, f.V, f.W, geo.dx, geo.dy, geo.dz, 1)
+    assert _same(out[geo.interior()], ref[geo.interior()])
+    ghost = out.copy()
+    ghost[geo.interior()] = 0.0
+    assert not ghost.any()  # the ghost layer of the output is untouched
+    g = dom.graph_stats()
+    assert (g.instantiations, g.replays) == (1, 1)
+
+
+@pytest.mark.parametrize("which", ["cdu", "cdv", "cdw"])
+def test_four_procedure_chain_equals_fused_entry(resident, which):
+    dom, fns = resident
+    f = wl.reference_driver_fields(33, 17, 9, seed=5)
+    geo = f.geometry
+    chained, fused = np.full_like(f.U, 7.0), np.zeros_like(f.U)
+    dom.begin_epoch()
+    hc, hf, hu, hv, hw = (dom.bind_real64(a) for a in (chained, fused, f.U, f.V, f.W))
+    spacing = [geo.dx, geo.dy, geo.dz]
+    n = [geo.nx, geo.ny, geo.nz]
+    assert _call(fns, dom, "momentumadvection::set", [hc], [0.0], n) == abi.OK
+    assert _call(fns, dom, f"momentumadvection::{which}div", [hc, hu, hv, hw], spacing, n) == abi.OK
+    assert _call(fns, dom, f"momentumadvection::{which}adv", [hc, hu, hv, hw], spacing, n) == abi.OK
+    assert _call(fns, dom, "momentumadvection::multiply", [hc], [0.5], n) == abi.OK
+    assert _call(fns, dom, f"momentumadvection::{which}", [hf, hu, hv, hw], spacing, n) == abi.OK
+    dom.end_epoch()
+    inner = geo.interior()
+    assert _same(chained[inner], fused[inner])
+    ref = api.momentum(which, np.zeros_like(f.U), f.U, f.V, f.W, geo.dx, geo.dy, geo.dz, 1)
+    assert _same(fused[inner], ref[inner])
+
+
+def test_step_entry_with_scalars(resident):
+    dom, fns = resident
+    geo = wl.Geometry(64, 64, 32, halo=2)
+    f = wl.advection_fields(geo, seed=0, nscalar=3)
+    outs = [np.zeros_like(f.U) for _ in range(6)]
+    dom.begin_epoch()
+    h_out = [dom.bind_real64(a) for a in outs]
+    h_in = [dom.bind_real64(a) for a in f.arrays()]
+    arrays = [*h_out[:3], *h_in[:3], *h_in[3:], *h_out[3:]]
+    assert _call(fns, dom, "advection::step3", arrays, [geo.dx, geo.dy, geo.dz],
+                 [geo.nx, geo.ny, geo.nz, geo.halo]) == abi.OK
+    dom.end_epoch()
+    ref = api.advection_step({"U": f.U, "V": f.V, "W": f.W}, geo.dx, geo.dy, geo.dz, geo.halo, f.scalars)
+    inner = geo.interior()
+    for got, name in zip(outs, ["U", "V", "W", "S0", "S1", "S2"]):
+        assert _same(got[inner], ref[name][inner])
+
+
+@pytest.mark.parametrize("nscalar", [0, 1, 3])
+def test_ten_euler_steps_with_boundary_fill(resident, nscalar):
+    """The 64x64x32 configuration: 10 steps at dt = 0.1, forward Euler, periodic x/y, walls in z."""
+    dom, fns = resident
+    geo = wl.Geometry(64, 64, 32, halo=2)
+    f = wl.advection_fields(geo, seed=0, nscalar=nscalar)
+    dt = 0.1
+    a = [x.copy() for x in f.arrays()]
+    b = [np.zeros_like(x) for x in a]
+    dom.begin_epoch()
+    ha = [dom.bind_real64(x) for x in a]
+    hb = [dom.bind_real64(x) for x in b]
+    grid = [geo.nx, geo.ny, geo.nz, geo.halo]
+    for _ in range(10):
+        arrays = [*hb[:3], *ha[:3], *ha[3:], *hb[3:]]
+        assert _call(fns, dom, f"advection::advance{nscalar}", arrays, [geo.dx, geo.dy, geo.dz, dt], grid) == 0
+        assert _call(fns, dom, f"advection::halo{nscalar}", hb, [], grid) == abi.OK
+        ha, hb = hb, ha
+    dom.end_epoch()
+    # reference: the oracle steps the same recipe
+    state = [x.copy() for x in f.arrays()]
+    for _ in range(10):
+        t = api.advection_step({"U": state[0], "V": state[1], "W": state[2]}, geo.dx, geo.dy, geo.dz, geo.halo,
+                               state[3:])
+        names = ["U", "V", "W", *[f"S{n}" for n in range(nscalar)]]
+        new = [api.euler(x.copy(), t[name], dt, geo.halo) for x, name in zip(state, names)]
+        for n, x in enumerate(new):
+            api.halo(x, 1 if n == 2 else 0, geo.halo)
+        state = new
+    final = a  # after an even number of steps the newest values are in the first buffer set
+    for got, want in zip(final, state):
+        assert _same(got, want)
+
+
+def test_native_mode_and_argument_errors(resident):
+    dom, fns = resident
+    f = wl.reference_driver_fields(8, 8, 8, seed=1)
+    geo = f.geometry
+    out = np.zeros_like(f.U)
+    dom.begin_epoch()
+    hs = [dom.bind_real64(x) for x in (out, f.U, f.V, f.W)]
+    spacing, n = [geo.dx, geo.dy, geo.dz], [geo.nx, geo.ny, geo.nz]
+    assert emission.call(fns, "momentumadvection::cdu", dom.context, abi.NATIVE, hs, spacing, n) == abi.DECLINED
+    assert emission.call(fns, "momentumadvection::cdu", dom.context, 5, hs, spacing, n) == abi.ARGUMENT
+    assert _call(fns, dom, "momentumadvection::cdu", [hs[1], hs[1], hs[2], hs[3]], spacing, n) == abi.ALIAS
+    assert _call(fns, dom, "momentumadvection::cdu", hs, spacing, [geo.nx + 1, geo.ny, geo.nz]) == abi.ARGUMENT
+    assert _call(fns, dom, "momentumadvection::cdu", hs, spacing, [0, geo.ny, geo.nz]) == abi.OK  # no iterations
+    flat = np.zeros((4, 4))
+    hflat = dom.bind_real64(flat)
+    assert _call(fns, dom, "momentumadvection::cdu", [hflat, *hs[1:]], spacing, n) == abi.ARGUMENT
+    other = np.zeros((geo.nz + 3, geo.ny + 2, geo.nx + 2))
+    hother = dom.bind_real64(other)
+    assert _call(fns, dom, "momentumadvection::cdu", [hother, *hs[1:]], spacing, n) == abi.DECLINED
+    dom.end_epoch()
+
+
+def test_budget_too_small_declines_before_any_work(cuda, capfd):
+    lib = native.runtime()
+    dom = ResidentDomain(lib)
+    fns = emission.bind(lib)
+    f = wl.reference_driver_fields(16, 16, 16, seed=2)
+    geo = f.geometry
+    out = np.full_like(f.U, 3.0)
+    dom.begin_epoch(budget=2 * f.U.nbytes)
+    hs = [dom.bind_real64(x) for x in (out, f.U, f.V, f.W)]
+    for _ in range(2):
+        assert _call(fns, dom, "momentumadvection::cdu", hs, [geo.dx, geo.dy, geo.dz],
+                     [geo.nx, geo.ny, geo.nz]) == abi.DECLINED
+    dom.end_epoch()
+    dom.close()
+    assert (out == 3.0).all()
+    assert capfd.readouterr().err.count("budget_warning") == 1
