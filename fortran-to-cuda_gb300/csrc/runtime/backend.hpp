@@ -184,6 +184,20 @@ struct Backend {
     }
     static bool copy(void *dst, const void *src, const CopyPlan &plan, const Box &box, bool to_device, Stream s) {
         const cudaMemcpyKind kind = to_device ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost;
+        const bool full_rows = box.lo[0] == 0 && box.hi[0] == plan.extents[0];
+        const bool full_planes = full_rows && box.lo[1] == 0 && box.hi[1] == plan.extents[1];
+        if (plan.rank == 3 && !full_planes) {
+            // one strided 3-D copy per box (host and device share the layout)
+            cudaMemcpy3DParms p{};
+            const size_t pitch = plan.extents[0] * plan.elem;
+            p.srcPtr = make_cudaPitchedPtr(const_cast<void *>(src), pitch, plan.extents[0], plan.extents[1]);
+            p.dstPtr = make_cudaPitchedPtr(dst, pitch, plan.extents[0], plan.extents[1]);
+            p.srcPos = make_cudaPos(box.lo[0] * plan.elem, box.lo[1], box.lo[2]);
+            p.dstPos = p.srcPos;
+            p.extent = make_cudaExtent((box.hi[0] - box.lo[0]) * plan.elem, box.hi[1] - box.lo[1], box.hi[2] - box.lo[2]);
+            p.kind = kind;
+            return ok(cudaMemcpy3DAsync(&p, s));
+        }
         bool good = true;
         for_each_run(plan, box, [&](size_t off, size_t width, size_t rows, size_t pitch) {
             if (!good) return;

@@ -274,6 +274,31 @@ void check_initialized(const Buffer *b, const Effects &e) {
 
 // ---- transfers ------------------------------------------------------------------------------
 
+Box bounding(const Region &r);
+
+// The region actually moved for a needed transfer `r`: the whole array or the
+// bounding box of `r` when that moves at most a quarter more bytes and cannot
+// overwrite values only the destination holds; `r` itself otherwise. Fewer,
+// larger copies keep the copy engines busy instead of the host.
+Region widened(const Buffer *b, const Region &r, bool to_device) {
+    if (r.boxes.size() <= 1) return r;
+    Region only_destination = to_device ? b->device_valid : b->host_valid;
+    only_destination.remove(to_device ? b->host_valid : b->device_valid);
+    only_destination = b->defined.clip(only_destination);
+    const size_t need = r.volume();
+    const Box candidates[2] = {b->full(), bounding(r)};
+    for (const Box &cand : candidates) {
+        if ((double)cand.volume() > 1.25 * (double)need) continue;
+        Region clash = only_destination.clip(cand);
+        clash.remove(r);
+        if (!clash.empty()) continue;
+        Region w;
+        w.add(cand);
+        return w;
+    }
+    return r;
+}
+
 void copy_region(Context *c, Buffer *b, const Region &r, bool to_device) {
     Domain *d = c->domain;
     const CopyPlan plan = b->plan();
@@ -360,9 +385,11 @@ void publish_buffer(Context *c, Buffer *b) {
     dirty.remove(b->host_valid);
     if (dirty.empty()) return;
     ensure_stream(c);
-    copy_region(c, b, dirty, false);
+    const Region moved = widened(b, dirty, false);
+    copy_region(c, b, moved, false);
     Region host = b->host_valid;
     host.add(dirty);
+    host.add(b->device_valid.clip(moved));
     settle(c, b, b->defined, host, b->device_valid);
 }
 
@@ -600,9 +627,11 @@ void device_acquire(Context *c, std::vector<Bound> &bound) {
         Region up = needed(b, x.effects);
         up.remove(b->device_valid);
         if (!up.empty()) {
-            copy_region(c, b, up, true);
+            const Region moved = widened(b, up, true);
+            copy_region(c, b, moved, true);
             Region device = b->device_valid;
             device.add(up);
+            device.add(b->host_valid.clip(moved));
             settle(c, b, b->defined, b->host_valid, device);
         }
     }
@@ -626,9 +655,11 @@ void host_acquire(Context *c, std::vector<Bound> &bound) {
         down.remove(x.buffer->host_valid);
         if (!down.empty()) {
             ensure_stream(c);
-            copy_region(c, x.buffer, down, false);
+            const Region moved = widened(x.buffer, down, false);
+            copy_region(c, x.buffer, moved, false);
             Region host = x.buffer->host_valid;
             host.add(down);
+            host.add(x.buffer->device_valid.clip(moved));
             settle(c, x.buffer, x.buffer->defined, host, x.buffer->device_valid);
         }
     }
