@@ -157,6 +157,17 @@ def registry() -> list[Entry]:
     entries += _momentum("V", "cdv", f"{stencils}/cvd.f90", {"div": "44-70", "adv": "73-98", "whole": "105-125"})
     entries += _momentum("W", "cdw", f"{stencils}/cdw.f90", {"div": "44-70", "adv": "73-98", "whole": "105-125"})
     entries += _step_entries()
+    entries += [
+        Entry("stencil::diffuse7", "Diffusion",
+              (_a("b", "out"), _a("a"), _r("dt"), _r("nu"), _r("dx"), _i("nx"), _i("ny"), _i("nz"), _i("halo")),
+              source="compiler/tests/apps/box/stepper.f90:8-30 (diffuse with laplacian)"),
+        Entry("stencil::jacobi5", "Jacobi", (_a("v", "out"), _a("u"), _i("nx"), _i("ny"), _i("halo")),
+              source="compiler/tests/apps/relax/relax.f90:28-33 (one Jacobi sweep)"),
+        Entry("stencil::yee2d", "Yee",
+              (_a("ez", "inout"), _a("hx", "inout"), _a("hy", "inout"), _r("ch"), _r("ce"), _i("nx"), _i("ny"),
+               _i("halo")),
+              source="2-D TM Yee leapfrog (no reference source in the mount)", notes="H task then E task"),
+    ]
     return entries
 
 
@@ -271,8 +282,8 @@ def render_report(entries) -> str:
             "procedure": e.procedure, "entry": e.symbol, "fortran_module": e.fortran_module,
             "fortran_procedure": "run", "template": e.template, "scalars": e.nscalar, "source": e.source,
             "argument_order": ["context", "mode", *[p.name for p in e.params]],
-            "array_parameters": [{"name": p.name, "rank": 3, "dtype": "real64", "written": p.intent != "in"}
-                                 for p in e.arrays()],
+            "array_parameters": [{"name": p.name, "rank": 2 if e.template in ("Jacobi", "Yee") else 3,
+                                  "dtype": "real64", "written": p.intent != "in"} for p in e.arrays()],
             "scalar_parameters": [{"name": p.name, "dtype": "real64" if p.kind == "real" else "integer32",
                                    "passing": "reference"} for p in e.params if p.kind != "array"],
             "definition_changes": [p.name for p in e.arrays() if p.intent == "out"],

@@ -20,6 +20,7 @@
 #include "../kernels/advection_faces.cuh"
 #include "../kernels/advection_kernels.cuh"
 #include "../kernels/procedures.cuh"
+#include "../kernels/stencils.cuh"
 #include "entry_runner.hpp"
 
 namespace f2c::entries {
@@ -75,11 +76,11 @@ void add_cdw_u(Sections &s, const Geometry &g) { add_box(s, g, -1, 0, 0, 0, 0, 1
 void add_cdw_v(Sections &s, const Geometry &g) { add_box(s, g, 0, 0, -1, 0, 0, 1); }
 
 struct Use {
-    fort_buffer_t handle;
-    bool written;
-    bool overwritten;   // every written element is written (an exact overwrite)
-    bool read;
-    bool intent_out;
+    fort_buffer_t handle = 0;
+    bool written = false;
+    bool overwritten = false; // every written element is written (an exact overwrite)
+    bool read = false;
+    bool intent_out = false;
     Sections reads, writes;
 };
 
@@ -129,6 +130,72 @@ const void *procedure_function(Template t) {
     }
 }
 
+int enqueue_one(const EntryCall &call, fort_scope_kernel_v1 kernel, void *argument, size_t argument_size,
+                std::deque<Use> &uses, uint64_t key) {
+    void *arguments[1] = {argument};
+    kernel.version = FORT_SCOPE_GRAPH_ABI_VERSION;
+    kernel.arguments = arguments;
+    kernel.argument_count = 1;
+    std::vector<fort_scope_plan_binding> bindings;
+    for (auto &u : uses) {
+        fort_scope_plan_binding b{};
+        b.buffer = u.handle;
+        b.access.read_count = u.reads.size();
+        b.access.reads = u.reads.size() ? u.reads.data() : nullptr;
+        if (u.written) {
+            b.access.write_count = u.writes.size();
+            b.access.writes = u.writes.data();
+            if (u.overwritten) {
+                b.access.overwrite_count = u.writes.size();
+                b.access.overwrites = b.access.writes;
+            }
+        }
+        bindings.push_back(b);
+    }
+    fort_scope_graph_task_v1 task{};
+    task.kernel = kernel;
+    task.bindings = bindings.data();
+    task.binding_count = bindings.size();
+    const size_t sizes[1] = {argument_size};
+    return fort_scope_graph_enqueue_v1(call.context, key, &task, sizes);
+}
+
+// The Yee step is two tasks: H from E, then E from H.
+int enqueue_yee(const EntryCall &call, const Geometry &g, std::deque<Use> &uses, std::vector<void *> &devices,
+                long long sx) {
+    YeeArgs y{static_cast<double *>(devices[0]), static_cast<double *>(devices[1]), static_cast<double *>(devices[2]),
+              *call.reals[0], *call.reals[1], (int)g.n[0], (int)g.n[1], (int)g.h, sx};
+    const dim3 grid = yee_grid(y);
+    fort_scope_kernel_v1 k{};
+    k.grid[0] = grid.x; k.grid[1] = grid.y; k.grid[2] = 1;
+    k.block[0] = kYeeBX; k.block[1] = kYeeBY; k.block[2] = 1;
+    // H task: Ez read at (i, j), (i+1, j), (i, j+1); Hx, Hy read and written on the interior
+    std::deque<Use> h(3);
+    for (int n = 0; n < 3; ++n) h[n].handle = uses[n].handle;
+    add_box(h[0].reads, g, 0, 1, 0, 0, 0, 0);
+    add_box(h[0].reads, g, 0, 0, 0, 1, 0, 0);
+    for (int n = 1; n < 3; ++n) {
+        h[n].written = h[n].overwritten = true;
+        add_interior(h[n].reads, g);
+        add_interior(h[n].writes, g);
+    }
+    k.function = (const void *)yee_h_kernel;
+    if (int s = enqueue_one(call, k, &y, sizeof y, h, call.code_key)) return s;
+    // E task: Hy read at (i-1, j), Hx at (i, j-1); Ez read and written on the interior
+    std::deque<Use> e(3);
+    for (int n = 0; n < 3; ++n) e[n].handle = uses[n].handle;
+    e[0].written = e[0].overwritten = true;
+    add_interior(e[0].reads, g);
+    add_interior(e[0].writes, g);
+    add_box(e[1].reads, g, 0, 0, -1, 0, 0, 0);
+    add_box(e[2].reads, g, -1, 0, 0, 0, 0, 0);
+    k.function = (const void *)yee_e_kernel;
+    const int s = enqueue_one(call, k, &y, sizeof y, e, call.code_key ^ 0x9e3779b97f4a7c15ULL);
+    // the H task was accepted: a failure now leaves half a step behind
+    if (s && s != FORT_SCOPE_EXECUTION) return fort_scope_execution_error(call.context, "second task of a step refused");
+    return s;
+}
+
 int run(const EntryCall &call) {
     if (fort_scope_abi_version() != FORT_SCOPE_ABI_VERSION)
         return fort_scope_report_error(FORT_SCOPE_ARGUMENT, "incompatible shared runtime ABI");
@@ -175,7 +242,16 @@ int run(const EntryCall &call) {
     case Template::Halo:
         for (int n = 0; n < call.narrays; ++n) role(n, true, true, true, false);
         break;
+    case Template::Diffusion: case Template::Jacobi:
+        role(0, false, true, true, true);
+        role(1, true, false, false, false);
+        break;
+    case Template::Yee:
+        for (int n = 0; n < 3; ++n) role(n, true, true, true, false);
+        break;
     }
+    const bool plane2d = t == Template::Jacobi || t == Template::Yee;
+    const int rank = plane2d ? 2 : 3;
     // writable arguments must not alias any other argument
     for (int a = 0; a < call.narrays; ++a)
         for (int b = 0; b < a; ++b)
@@ -187,23 +263,24 @@ int run(const EntryCall &call) {
     for (int n = 0; n < call.narrays; ++n) {
         fort_scope_layout layout{};
         if (int s = fort_scope_layout_get(call.context, uses[n].handle, &layout)) return s;
-        if (layout.rank != 3 || layout.type != FORT_SCOPE_REAL64 || layout.element_bytes != sizeof(double))
+        if ((int)layout.rank != rank || layout.type != FORT_SCOPE_REAL64 || layout.element_bytes != sizeof(double))
             return fort_scope_report_error(FORT_SCOPE_ARGUMENT, "entry layout/type mismatch");
         if (n == 0) {
-            for (int d = 0; d < 3; ++d) g.ext[d] = layout.extents[d];
+            for (int d = 0; d < 3; ++d) g.ext[d] = d < rank ? layout.extents[d] : 1;
         } else {
-            for (int d = 0; d < 3; ++d)
+            for (int d = 0; d < rank; ++d)
                 if (layout.extents[d] != g.ext[d]) return declined(); // templates take one shape per call
         }
     }
     // ---- loop extents and the interior offset ----
     const int *ints[8];
     for (int n = 0; n < call.nints; ++n) ints[n] = call.ints[n];
-    for (int d = 0; d < 3; ++d) g.n[d] = *ints[d];
-    g.h = procedure ? 1 : *ints[3];
+    for (int d = 0; d < rank; ++d) g.n[d] = *ints[d];
+    if (plane2d) g.n[2] = 1;
+    g.h = procedure ? 1 : *ints[rank];
     if (g.n[0] < 1 || g.n[1] < 1 || g.n[2] < 1) return FORT_SCOPE_OK; // no iterations: nothing to do
     if (g.h < 1) return fort_scope_report_error(FORT_SCOPE_ARGUMENT, "halo width must be at least one");
-    for (int d = 0; d < 3; ++d)
+    for (int d = 0; d < rank; ++d)
         if ((size_t)(g.n[d] + 2 * g.h) > g.ext[d])
             return fort_scope_report_error(FORT_SCOPE_ARGUMENT, "invalid physical entry footprint");
     if (halo) {
@@ -255,6 +332,17 @@ int run(const EntryCall &call) {
         }
         break;
     }
+    case Template::Diffusion:
+        out_sections(uses[0]);
+        add_cross(uses[1].reads, g);
+        break;
+    case Template::Jacobi:
+        out_sections(uses[0]);
+        add_box(uses[1].reads, g, -1, 1, 0, 0, 0, 0);
+        add_box(uses[1].reads, g, 0, 0, -1, 1, 0, 0);
+        break;
+    case Template::Yee:
+        break; // two tasks with their own sections, below
     case Template::Halo: {
         for (int n = 0; n < call.narrays; ++n) {
             Use &u = uses[n];
@@ -290,6 +378,8 @@ int run(const EntryCall &call) {
     AdvArgs adv{};
     ProcedureArgs proc{};
     HaloArgs hal{};
+    DiffusionArgs diff{};
+    JacobiArgs jac{};
     fort_scope_kernel_v1 kernel{};
     kernel.version = FORT_SCOPE_GRAPH_ABI_VERSION;
     void *argument = nullptr;
@@ -340,6 +430,30 @@ int run(const EntryCall &call) {
         faces_spec_ns<7>(ns, adv, kernel);
         argument = &adv;
         argument_size = sizeof adv;
+    } else if (t == Template::Diffusion) {
+        diff.b = dev(0);
+        diff.a = dev(1);
+        diff.dtnu = *call.reals[0] * *call.reals[1];
+        diff.dx2 = *call.reals[2] * *call.reals[2];
+        diff.dx2_pow2 = power_of_two(diff.dx2, &diff.dx2_exp) ? 1 : 0;
+        diff.nx = (int)g.n[0]; diff.ny = (int)g.n[1]; diff.nz = (int)g.n[2]; diff.h = (int)g.h;
+        diff.sx = sx; diff.plane = plane;
+        kernel.function = (const void *)diffusion7_kernel;
+        const dim3 grid = diffusion_grid(diff);
+        kernel.grid[0] = grid.x; kernel.grid[1] = grid.y; kernel.grid[2] = grid.z;
+        kernel.block[0] = kDiffBX; kernel.block[1] = kDiffBY; kernel.block[2] = 1;
+        argument = &diff;
+        argument_size = sizeof diff;
+    } else if (t == Template::Jacobi) {
+        jac = JacobiArgs{dev(1), dev(0), (int)g.n[0], (int)g.n[1], (int)g.h, sx};
+        kernel.function = (const void *)jacobi5_kernel;
+        const dim3 grid = jacobi_grid(jac);
+        kernel.grid[0] = grid.x; kernel.grid[1] = grid.y; kernel.grid[2] = grid.z;
+        kernel.block[0] = kJacBX; kernel.block[1] = kJacBY; kernel.block[2] = 1;
+        argument = &jac;
+        argument_size = sizeof jac;
+    } else if (t == Template::Yee) {
+        return enqueue_yee(call, g, uses, devices, sx);
     } else {
         hal.count = call.narrays;
         for (int n = 0; n < call.narrays; ++n) {

@@ -23,6 +23,9 @@ enum class Template : int {
     Step = 11,      // advection::step: U, V, W and scalar tendencies in one launch
     StepAdvance = 12, // advection::advance: forward-Euler step, double-buffered
     Halo = 13,      // advection::halo: periodic x/y, walls in z
+    Diffusion = 14, // stencil::diffuse7 (box app stepper)
+    Jacobi = 15,    // stencil::jacobi5 (relax app sweep)
+    Yee = 16,       // stencil::yee2d (H then E)
 };
 
 constexpr int kMaxEntryArrays = 16;

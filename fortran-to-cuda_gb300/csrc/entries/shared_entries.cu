@@ -689,3 +689,67 @@ extern "C" int cpp_fort_shared_073d04efb82a(fort_scope_t fort_context, int fort_
     call.ints[3] = halo;
     return run_entry(call);
 }
+
+// stencil::diffuse7: compiler/tests/apps/box/stepper.f90:8-30 (diffuse with laplacian)
+extern "C" int cpp_fort_shared_242ee4413593(fort_scope_t fort_context, int fort_mode, fort_buffer_t b_handle, fort_buffer_t a_handle, const double *dt, const double *nu, const double *dx, const int *nx, const int *ny, const int *nz, const int *halo) {
+    EntryCall call{};
+    call.context = fort_context;
+    call.mode = fort_mode;
+    call.kind = Template::Diffusion;
+    call.code_key = 0x29cf3c886ce4c0c3ULL;
+    call.nscalar = 0;
+    call.narrays = 2;
+    call.arrays[0] = b_handle;
+    call.arrays[1] = a_handle;
+    call.nreals = 3;
+    call.reals[0] = dt;
+    call.reals[1] = nu;
+    call.reals[2] = dx;
+    call.nints = 4;
+    call.ints[0] = nx;
+    call.ints[1] = ny;
+    call.ints[2] = nz;
+    call.ints[3] = halo;
+    return run_entry(call);
+}
+
+// stencil::jacobi5: compiler/tests/apps/relax/relax.f90:28-33 (one Jacobi sweep)
+extern "C" int cpp_fort_shared_aa40c606bdea(fort_scope_t fort_context, int fort_mode, fort_buffer_t v_handle, fort_buffer_t u_handle, const int *nx, const int *ny, const int *halo) {
+    EntryCall call{};
+    call.context = fort_context;
+    call.mode = fort_mode;
+    call.kind = Template::Jacobi;
+    call.code_key = 0x3575cd74530954adULL;
+    call.nscalar = 0;
+    call.narrays = 2;
+    call.arrays[0] = v_handle;
+    call.arrays[1] = u_handle;
+    call.nreals = 0;
+    call.nints = 3;
+    call.ints[0] = nx;
+    call.ints[1] = ny;
+    call.ints[2] = halo;
+    return run_entry(call);
+}
+
+// stencil::yee2d: 2-D TM Yee leapfrog (no reference source in the mount)
+extern "C" int cpp_fort_shared_82041a3f2b68(fort_scope_t fort_context, int fort_mode, fort_buffer_t ez_handle, fort_buffer_t hx_handle, fort_buffer_t hy_handle, const double *ch, const double *ce, const int *nx, const int *ny, const int *halo) {
+    EntryCall call{};
+    call.context = fort_context;
+    call.mode = fort_mode;
+    call.kind = Template::Yee;
+    call.code_key = 0x467690fb19941ed3ULL;
+    call.nscalar = 0;
+    call.narrays = 3;
+    call.arrays[0] = ez_handle;
+    call.arrays[1] = hx_handle;
+    call.arrays[2] = hy_handle;
+    call.nreals = 2;
+    call.reals[0] = ch;
+    call.reals[1] = ce;
+    call.nints = 3;
+    call.ints[0] = nx;
+    call.ints[1] = ny;
+    call.ints[2] = halo;
+    return run_entry(call);
+}

@@ -761,3 +761,73 @@ module fort_shared_073d04efb82a
     end function
   end interface
 end module fort_shared_073d04efb82a
+
+module fort_shared_242ee4413593
+  use iso_c_binding
+  implicit none
+  private
+  public :: run
+  interface
+    function run( &
+      fort_context, fort_mode, b_handle, a_handle, dt, nu, dx, nx, ny, nz, halo) bind(C, name='cpp_fort_shared_242ee4413593') result(fort_status)
+      import :: c_int, c_int64_t, c_double
+      integer(c_int) :: fort_status
+      integer(c_int64_t), value :: fort_context
+      integer(c_int), value :: fort_mode
+      integer(c_int64_t), value :: b_handle
+      integer(c_int64_t), value :: a_handle
+      real(c_double), intent(in) :: dt
+      real(c_double), intent(in) :: nu
+      real(c_double), intent(in) :: dx
+      integer(c_int), intent(in) :: nx
+      integer(c_int), intent(in) :: ny
+      integer(c_int), intent(in) :: nz
+      integer(c_int), intent(in) :: halo
+    end function
+  end interface
+end module fort_shared_242ee4413593
+
+module fort_shared_aa40c606bdea
+  use iso_c_binding
+  implicit none
+  private
+  public :: run
+  interface
+    function run( &
+      fort_context, fort_mode, v_handle, u_handle, nx, ny, halo) bind(C, name='cpp_fort_shared_aa40c606bdea') result(fort_status)
+      import :: c_int, c_int64_t, c_double
+      integer(c_int) :: fort_status
+      integer(c_int64_t), value :: fort_context
+      integer(c_int), value :: fort_mode
+      integer(c_int64_t), value :: v_handle
+      integer(c_int64_t), value :: u_handle
+      integer(c_int), intent(in) :: nx
+      integer(c_int), intent(in) :: ny
+      integer(c_int), intent(in) :: halo
+    end function
+  end interface
+end module fort_shared_aa40c606bdea
+
+module fort_shared_82041a3f2b68
+  use iso_c_binding
+  implicit none
+  private
+  public :: run
+  interface
+    function run( &
+      fort_context, fort_mode, ez_handle, hx_handle, hy_handle, ch, ce, nx, ny, halo) bind(C, name='cpp_fort_shared_82041a3f2b68') result(fort_status)
+      import :: c_int, c_int64_t, c_double
+      integer(c_int) :: fort_status
+      integer(c_int64_t), value :: fort_context
+      integer(c_int), value :: fort_mode
+      integer(c_int64_t), value :: ez_handle
+      integer(c_int64_t), value :: hx_handle
+      integer(c_int64_t), value :: hy_handle
+      real(c_double), intent(in) :: ch
+      real(c_double), intent(in) :: ce
+      integer(c_int), intent(in) :: nx
+      integer(c_int), intent(in) :: ny
+      integer(c_int), intent(in) :: halo
+    end function
+  end interface
+end module fort_shared_82041a3f2b68

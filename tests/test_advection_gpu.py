@@ -172,3 +172,20 @@ def test_argument_errors(cuda):
     bad = native.make_grid(4, 4, 4, 1, 1.0, 1.0, 1.0, sx=3)
     with pytest.raises(native.NativeError):
         native.advection(bad, t.data_ptr(), t.data_ptr(), t.data_ptr())
+
+
+def test_golden_fixtures_on_the_gpu(cuda):
+    from pathlib import Path
+
+    z = np.load(Path(__file__).with_name("golden") / "advection_small.npz")
+    dx, dy, dz = (float(v) for v in z["spacing"])
+    nz, ny, nx = (s - 2 for s in z["U"].shape)
+    geo = wl.Geometry(nx, ny, nz, halo=1, dx=dx, dy=dy, dz=dz)
+    got = _run(cuda, wl.Fields(geo, z["U"], z["V"], z["W"], []))
+    for g, which in zip(got, ("cdu", "cdv", "cdw")):
+        assert np.array_equal(_bits(_interior(g, geo)), _bits(_interior(z[which], geo)))
+    ins = [z[f"h2_in{n}"] for n in range(6)]
+    geo2 = wl.Geometry(12, 10, 6, halo=2)
+    got = _run(cuda, wl.Fields(geo2, *ins[:3], ins[3:]))
+    for n, g in enumerate(got):
+        assert np.array_equal(_bits(_interior(g, geo2)), _bits(_interior(z[f"h2_tend{n}"], geo2)))
