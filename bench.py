@@ -360,6 +360,196 @@ def run_reference(args):
     }), flush=True)
 
 
+def _graph_time(torch, stream, fn, steps, warmup):
+    """Milliseconds per replay of a CUDA graph that captures ``fn(stream)``, timed with events on ``stream``."""
+    with torch.cuda.stream(stream):
+        fn(stream.cuda_stream)
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph, stream=stream):
+        fn(stream.cuda_stream)
+    for _ in range(warmup):
+        graph.replay()
+    torch.cuda.synchronize()
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        start.record(stream)
+        for _ in range(steps):
+            graph.replay()
+        stop.record(stream)
+    torch.cuda.synchronize()
+    return start.elapsed_time(stop) / steps
+
+
+def run_batched(args):
+    """64 uneven instances (nx, ny from {64..256}, nz from {32, 64, 96}, seed 1), U, V, W + 1 scalar."""
+    import torch
+
+    from compiler import native, scheduling
+    from compiler import workloads as wl
+
+    torch.cuda.set_device(0)
+    shapes = wl.ensemble_shapes(64, seed=1)
+    nscalar = 1
+    inst = []
+    for n, (nx, ny, nz) in enumerate(shapes):
+        geo = wl.Geometry(nx, ny, nz, halo=HALO, dx=DX, dy=DY, dz=DZ)
+        ins = wl.advection_fields_device(geo, 1000 + n, nscalar, torch)
+        outs = [torch.empty_like(t) for t in ins]
+        p, q = [t.data_ptr() for t in ins], [t.data_ptr() for t in outs]
+        grid = native.make_grid(nx, ny, nz, HALO, DX, DY, DZ)
+        inst.append((geo, ins, outs, grid, native.make_fields(*p[:3], *q[:3], scalars=p[3:], scalar_out=q[3:])))
+    points = sum(x[0].points for x in inst)
+    stream = torch.cuda.Stream()
+    gpu = torch.cuda.get_device_name(0)
+
+    def batch_time(kz, steps=5, warmup=3):
+        batch = native.Batch([x[3] for x in inst], [x[4] for x in inst], kz=kz)
+        ws = torch.empty(batch.workspace_bytes(), dtype=torch.uint8, device="cuda")
+        batch.prepare(ws.data_ptr(), ws.numel(), stream.cuda_stream)
+        return _graph_time(torch, stream, lambda s: batch.step(s), steps, warmup) * 1e-3, batch, ws
+
+    tuned = None
+    if args.tune:
+        tuned = scheduling.tune(shapes, gpu, nscalar, lambda kz: batch_time(kz)[0])
+    kz = scheduling.kz_for(shapes, gpu, nscalar)
+    with ClockSampler(0) as sampler:
+        batched_s, _, _ = batch_time(kz, steps=args.steps, warmup=args.warmup)
+
+        def one_at_a_time(s):
+            for geo, ins, outs, grid, fields in inst:
+                p, q = [t.data_ptr() for t in ins], [t.data_ptr() for t in outs]
+                native.advection(grid, *p[:3], *q[:3], scalars=p[3:], scalar_out=q[3:], stream=s)
+
+        plain_ms = _graph_time(torch, stream, one_at_a_time, args.steps, args.warmup)
+
+        def per_procedure(s):
+            # the reference resident build's structure: set, div, adv, multiply per component, one instance
+            # at a time, and the scalar as its own launch
+            ops = ((native.CDU_DIV, native.CDU_ADV), (native.CDV_DIV, native.CDV_ADV), (native.CDW_DIV, native.CDW_ADV))
+            for geo, ins, outs, grid, fields in inst:
+                u, v, w = (t.data_ptr() for t in ins[:3])
+                for out, (div, adv) in zip(outs[:3], ops):
+                    o = out.data_ptr()
+                    native.procedure(native.SET, grid, o, value=0.0, stream=s)
+                    native.procedure(div, grid, o, u, v, w, stream=s)
+                    native.procedure(adv, grid, o, u, v, w, stream=s)
+                    native.procedure(native.MULTIPLY, grid, o, value=0.5, stream=s)
+                native.advection(grid, u, v, w, scalars=[ins[3].data_ptr()], scalar_out=[outs[3].data_ptr()],
+                                 stream=s)
+
+        procedure_ms = _graph_time(torch, stream, per_procedure, max(3, args.steps // 4), args.warmup)
+    value = points / batched_s / 1e9
+    plain = points / (plain_ms * 1e-3) / 1e9
+    procedure_rate = points / (procedure_ms * 1e-3) / 1e9
+    print(json.dumps({
+        "metric": "batched ensemble Gpts/s (64 uneven instances, U,V,W + 1 scalar, one persistent launch per step)",
+        "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": batched_s * 1e3, "higher_is_better": True, "dtype": "f64", "data": "synthetic (seeded)",
+        "config": {"workload": "64 instances, nx,ny in {64..256}, nz in {32,64,96}, seed 1", "points": points,
+                   "kz": {scheduling.bucket(nz): k for (_, _, nz), k in zip(shapes, kz)}},
+        "plain_resident": {"value": plain, "ms_per_step": plain_ms,
+                           "how": "64 launches of the single-instance kernel per step, one graph"},
+        "reference_style_resident": {"value": procedure_rate, "ms_per_step": procedure_ms,
+                                     "how": "per instance: set, div, adv, multiply for U, V, W + 1 scalar launch "
+                                            "(13 launches), 64 instances one at a time, one graph"},
+        "batched_over_plain": value / plain, "batched_over_reference_style": value / procedure_rate,
+        "tuned": tuned, "gpu_launches": args.steps,
+        "clocks": sampler.summary()}), flush=True)
+
+
+def run_small(args):
+    """The 64 x 64 x 32 configuration: 10 forward-Euler steps at dt = 0.1 with the boundary fill, as one graph."""
+    import torch
+
+    from compiler import native
+    from compiler import workloads as wl
+
+    geo = wl.Geometry(64, 64, 32, halo=HALO, dx=DX, dy=DY, dz=DZ)
+    f = wl.advection_fields(geo, seed=0, nscalar=0)
+    a = [torch.from_numpy(x).cuda() for x in f.arrays()]
+    b = [torch.zeros_like(x) for x in a]
+    grid = native.make_grid(geo.nx, geo.ny, geo.nz, geo.halo, geo.dx, geo.dy, geo.dz)
+
+    def ten_steps(s):
+        src, dst = a, b
+        for _ in range(10):
+            native.advection(grid, *[t.data_ptr() for t in src], *[t.data_ptr() for t in dst], mode=native.ADVANCE,
+                             dt=0.1, stream=s)
+            native.halo_fill(grid, [t.data_ptr() for t in dst], [0, 0, 1], stream=s)
+            src, dst = dst, src
+
+    stream = torch.cuda.Stream()
+    ms = _graph_time(torch, stream, ten_steps, args.steps, args.warmup)
+    print(json.dumps({
+        "metric": "64x64x32 advance step latency (U,V,W Euler dt=0.1 + boundary fill; 10 steps per graph)",
+        "value": ms * 1e3 / 10, "unit": "us/step", "higher_is_better": False, "gpts_per_s": geo.points * 10 / ms / 1e6,
+        "steps": args.steps * 10, "warmup": args.warmup, "dtype": "f64", "data": "synthetic (seeded sine modes)",
+        "config": {"workload": "64x64x32 halo 2, 2 launches per step", "l2": "resident in L2: latency, not roofline"},
+        "gpu_launches": args.steps * 20}), flush=True)
+
+
+def run_stencils(args):
+    """Diffusion 7-point on 384^3, Jacobi 5-point on 8192^2, Yee on 4096^2; uniform[0,1) inputs, zero boundaries."""
+    import ctypes
+
+    import torch
+
+    from compiler import native
+
+    lib = native.load()
+    lib.f2c_diffusion7_v1.argtypes = [ctypes.POINTER(native.Grid), ctypes.c_void_p, ctypes.c_void_p,
+                                      ctypes.c_double, ctypes.c_double, ctypes.c_void_p]
+    lib.f2c_jacobi5_v1.argtypes = [ctypes.c_void_p] * 2 + [ctypes.c_int64] * 4 + [ctypes.c_void_p]
+    lib.f2c_yee2d_v1.argtypes = [ctypes.c_void_p] * 3 + [ctypes.c_int64] * 4 + [ctypes.c_double] * 2 + [ctypes.c_void_p]
+    peak, _ = hbm_peak()
+    g = torch.Generator(device="cuda").manual_seed(0)
+    stream = torch.cuda.Stream()
+    results = {}
+
+    def field(shape):
+        t = torch.zeros(shape, dtype=torch.float64, device="cuda")
+        inner = t[(slice(1, -1),) * len(shape)]
+        inner.copy_(torch.rand(inner.shape, generator=g, device="cuda", dtype=torch.float64))
+        return t
+
+    n = 384
+    a, b = field((n + 2,) * 3), torch.zeros((n + 2,) * 3, dtype=torch.float64, device="cuda")
+    grid = native.make_grid(n, n, n, 1, 1.0, 1.0, 1.0)
+
+    def diffuse(s):
+        native.check(lib.f2c_diffusion7_v1(ctypes.byref(grid), a.data_ptr(), b.data_ptr(), 0.125, 1.0, s))
+        native.check(lib.f2c_diffusion7_v1(ctypes.byref(grid), b.data_ptr(), a.data_ptr(), 0.125, 1.0, s))
+
+    ms = _graph_time(torch, stream, diffuse, args.steps, args.warmup) / 2
+    results["diffusion7_384^3"] = {"ms_per_step": ms, "gpts_per_s": n ** 3 / ms / 1e6,
+                                   "hbm_frac": 16 * n ** 3 / (ms * 1e-3) / 1e9 / peak, "fp64_ops_per_point": 9}
+    del a, b
+    n = 8192
+    u, v = field((n + 2, n + 2)), torch.zeros((n + 2, n + 2), dtype=torch.float64, device="cuda")
+
+    def sweep(s):
+        native.check(lib.f2c_jacobi5_v1(u.data_ptr(), v.data_ptr(), n, n, 1, n + 2, s))
+        native.check(lib.f2c_jacobi5_v1(v.data_ptr(), u.data_ptr(), n, n, 1, n + 2, s))
+
+    ms = _graph_time(torch, stream, sweep, args.steps, args.warmup) / 2
+    results["jacobi5_8192^2"] = {"ms_per_step": ms, "gpts_per_s": n * n / ms / 1e6,
+                                 "hbm_frac": 16 * n * n / (ms * 1e-3) / 1e9 / peak, "fp64_ops_per_point": 3}
+    del u, v
+    n = 4096
+    ez, hx, hy = (field((n + 2, n + 2)) for _ in range(3))
+
+    def leap(s):
+        native.check(lib.f2c_yee2d_v1(ez.data_ptr(), hx.data_ptr(), hy.data_ptr(), n, n, 1, n + 2, 0.5, 0.7, s))
+
+    ms = _graph_time(torch, stream, leap, args.steps, args.warmup)
+    results["yee2d_4096^2"] = {"ms_per_step": ms, "gpts_per_s": n * n / ms / 1e6,
+                               "hbm_frac": 48 * n * n / (ms * 1e-3) / 1e9 / peak, "fp64_ops_per_point": 11}
+    print(json.dumps({"metric": "generality stencils Gpts/s (100-step graphs)", "unit": UNIT, "dtype": "f64",
+                      "steps": args.steps, "warmup": args.warmup, "results": results,
+                      "peak_hbm_gbs": peak}), flush=True)
+
+
 def main():
     parser = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     parser.add_argument("--gpus", type=int, default=1)
@@ -369,6 +559,9 @@ def main():
     parser.add_argument("--no-cpu-baseline", action="store_true")
     parser.add_argument("--size", type=int, nargs=3, metavar=("NX", "NY", "NZ"),
                         help="override the grid (profiling captures of a smaller case)")
+    parser.add_argument("--workload", choices=("advection", "batched", "small", "stencils", "serving"),
+                        default="advection", help="the headline step (default) or another configuration")
+    parser.add_argument("--tune", action="store_true", help="batched: run the z-chunk autotuner first")
     args = parser.parse_args()
     args.warmup = max(3, args.warmup)
     if args.size:
@@ -376,6 +569,16 @@ def main():
         NX, NY, NZ = args.size
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "batched":
+        run_batched(args)
+    elif args.workload == "small":
+        run_small(args)
+    elif args.workload == "stencils":
+        run_stencils(args)
+    elif args.workload == "serving":
+        from compiler.serving import bench_main
+
+        bench_main(args)
     else:
         run_gb300(args)
 

@@ -152,6 +152,12 @@ class Fields(ctypes.Structure):
 TENDENCY, ADVANCE = 0, 1
 
 
+class BatchPlan(ctypes.Structure):
+    _fields_ = [("workspace", ctypes.c_void_p), ("workspace_bytes", ctypes.c_size_t), ("count", ctypes.c_int32),
+                ("nscalar", ctypes.c_int32), ("mask", ctypes.c_int32), ("items", ctypes.c_int32),
+                ("ctas", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+
+
 @lru_cache(maxsize=1)
 def load() -> ctypes.CDLL:
     """Load the native library (building it first if needed). Raises if it cannot be had."""
@@ -169,6 +175,17 @@ def load() -> ctypes.CDLL:
     lib.f2c_halo_fill_v1.restype = ctypes.c_int
     lib.f2c_fp64_rate_v1.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_double)]
     lib.f2c_fp64_rate_v1.restype = ctypes.c_int
+    lib.f2c_batch_workspace_bytes_v1.argtypes = [ctypes.POINTER(Grid), ctypes.POINTER(ctypes.c_int32), ctypes.c_int32]
+    lib.f2c_batch_workspace_bytes_v1.restype = ctypes.c_size_t
+    lib.f2c_batch_prepare_v1.argtypes = [ctypes.POINTER(Grid), ctypes.POINTER(Fields), ctypes.POINTER(ctypes.c_int32),
+                                         ctypes.c_int32, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p,
+                                         ctypes.POINTER(BatchPlan)]
+    lib.f2c_batch_prepare_v1.restype = ctypes.c_int
+    lib.f2c_batch_step_v1.argtypes = [ctypes.POINTER(BatchPlan), ctypes.c_void_p]
+    lib.f2c_batch_step_v1.restype = ctypes.c_int
+    lib.f2c_procedure_v1.argtypes = [ctypes.c_int, ctypes.POINTER(Grid), ctypes.c_void_p, ctypes.c_void_p,
+                                     ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double, ctypes.c_void_p]
+    lib.f2c_procedure_v1.restype = ctypes.c_int
     return lib
 
 
@@ -222,3 +239,45 @@ def fp64_rate(op: int, scratch_ptr: int, scratch_elems: int) -> float:
     out = ctypes.c_double(0.0)
     check(load().f2c_fp64_rate_v1(op, ctypes.c_void_p(scratch_ptr), scratch_elems, ctypes.byref(out)))
     return out.value
+
+
+def make_fields(u, v, w, ut=None, vt=None, wt=None, scalars=(), scalar_out=(), mode=TENDENCY, dt=0.0) -> Fields:
+    fields = Fields()
+    fields.u, fields.v, fields.w = u, v, w
+    fields.ut, fields.vt, fields.wt = ut, vt, wt
+    fields.nscalar = len(scalars)
+    fields.mode = mode
+    fields.dt = dt
+    for n, (s, st) in enumerate(zip(scalars, scalar_out, strict=True)):
+        fields.s[n] = s
+        fields.st[n] = st
+    return fields
+
+
+class Batch:
+    """A prepared batch: instances' grids and fields, a device workspace (caller-owned pointer) and the plan."""
+
+    def __init__(self, grids, fields, kz=None):
+        self.count = len(grids)
+        self.grids = (Grid * self.count)(*grids)
+        self.fields = (Fields * self.count)(*fields)
+        self.kz = (ctypes.c_int32 * self.count)(*kz) if kz else None
+        self.plan = BatchPlan()
+
+    def workspace_bytes(self) -> int:
+        return load().f2c_batch_workspace_bytes_v1(self.grids, self.kz, self.count)
+
+    def prepare(self, workspace: int, nbytes: int, stream: int = 0) -> None:
+        check(load().f2c_batch_prepare_v1(self.grids, self.fields, self.kz, self.count, ctypes.c_void_p(workspace),
+                                          nbytes, ctypes.c_void_p(stream), ctypes.byref(self.plan)))
+
+    def step(self, stream: int = 0) -> None:
+        check(load().f2c_batch_step_v1(ctypes.byref(self.plan), ctypes.c_void_p(stream)))
+
+
+SET, MULTIPLY, CDU_DIV, CDU_ADV, CDV_DIV, CDV_ADV, CDW_DIV, CDW_ADV = range(8)
+
+
+def procedure(op: int, grid: Grid, out, u=None, v=None, w=None, value=0.0, stream=0) -> None:
+    """One reference procedure as one launch (device pointers)."""
+    check(load().f2c_procedure_v1(op, ctypes.byref(grid), out, u, v, w, value, ctypes.c_void_p(stream)))

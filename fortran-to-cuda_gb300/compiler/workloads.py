@@ -170,3 +170,38 @@ def ensemble_shapes(count: int = 64, seed: int = 1):
         nz = ENSEMBLE_Z[int(rng.integers(0, len(ENSEMBLE_Z)))]
         shapes.append((nx, ny, nz))
     return shapes
+
+
+def advection_fields_device(geo: Geometry, seed: int, nscalar: int, torch, device="cuda"):
+    """The sine-mode recipe generated on the GPU with torch's generator (fast; not bit-equal to the numpy draw).
+
+    Used by the benchmark's large ensembles; parity tests use ``advection_fields``.
+    Returns a list of device tensors U, V, W, S1.. of shape ``geo.shape``.
+    """
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    h = geo.halo
+    lx, ly, lz = geo.nx * geo.dx, geo.ny * geo.dy, geo.nz * geo.dz
+    out = []
+    for stagger in ((True, False, False), (False, True, False), (False, False, True)):
+        x, y, z = (torch.as_tensor(c, device=device) for c in _coordinates(geo, stagger))
+        field = torch.zeros(geo.shape, dtype=torch.float64, device=device)
+        for _ in range(4):
+            k = torch.randint(1, 5, (3,), generator=g, device=device).tolist()
+            phi = float(torch.rand((), generator=g, device=device, dtype=torch.float64)) * 2.0 * math.pi
+            field += torch.sin((2.0 * math.pi * k[2] / lz) * z[:, None, None] + (2.0 * math.pi * k[1] / ly) *
+                               y[None, :, None] + ((2.0 * math.pi * k[0] / lx) * x[None, None, :] + phi))
+        inner = field[h:h + geo.nz, h:h + geo.ny, h:h + geo.nx]
+        inner += 0.05 * torch.randn(inner.shape, generator=g, device=device, dtype=torch.float64)
+        out.append(field)
+    for n in range(nscalar):
+        s = torch.zeros(geo.shape, dtype=torch.float64, device=device)
+        inner = s[h:h + geo.nz, h:h + geo.ny, h:h + geo.nx]
+        if n == 0:
+            inner.copy_(280.0 + 20.0 * torch.rand(inner.shape, generator=g, device=device, dtype=torch.float64))
+        elif n == 1:
+            inner.copy_(0.02 * torch.rand(inner.shape, generator=g, device=device, dtype=torch.float64))
+        else:
+            s.copy_(torch.as_tensor(blob(geo, centre=(0.5, 0.5, 0.25 + 0.25 * (n - 2))), device=device))
+        out.append(s)
+    return out

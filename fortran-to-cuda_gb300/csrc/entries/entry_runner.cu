@@ -98,7 +98,7 @@ void faces_spec(const AdvArgs &a, fort_scope_kernel_v1 &k) {
     k.function = (const void *)advection_faces_kernel<NS, MASK>;
     k.grid[0] = (a.nx + kFaceTX - 1) / kFaceTX;
     k.grid[1] = (a.ny + kFaceTY - 1) / kFaceTY;
-    k.grid[2] = (a.nz + kFaceKZ - 1) / kFaceKZ;
+    k.grid[2] = (a.nz + a.kz - 1) / a.kz;
     k.block[0] = kFaceTX;
     k.block[1] = kFaceTY + 1;
     k.block[2] = 1;
@@ -211,7 +211,7 @@ int run(const EntryCall &call) {
     const int ns = call.nscalar;
     const bool step = t == Template::Step || t == Template::StepAdvance;
     const bool halo = t == Template::Halo;
-    const bool procedure = !step && !halo;
+    const bool procedure = static_cast<int>(t) <= static_cast<int>(Template::Cdw); // MomentumAdvection procedures
 
     // ---- roles of the arrays, in the declared argument order ----
     std::deque<Use> uses(call.narrays);
@@ -393,6 +393,7 @@ int run(const EntryCall &call) {
         adv.nx = (int)g.n[0]; adv.ny = (int)g.n[1]; adv.nz = (int)g.n[2]; adv.h = (int)g.h;
         adv.sx = sx; adv.plane = plane;
         adv.c = make_coefficients(*call.reals[0], *call.reals[1], *call.reals[2]);
+        adv.kz = chunk_depth(adv.nx, adv.ny, adv.nz);
         if (t == Template::Cdu) faces_spec_ns<1>(0, adv, kernel);
         else if (t == Template::Cdv) faces_spec_ns<2>(0, adv, kernel);
         else faces_spec_ns<4>(0, adv, kernel);
@@ -427,6 +428,7 @@ int run(const EntryCall &call) {
         adv.nx = (int)g.n[0]; adv.ny = (int)g.n[1]; adv.nz = (int)g.n[2]; adv.h = (int)g.h;
         adv.sx = sx; adv.plane = plane;
         adv.c = make_coefficients(*call.reals[0], *call.reals[1], *call.reals[2]);
+        adv.kz = chunk_depth(adv.nx, adv.ny, adv.nz);
         faces_spec_ns<7>(ns, adv, kernel);
         argument = &adv;
         argument_size = sizeof adv;

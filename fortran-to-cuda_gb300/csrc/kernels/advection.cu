@@ -8,6 +8,7 @@
 // launches per procedure (compiler/emission/cuda/kernels.py:37-69).
 #include "advection_faces.cuh"
 #include "advection_kernels.cuh"
+#include "procedures.cuh"
 
 #include <cuda_runtime.h>
 
@@ -147,4 +148,35 @@ extern "C" int f2c_halo_fill_v1(const f2c_grid_v1 *grid, double *const *fields, 
     const cudaError_t e = launch_halo(h, static_cast<cudaStream_t>(stream));
     if (e != cudaSuccess) return fail(6, std::string("halo launch: ") + cudaGetErrorString(e));
     return 0;
+}
+
+extern "C" int f2c_procedure_v1(int op, const f2c_grid_v1 *grid, double *out, const double *u, const double *v,
+                                const double *w, double value, void *stream) {
+    if (int s = check_grid(grid)) return s;
+    if (op < kOpSet || op > kOpCdwAdv) return fail(1, "unknown procedure");
+    if (!out) return fail(1, "null procedure output");
+    if (op >= kOpCduDiv && (!u || !v || !w)) return fail(1, "null velocity");
+    if (out == u || out == v || out == w) return fail(3, "procedure output aliases a velocity");
+    ProcedureArgs p{};
+    p.out = out;
+    p.u = u; p.v = v; p.w = w;
+    p.value = value;
+    p.nx = (int)grid->nx; p.ny = (int)grid->ny; p.nz = (int)grid->nz; p.h = (int)grid->halo;
+    p.sx = grid->sx;
+    p.plane = grid->sx * grid->sy;
+    p.c = make_coefficients(grid->dx, grid->dy, grid->dz);
+    const dim3 g = procedure_grid(p), b(kProcBX, kProcBY, 1);
+    const cudaStream_t st = static_cast<cudaStream_t>(stream);
+    switch (op) {
+    case kOpSet: procedure_kernel<kOpSet><<<g, b, 0, st>>>(p); break;
+    case kOpMultiply: procedure_kernel<kOpMultiply><<<g, b, 0, st>>>(p); break;
+    case kOpCduDiv: procedure_kernel<kOpCduDiv><<<g, b, 0, st>>>(p); break;
+    case kOpCduAdv: procedure_kernel<kOpCduAdv><<<g, b, 0, st>>>(p); break;
+    case kOpCdvDiv: procedure_kernel<kOpCdvDiv><<<g, b, 0, st>>>(p); break;
+    case kOpCdvAdv: procedure_kernel<kOpCdvAdv><<<g, b, 0, st>>>(p); break;
+    case kOpCdwDiv: procedure_kernel<kOpCdwDiv><<<g, b, 0, st>>>(p); break;
+    default: procedure_kernel<kOpCdwAdv><<<g, b, 0, st>>>(p); break;
+    }
+    const cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? 0 : fail(6, std::string("procedure launch: ") + cudaGetErrorString(e));
 }

@@ -64,21 +64,21 @@ struct FaceSmem {
     static constexpr size_t bytes = sizeof(double) * 2 * NF * (XF + YF);
 };
 
+// One tile: columns [tx*32, tx*32+32) x [ty*8, ty*8+8) of the interior, levels
+// [k0, k1). Called by every thread of a (32, 9) block; `smem` holds
+// FaceSmem<NS, MASK>::bytes. Starts and ends with the shared face buffers free.
 template <int NS, int MASK>
-__global__ void __launch_bounds__(kFaceThreads, 1) advection_faces_kernel(const AdvArgs a) {
+__device__ __forceinline__ void faces_tile(const AdvArgs &a, int tile_x, int tile_y, int k0, int k1, double *smem) {
     constexpr bool DO_U = MASK & 1, DO_V = MASK & 2, DO_W = MASK & 4;
     using Smem = FaceSmem<NS, MASK>;
     constexpr int NF = Smem::NF;
-    extern __shared__ double smem[];
     double *xface = smem;                         // [2][NF][XF]
     double *yface = smem + 2 * NF * Smem::XF;     // [2][NF][YF]
 
     const int lane = threadIdx.x;
     const int warp = threadIdx.y;
     const bool edge = warp == kFaceTY;
-    const int i0 = blockIdx.x * kFaceTX, j0 = blockIdx.y * kFaceTY;
-    const int k0 = blockIdx.z * kFaceKZ;
-    const int k1 = min(k0 + kFaceKZ, a.nz);
+    const int i0 = tile_x * kFaceTX, j0 = tile_y * kFaceTY;
     const long long sx = a.sx, plane = a.plane;
     const double *__restrict__ U = a.u;
     const double *__restrict__ V = a.v;
@@ -285,6 +285,32 @@ __global__ void __launch_bounds__(kFaceThreads, 1) advection_faces_kernel(const 
 }
 
 template <int NS, int MASK>
+__global__ void __launch_bounds__(kFaceThreads, 1) advection_faces_kernel(const AdvArgs a) {
+    extern __shared__ double smem[];
+    const int k0 = blockIdx.z * a.kz;
+    faces_tile<NS, MASK>(a, blockIdx.x, blockIdx.y, k0, min(k0 + a.kz, a.nz), smem);
+}
+
+// Depth of the z-chunks of one launch: deep (kFaceKZ) when the grid has work
+// for several waves of CTAs, shallower for small grids so that at least four
+// CTAs per SM are available (down to two levels, where the per-chunk prologue
+// stays a small fraction of the work).
+inline int chunk_depth(int nx, int ny, int nz) {
+    static int sms = 0;
+    if (!sms) {
+        int device = 0;
+        cudaGetDevice(&device);
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess || sms < 1) sms = 152;
+    }
+    const long long tiles = (long long)((nx + kFaceTX - 1) / kFaceTX) * ((ny + kFaceTY - 1) / kFaceTY);
+    const long long want = 4LL * sms;
+    long long kz = (tiles * nz + want - 1) / want;
+    if (kz > kFaceKZ) kz = kFaceKZ;
+    if (kz < 2) kz = 2;
+    return (int)kz;
+}
+
+template <int NS, int MASK>
 cudaError_t launch_faces(const AdvArgs &a, cudaStream_t stream) {
     using Smem = FaceSmem<NS, MASK>;
     static bool configured = false;
@@ -294,9 +320,11 @@ cudaError_t launch_faces(const AdvArgs &a, cudaStream_t stream) {
         if (e != cudaSuccess) return e;
         configured = true;
     }
+    AdvArgs b = a;
+    if (b.kz <= 0) b.kz = chunk_depth(b.nx, b.ny, b.nz);
     const dim3 block(kFaceTX, kFaceTY + 1, 1);
-    const dim3 grid((a.nx + kFaceTX - 1) / kFaceTX, (a.ny + kFaceTY - 1) / kFaceTY, (a.nz + kFaceKZ - 1) / kFaceKZ);
-    advection_faces_kernel<NS, MASK><<<grid, block, Smem::bytes, stream>>>(a);
+    const dim3 grid((b.nx + kFaceTX - 1) / kFaceTX, (b.ny + kFaceTY - 1) / kFaceTY, (b.nz + b.kz - 1) / b.kz);
+    advection_faces_kernel<NS, MASK><<<grid, block, Smem::bytes, stream>>>(b);
     return cudaGetLastError();
 }
 

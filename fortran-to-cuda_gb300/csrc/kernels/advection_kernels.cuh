@@ -20,6 +20,7 @@ struct AdvArgs {
     int nscalar, mode;
     double dt;
     int nx, ny, nz, h;
+    int kz;  // levels per z-chunk of the face-sharing kernel
     long long sx, plane;
     Coefficients c;
 };

@@ -1,0 +1,216 @@
+// Persistent batched advection over a flattened tile queue (include/f2c_batch.h).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../../include/f2c_batch.h"
+#include "advection_faces.cuh"
+
+namespace f2c {
+int fail(int status, const std::string &message);
+int check_grid(const f2c_grid_v1 *g);
+
+struct BatchItem {
+    int instance;
+    short tile_x, tile_y;
+    int k0, k1;
+};
+static_assert(sizeof(BatchItem) == 16, "batch item layout");
+
+struct BatchHeader {
+    unsigned counter;
+    unsigned pad[63];
+};
+
+namespace {
+
+constexpr size_t kAlign = 256;
+size_t align_up(size_t v) { return (v + kAlign - 1) / kAlign * kAlign; }
+
+template <int NS, int MASK>
+__global__ void __launch_bounds__(kFaceThreads, 1)
+    advection_batched_kernel(const AdvArgs *__restrict__ instances, const BatchItem *__restrict__ items, int nitems,
+                             unsigned *counter) {
+    extern __shared__ double smem[];
+    __shared__ int slot;
+    for (;;) {
+        if (threadIdx.x == 0 && threadIdx.y == 0) slot = (int)atomicAdd(counter, 1u);
+        __syncthreads();
+        const int n = slot;
+        __syncthreads();  // every thread has read the slot before thread 0 takes the next one
+        if (n >= nitems) return;
+        const BatchItem it = items[n];
+        faces_tile<NS, MASK>(instances[it.instance], it.tile_x, it.tile_y, it.k0, it.k1, smem);
+    }
+}
+
+struct Kernel {
+    const void *fn;
+    size_t smem;
+};
+
+template <int NS, int MASK>
+Kernel kernel_of() {
+    static bool configured = false;
+    if (!configured) {
+        cudaFuncSetAttribute(advection_batched_kernel<NS, MASK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)FaceSmem<NS, MASK>::bytes);
+        configured = true;
+    }
+    return {(const void *)advection_batched_kernel<NS, MASK>, FaceSmem<NS, MASK>::bytes};
+}
+
+template <int MASK>
+Kernel kernel_for_ns(int ns) {
+    switch (ns) {
+    case 0: return kernel_of<0, MASK>();
+    case 1: return kernel_of<1, MASK>();
+    case 2: return kernel_of<2, MASK>();
+    case 3: return kernel_of<3, MASK>();
+    default: return kernel_of<4, MASK>();
+    }
+}
+
+Kernel kernel_for(int ns, int mask) {
+    switch (mask) {
+    case 1: return kernel_for_ns<1>(ns);
+    case 2: return kernel_for_ns<2>(ns);
+    case 4: return kernel_for_ns<4>(ns);
+    case 0: return kernel_for_ns<0>(ns);
+    default: return kernel_for_ns<7>(ns);
+    }
+}
+
+int chunk(const int32_t *kz, int n) { return kz && kz[n] > 0 ? kz[n] : kFaceKZ; }
+
+size_t item_count(const f2c_grid_v1 *grids, const int32_t *kz, int count) {
+    size_t items = 0;
+    for (int n = 0; n < count; ++n) {
+        const f2c_grid_v1 &g = grids[n];
+        const int c = chunk(kz, n);
+        items += (size_t)((g.nx + kFaceTX - 1) / kFaceTX) * ((g.ny + kFaceTY - 1) / kFaceTY) * ((g.nz + c - 1) / c);
+    }
+    return items;
+}
+
+}  // namespace
+}  // namespace f2c
+
+using namespace f2c;
+
+extern "C" size_t f2c_batch_workspace_bytes_v1(const f2c_grid_v1 *grids, const int32_t *kz, int32_t count) {
+    if (!grids || count <= 0) return 0;
+    return align_up(sizeof(BatchHeader)) + align_up(sizeof(AdvArgs) * (size_t)count) +
+           align_up(sizeof(BatchItem) * item_count(grids, kz, count));
+}
+
+extern "C" int f2c_batch_prepare_v1(const f2c_grid_v1 *grids, const f2c_fields_v1 *fields, const int32_t *kz,
+                                    int32_t count, void *workspace, size_t workspace_bytes, void *stream,
+                                    f2c_batch_plan_v1 *plan) {
+    if (!grids || !fields || count <= 0 || !plan) return fail(1, "empty batch");
+    if (!workspace) return fail(1, "null batch workspace");
+    if (workspace_bytes < f2c_batch_workspace_bytes_v1(grids, kz, count)) return fail(4, "batch workspace too small");
+    std::vector<AdvArgs> descs((size_t)count);
+    int ns = -1, mask = -1;
+    for (int n = 0; n < count; ++n) {
+        if (int s = check_grid(&grids[n])) return s;
+        const f2c_fields_v1 &f = fields[n];
+        if (!f.u || !f.v || !f.w) return fail(1, "batch instance without velocities");
+        if (f.nscalar < 0 || f.nscalar > F2C_MAX_SCALARS) return fail(1, "scalar count out of range");
+        const int m = (f.ut ? 1 : 0) | (f.vt ? 2 : 0) | (f.wt ? 4 : 0);
+        if (n == 0) {
+            ns = f.nscalar;
+            mask = m;
+        } else if (f.nscalar != ns || m != mask || f.mode != fields[0].mode) {
+            return fail(1, "batch instances differ in scalars, outputs or mode");
+        }
+        if (kz && kz[n] < 0) return fail(1, "negative z-chunk depth");
+        AdvArgs &a = descs[(size_t)n];
+        std::memset(&a, 0, sizeof a);
+        a.u = f.u; a.v = f.v; a.w = f.w;
+        a.out[0] = f.ut; a.out[1] = f.vt; a.out[2] = f.wt;
+        a.nscalar = f.nscalar;
+        for (int s = 0; s < f.nscalar; ++s) {
+            if (!f.s[s]) return fail(1, "null scalar input");
+            a.s[s] = f.s[s];
+            a.st[s] = f.st[s];
+        }
+        a.mode = f.mode;
+        a.dt = f.dt;
+        const f2c_grid_v1 &g = grids[n];
+        a.nx = (int)g.nx; a.ny = (int)g.ny; a.nz = (int)g.nz; a.h = (int)g.halo;
+        a.sx = g.sx;
+        a.plane = g.sx * g.sy;
+        a.c = make_coefficients(g.dx, g.dy, g.dz);
+    }
+    if (mask != 7 && mask != 1 && mask != 2 && mask != 4 && mask != 0) mask = 7;
+    if (mask == 0 && ns == 0) return fail(1, "batch computes nothing");
+    // the flattened queue: full-depth items first (largest first), then the partial ones
+    std::vector<BatchItem> items;
+    items.reserve(item_count(grids, kz, count));
+    for (int n = 0; n < count; ++n) {
+        const f2c_grid_v1 &g = grids[n];
+        const int c = chunk(kz, n);
+        const int tx = (int)((g.nx + kFaceTX - 1) / kFaceTX), ty = (int)((g.ny + kFaceTY - 1) / kFaceTY);
+        if (tx > 32767 || ty > 32767) return fail(1, "instance too wide for the tile queue");
+        for (int k0 = 0; k0 < g.nz; k0 += c)
+            for (int y = 0; y < ty; ++y)
+                for (int x = 0; x < tx; ++x)
+                    items.push_back({n, (short)x, (short)y, k0, (int)std::min<int64_t>(k0 + c, g.nz)});
+    }
+    auto cost = [&](const BatchItem &it) {
+        const f2c_grid_v1 &g = grids[it.instance];
+        const long long w = std::min<long long>(kFaceTX, g.nx - (long long)it.tile_x * kFaceTX);
+        const long long h = std::min<long long>(kFaceTY, g.ny - (long long)it.tile_y * kFaceTY);
+        return w * h * (it.k1 - it.k0);
+    };
+    std::stable_sort(items.begin(), items.end(),
+                     [&](const BatchItem &a, const BatchItem &b) { return cost(a) > cost(b); });
+    char *base = static_cast<char *>(workspace);
+    const size_t desc_off = align_up(sizeof(BatchHeader));
+    const size_t item_off = desc_off + align_up(sizeof(AdvArgs) * (size_t)count);
+    const cudaStream_t s = static_cast<cudaStream_t>(stream);
+    cudaError_t e = cudaMemcpyAsync(base + desc_off, descs.data(), sizeof(AdvArgs) * descs.size(),
+                                    cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(base + item_off, items.data(), sizeof(BatchItem) * items.size(), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return fail(6, std::string("batch prepare: ") + cudaGetErrorString(e));
+    const Kernel k = kernel_for(ns, mask);
+    int device = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&device);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k.fn, kFaceThreads, k.smem);
+    if (e != cudaSuccess || per_sm < 1) return fail(6, "batch kernel does not fit on an SM");
+    plan->workspace = workspace;
+    plan->workspace_bytes = workspace_bytes;
+    plan->count = count;
+    plan->nscalar = ns;
+    plan->mask = mask;
+    plan->items = (int32_t)items.size();
+    plan->ctas = (uint32_t)std::min<size_t>((size_t)sms * per_sm, items.size());
+    plan->reserved = 0;
+    return 0;
+}
+
+extern "C" int f2c_batch_step_v1(const f2c_batch_plan_v1 *plan, void *stream) {
+    if (!plan || !plan->workspace || plan->items <= 0) return fail(1, "batch plan not prepared");
+    const cudaStream_t s = static_cast<cudaStream_t>(stream);
+    char *base = static_cast<char *>(plan->workspace);
+    const size_t desc_off = align_up(sizeof(BatchHeader));
+    const size_t item_off = desc_off + align_up(sizeof(AdvArgs) * (size_t)plan->count);
+    unsigned *counter = reinterpret_cast<unsigned *>(base);
+    const AdvArgs *descs = reinterpret_cast<const AdvArgs *>(base + desc_off);
+    const BatchItem *items = reinterpret_cast<const BatchItem *>(base + item_off);
+    cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(unsigned), s);
+    if (e != cudaSuccess) return fail(6, std::string("batch counter reset: ") + cudaGetErrorString(e));
+    const Kernel k = kernel_for(plan->nscalar, plan->mask);
+    int nitems = plan->items;
+    void *args[] = {(void *)&descs, (void *)&items, (void *)&nitems, (void *)&counter};
+    e = cudaLaunchKernel(k.fn, dim3(plan->ctas), dim3(kFaceTX, kFaceTY + 1, 1), args, k.smem, s);
+    if (e != cudaSuccess) return fail(6, std::string("batch launch: ") + cudaGetErrorString(e));
+    return 0;
+}

@@ -66,6 +66,14 @@ int f2c_advection_v1(const f2c_grid_v1 *grid, const f2c_fields_v1 *fields, void 
  * Both are bit-identical to the oracle. */
 int f2c_advection_variant_v1(const f2c_grid_v1 *grid, const f2c_fields_v1 *fields, int variant, void *stream);
 
+/* One reference procedure as one launch (the reference resident build's
+ * structure: benchmarks/cdu/src/cdu.f90:12-106, cvd.f90/cdw.f90:44-98):
+ * op 0 set (out = value), 1 multiply (out *= value), 2 CDUdiv, 3 CDUadv,
+ * 4 CDVdiv, 5 CDVadv, 6 CDWdiv, 7 CDWadv. The sequence set, div, adv,
+ * multiply(0.5) equals the fused launch bit for bit. */
+int f2c_procedure_v1(int op, const f2c_grid_v1 *grid, double *out, const double *u, const double *v, const double *w,
+                     double value, void *stream);
+
 /* Boundary fill of `count` fields: periodic in x and y; vertical walls by
  * kind: 0 mirrors the interior (U, V, scalars), 1 is a face-staggered W with
  * zero wall faces and sign-changed mirrors. Requires nz >= halo. One launch. */

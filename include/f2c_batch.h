@@ -1,0 +1,51 @@
+/* Batched ensembles: many independent advection instances of uneven grid
+ * sizes advanced by ONE persistent launch over a flattened tile queue.
+ *
+ * Each instance is an f2c_grid_v1 + f2c_fields_v1 pair (include/f2c_advection.h);
+ * all instances of a batch share the scalar count, the output mode and the set
+ * of requested outputs. The work is cut into items of one 32 x 8 column tile
+ * and a z-range of `kz` levels (per instance, chosen by the autotuner in
+ * compiler/scheduling); a fixed grid of CTAs (the SM count times the resident
+ * CTAs per SM) takes items from an atomic counter, largest items first. Every
+ * item runs the same face-sharing arithmetic as f2c_advection_v1, so a batch
+ * is bit-identical to one launch per instance.
+ *
+ * The caller owns the device workspace (descriptors, items, the counter):
+ * f2c_batch_workspace_bytes_v1 sizes it, f2c_batch_prepare_v1 fills it (a
+ * setup call: synchronous on `stream`), f2c_batch_step_v1 resets the counter
+ * and launches (asynchronous; capturable in a CUDA graph). Calls that overlap
+ * on the GPU with the same workspace race on its counter.
+ *
+ * No counterpart exists in the reference (its resident build runs one
+ * procedure call at a time); statuses are fort_scope_status values.
+ */
+#ifndef F2C_BATCH_H
+#define F2C_BATCH_H
+#include <stddef.h>
+#include <stdint.h>
+
+#include "f2c_advection.h"
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct f2c_batch_plan_v1 {
+    void *workspace;           /* device memory of at least f2c_batch_workspace_bytes_v1 bytes */
+    size_t workspace_bytes;
+    int32_t count, nscalar, mask, items;
+    uint32_t ctas;             /* persistent grid size */
+    uint32_t reserved;
+} f2c_batch_plan_v1;
+
+/* Bytes of workspace for `count` instances cut into z-chunks of kz[i] levels (kz NULL: 32). */
+size_t f2c_batch_workspace_bytes_v1(const f2c_grid_v1 *grids, const int32_t *kz, int32_t count);
+/* Validate the instances, build descriptors and the item queue into `workspace`. */
+int f2c_batch_prepare_v1(const f2c_grid_v1 *grids, const f2c_fields_v1 *fields, const int32_t *kz, int32_t count,
+                         void *workspace, size_t workspace_bytes, void *stream, f2c_batch_plan_v1 *plan);
+/* One step of every instance: counter reset + one persistent launch on `stream`. */
+int f2c_batch_step_v1(const f2c_batch_plan_v1 *plan, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -189,3 +189,23 @@ def test_golden_fixtures_on_the_gpu(cuda):
     got = _run(cuda, wl.Fields(geo2, *ins[:3], ins[3:]))
     for n, g in enumerate(got):
         assert np.array_equal(_bits(_interior(g, geo2)), _bits(_interior(z[f"h2_tend{n}"], geo2)))
+
+
+@pytest.mark.parametrize("component", [0, 1, 2])
+def test_procedure_launch_chain_equals_fused(cuda, component):
+    """set, div, adv, multiply(0.5) as four launches gives the fused launch's bits."""
+    geo = wl.Geometry(41, 23, 19, halo=2)
+    fields = wl.advection_fields(geo, seed=4)
+    ins = [cuda.from_numpy(a).cuda() for a in fields.arrays()]
+    chained = cuda.full_like(ins[0], 5.0)
+    grid = native.make_grid(geo.nx, geo.ny, geo.nz, geo.halo, geo.dx, geo.dy, geo.dz)
+    u, v, w = (t.data_ptr() for t in ins)
+    div, adv = [(native.CDU_DIV, native.CDU_ADV), (native.CDV_DIV, native.CDV_ADV),
+                (native.CDW_DIV, native.CDW_ADV)][component]
+    native.procedure(native.SET, grid, chained.data_ptr(), value=0.0)
+    native.procedure(div, grid, chained.data_ptr(), u, v, w)
+    native.procedure(adv, grid, chained.data_ptr(), u, v, w)
+    native.procedure(native.MULTIPLY, grid, chained.data_ptr(), value=0.5)
+    cuda.cuda.synchronize()
+    got = _run(cuda, fields)[component]
+    assert np.array_equal(_bits(_interior(chained.cpu().numpy(), geo)), _bits(_interior(got, geo)))
