@@ -159,9 +159,9 @@ def registry() -> list[Entry]:
     entries += _step_entries()
     entries += [
         Entry("stencil::diffuse7", "Diffusion",
-              (_a("b", "out"), _a("a"), _r("dt"), _r("nu"), _r("dx"), _i("nx"), _i("ny"), _i("nz"), _i("halo")),
+              (_a("b", "inout"), _a("a"), _r("dt"), _r("nu"), _r("dx"), _i("nx"), _i("ny"), _i("nz"), _i("halo")),
               source="compiler/tests/apps/box/stepper.f90:8-30 (diffuse with laplacian)"),
-        Entry("stencil::jacobi5", "Jacobi", (_a("v", "out"), _a("u"), _i("nx"), _i("ny"), _i("halo")),
+        Entry("stencil::jacobi5", "Jacobi", (_a("v", "inout"), _a("u"), _i("nx"), _i("ny"), _i("halo")),
               source="compiler/tests/apps/relax/relax.f90:28-33 (one Jacobi sweep)"),
         Entry("stencil::yee2d", "Yee",
               (_a("ez", "inout"), _a("hx", "inout"), _a("hy", "inout"), _r("ch"), _r("ce"), _i("nx"), _i("ny"),

@@ -243,7 +243,9 @@ int run(const EntryCall &call) {
         for (int n = 0; n < call.narrays; ++n) role(n, true, true, true, false);
         break;
     case Template::Diffusion: case Template::Jacobi:
-        role(0, false, true, true, true);
+        // the output is intent(inout) in the sources (stepper.f90:17-20; relax's v keeps its boundary):
+        // its interior is overwritten and its ghost values stay defined
+        role(0, false, true, true, false);
         role(1, true, false, false, false);
         break;
     case Template::Yee:

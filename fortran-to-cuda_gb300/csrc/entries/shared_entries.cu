@@ -691,12 +691,12 @@ extern "C" int cpp_fort_shared_073d04efb82a(fort_scope_t fort_context, int fort_
 }
 
 // stencil::diffuse7: compiler/tests/apps/box/stepper.f90:8-30 (diffuse with laplacian)
-extern "C" int cpp_fort_shared_242ee4413593(fort_scope_t fort_context, int fort_mode, fort_buffer_t b_handle, fort_buffer_t a_handle, const double *dt, const double *nu, const double *dx, const int *nx, const int *ny, const int *nz, const int *halo) {
+extern "C" int cpp_fort_shared_e331fbb8bf9a(fort_scope_t fort_context, int fort_mode, fort_buffer_t b_handle, fort_buffer_t a_handle, const double *dt, const double *nu, const double *dx, const int *nx, const int *ny, const int *nz, const int *halo) {
     EntryCall call{};
     call.context = fort_context;
     call.mode = fort_mode;
     call.kind = Template::Diffusion;
-    call.code_key = 0x29cf3c886ce4c0c3ULL;
+    call.code_key = 0x297afd6e2ec2445bULL;
     call.nscalar = 0;
     call.narrays = 2;
     call.arrays[0] = b_handle;
@@ -714,12 +714,12 @@ extern "C" int cpp_fort_shared_242ee4413593(fort_scope_t fort_context, int fort_
 }
 
 // stencil::jacobi5: compiler/tests/apps/relax/relax.f90:28-33 (one Jacobi sweep)
-extern "C" int cpp_fort_shared_aa40c606bdea(fort_scope_t fort_context, int fort_mode, fort_buffer_t v_handle, fort_buffer_t u_handle, const int *nx, const int *ny, const int *halo) {
+extern "C" int cpp_fort_shared_03470f69376f(fort_scope_t fort_context, int fort_mode, fort_buffer_t v_handle, fort_buffer_t u_handle, const int *nx, const int *ny, const int *halo) {
     EntryCall call{};
     call.context = fort_context;
     call.mode = fort_mode;
     call.kind = Template::Jacobi;
-    call.code_key = 0x3575cd74530954adULL;
+    call.code_key = 0x6d2a628ad5006681ULL;
     call.nscalar = 0;
     call.narrays = 2;
     call.arrays[0] = v_handle;

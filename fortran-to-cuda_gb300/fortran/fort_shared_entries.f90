@@ -762,14 +762,14 @@ module fort_shared_073d04efb82a
   end interface
 end module fort_shared_073d04efb82a
 
-module fort_shared_242ee4413593
+module fort_shared_e331fbb8bf9a
   use iso_c_binding
   implicit none
   private
   public :: run
   interface
     function run( &
-      fort_context, fort_mode, b_handle, a_handle, dt, nu, dx, nx, ny, nz, halo) bind(C, name='cpp_fort_shared_242ee4413593') result(fort_status)
+      fort_context, fort_mode, b_handle, a_handle, dt, nu, dx, nx, ny, nz, halo) bind(C, name='cpp_fort_shared_e331fbb8bf9a') result(fort_status)
       import :: c_int, c_int64_t, c_double
       integer(c_int) :: fort_status
       integer(c_int64_t), value :: fort_context
@@ -785,16 +785,16 @@ module fort_shared_242ee4413593
       integer(c_int), intent(in) :: halo
     end function
   end interface
-end module fort_shared_242ee4413593
+end module fort_shared_e331fbb8bf9a
 
-module fort_shared_aa40c606bdea
+module fort_shared_03470f69376f
   use iso_c_binding
   implicit none
   private
   public :: run
   interface
     function run( &
-      fort_context, fort_mode, v_handle, u_handle, nx, ny, halo) bind(C, name='cpp_fort_shared_aa40c606bdea') result(fort_status)
+      fort_context, fort_mode, v_handle, u_handle, nx, ny, halo) bind(C, name='cpp_fort_shared_03470f69376f') result(fort_status)
       import :: c_int, c_int64_t, c_double
       integer(c_int) :: fort_status
       integer(c_int64_t), value :: fort_context
@@ -806,7 +806,7 @@ module fort_shared_aa40c606bdea
       integer(c_int), intent(in) :: halo
     end function
   end interface
-end module fort_shared_aa40c606bdea
+end module fort_shared_03470f69376f
 
 module fort_shared_82041a3f2b68
   use iso_c_binding

@@ -67,9 +67,9 @@ int cpp_fort_shared_cbf2341c8e18(fort_scope_t fort_context, int fort_mode, fort_
 /* advection::halo4 -- replaces periodic x/y boundary fill in the order of compiler/tests/apps/box/boundaries.f90:6-41; walls in z (W zero, mirrored) */
 int cpp_fort_shared_073d04efb82a(fort_scope_t fort_context, int fort_mode, fort_buffer_t u_handle, fort_buffer_t v_handle, fort_buffer_t w_handle, fort_buffer_t s1_handle, fort_buffer_t s2_handle, fort_buffer_t s3_handle, fort_buffer_t s4_handle, const int *nx, const int *ny, const int *nz, const int *halo);
 /* stencil::diffuse7 -- replaces compiler/tests/apps/box/stepper.f90:8-30 (diffuse with laplacian) */
-int cpp_fort_shared_242ee4413593(fort_scope_t fort_context, int fort_mode, fort_buffer_t b_handle, fort_buffer_t a_handle, const double *dt, const double *nu, const double *dx, const int *nx, const int *ny, const int *nz, const int *halo);
+int cpp_fort_shared_e331fbb8bf9a(fort_scope_t fort_context, int fort_mode, fort_buffer_t b_handle, fort_buffer_t a_handle, const double *dt, const double *nu, const double *dx, const int *nx, const int *ny, const int *nz, const int *halo);
 /* stencil::jacobi5 -- replaces compiler/tests/apps/relax/relax.f90:28-33 (one Jacobi sweep) */
-int cpp_fort_shared_aa40c606bdea(fort_scope_t fort_context, int fort_mode, fort_buffer_t v_handle, fort_buffer_t u_handle, const int *nx, const int *ny, const int *halo);
+int cpp_fort_shared_03470f69376f(fort_scope_t fort_context, int fort_mode, fort_buffer_t v_handle, fort_buffer_t u_handle, const int *nx, const int *ny, const int *halo);
 /* stencil::yee2d -- replaces 2-D TM Yee leapfrog (no reference source in the mount); H task then E task */
 int cpp_fort_shared_82041a3f2b68(fort_scope_t fort_context, int fort_mode, fort_buffer_t ez_handle, fort_buffer_t hx_handle, fort_buffer_t hy_handle, const double *ch, const double *ce, const int *nx, const int *ny, const int *halo);
 
