@@ -45,6 +45,34 @@ int f2c_batch_prepare_v1(const f2c_grid_v1 *grids, const f2c_fields_v1 *fields, 
 /* One step of every instance: counter reset + one persistent launch on `stream`. */
 int f2c_batch_step_v1(const f2c_batch_plan_v1 *plan, void *stream);
 
+/* The same batched step for callers that cannot allocate device memory. It has
+ * no counterpart in the reference.
+ *
+ * Who needs it: a caller whose device memory is already fully handed to
+ * another allocator (a caching allocator, or a residency budget sized to the
+ * whole device) has no room for the workspace f2c_batch_step_v1 needs, and a
+ * caller stepping an ensemble inside a time loop may not accept the
+ * device-wide synchronisation that freeing device memory implies. This entry
+ * allocates nothing: the work counter, instance descriptors and tile queue
+ * live in one fixed array of F2C_BATCH_NO_ALLOC_SCRATCH_BYTES (1088 KiB) that
+ * the library keeps in device memory; every GPU that loads the library holds it
+ * until the process exits. The caller passes only its instances' grids and
+ * fields (and optional z-chunk depths, as for f2c_batch_workspace_bytes_v1).
+ *
+ * Limits: at most F2C_BATCH_NO_ALLOC_MAX_INSTANCES instances and
+ * F2C_BATCH_NO_ALLOC_MAX_ITEMS work items (32 x 8 column tiles times z-chunks);
+ * larger batches are rejected with FORT_SCOPE_ARGUMENT and a message naming the
+ * limit. The first call on a device looks up the array's device address (with
+ * that device current); make that first call before any stream capture. Every
+ * call shares and overwrites the array (the counter is cleared each call), so
+ * calls that overlap on the GPU, or that come from several host threads at
+ * once, race. Results are bit-identical to f2c_batch_step_v1. */
+#define F2C_BATCH_NO_ALLOC_MAX_INSTANCES 128
+#define F2C_BATCH_NO_ALLOC_MAX_ITEMS 65536
+#define F2C_BATCH_NO_ALLOC_SCRATCH_BYTES 1114112
+int f2c_batch_step_static_v1(const f2c_grid_v1 *grids, const f2c_fields_v1 *fields, const int32_t *kz, int32_t count,
+                             void *stream);
+
 #ifdef __cplusplus
 }
 #endif
