@@ -1,0 +1,277 @@
+"""Serving advection jobs with continuous batching.
+
+A job asks for ``steps`` forward-Euler steps (dt = 0.1, with the boundary fill
+after each) of an advection instance: seeded sine-mode U, V, W and 0-3
+scalars on an nx x ny x nz grid. The server keeps every admitted job's fields
+resident on the device (two buffer sets, ping-pong) until its last step, and
+advances ALL admitted jobs by one step per tick: one persistent batched launch
+per scalar count over the union of their tiles (``f2c_batch_*``), then each
+job's boundary fill. Jobs that arrive while others run are admitted at the
+next tick as slots and memory allow (a device-memory budget, 150 GB by
+default), so their steps overlap on the device with the running jobs' steps.
+Every job's arithmetic is the single-instance kernel's, so a job's result is
+the same alone and in any mix, bit for bit.
+
+The open-loop arrival stream and the job sizes follow the serving
+configuration: Poisson arrivals at a given rate; nx and ny drawn independently
+log-uniform in [48, 320], nz log-uniform in [24, 128]; 0-3 scalars and 1-100
+steps uniform. ``serial_timeline`` gives the comparison: the same stream served
+one job at a time through the single-instance path.
+"""
+
+from __future__ import annotations
+
+import math
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import native
+from . import workloads as wl
+
+DT = 0.1
+BUDGET_BYTES = 150 * 10**9
+MAX_ACTIVE = 256
+
+
+@dataclass
+class Job:
+    ident: int
+    arrival: float              # seconds after the stream starts
+    nx: int
+    ny: int
+    nz: int
+    nscalar: int
+    steps: int
+    seed: int
+    halo: int = 2
+    # server state
+    admitted: float = -1.0
+    finished: float = -1.0
+    done: int = 0
+    buffers: list = field(default_factory=list)   # [set A tensors, set B tensors]
+    grid: object = None
+    result: list = field(default_factory=list)
+
+    @property
+    def geometry(self) -> wl.Geometry:
+        return wl.Geometry(self.nx, self.ny, self.nz, halo=self.halo)
+
+    @property
+    def points(self) -> int:
+        return self.nx * self.ny * self.nz
+
+    def device_bytes(self) -> int:
+        g = self.geometry
+        return 2 * (3 + self.nscalar) * int(np.prod(g.shape)) * 8
+
+
+def log_uniform_int(rng, lo, hi):
+    return int(round(math.exp(rng.uniform(math.log(lo), math.log(hi)))))
+
+
+def poisson_jobs(count: int, rate: float, seed: int = 0) -> list[Job]:
+    """An open-loop stream: exponential inter-arrival gaps; per job draws in the order nx, ny, nz, scalars, steps."""
+    rng = np.random.default_rng(seed)
+    jobs, t = [], 0.0
+    for n in range(count):
+        t += float(rng.exponential(1.0 / rate))
+        nx = log_uniform_int(rng, 48, 320)
+        ny = log_uniform_int(rng, 48, 320)
+        nz = log_uniform_int(rng, 24, 128)
+        nscalar = int(rng.integers(0, 4))
+        steps = int(rng.integers(1, 101))
+        jobs.append(Job(n, t, nx, ny, nz, nscalar, steps, seed=10_000 + n))
+    return jobs
+
+
+class Server:
+    """Continuous-batching server on one GPU (``torch`` provides device memory and the stream)."""
+
+    def __init__(self, torch, budget_bytes: int = BUDGET_BYTES, max_active: int = MAX_ACTIVE, keep_results=False):
+        self.torch = torch
+        self.budget = budget_bytes
+        self.max_active = max_active
+        self.keep_results = keep_results
+        self.stream = torch.cuda.Stream()
+        self.active: list[Job] = []
+        self.claimed = 0
+        self.ticks = 0
+        self.launches = 0
+        self.workspaces = {}
+
+    # -- job lifetime ---------------------------------------------------------------------------
+    def _admit(self, job: Job, now: float) -> None:
+        torch = self.torch
+        geo = job.geometry
+        with torch.cuda.stream(self.stream):
+            first = wl.advection_fields_device(geo, job.seed, job.nscalar, torch)
+            second = [torch.empty_like(t) for t in first]
+        job.grid = native.make_grid(geo.nx, geo.ny, geo.nz, geo.halo, geo.dx, geo.dy, geo.dz)
+        kinds = [0, 0, 1] + [0] * job.nscalar
+        native.halo_fill(job.grid, [t.data_ptr() for t in first], kinds, stream=self.stream.cuda_stream)
+        job.buffers = [first, second]
+        job.admitted = now
+        self.claimed += job.device_bytes()
+        self.active.append(job)
+
+    def _retire(self, job: Job, now: float) -> None:
+        current = job.buffers[job.done % 2]
+        if self.keep_results:
+            job.result = [t.cpu().numpy() for t in current]
+        else:
+            current[0].view(-1)[:1].cpu()  # the job's answer is read back (one value; fields stay for inspection)
+        job.finished = now
+        job.buffers = []
+        self.claimed -= job.device_bytes()
+
+    def fits(self, job: Job) -> bool:
+        return len(self.active) < self.max_active and self.claimed + job.device_bytes() <= self.budget
+
+    # -- one tick: every active job advances one step --------------------------------------------
+    def tick(self) -> None:
+        torch = self.torch
+        groups = {}
+        for job in self.active:
+            groups.setdefault(job.nscalar, []).append(job)
+        s = self.stream.cuda_stream
+        for nscalar, jobs in sorted(groups.items()):
+            grids, fields = [], []
+            for job in jobs:
+                src, dst = job.buffers[job.done % 2], job.buffers[1 - job.done % 2]
+                p, q = [t.data_ptr() for t in src], [t.data_ptr() for t in dst]
+                grids.append(job.grid)
+                fields.append(native.make_fields(*p[:3], *q[:3], scalars=p[3:], scalar_out=q[3:],
+                                                 mode=native.ADVANCE, dt=DT))
+            batch = native.Batch(grids, fields)
+            need = batch.workspace_bytes()
+            ws = self.workspaces.get(nscalar)
+            if ws is None or ws.numel() < need:
+                ws = torch.empty(max(need, 1 << 20) * 2, dtype=torch.uint8, device="cuda")
+                self.workspaces[nscalar] = ws
+            batch.prepare(ws.data_ptr(), ws.numel(), s)
+            batch.step(s)
+            self.launches += 1
+        for job in self.active:
+            dst = job.buffers[1 - job.done % 2]
+            native.halo_fill(job.grid, [t.data_ptr() for t in dst], [0, 0, 1] + [0] * job.nscalar, stream=s)
+            self.launches += 1
+            job.done += 1
+        self.ticks += 1
+
+    # -- the open-loop run ------------------------------------------------------------------------
+    def run(self, jobs: list[Job]) -> dict:
+        torch = self.torch
+        pending = sorted(jobs, key=lambda j: j.arrival)
+        waiting: list[Job] = []
+        start = time.perf_counter()
+        i = 0
+        finished = []
+        while i < len(pending) or waiting or self.active:
+            now = time.perf_counter() - start
+            while i < len(pending) and pending[i].arrival <= now:
+                waiting.append(pending[i])
+                i += 1
+            while waiting and self.fits(waiting[0]):
+                self._admit(waiting.pop(0), now)
+            if not self.active:
+                if i < len(pending):  # idle until the next arrival
+                    delay = pending[i].arrival - (time.perf_counter() - start)
+                    if delay > 0:
+                        time.sleep(delay)
+                    continue
+                if waiting:
+                    raise RuntimeError("a job does not fit the device budget on its own")
+                break
+            self.tick()
+            torch.cuda.current_stream().wait_stream(self.stream)
+            self.stream.synchronize()
+            now = time.perf_counter() - start
+            still = []
+            for job in self.active:
+                if job.done >= job.steps:
+                    self._retire(job, now)
+                    finished.append(job)
+                else:
+                    still.append(job)
+            self.active = still
+        wall = time.perf_counter() - start
+        return summarise(finished, wall, self.ticks, self.launches)
+
+
+def summarise(jobs: list[Job], wall: float, ticks: int = 0, launches: int = 0) -> dict:
+    lat = np.array([(j.finished - j.arrival) * 1e3 for j in jobs])
+    points = sum(j.points * j.steps for j in jobs)
+    return {"jobs": len(jobs), "wall_s": wall, "jobs_per_s": len(jobs) / wall if wall > 0 else 0.0,
+            "gpts_per_s": points / wall / 1e9 if wall > 0 else 0.0,
+            "p50_ms": float(np.percentile(lat, 50)) if len(lat) else None,
+            "p99_ms": float(np.percentile(lat, 99)) if len(lat) else None,
+            "ticks": ticks, "launches": launches}
+
+
+def solo_seconds(torch, job: Job) -> float:
+    """Device time of one job run alone through the single-instance path (direct launches, one stream)."""
+    geo = job.geometry
+    stream = torch.cuda.Stream()
+    with torch.cuda.stream(stream):
+        a = wl.advection_fields_device(geo, job.seed, job.nscalar, torch)
+        b = [torch.empty_like(t) for t in a]
+    grid = native.make_grid(geo.nx, geo.ny, geo.nz, geo.halo, geo.dx, geo.dy, geo.dz)
+    kinds = [0, 0, 1] + [0] * job.nscalar
+    native.halo_fill(grid, [t.data_ptr() for t in a], kinds, stream=stream.cuda_stream)
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    stream.synchronize()
+    start.record(stream)
+    bufs = [a, b]
+    for n in range(job.steps):
+        src, dst = bufs[n % 2], bufs[1 - n % 2]
+        p, q = [t.data_ptr() for t in src], [t.data_ptr() for t in dst]
+        native.advection(grid, *p[:3], *q[:3], scalars=p[3:], scalar_out=q[3:], mode=native.ADVANCE, dt=DT,
+                         stream=stream.cuda_stream)
+        native.halo_fill(grid, q, kinds, stream=stream.cuda_stream)
+    stop.record(stream)
+    stream.synchronize()
+    return start.elapsed_time(stop) * 1e-3
+
+
+def serial_timeline(jobs: list[Job], solo: dict) -> dict:
+    """The stream served one job at a time (FIFO): start = max(arrival, previous finish)."""
+    t = 0.0
+    out = []
+    for job in sorted(jobs, key=lambda j: j.arrival):
+        begin = max(t, job.arrival)
+        t = begin + solo[job.ident]
+        out.append(Job(job.ident, job.arrival, job.nx, job.ny, job.nz, job.nscalar, job.steps, job.seed,
+                       finished=t))
+    return summarise(out, t)
+
+
+def bench_main(args) -> None:
+    """``bench.py --workload serving``: rates swept over {50, ..., 2000} jobs/s; continuous batching vs serial."""
+    import json
+
+    import torch
+
+    rates = (50, 100, 200, 500, 1000, 2000)
+    count = max(20, args.steps)
+    results = []
+    for rate in rates:
+        jobs = poisson_jobs(count, rate, seed=int(rate))
+        solo = {j.ident: solo_seconds(torch, j) for j in jobs}
+        torch.cuda.synchronize()
+        served = Server(torch).run(poisson_jobs(count, rate, seed=int(rate)))
+        serial = serial_timeline(jobs, solo)
+        results.append({"rate_jobs_per_s": rate, "continuous_batching": served, "serial_plain": serial,
+                        "throughput_ratio": served["gpts_per_s"] / serial["gpts_per_s"] if serial["gpts_per_s"]
+                        else None})
+        torch.cuda.empty_cache()
+    print(json.dumps({"metric": "serving: jobs/s, Gpts/s and p50/p99 job latency (continuous batching vs serial)",
+                      "unit": "Gpts/s", "jobs_per_rate": count, "dtype": "f64",
+                      "config": {"workload": "Poisson arrivals; nx,ny log-uniform [48,320] (independent draws), "
+                                             "nz log-uniform [24,128], 0-3 scalars, 1-100 Euler steps",
+                                 "budget_bytes": BUDGET_BYTES},
+                      "results": results}), flush=True)
+
+
+__all__ = ["Job", "Server", "poisson_jobs", "serial_timeline", "solo_seconds", "bench_main", "summarise"]
