@@ -123,7 +123,7 @@ struct Backend {
         return true;
     }
     static bool sync(Stream) { return !std::getenv("F2C_TEST_FAIL_WAIT"); }
-    static bool pin(void *, size_t) { return false; }
+    static bool pin(void *, size_t, void **) { return false; }
     static void unpin(void *) {}
     static bool memory_info(size_t *free_bytes, size_t *total) {
         *total = size_t(16) << 30;
@@ -212,11 +212,18 @@ struct Backend {
         return good;
     }
     static bool sync(Stream s) { return ok(cudaStreamSynchronize(s)); }
-    static bool pin(void *p, size_t bytes) {
-        const cudaError_t e = cudaHostRegister(p, bytes, cudaHostRegisterDefault);
+    // Pin a host array in place and map it into the device address space;
+    // `mapped` receives the address a kernel uses to reach it over NVLink-C2C.
+    static bool pin(void *p, size_t bytes, void **mapped) {
+        cudaError_t e = cudaHostRegister(p, bytes, cudaHostRegisterMapped | cudaHostRegisterPortable);
         if (e != cudaSuccess) {
             cudaGetLastError();
             return false;
+        }
+        e = cudaHostGetDevicePointer(mapped, p, 0);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            *mapped = nullptr;
         }
         return true;
     }

@@ -19,7 +19,11 @@
 //    (the reference's policy, compiler/runtime/scoped_graphs.hpp:140-235).
 //  * Host arrays of 1 MiB or more are pinned in place at registration
 //    (FORT_SCOPE_PIN_HOST=0 disables it) so uploads and downloads run as DMA
-//    over NVLink-C2C without staging.
+//    over NVLink-C2C without staging, and are mapped into the device address
+//    space. An array the host writes or reads back between every device use
+//    (two uses in a row) is then accessed IN PLACE: its tasks get the mapped
+//    host address, their kernels stream it over NVLink-C2C, and no copy or
+//    device mirror is involved (FORT_SCOPE_HOST_IN_PLACE=0 disables it).
 //  * Failures after numerical work started poison the context and its domain;
 //    nothing is replayed (scoped_runtime.h:428-438 of the reference).
 #include "../../../include/scoped_runtime.h"
@@ -86,6 +90,10 @@ struct Buffer {
     int64_t lower[kMaxRank] = {};
     void *device = nullptr;
     bool pinned_host = false;
+    void *mapped = nullptr;      // device-usable address of the pinned host array
+    bool host_touched = true;    // the host wrote or read it since its last device use
+    int host_rounds = 0;         // consecutive device uses, each preceded by host access
+    bool in_place = false;       // the pending reservation hands out `mapped`
     Region defined, host_valid, device_valid;
     enum { NONE, HOST, DEVICE } prepared = NONE;
     Region prep_writes, prep_overwrites;
@@ -452,12 +460,19 @@ void make_room(Context *c, size_t bytes, const std::set<uint64_t> &keep) {
     }
 }
 
-void reserve(Context *c, const std::vector<Buffer *> &list) {
+bool in_place_allowed() {
+    static const bool on = env_flag("FORT_SCOPE_HOST_IN_PLACE", true);
+    return on;
+}
+
+void reserve(Context *c, const std::vector<Buffer *> &list, bool allow_in_place) {
     std::set<uint64_t> keep;
     size_t need = 0;
     for (Buffer *b : list) {
         keep.insert(b->handle);
-        if (!b->device) need += b->bytes;
+        b->in_place = allow_in_place && in_place_allowed() && b->mapped && b->prepared == Buffer::NONE &&
+                      b->host_touched && b->host_rounds >= 1;
+        if (!b->device && !b->in_place) need += b->bytes;
     }
     Domain *d = c->domain;
     d->residency.reserve_batches++;
@@ -468,6 +483,7 @@ void reserve(Context *c, const std::vector<Buffer *> &list) {
     }
     for (Buffer *b : list) {
         b->last_use = ++d->tick;
+        if (b->in_place) continue;
         if (b->device) {
             d->residency.reuse_hits++;
             continue;
@@ -710,13 +726,43 @@ Task make_task(uint64_t code_key, const fort_scope_kernel_v1 &k, const size_t *s
     return t;
 }
 
+// A device use of an array: count consecutive uses preceded by host access.
+void note_device_use(Buffer *b) {
+    b->host_rounds = b->host_touched ? b->host_rounds + 1 : 0;
+    b->host_touched = false;
+    b->in_place = false;
+}
+
 void accept(Context *c, Task &&task, std::vector<Bound> &bound) {
     for (auto &x : bound)
-        if (!x.buffer->device) raise(FORT_SCOPE_STATE, "task binds an array whose device storage is not reserved");
+        if (!x.buffer->device && !x.buffer->in_place)
+            raise(FORT_SCOPE_STATE, "task binds an array whose device storage is not reserved");
     ensure_stream(c);
-    device_acquire(c, bound);
+    std::vector<Bound> mirrored, in_place;
+    for (auto &x : bound) (x.buffer->in_place ? in_place : mirrored).push_back(x);
+    device_acquire(c, mirrored);
+    // arrays accessed in place: the host copy must hold what the task reads
+    bool drained = false;
+    for (auto &x : in_place) {
+        Region down = needed(x.buffer, x.effects);
+        down.remove(x.buffer->host_valid);
+        if (down.empty()) continue;
+        if (!drained) {
+            flush(c);  // queued tasks that write the device copy run first
+            drained = true;
+        }
+        copy_region(c, x.buffer, down, false);
+        Region host = x.buffer->host_valid;
+        host.add(down);
+        settle(c, x.buffer, x.buffer->defined, host, x.buffer->device_valid);
+    }
+    for (auto &x : mirrored) device_commit(c, x.buffer, x.effects.writes, x.effects.overwrites);
+    for (auto &x : in_place) {
+        host_commit(c, x.buffer, x.effects.writes, x.effects.overwrites);
+        trace_line(c, "in_place", x.buffer->handle, x.buffer->bytes);
+    }
     for (auto &x : bound) {
-        device_commit(c, x.buffer, x.effects.writes, x.effects.overwrites);
+        note_device_use(x.buffer);
         x.buffer->queued++;
         task.buffers.push_back(x.buffer->handle);
     }
@@ -1178,7 +1224,7 @@ static int register_impl(fort_scope_t context, uint64_t identity, uint64_t gener
             for (size_t n = 0; n < initialized_count; ++n) b->defined.add(section_box(b.get(), initialized[n]));
         }
         if (!Backend::cpu && bytes >= (size_t(1) << 20) && env_flag("FORT_SCOPE_PIN_HOST", true))
-            b->pinned_host = Backend::pin(b->host, bytes);
+            b->pinned_host = Backend::pin(b->host, bytes, &b->mapped);
         *out = b->handle;
         trace_line(c, "register", b->handle, bytes);
         d->by_identity[identity] = b->handle;
@@ -1276,8 +1322,9 @@ int fort_scope_access_begin_v1(fort_scope_t context, const fort_scope_plan_bindi
             flush(c);
             std::vector<Buffer *> list;
             for (auto &x : bound) list.push_back(x.buffer);
-            reserve(c, list);
+            reserve(c, list, false);
             device_acquire(c, bound);
+            for (auto &x : bound) note_device_use(x.buffer);
         } else {
             host_acquire(c, bound);
         }
@@ -1334,6 +1381,7 @@ static int end_impl(fort_scope_t context, fort_buffer_t buffer, bool device) {
             device_commit(c, b, b->prep_writes, b->prep_overwrites);
         } else {
             host_commit(c, b, b->prep_writes, b->prep_overwrites);
+            b->host_touched = true;
         }
         b->prepared = Buffer::NONE;
         b->prep_writes.clear();
@@ -1373,8 +1421,11 @@ int fort_scope_device_reserve_many_v1(fort_scope_t context, const fort_buffer_t 
             if (seen.insert(b->handle).second) list.push_back(b);
         }
         if (list.empty()) return FORT_SCOPE_OK;
-        reserve(c, list);
-        for (size_t n = 0; n < count; ++n) devices[n] = find_buffer(c, buffers[n])->device;
+        reserve(c, list, true);
+        for (size_t n = 0; n < count; ++n) {
+            const Buffer *b = find_buffer(c, buffers[n]);
+            devices[n] = b->in_place ? b->mapped : b->device;
+        }
         return FORT_SCOPE_OK;
     });
 }
@@ -1395,6 +1446,7 @@ int fort_scope_observe_v1(fort_scope_t context, const fort_buffer_t *buffers, si
         flush(c);
         bool any = false;
         for (Buffer *b : list) {
+            b->host_touched = true;
             if (!b->device) continue;
             Region dirty = b->defined.clip(b->device_valid);
             dirty.remove(b->host_valid);
