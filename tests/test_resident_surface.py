@@ -1,0 +1,278 @@
+"""The resident build surface: TOML description, procedure splice, !$fort directives, CMake (CPU only).
+
+Follows the reference's own surface tests (tests/test_resident_directives.py,
+tests/test_resident_application.py): directives expand to calls on the
+application's residency object, malformed ones are refused with the line,
+selected procedures get a call block that falls back to the original
+statements, and a described application prepares into resident and native
+source trees with one build. The Fortran produced is checked structurally
+here; no Fortran compiler exists on these machines to compile it.
+"""
+
+import json
+import re
+from pathlib import Path
+
+import pytest
+
+from compiler import emission
+from compiler.resident import __main__ as cli
+from compiler.resident import application, directives, fortran, splice
+
+CDU_TOML = Path("/root/reference/benchmarks/cdu/cdu.toml")
+
+SYNTHETIC = """\
+! kernels
+module MomentumAdvection
+  implicit none
+  private
+  integer, parameter :: knd = kind(1.0d0)
+contains
+
+  ! kernel
+  subroutine set(arr, val, Unx, Uny, &
+                 Unz)
+    real(knd), contiguous, intent(out) :: arr(:,:,:)
+    real(knd), intent(in) :: val
+    integer, intent(in) :: Unx, Uny, Unz
+    integer :: i, j, k
+
+    !$OMP PARALLEL DO PRIVATE(i, j)
+    do k = 2, Unz + 1
+      do j = 2, Uny + 1
+        do i = 2, Unx + 1
+          arr(i,j,k) = val
+        end do
+      end do
+    end do
+    !$OMP END PARALLEL DO
+  end subroutine set
+
+  pure recursive function helper(n) result(r)
+    integer, intent(in) :: n
+    integer :: r
+    r = n + 1
+  contains
+    pure function inner(x) result(y)
+      integer, intent(in) :: x
+      integer :: y
+      y = x
+    end function inner
+  end function helper
+end module MomentumAdvection
+"""
+
+
+def _balanced(text: str):
+    blocks = ends = ifs = endifs = 0
+    for line in text.splitlines():
+        code = line.split("!", 1)[0].strip().lower()
+        blocks += code == "block"
+        ends += code == "end block"
+        ifs += bool(re.match(r"if\s*\(.*\)\s*then$", code))
+        endifs += code in ("endif", "end if")
+    assert blocks == ends and ifs == endifs, (blocks, ends, ifs, endifs)
+
+
+def test_procedure_finder_locates_executable_parts():
+    found = {p.qualified: p for p in fortran.procedures(SYNTHETIC)}
+    assert set(found) == {"momentumadvection::set", "momentumadvection::helper"}
+    lines = SYNTHETIC.splitlines()
+    s = found["momentumadvection::set"]
+    assert lines[s.header].strip().startswith("subroutine set(")
+    assert lines[s.body].strip() == "!$OMP PARALLEL DO PRIVATE(i, j)"
+    assert lines[s.end].strip() == "end subroutine set"
+    h = found["momentumadvection::helper"]
+    assert lines[h.body].strip() == "r = n + 1"
+    assert lines[h.end].strip() == "contains"
+
+
+@pytest.mark.parametrize("line, call", [
+    ("!$fort enter", "call resident%begin_epoch(int(0, c_int))"),
+    ("!$fort enter budget(2_8**30) device(1)", "call resident%begin_epoch(int(1, c_int), int(2_8**30, c_size_t))"),
+    ("!$fort leave", "if (resident%active) call resident%end_epoch()"),
+    ("!$fort close", "call resident%close()"),
+    ("!$fort publish if(step == n)", "if (resident%active .and. (step == n)) call resident%publish()"),
+    ("!$fort active(on_device)", "on_device = resident%active"),
+    ("!$fort release(tmp, work%buf)", "call resident%release(work%buf)"),
+])
+def test_directives_expand_to_residency_calls(line, call):
+    text, records = directives.expand("program p\n    " + line + "\nend program p\n", origin="p")
+    assert call in text
+    assert "!$fort" not in text
+    assert records[0]["line"] == 2
+    _balanced(text)
+
+
+def test_observe_binds_and_observes_named_arrays():
+    text, _ = directives.expand("  !$fort observe(U, V) if(mod(step, 10) == 0)\n", origin="main")
+    assert "integer(c_int64_t) :: fort_observed(2)" in text
+    assert "fort_observed(2) = resident%bind_real64(V, lbound(V), .true., origin='main::v')" in text
+    assert "if (resident%active .and. (mod(step, 10) == 0)) then" in text
+    assert "call resident%observe(fort_observed)" in text
+
+
+def test_annotations_generate_no_code():
+    text, records = directives.expand("  !$fort host\n  !$fort reduction(+: total)\n")
+    assert text.strip() == ""
+    assert [r["directive"] for r in records] == ["host", "reduction"]
+
+
+@pytest.mark.parametrize("line, message", [
+    ("!$fort launch", "unknown residency directive"),
+    ("!$fort enter budget", "unsupported clause"),
+    ("!$fort leave if(x)", "unsupported clause"),
+    ("!$fort observe", "needs a list"),
+    ("!$fort close(U)", "takes no list"),
+    ("!$fort observe(U(1:3))", "array names"),
+    ("!$fort active(a, b)", "one logical variable"),
+    ("!$fort observe(U", "unbalanced"),
+])
+def test_malformed_directives_are_refused_with_their_line(line, message):
+    with pytest.raises(directives.DirectiveError, match=message) as info:
+        directives.expand("program p\n\n  " + line + "\nend program p\n")
+    assert "line 3" in str(info.value)
+
+
+def test_splice_calls_the_entry_and_keeps_the_original_statements():
+    text, done = splice.splice(SYNTHETIC, ["momentumadvection::*"])
+    entry = emission.entry_for("MomentumAdvection::set")
+    assert [(d.procedure, d.entry, d.nests) for d in done] == [("momentumadvection::set", entry.symbol, 1)]
+    assert f"use {entry.fortran_module}, only: fort_device_run => run" in text
+    call = re.search(r"fort_status = fort_device_run\((.*?)\)\n", text, re.S).group(1)
+    args = [a.strip(" &\n") for a in call.split(",")]
+    assert args == ["resident%context", "FORT_SCOPE_GPU", "fort_handle_arr", "val", "Unx", "Uny", "Unz"]
+    # the fallback holds the original loop nest, unchanged
+    fallback = text[text.index("if (.not. fort_resident) then"):]
+    assert "          arr(i,j,k) = val" in fallback
+    assert fallback.index("call resident%publish()") < fallback.index("arr(i,j,k) = val")
+    # the helper has no template and is left alone
+    assert "r = n + 1\n  contains" in text
+    _balanced(text)
+
+
+def test_call_block_arguments_follow_the_generated_interfaces():
+    """Every spliceable entry's call passes what its Fortran interface declares, in that order."""
+    interfaces = (Path(emission.__file__).parents[2] / "fortran" / "fort_shared_entries.f90").read_text()
+    for entry in emission.registry():
+        block = splice.call_block(entry, "")
+        call = re.search(r"fort_status = fort_device_run\((.*?)\)\n", block, re.S).group(1)
+        args = [a.strip(" &\n").lower() for a in call.split(",")]
+        module = interfaces[interfaces.index(f"module {entry.fortran_module}\n"):]
+        header = re.search(r"function run\((.*?)\) bind", module, re.S).group(1)
+        declared = [a.strip(" &\n") for a in header.split(",")]
+        assert len(args) == len(declared)
+        for a, d in zip(args[2:], declared[2:]):
+            assert d == (a.removeprefix("fort_handle_") + "_handle" if a.startswith("fort_handle_") else a)
+
+
+def _write_app(tmp_path, minimum=1, extra=""):
+    (tmp_path / "src").mkdir()
+    (tmp_path / "src" / "kernels.f90").write_text(SYNTHETIC)
+    (tmp_path / "src" / "main.f90").write_text(
+        "program main\n  use MomentumAdvection\n  implicit none\n  ! timed\n  call work()\nend program main\n")
+    (tmp_path / "app.toml").write_text(f"""
+name = "Synthetic"
+sources = ["src/kernels.f90", "src/main.f90"]
+program = "src/main.f90"
+[variants.default]
+defines = ["SMALL"]
+[[selection]]
+label = "advection"
+procedures = ["momentumadvection::*"]
+minimum_nests = {minimum}
+[[edit]]
+file = "main.f90"
+at = "  ! timed\\n"
+action = "before"
+text = "  !$fort enter\\n"
+[[edit]]
+file = "main.f90"
+at = "end program main"
+action = "before"
+text = "  !$fort close\\n"
+[build]
+fortran_options = ["-O2"]
+[[executable]]
+name = "synthetic"
+library = "resident"
+[[executable]]
+name = "synthetic-native"
+library = "native"
+{extra}""")
+    return tmp_path / "app.toml"
+
+
+def test_described_application_prepares_resident_and_native_trees(tmp_path):
+    app = application.load(_write_app(tmp_path))
+    application.prepare(app, tmp_path / "out")
+    out = tmp_path / "out"
+    assert (out / "native" / "kernels.f90").read_text() == SYNTHETIC
+    resident_main = (out / "resident" / "main.f90").read_text()
+    assert resident_main.index("begin_epoch") < resident_main.index("! timed")
+    assert resident_main.index("call resident%close()") < resident_main.index("end program main")
+    _balanced(resident_main)
+    cmake = (out / "CMakeLists.txt").read_text()
+    assert "project(Synthetic LANGUAGES Fortran)" in cmake
+    assert "-ffp-contract=off" in cmake and "-DSMALL" in cmake
+    assert 'add_executable(synthetic "resident/main.f90")' in cmake
+    assert 'add_executable(synthetic-native "native/main.f90")' in cmake
+    assert "fort_resident_domain.f90" in cmake and "fort_shared_entries.f90" in cmake
+    report = json.loads((out / "resident_build.json").read_text())
+    assert report["nests"] == {"advection": 1}
+    assert [d["directive"] for d in report["directives"]] == ["enter", "close"]
+
+
+def test_minimum_nests_is_enforced(tmp_path):
+    app = application.load(_write_app(tmp_path, minimum=2))
+    with pytest.raises(application.DescriptionError, match="fewer than minimum_nests = 2"):
+        application.prepare(app, tmp_path / "out")
+
+
+@pytest.mark.parametrize("extra, message", [
+    ("[[patch]]\nfile = 'x'\n", "outside the advection path"),
+    ("[unexpected]\nx = 1\n", "unknown keys"),
+    ("[[edit]]\nfile = 'main.f90'\nat = 'nowhere'\naction = 'before'\ntext = 'x'\n", "anchor found 0 times"),
+    ("[[edit]]\nfile = 'main.f90'\nat = 'x'\naction = 'sideways'\ntext = 'x'\n", "before, after or replace"),
+])
+def test_description_errors(tmp_path, extra, message):
+    path = _write_app(tmp_path, extra=extra)
+    with pytest.raises(application.DescriptionError, match=message):
+        application.prepare(application.load(path), tmp_path / "out")
+
+
+def test_cli_prepare_only(tmp_path, capsys):
+    assert cli.main([str(_write_app(tmp_path)), "--output", str(tmp_path / "out"), "--prepare-only"]) == 0
+    line = json.loads(capsys.readouterr().out)
+    assert line == {"application": "Synthetic", "entries": 1, "nests": {"advection": 1}, "directives": 2,
+                    "outcome": "prepared"}
+    (tmp_path / "bad").mkdir()
+    assert cli.main([str(_write_app(tmp_path / "bad", minimum=5)), "--output", str(tmp_path / "o2")]) == 2
+
+
+@pytest.mark.skipif(not CDU_TOML.exists(), reason="the reference's cdu benchmark is not on this machine")
+def test_reference_cdu_description_prepares(tmp_path):
+    app = application.load(CDU_TOML)
+    application.prepare(app, tmp_path)
+    report = app.report
+    spliced = {e["procedure"]: e["entry"] for e in report["entries"]}
+    for name in ("set", "multiply", "cdudiv", "cduadv", "cdu"):
+        assert spliced[f"momentumadvection::{name}"] == emission.entry_for(f"MomentumAdvection::{name}").symbol
+    assert report["nests"]["advection"] >= 4
+    main = (tmp_path / "resident" / "main.f90").read_text()
+    assert main.index("begin_epoch") < main.index("! ---- warm-up ----")
+    assert main.index("end_epoch") < main.index("call system_clock(t_end)")
+    assert main.index("call resident%close()") < main.index("deallocate(U, V, W, U2)")
+    kernels = (tmp_path / "resident" / "cdu.f90").read_text()
+    _balanced(kernels)
+    _balanced(main)
+    assert (tmp_path / "native" / "cdu.f90").read_text() == (CDU_TOML.parent / "src" / "cdu.f90").read_text()
+
+
+def test_fortran_modules_bind_only_declared_c_entry_points():
+    """Every bind(C) name the Fortran modules call is declared by the C ABI headers."""
+    root = Path(emission.__file__).parents[2]
+    headers = "".join(p.read_text() for p in (root.parent / "include").glob("*.h"))
+    for source in (root / "fortran").glob("*.f90"):
+        for name in re.findall(r"bind\(C,\s*name='(\w+)'\)", source.read_text()):
+            assert re.search(rf"\b{name}\s*\(", headers), f"{source.name}: {name} is not in include/*.h"
