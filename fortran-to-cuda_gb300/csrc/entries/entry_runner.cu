@@ -12,7 +12,9 @@
 // then publishes the domain and runs the original Fortran statements.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <array>
+#include <cstdlib>
 #include <cstring>
 #include <deque>
 #include <vector>
@@ -51,9 +53,10 @@ struct Geometry {
     long long n[3];
     long long h;
     size_t ext[3];
-    // [h+a, h+n+b) on axis d
-    size_t lo(int d, int a) const { return (size_t)(h + a); }
-    size_t hi(int d, int b) const { return (size_t)(h + n[d] + b); }
+    long long z0 = 0; // first interior plane of a slab (0 for the whole domain)
+    // [h+a, h+n+b) on axis d, shifted by z0 along the last axis
+    size_t lo(int d, int a) const { return (size_t)(h + a + (d == 2 ? z0 : 0)); }
+    size_t hi(int d, int b) const { return (size_t)(h + n[d] + b + (d == 2 ? z0 : 0)); }
     Triple box_lo(int ax, int ay, int az) const { return {lo(0, ax), lo(1, ay), lo(2, az)}; }
     Triple box_hi(int bx, int by, int bz) const { return {hi(0, bx), hi(1, by), hi(2, bz)}; }
 };
@@ -86,6 +89,48 @@ struct Use {
 
 int declined() { return FORT_SCOPE_DECLINED; }
 
+// Sections of the advection step (U, V, W tendencies and ns scalars): outputs
+// write the interior, each velocity is read on its own cross and on the
+// staggered neighbours of the other two momentum equations, scalars on their cross.
+void step_sections(std::deque<Use> &uses, const Geometry &g, int ns) {
+    for (int n = 0; n < 3; ++n) add_interior(uses[n].writes, g);
+    Use &U = uses[3], &V = uses[4], &W = uses[5];
+    add_cross(U.reads, g);
+    add_cdv_u(U.reads, g);
+    add_cdw_u(U.reads, g);
+    add_cross(V.reads, g);
+    add_cdu_v(V.reads, g);
+    add_cdw_v(V.reads, g);
+    add_cross(W.reads, g);
+    add_cdu_w(W.reads, g);
+    add_cdv_w(W.reads, g);
+    for (int n = 0; n < ns; ++n) {
+        add_cross(uses[6 + n].reads, g);
+        add_interior(uses[6 + ns + n].writes, g);
+    }
+}
+
+// Bindings of one task: each array's reads, and its writes (exact overwrites where every written element is written).
+std::vector<fort_scope_plan_binding> bindings_of(std::deque<Use> &uses) {
+    std::vector<fort_scope_plan_binding> bindings;
+    for (auto &u : uses) {
+        fort_scope_plan_binding b{};
+        b.buffer = u.handle;
+        b.access.read_count = u.reads.size();
+        b.access.reads = u.reads.size() ? u.reads.data() : nullptr;
+        if (u.written) {
+            b.access.write_count = u.writes.size();
+            b.access.writes = u.writes.data();
+            if (u.overwritten) {
+                b.access.overwrite_count = u.writes.size();
+                b.access.overwrites = b.access.writes;
+            }
+        }
+        bindings.push_back(b);
+    }
+    return bindings;
+}
+
 template <int NS, int MASK>
 void faces_spec(const AdvArgs &a, fort_scope_kernel_v1 &k) {
     using Smem = FaceSmem<NS, MASK>;
@@ -114,6 +159,92 @@ void faces_spec_ns(int ns, const AdvArgs &a, fort_scope_kernel_v1 &k) {
     case 3: faces_spec<3, MASK>(a, k); break;
     default: faces_spec<4, MASK>(a, k); break;
     }
+}
+
+// Planes per slab when a step is cut into slabs to overlap host transfers with
+// the kernels (F2C_SLAB_PLANES overrides, read once per process).
+constexpr int kSlabPlanes = 12;
+int slab_planes() {
+    static const int planes = [] {
+        const char *v = std::getenv("F2C_SLAB_PLANES");
+        const int p = v ? std::atoi(v) : 0;
+        return p >= 2 ? p : kSlabPlanes;
+    }();
+    return planes;
+}
+
+// Slab boundaries along z: slabs of `planes` levels between a first and a last
+// slab of half that depth (thin ends shorten the pipeline's fill, when only
+// uploads run, and its drain, when only publications run); at most 62 slabs.
+std::vector<int> slab_bounds(int nz, int planes) {
+    planes = std::max(planes, (nz + 59) / 60);
+    const int edge = std::max(1, planes / 2);
+    std::vector<int> b{0};
+    if (nz < 2 * edge + planes) {
+        const int count = std::max(1, nz / std::max(1, planes));
+        for (int s = 1; s <= count; ++s) b.push_back((int)((long long)s * nz / count));
+        return b;
+    }
+    const int middle = nz - 2 * edge;
+    const int count = (middle + planes - 1) / planes;
+    b.push_back(edge);
+    for (int s = 1; s <= count; ++s) b.push_back(edge + (int)((long long)s * middle / count));
+    b.push_back(nz);
+    return b;
+}
+
+// The step as a sequence of slab tasks along z: task s computes interior planes
+// [k0, k1) with every array pointer moved to plane k0 (the kernel addresses
+// planes relative to its interior start and reads one plane either side).
+int enqueue_step_slabs(const EntryCall &call, const Geometry &g, const std::deque<Use> &roles, const AdvArgs &whole,
+                       int ns) {
+    const std::vector<int> bounds = slab_bounds((int)g.n[2], slab_planes());
+    const int count = (int)bounds.size() - 1;
+    std::vector<AdvArgs> args(count);
+    std::vector<void *> argument_of(count);
+    std::vector<std::deque<Use>> uses(count);
+    std::vector<std::vector<fort_scope_plan_binding>> bindings(count);
+    std::vector<fort_scope_graph_task_v1> tasks(count);
+    std::vector<size_t> sizes(count, sizeof(AdvArgs));
+    for (int s = 0; s < count; ++s) {
+        const int k0 = bounds[s], k1 = bounds[s + 1];
+        const long long shift = (long long)k0 * whole.plane;
+        AdvArgs &a = args[s];
+        a = whole;
+        a.u += shift;
+        a.v += shift;
+        a.w += shift;
+        for (int n = 0; n < 3; ++n) a.out[n] += shift;
+        for (int n = 0; n < ns; ++n) {
+            a.s[n] += shift;
+            a.st[n] += shift;
+        }
+        a.nz = k1 - k0;
+        a.kz = chunk_depth(a.nx, a.ny, a.nz);
+        Geometry slab = g;
+        slab.n[2] = k1 - k0;
+        slab.z0 = k0;
+        for (const Use &r : roles) {
+            uses[s].emplace_back();
+            Use &u = uses[s].back();
+            u.handle = r.handle;
+            u.read = r.read;
+            u.written = r.written;
+            u.overwritten = r.overwritten;
+            u.intent_out = r.intent_out;
+        }
+        step_sections(uses[s], slab, ns);
+        bindings[s] = bindings_of(uses[s]);
+        argument_of[s] = &args[s];
+        fort_scope_kernel_v1 &k = tasks[s].kernel;
+        k.version = FORT_SCOPE_GRAPH_ABI_VERSION;
+        faces_spec_ns<7>(ns, a, k);
+        k.arguments = &argument_of[s];
+        k.argument_count = 1;
+        tasks[s].bindings = bindings[s].data();
+        tasks[s].binding_count = bindings[s].size();
+    }
+    return fort_scope_slab_enqueue_v1(call.context, call.code_key, tasks.data(), tasks.size(), sizes.data());
 }
 
 const void *procedure_function(Template t) {
@@ -316,24 +447,9 @@ int run(const EntryCall &call) {
         add_cdw_v(uses[2].reads, g);
         add_cross(uses[3].reads, g);
         break;
-    case Template::Step: case Template::StepAdvance: {
-        for (int n = 0; n < 3; ++n) out_sections(uses[n]);
-        Use &U = uses[3], &V = uses[4], &W = uses[5];
-        add_cross(U.reads, g);
-        add_cdv_u(U.reads, g);
-        add_cdw_u(U.reads, g);
-        add_cross(V.reads, g);
-        add_cdu_v(V.reads, g);
-        add_cdw_v(V.reads, g);
-        add_cross(W.reads, g);
-        add_cdu_w(W.reads, g);
-        add_cdv_w(W.reads, g);
-        for (int n = 0; n < ns; ++n) {
-            add_cross(uses[6 + n].reads, g);
-            out_sections(uses[6 + ns + n]);
-        }
+    case Template::Step: case Template::StepAdvance:
+        step_sections(uses, g, ns);
         break;
-    }
     case Template::Diffusion:
         out_sections(uses[0]);
         add_cross(uses[1].reads, g);
@@ -367,8 +483,14 @@ int run(const EntryCall &call) {
     std::vector<fort_buffer_t> handles;
     for (auto &u : uses) handles.push_back(u.handle);
     std::vector<void *> devices(handles.size(), nullptr);
+    // a deep step may run as slabs, its host transfers overlapped with the kernels
+    const bool sliceable = step && g.n[2] >= 2 * slab_planes();
+    int pipelined = 0;
     {
-        const int s = fort_scope_device_reserve_many_v1(call.context, handles.data(), handles.size(), devices.data());
+        const int s = sliceable ? fort_scope_device_reserve_slabs_v1(call.context, handles.data(), handles.size(),
+                                                                     devices.data(), &pipelined)
+                                : fort_scope_device_reserve_many_v1(call.context, handles.data(), handles.size(),
+                                                                    devices.data());
         if (s == FORT_SCOPE_RESOURCE) return declined();
         if (s) return s;
     }
@@ -431,6 +553,7 @@ int run(const EntryCall &call) {
         adv.sx = sx; adv.plane = plane;
         adv.c = make_coefficients(*call.reals[0], *call.reals[1], *call.reals[2]);
         adv.kz = chunk_depth(adv.nx, adv.ny, adv.nz);
+        if (pipelined) return enqueue_step_slabs(call, g, uses, adv, ns);
         faces_spec_ns<7>(ns, adv, kernel);
         argument = &adv;
         argument_size = sizeof adv;
@@ -481,22 +604,7 @@ int run(const EntryCall &call) {
     kernel.argument_count = 1;
 
     // ---- one queued task with the exact effects ----
-    std::vector<fort_scope_plan_binding> bindings;
-    for (auto &u : uses) {
-        fort_scope_plan_binding b{};
-        b.buffer = u.handle;
-        b.access.read_count = u.reads.size();
-        b.access.reads = u.reads.size() ? u.reads.data() : nullptr;
-        if (u.written) {
-            b.access.write_count = u.writes.size();
-            b.access.writes = u.writes.data();
-            if (u.overwritten) {
-                b.access.overwrite_count = u.writes.size();
-                b.access.overwrites = b.access.writes;
-            }
-        }
-        bindings.push_back(b);
-    }
+    std::vector<fort_scope_plan_binding> bindings = bindings_of(uses);
     fort_scope_graph_task_v1 task{};
     task.kernel = kernel;
     task.bindings = bindings.data();

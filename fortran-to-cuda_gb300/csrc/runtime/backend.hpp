@@ -123,8 +123,16 @@ struct Backend {
         return true;
     }
     static bool sync(Stream) { return !std::getenv("F2C_TEST_FAIL_WAIT"); }
-    static bool pin(void *, size_t, void **) { return false; }
+    // Host arrays are never pinned here, unless a test asks for the mapped
+    // case (F2C_TEST_MAPPED): then the "device-usable" address is the array.
+    static bool pin(void *p, size_t, void **mapped) {
+        if (!std::getenv("F2C_TEST_MAPPED")) return false;
+        *mapped = p;
+        return true;
+    }
     static void unpin(void *) {}
+    // Work is synchronous: every stream is already joined.
+    static bool join(Stream, Stream) { return true; }
     static bool memory_info(size_t *free_bytes, size_t *total) {
         *total = size_t(16) << 30;
         *free_bytes = size_t(12) << 30;
@@ -182,6 +190,16 @@ struct Backend {
     static void free(void *p, Stream s) {
         if (p) cudaFreeAsync(p, s);
     }
+    // One contiguous host<->device copy. A large copy whose host start is not on
+    // a 2 MiB boundary goes as a head up to that boundary and an aligned body:
+    // with uploads and downloads running at once, a copy from a misaligned host
+    // start moves about 116 GB/s each way on GB300 and an aligned one 171 GB/s.
+    static bool contiguous(char *d, const char *sp, size_t bytes, cudaMemcpyKind kind, const char *host, Stream s) {
+        constexpr size_t kAlign = size_t(2) << 20;
+        const size_t head = (kAlign - reinterpret_cast<uintptr_t>(host) % kAlign) % kAlign;
+        if (bytes < 4 * kAlign || head == 0) return ok(cudaMemcpyAsync(d, sp, bytes, kind, s));
+        return ok(cudaMemcpyAsync(d, sp, head, kind, s)) && ok(cudaMemcpyAsync(d + head, sp + head, bytes - head, kind, s));
+    }
     static bool copy(void *dst, const void *src, const CopyPlan &plan, const Box &box, bool to_device, Stream s) {
         const cudaMemcpyKind kind = to_device ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost;
         const bool full_rows = box.lo[0] == 0 && box.hi[0] == plan.extents[0];
@@ -204,7 +222,7 @@ struct Backend {
             char *d = static_cast<char *>(dst) + off * plan.elem;
             const char *sp = static_cast<const char *>(src) + off * plan.elem;
             if (rows == 1)
-                good = ok(cudaMemcpyAsync(d, sp, width * plan.elem, kind, s));
+                good = contiguous(d, sp, width * plan.elem, kind, to_device ? sp : d, s);
             else
                 good = ok(cudaMemcpy2DAsync(d, pitch * plan.elem, sp, pitch * plan.elem, width * plan.elem, rows, kind,
                                             s));
@@ -212,6 +230,14 @@ struct Backend {
         return good;
     }
     static bool sync(Stream s) { return ok(cudaStreamSynchronize(s)); }
+    // `waiter` runs its later work after everything queued so far on `signaller`.
+    static bool join(Stream waiter, Stream signaller) {
+        cudaEvent_t e;
+        if (!ok(cudaEventCreateWithFlags(&e, cudaEventDisableTiming))) return false;
+        const bool good = ok(cudaEventRecord(e, signaller)) && ok(cudaStreamWaitEvent(waiter, e, 0));
+        cudaEventDestroy(e);
+        return good;
+    }
     // Pin a host array in place and map it into the device address space;
     // `mapped` receives the address a kernel uses to reach it over NVLink-C2C.
     static bool pin(void *p, size_t bytes, void **mapped) {

@@ -149,6 +149,9 @@ struct Context {
     bool poisoned = false;
     Stream stream = nullptr;
     bool stream_ready = false;
+    // copy streams of slab pipelines: uploads ahead of the kernels, publication behind them
+    Stream copy_in = nullptr, copy_out = nullptr;
+    bool copies_ready = false;
     bool queue_enabled = true, graphs_enabled = true;
     uint64_t queue_work_limit = uint64_t(1) << 18;
     std::vector<Task> pending;
@@ -229,6 +232,17 @@ void ensure_stream(Context *c) {
     c->stream_ready = true;
 }
 
+void ensure_copy_streams(Context *c) {
+    ensure_stream(c);
+    if (c->copies_ready) return;
+    if (!Backend::make_stream(&c->copy_in)) raise(FORT_SCOPE_RESOURCE, "cannot create stream: " + Backend::last_error());
+    if (!Backend::make_stream(&c->copy_out)) {
+        Backend::destroy_stream(c->copy_in);
+        raise(FORT_SCOPE_RESOURCE, "cannot create stream: " + Backend::last_error());
+    }
+    c->copies_ready = true;
+}
+
 // ---- effects --------------------------------------------------------------------------------
 
 struct Effects {
@@ -284,17 +298,24 @@ void check_initialized(const Buffer *b, const Effects &e) {
 
 Box bounding(const Region &r);
 
-// The region actually moved for a needed transfer `r`: the whole array or the
-// bounding box of `r` when that moves at most a quarter more bytes and cannot
-// overwrite values only the destination holds; `r` itself otherwise. Fewer,
-// larger copies keep the copy engines busy instead of the host.
+// The region actually moved for a needed transfer `r`: the whole array, the
+// whole planes (every dimension but the last complete) spanning `r`, or the
+// bounding box of `r`, the first of these that moves at most a quarter more
+// bytes and cannot overwrite values only the destination holds; `r` itself
+// otherwise. Fewer, larger (and, for whole planes, contiguous) copies keep the
+// copy engines busy instead of the host.
 Region widened(const Buffer *b, const Region &r, bool to_device) {
     if (r.boxes.size() <= 1) return r;
     Region only_destination = to_device ? b->device_valid : b->host_valid;
     only_destination.remove(to_device ? b->host_valid : b->device_valid);
     only_destination = b->defined.clip(only_destination);
     const size_t need = r.volume();
-    const Box candidates[2] = {b->full(), bounding(r)};
+    Box planes = bounding(r);
+    for (int d = 0; d + 1 < planes.rank; ++d) {
+        planes.lo[d] = 0;
+        planes.hi[d] = b->extents[d];
+    }
+    const Box candidates[3] = {b->full(), planes, bounding(r)};
     for (const Box &cand : candidates) {
         if ((double)cand.volume() > 1.25 * (double)need) continue;
         Region clash = only_destination.clip(cand);
@@ -307,14 +328,14 @@ Region widened(const Buffer *b, const Region &r, bool to_device) {
     return r;
 }
 
-void copy_region(Context *c, Buffer *b, const Region &r, bool to_device) {
+void copy_region(Context *c, Buffer *b, const Region &r, bool to_device, Stream stream) {
     Domain *d = c->domain;
     const CopyPlan plan = b->plan();
     for (const auto &box : r.boxes) {
         const size_t bytes = box.volume() * b->elem;
         if (!bytes) continue;
-        bool good = to_device ? Backend::copy(b->device, b->host, plan, box, true, c->stream)
-                              : Backend::copy(b->host, b->device, plan, box, false, c->stream);
+        bool good = to_device ? Backend::copy(b->device, b->host, plan, box, true, stream)
+                              : Backend::copy(b->host, b->device, plan, box, false, stream);
         if (!good) poison(c, std::string("transfer failed: ") + Backend::last_error());
         if (to_device) {
             d->stats.uploads++;
@@ -327,6 +348,8 @@ void copy_region(Context *c, Buffer *b, const Region &r, bool to_device) {
         }
     }
 }
+
+void copy_region(Context *c, Buffer *b, const Region &r, bool to_device) { copy_region(c, b, r, to_device, c->stream); }
 
 void wait_stream(Context *c) {
     if (!c->stream_ready) return;
@@ -778,6 +801,101 @@ void accept(Context *c, Task &&task, std::vector<Bound> &bound) {
     if (!c->queue_enabled || (c->queue_work_limit && c->pending_threads >= c->queue_work_limit)) flush(c);
 }
 
+// ---- slab pipelines -------------------------------------------------------------------------
+
+constexpr size_t kMaxSlabs = 64;
+
+bool streaming_allowed() {
+    static const bool on = env_flag("FORT_SCOPE_HOST_STREAM", true);
+    return on;
+}
+
+// An array in pinned host memory that the host read or rewrote before each of
+// its recent device uses: its transfers are worth overlapping with the kernels.
+bool host_round(const Buffer *b) {
+    return b->mapped && b->prepared == Buffer::NONE && b->host_touched && b->host_rounds >= 1;
+}
+
+// Run tasks over successive slabs of the same arrays three streams deep:
+// copy_in uploads what task n reads ahead of its kernel, the context stream
+// runs the kernels in order, copy_out publishes what task n wrote into
+// host-round arrays behind it. A kernel waits for its own uploads and, where
+// it writes what an earlier publication still reads, for that publication.
+// Uploads of an array being published move exactly what is stale on the device
+// (never widened over values in flight), and publications move exactly what a
+// task wrote. Finally the context stream joins both copy streams, so every
+// later operation of the context, and a wait on it, orders after the sequence.
+void run_slabs(Context *c, std::vector<Task> &tasks, std::vector<std::vector<Bound>> &bound) {
+    std::set<Buffer *> publish, all;
+    for (auto &list : bound)
+        for (auto &x : list) {
+            all.insert(x.buffer);
+            if (host_round(x.buffer) && !x.effects.writes.empty()) publish.insert(x.buffer);
+        }
+    flush(c);
+    ensure_copy_streams(c);
+    auto join = [&](Stream waiter, Stream signaller) {
+        if (!Backend::join(waiter, signaller)) poison(c, std::string("stream ordering failed: ") + Backend::last_error());
+    };
+    join(c->copy_in, c->stream);
+    join(c->copy_out, c->stream);
+    std::map<Buffer *, Region> publishing;
+    for (size_t n = 0; n < tasks.size(); ++n) {
+        bool uploaded = false;
+        for (auto &x : bound[n]) {
+            Buffer *b = x.buffer;
+            Region up = needed(b, x.effects);
+            up.remove(b->device_valid);
+            if (up.empty()) continue;
+            const Region moved = publish.count(b) ? up : widened(b, up, true);
+            copy_region(c, b, moved, true, c->copy_in);
+            Region device = b->device_valid;
+            device.add(up);
+            device.add(b->host_valid.clip(moved));
+            settle(c, b, b->defined, b->host_valid, device);
+            uploaded = true;
+        }
+        if (uploaded) join(c->stream, c->copy_in);
+        bool clash = false;
+        for (auto &x : bound[n]) {
+            auto it = publishing.find(x.buffer);
+            if (it != publishing.end() && !it->second.clip(x.effects.writes).empty()) clash = true;
+        }
+        if (clash) join(c->stream, c->copy_out);
+        trace_line(c, "slab_launch", 0, n);
+        if (!Backend::launch(tasks[n].spec, c->stream))
+            poison(c, std::string("kernel launch failed: ") + Backend::last_error());
+        for (auto &x : bound[n]) device_commit(c, x.buffer, x.effects.writes, x.effects.overwrites);
+        bool ordered = false;
+        for (auto &x : bound[n]) {
+            Buffer *b = x.buffer;
+            if (!publish.count(b)) continue;
+            Region down = b->defined.clip(x.effects.writes);
+            down.remove(b->host_valid);
+            if (down.empty()) continue;
+            if (!ordered) {
+                join(c->copy_out, c->stream);
+                ordered = true;
+            }
+            copy_region(c, b, down, false, c->copy_out);
+            publishing[b].add(down);
+            Region host = b->host_valid;
+            host.add(down);
+            settle(c, b, b->defined, host, b->device_valid);
+        }
+    }
+    join(c->stream, c->copy_in);
+    join(c->stream, c->copy_out);
+    for (Buffer *b : all) note_device_use(b);
+    Domain *d = c->domain;
+    d->stats.launches += tasks.size();
+    c->graph_stats.submissions++;
+    c->graph_stats.logical_kernels += tasks.size();
+    c->queue_stats.accepted_tasks += tasks.size();
+    c->queue_stats.direct_submissions++;
+    c->queue_stats.direct_kernels += tasks.size();
+}
+
 Context *make_context(Domain *d, bool private_domain) {
     auto c = std::make_unique<Context>();
     c->handle = new_handle();
@@ -827,6 +945,13 @@ void release_scratch(Context *c) {
 }
 
 void detach(Context *c) {
+    if (c->copies_ready) {
+        Backend::sync(c->copy_in);
+        Backend::sync(c->copy_out);
+        Backend::destroy_stream(c->copy_in);
+        Backend::destroy_stream(c->copy_out);
+        c->copies_ready = false;
+    }
     if (c->stream_ready) {
         Backend::sync(c->stream);
         for (auto &kv : c->graphs)
@@ -1223,7 +1348,8 @@ static int register_impl(fort_scope_t context, uint64_t identity, uint64_t gener
                 raise(FORT_SCOPE_ARGUMENT, "initialized section list exceeds the bounded interface");
             for (size_t n = 0; n < initialized_count; ++n) b->defined.add(section_box(b.get(), initialized[n]));
         }
-        if (!Backend::cpu && bytes >= (size_t(1) << 20) && env_flag("FORT_SCOPE_PIN_HOST", true))
+        // arrays of 1 MiB or more are pinned in place (the CPU test backend pins only when a test asks)
+        if (bytes >= (Backend::cpu ? size_t(0) : size_t(1) << 20) && env_flag("FORT_SCOPE_PIN_HOST", true))
             b->pinned_host = Backend::pin(b->host, bytes, &b->mapped);
         *out = b->handle;
         trace_line(c, "register", b->handle, bytes);
@@ -1641,6 +1767,53 @@ int fort_scope_graph_enqueue_v1(fort_scope_t context, uint64_t code_key, const f
         Task t = make_task(code_key, task->kernel, argument_sizes);
         std::vector<Bound> bound = bind_all(c, task->bindings, task->binding_count);
         accept(c, std::move(t), bound);
+        return FORT_SCOPE_OK;
+    });
+}
+
+int fort_scope_device_reserve_slabs_v1(fort_scope_t context, const fort_buffer_t *buffers, size_t count,
+                                       void **devices, int *pipelined) {
+    return guarded([&] {
+        Context *c = live_context(context);
+        if (!pipelined || (count && (!buffers || !devices))) raise(FORT_SCOPE_ARGUMENT, "null reservation arrays");
+        *pipelined = 0;
+        std::vector<Buffer *> list;
+        std::set<uint64_t> seen;
+        for (size_t n = 0; n < count; ++n) {
+            Buffer *b = find_buffer(c, buffers[n]);
+            if (seen.insert(b->handle).second) list.push_back(b);
+        }
+        if (list.empty()) return FORT_SCOPE_OK;
+        const bool stream = streaming_allowed();
+        bool any = false;
+        for (Buffer *b : list) any = any || (stream && host_round(b));
+        reserve(c, list, !stream);
+        for (size_t n = 0; n < count; ++n) {
+            const Buffer *b = find_buffer(c, buffers[n]);
+            devices[n] = b->in_place ? b->mapped : b->device;
+        }
+        *pipelined = any ? 1 : 0;
+        return FORT_SCOPE_OK;
+    });
+}
+
+int fort_scope_slab_enqueue_v1(fort_scope_t context, uint64_t code_key, const fort_scope_graph_task_v1 *tasks,
+                               size_t count, const size_t *argument_sizes) {
+    return guarded([&] {
+        if (!tasks || count == 0 || count > kMaxSlabs) raise(FORT_SCOPE_ARGUMENT, "a slab sequence holds 1 to 64 tasks");
+        Context *c = live_context(context);
+        std::vector<Task> list;
+        std::vector<std::vector<Bound>> bound;
+        size_t offset = 0;
+        for (size_t n = 0; n < count; ++n) {
+            list.push_back(make_task(code_key, tasks[n].kernel, argument_sizes ? argument_sizes + offset : nullptr));
+            offset += tasks[n].kernel.argument_count;
+            bound.push_back(bind_all(c, tasks[n].bindings, tasks[n].binding_count));
+            for (auto &x : bound.back())
+                if (!x.buffer->device || x.buffer->in_place)
+                    raise(FORT_SCOPE_STATE, "a slab task binds an array without reserved device storage");
+        }
+        run_slabs(c, list, bound);
         return FORT_SCOPE_OK;
     });
 }

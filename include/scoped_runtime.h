@@ -285,6 +285,37 @@ int fort_scope_external_execute_v1(fort_scope_t context, const fort_scope_extern
                                    fort_scope_external_worker_v1 worker, void *user,
                                    fort_scope_external_report_v1 *report);
 
+/* ---- slab pipelines (extensions of this runtime; the reference has no counterpart) ----
+ *
+ * For a step whose arrays the host rewrites or reads between device uses
+ * (pinned host arrays, host-round: two or more consecutive uses each preceded
+ * by host access), the transfers can overlap the kernels when the step is cut
+ * into slabs along its last dimension.
+ *
+ * fort_scope_device_reserve_slabs_v1 reserves device storage like
+ * fort_scope_device_reserve_many_v1, except that no array is handed out in
+ * place while pipelines are enabled (FORT_SCOPE_HOST_STREAM, default 1), and
+ * sets *pipelined to 1 when at least one array is host-round: the caller then
+ * submits the step as slab tasks through fort_scope_slab_enqueue_v1, otherwise
+ * as one task through fort_scope_graph_enqueue_v1. With FORT_SCOPE_HOST_STREAM=0
+ * it is fort_scope_device_reserve_many_v1 and *pipelined is 0.
+ *
+ * fort_scope_slab_enqueue_v1 runs `count` (1..64) tasks in order, after every
+ * queued task: uploads of what task n reads run on a copy stream ahead of its
+ * kernel, the kernels run in order on the context's stream, and what task n
+ * writes into host-round arrays is published to the host on a second copy
+ * stream behind it, so the host copies are current when the call's work
+ * completes (a later host access or fort_scope_wait orders after all of it).
+ * Every bound array needs device storage from fort_scope_device_reserve_slabs_v1
+ * (FORT_SCOPE_STATE otherwise); each task's reads must be defined before the
+ * sequence starts; argument_sizes holds the sizes of every task's kernel
+ * arguments, task after task. Validation happens before any work; a failure
+ * after work started poisons the context (FORT_SCOPE_EXECUTION). */
+int fort_scope_device_reserve_slabs_v1(fort_scope_t context, const fort_buffer_t *buffers, size_t count,
+                                       void **devices, int *pipelined);
+int fort_scope_slab_enqueue_v1(fort_scope_t context, uint64_t code_key, const fort_scope_graph_task_v1 *tasks,
+                               size_t count, const size_t *argument_sizes);
+
 #ifdef __cplusplus
 }
 #endif

@@ -175,11 +175,14 @@ def test_budget_too_small_declines_before_any_work(cuda, capfd):
     assert capfd.readouterr().err.count("budget_warning") == 1
 
 
-def test_arrays_the_host_rewrites_every_step_are_streamed_in_place(resident, capfd):
-    """Host writes the inputs and reads the outputs between every step: after two such rounds the runtime
-    hands the kernel the mapped host arrays (no copies); results stay bit-identical to the oracle."""
+@pytest.mark.parametrize("nz, path", [(16, "in place"), (48, "slabs")])
+def test_arrays_the_host_rewrites_every_step_are_streamed(resident, nz, path):
+    """Host writes the inputs and reads the outputs between every step. After two such rounds the runtime
+    either hands the kernel the mapped host arrays (a shallow step: no copies at all) or, for a step of 24
+    levels or more, cuts it into slabs of about 12 levels whose uploads, kernels and publications overlap
+    on three streams. Results stay bit-identical to the oracle either way."""
     dom, fns = resident
-    geo = wl.Geometry(64, 64, 32, halo=2)
+    geo = wl.Geometry(96, 64, nz, halo=2)  # arrays of 1 MiB or more are pinned
     f = wl.advection_fields(geo, seed=8, nscalar=1)
     ins = [a.copy() for a in f.arrays()]
     outs = [np.zeros_like(a) for a in ins]
@@ -187,18 +190,30 @@ def test_arrays_the_host_rewrites_every_step_are_streamed_in_place(resident, cap
     h_in = [dom.bind_real64(a) for a in ins]
     h_out = [dom.bind_real64(a) for a in outs]
     arrays = [*h_out[:3], *h_in[:3], h_in[3], h_out[3]]
+    interior_bytes = sum(8 * geo.nx * geo.ny * geo.nz for _ in outs)
     for step in range(5):
         scale = 1.0 + 0.25 * step
         dom.host_modify(h_in)
         for a, src in zip(ins, f.arrays()):
             a[...] = src * scale
+        before = dom.stats()
         assert _call(fns, dom, "advection::step1", arrays, [geo.dx, geo.dy, geo.dz],
                      [geo.nx, geo.ny, geo.nz, geo.halo]) == abi.OK
+        called = dom.stats()
         dom.observe(h_out)
+        after = dom.stats()
+        if path == "slabs" and step >= 1:
+            # published slab by slab inside the call (one copy per slab and output), nothing left for the observation
+            slabs = called.launches - before.launches
+            assert slabs >= 3
+            assert called.downloads - before.downloads == slabs * len(outs)
+            assert called.download_bytes - before.download_bytes == interior_bytes
+            assert after.downloads == called.downloads
         ref = api.advection_step({"U": ins[0], "V": ins[1], "W": ins[2]}, geo.dx, geo.dy, geo.dz, geo.halo, ins[3:])
         for got, name in zip(outs, ["U", "V", "W", "S0"]):
             assert _same(got[geo.interior()], ref[name][geo.interior()])
     stats = dom.stats()
     dom.end_epoch()
-    # only the first two steps moved field data through copies
-    assert stats.upload_bytes <= 2 * sum(a.nbytes for a in ins)
+    if path == "in place":
+        # only the first two steps moved field data through copies
+        assert stats.upload_bytes <= 2 * sum(a.nbytes for a in ins)

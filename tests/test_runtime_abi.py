@@ -537,3 +537,133 @@ def test_trace_lines(tmp_path):
     assert out.returncode == 0, out.stderr
     events = [line.split()[1] for line in out.stderr.splitlines() if line.startswith("FORT_SCOPED ")]
     assert events.count("upload") == 1 and events.count("download") == 1 and "register" in events
+
+
+# ------------------------------------------------------------------------------- slab pipelines
+
+NX_S, NY_S, NZ_S = 4, 3, 10  # extents; planes 1..8 are the interior along the last dimension
+
+
+def _plane_sum_kernel(log):
+    """Host 'kernel': y[k] = x[k-1] + x[k] + x[k+1] on whole planes k0..k1-1; arguments (double*, double*, int, int)."""
+
+    def run(args):
+        x = _dev(c.cast(args[0], c.POINTER(c.c_void_p))[0], NX_S * NY_S * NZ_S).reshape(NZ_S, NY_S * NX_S)
+        y = _dev(c.cast(args[1], c.POINTER(c.c_void_p))[0], NX_S * NY_S * NZ_S).reshape(NZ_S, NY_S * NX_S)
+        k0 = c.cast(args[2], c.POINTER(c.c_int))[0]
+        k1 = c.cast(args[3], c.POINTER(c.c_int))[0]
+        y[k0:k1] = x[k0 - 1:k1 - 1] + x[k0:k1] + x[k0 + 1:k1 + 1]
+        log.append((k0, k1))
+
+    return KERNEL(run)
+
+
+def _slab_tasks(fn, devices, hx, hy, bounds):
+    keep, tasks, sizes = [], [], []
+    for k0, k1 in bounds:
+        values = [c.c_void_p(devices[0]), c.c_void_p(devices[1]), c.c_int(k0), c.c_int(k1)]
+        argv = (c.c_void_p * 4)(*[c.cast(c.pointer(v), c.c_void_p) for v in values])
+        kernel = abi.Kernel(1, 0, c.cast(fn, c.c_void_p), (c.c_uint32 * 3)(1, 1, 1), (c.c_uint32 * 3)(32, 1, 1), 0,
+                            argv, 4)
+        read = abi.access(read=[((0, 0, k0 - 1), (NX_S, NY_S, k1 + 1))])
+        write = abi.access(write=[((0, 0, k0), (NX_S, NY_S, k1))], overwrite=[((0, 0, k0), (NX_S, NY_S, k1))])
+        binding = (abi.Binding * 2)(abi.Binding(hx, read), abi.Binding(hy, write))
+        keep += [values, argv, read, write, binding]
+        tasks.append(abi.Task(kernel, binding, 2))
+        sizes += [8, 8, 4, 4]
+    return (abi.Task * len(tasks))(*tasks), (c.c_size_t * len(sizes))(*sizes), keep
+
+
+def _reserve_slabs(lib, scope, handles):
+    devices = (c.c_void_p * len(handles))()
+    pipelined = c.c_int(-1)
+    status = lib.fort_scope_device_reserve_slabs_v1(scope.handle, (abi.U64 * len(handles))(*handles), len(handles),
+                                                    devices, c.byref(pipelined))
+    return status, list(devices), pipelined.value
+
+
+def test_slab_pipeline_publishes_host_round_writes(monkeypatch):
+    monkeypatch.setenv("F2C_TEST_MAPPED", "1")
+    lib = _ours()
+    scope = abi.Scope(lib)
+    x, xa = _array(np.arange(NX_S * NY_S * NZ_S, dtype=np.float64))
+    y, ya = _array(np.full(NX_S * NY_S * NZ_S, -1.0))
+    _, hx = scope.register(xa, [NX_S, NY_S, NZ_S])
+    _, hy = scope.register(ya, [NX_S, NY_S, NZ_S])
+    log = []
+    fn = _plane_sum_kernel(log)
+    bounds = [(1, 4), (4, 7), (7, 9)]
+
+    def expected():
+        p = x.reshape(NZ_S, -1)
+        out = np.full_like(p, -1.0)
+        out[1:9] = p[0:8] + p[1:9] + p[2:10]
+        return out.ravel()
+
+    for round_ in range(3):
+        status, devices, pipelined = _reserve_slabs(lib, scope, [hx, hy])
+        assert status == abi.OK
+        # the first use has no history; later rounds are host-round for both arrays
+        assert pipelined == (0 if round_ == 0 else 1)
+        assert devices[0] != xa and devices[1] != ya  # never handed out in place
+        tasks, sizes, keep = _slab_tasks(fn, devices, hx, hy, bounds)
+        before = scope.stats()
+        assert lib.fort_scope_slab_enqueue_v1(scope.handle, 11, tasks, len(bounds), sizes) == abi.OK
+        after = scope.stats()
+        assert log[-3:] == bounds
+        if pipelined:
+            # published slab by slab, before any host access asks for it
+            assert after.downloads - before.downloads == len(bounds)
+            assert np.array_equal(y, expected())
+        assert lib.fort_scope_observe_v1(scope.handle, (abi.U64 * 1)(hy), 1) == abi.OK
+        assert scope.stats().downloads == after.downloads + (0 if pipelined else 1)
+        assert np.array_equal(y, expected())
+        # the host rewrites the input: the next round uploads it slab by slab, whole planes each
+        assert lib.fort_scope_host_begin(scope.handle, hx, c.byref(abi.access(flags=abi.WRITE_ALL))) == abi.OK
+        x[:] = x * 0.5 + round_
+        assert lib.fort_scope_host_end(scope.handle, hx) == abi.OK
+        if round_ == 1:
+            assert after.uploads - before.uploads == len(bounds)
+    assert lib.fort_scope_close(scope.handle) == abi.OK
+
+
+def test_slab_enqueue_validates_before_work(monkeypatch):
+    monkeypatch.setenv("F2C_TEST_MAPPED", "1")
+    lib = _ours()
+    scope = abi.Scope(lib)
+    _, xa = _array(np.zeros(NX_S * NY_S * NZ_S))
+    _, ya = _array(np.zeros(NX_S * NY_S * NZ_S))
+    _, hx = scope.register(xa, [NX_S, NY_S, NZ_S])
+    _, hy = scope.register(ya, [NX_S, NY_S, NZ_S], initialized=False)
+    log = []
+    fn = _plane_sum_kernel(log)
+    tasks, sizes, keep = _slab_tasks(fn, [xa, ya], hx, hy, [(1, 9)])
+    # no device storage reserved yet
+    assert lib.fort_scope_slab_enqueue_v1(scope.handle, 11, tasks, 1, sizes) == abi.STATE
+    assert lib.fort_scope_slab_enqueue_v1(scope.handle, 11, tasks, 0, sizes) == abi.ARGUMENT
+    assert lib.fort_scope_slab_enqueue_v1(scope.handle, 11, tasks, 65, sizes) == abi.ARGUMENT
+    status, devices, pipelined = _reserve_slabs(lib, scope, [hx, hy])
+    assert (status, pipelined) == (abi.OK, 0)
+    # a task that reads undefined values is refused and nothing runs
+    tasks, sizes, keep = _slab_tasks(fn, devices, hy, hx, [(1, 9)])
+    assert lib.fort_scope_slab_enqueue_v1(scope.handle, 11, tasks, 1, sizes) == abi.UNINITIALIZED
+    assert log == []
+    assert lib.fort_scope_close(scope.handle) == abi.OK
+
+
+def test_reserve_many_hands_host_round_arrays_out_in_place(monkeypatch):
+    """The single-task path still maps host-round arrays in place; the slab reservation never does."""
+    monkeypatch.setenv("F2C_TEST_MAPPED", "1")
+    lib = _ours()
+    scope = abi.Scope(lib)
+    _, xa = _array(np.ones(8))
+    _, hx = scope.register(xa, [8])
+    log = []
+    fn = _axpy_kernel(log)
+    for round_ in range(2):
+        devices = (c.c_void_p * 1)()
+        assert lib.fort_scope_device_reserve_many_v1(scope.handle, (abi.U64 * 1)(hx), 1, devices) == abi.OK
+        assert (devices[0] == xa) == (round_ == 1)
+        assert _enqueue(scope, fn, hx, 8, 1.0, 1.0) == abi.OK
+        assert lib.fort_scope_observe_v1(scope.handle, (abi.U64 * 1)(hx), 1) == abi.OK
+    assert lib.fort_scope_close(scope.handle) == abi.OK
