@@ -173,16 +173,15 @@ def cpu_oracle_sample(fields, budget_s: float = 12.0):
 def run_e2e(fields, steps, dist, torch):
     """Gpts/s of the step through the residency runtime and the generated entry, host buffers in and out."""
     from compiler import emission, native
-    from compiler.resident.domain import ResidentDomain, host_array, host_copy
+    from compiler.resident.domain import ResidentDomain
     from compiler.runtime import abi
 
     geo = fields.geometry
     lib = native.runtime()
     functions = emission.bind(lib)
     dom = ResidentDomain(lib)
-    # host arrays on 2 MiB boundaries, as a caller allocates them for full-rate transfers both ways
-    inputs = [host_copy(a) for a in fields.arrays()]
-    outputs = [host_array(a.shape) for a in inputs]
+    inputs = fields.arrays()
+    outputs = [np.zeros_like(a) for a in inputs]
     dom.begin_epoch()
     h_in = [dom.bind_real64(a) for a in inputs]
     h_out = [dom.bind_real64(a) for a in outputs]

@@ -21,29 +21,6 @@ import numpy as np
 from ..runtime import abi
 
 
-# Registered host memory whose data start on a 2 MiB boundary keeps host->device
-# and device->host copies at the link's full rate while both run (measured on
-# GB300: 172 GB/s each way, against 117 GB/s for arrays from the ordinary
-# allocator, which start only on a 64 KiB page).
-HOST_ALIGNMENT = 2 << 20
-
-
-def host_array(shape, dtype=np.float64) -> np.ndarray:
-    """A zeroed C-ordered host array whose data start on a HOST_ALIGNMENT boundary."""
-    dtype = np.dtype(dtype)
-    nbytes = int(np.prod(shape)) * dtype.itemsize
-    raw = np.zeros(nbytes + HOST_ALIGNMENT, dtype=np.uint8)
-    start = (-raw.ctypes.data) % HOST_ALIGNMENT
-    return raw[start:start + nbytes].view(dtype).reshape(shape)
-
-
-def host_copy(a: np.ndarray) -> np.ndarray:
-    """``a`` copied into a host_array of the same shape and type."""
-    out = host_array(a.shape, a.dtype)
-    out[...] = a
-    return out
-
-
 class ResidentError(RuntimeError):
     def __init__(self, status: int, message: str):
         super().__init__(f"Resident runtime failed: status {status}: {message}; source work will not be replayed")
