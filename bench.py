@@ -128,29 +128,39 @@ class ClockSampler:
 
 
 def dist_setup():
+    """One process per GPU under torchrun: (dist or None, rank, world, local rank). NCCL with GPUs, gloo without."""
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if world > 1:
+        import torch
         import torch.distributed as dist
 
-        backend = "nccl"
-        dist.init_process_group(backend=backend)
+        dist.init_process_group(backend="nccl" if torch.cuda.is_available() else "gloo")
         return dist, rank, world, local
     return None, rank, world, local
 
 
 def barrier(dist, torch):
-    if dist is not None:
+    if dist is None:
+        return
+    if dist.get_backend() == "nccl":
         dist.barrier(device_ids=[torch.cuda.current_device()])
+    else:
+        dist.barrier()
 
 
 def max_over_ranks(dist, torch, value: float) -> float:
     if dist is None:
         return value
-    t = torch.tensor([value], dtype=torch.float64, device="cuda")
+    t = torch.tensor([value], dtype=torch.float64, device="cuda" if dist.get_backend() == "nccl" else "cpu")
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def whole_job_value(points_per_rank: int, world: int, steps: int, slowest_ms: float) -> float:
+    """Gpts/s of the whole job: every rank's points x steps over the slowest rank's time (replicas, weak scaling)."""
+    return points_per_rank * world * steps / (slowest_ms * 1e-3) / 1e9
 
 
 def cpu_oracle_sample(fields, budget_s: float = 12.0):
@@ -260,7 +270,7 @@ def run_gb300(args):
     elapsed_ms = max_over_ranks(dist, torch, elapsed_ms)
     ms_per_step = elapsed_ms / args.steps
     points = geo.points
-    value = points * world * args.steps / (elapsed_ms * 1e-3) / 1e9
+    value = whole_job_value(points, world, args.steps, elapsed_ms)
 
     # FP64 pipe rate of this GPU (the roofline that binds first on GB300)
     scratch = torch.empty(8 * torch.cuda.get_device_properties(local).multi_processor_count * 256,
