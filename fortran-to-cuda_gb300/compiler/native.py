@@ -183,6 +183,13 @@ def load() -> ctypes.CDLL:
     lib.f2c_batch_prepare_v1.restype = ctypes.c_int
     lib.f2c_batch_step_v1.argtypes = [ctypes.POINTER(BatchPlan), ctypes.c_void_p]
     lib.f2c_batch_step_v1.restype = ctypes.c_int
+    lib.f2c_batch_prepare_async_v1.argtypes = [ctypes.POINTER(Grid), ctypes.POINTER(Fields),
+                                               ctypes.POINTER(ctypes.c_int32), ctypes.c_int32, ctypes.c_void_p,
+                                               ctypes.c_size_t, ctypes.c_void_p, ctypes.c_void_p,
+                                               ctypes.POINTER(BatchPlan)]
+    lib.f2c_batch_prepare_async_v1.restype = ctypes.c_int
+    lib.f2c_batch_halo_v1.argtypes = [ctypes.POINTER(BatchPlan), ctypes.c_void_p]
+    lib.f2c_batch_halo_v1.restype = ctypes.c_int
     lib.f2c_procedure_v1.argtypes = [ctypes.c_int, ctypes.POINTER(Grid), ctypes.c_void_p, ctypes.c_void_p,
                                      ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double, ctypes.c_void_p]
     lib.f2c_procedure_v1.restype = ctypes.c_int
@@ -271,8 +278,18 @@ class Batch:
         check(load().f2c_batch_prepare_v1(self.grids, self.fields, self.kz, self.count, ctypes.c_void_p(workspace),
                                           nbytes, ctypes.c_void_p(stream), ctypes.byref(self.plan)))
 
+    def prepare_async(self, workspace: int, nbytes: int, staging: int, stream: int = 0) -> None:
+        """Plan through host ``staging`` memory without waiting (see f2c_batch_prepare_async_v1)."""
+        check(load().f2c_batch_prepare_async_v1(self.grids, self.fields, self.kz, self.count,
+                                                ctypes.c_void_p(workspace), nbytes, ctypes.c_void_p(staging),
+                                                ctypes.c_void_p(stream), ctypes.byref(self.plan)))
+
     def step(self, stream: int = 0) -> None:
         check(load().f2c_batch_step_v1(ctypes.byref(self.plan), ctypes.c_void_p(stream)))
+
+    def halo(self, stream: int = 0) -> None:
+        """Boundary fill of every instance's outputs, one launch."""
+        check(load().f2c_batch_halo_v1(ctypes.byref(self.plan), ctypes.c_void_p(stream)))
 
 
 SET, MULTIPLY, CDU_DIV, CDU_ADV, CDV_DIV, CDV_ADV, CDW_DIV, CDW_ADV = range(8)

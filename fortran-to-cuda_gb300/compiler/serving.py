@@ -33,6 +33,11 @@ from . import workloads as wl
 DT = 0.1
 BUDGET_BYTES = 150 * 10**9
 MAX_ACTIVE = 256
+# grid points advanced per tick before further jobs wait for the next tick: about 1 ms of work. Measured on
+# GB300 (50 jobs per rate): ticks of 4M points keep throughput equal to serving one job at a time and halve the
+# median latency at low rates; larger ticks trade median latency for a few percent of throughput, and 2M-point
+# ticks leave the GPU waiting for the host
+TICK_POINTS = 4_000_000
 
 
 @dataclass
@@ -67,6 +72,13 @@ class Job:
         return 2 * (3 + self.nscalar) * int(np.prod(g.shape)) * 8
 
 
+def tick_chunk_depth(shapes, sms: int) -> int:
+    """One z-chunk depth for a tick's batch: deep chunks (up to 32 levels) while the tick has work for four
+    CTAs per SM, shallower (down to 2) for small ticks, so that their tiles still spread over every SM."""
+    columns = sum(((nx + 31) // 32) * ((ny + 7) // 8) * nz for (nx, ny, nz) in shapes)
+    return int(min(32, max(2, -(-columns // (4 * sms)))))
+
+
 def log_uniform_int(rng, lo, hi):
     return int(round(math.exp(rng.uniform(math.log(lo), math.log(hi)))))
 
@@ -87,19 +99,42 @@ def poisson_jobs(count: int, rate: float, seed: int = 0) -> list[Job]:
 
 
 class Server:
-    """Continuous-batching server on one GPU (``torch`` provides device memory and the stream)."""
+    """Continuous-batching server on one GPU (``torch`` provides device memory and the stream).
 
-    def __init__(self, torch, budget_bytes: int = BUDGET_BYTES, max_active: int = MAX_ACTIVE, keep_results=False):
+    A tick advances the selected jobs by one step: per scalar count, one
+    batched step over all their tiles and one batched boundary fill. A plan
+    depends only on which jobs step and which of their two buffer sets is
+    current, so it repeats every other tick while the selection holds: plans
+    are cached (each with its own device workspace, built once without
+    stalling the stream through ``prepare_async``), ticks are ordered by
+    events, and the host runs at most ``depth`` ticks ahead of the device. A
+    job whose last step is issued is retired once that tick's event has
+    completed.
+
+    Which jobs step in a tick: those with the least remaining work (steps left
+    x points) first, until the tick holds ``tick_points`` grid points; the rest
+    stay resident and wait (shortest remaining work first, so short jobs leave
+    early while every tick still fills the GPU). ``tick_points=None`` steps every
+    active job every tick.
+    """
+
+    def __init__(self, torch, budget_bytes: int = BUDGET_BYTES, max_active: int = MAX_ACTIVE, keep_results=False,
+                 depth: int = 2, tick_points: int | None = TICK_POINTS):
         self.torch = torch
+        self.tick_points = tick_points
         self.budget = budget_bytes
         self.max_active = max_active
         self.keep_results = keep_results
+        self.depth = depth
         self.stream = torch.cuda.Stream()
         self.active: list[Job] = []
         self.claimed = 0
         self.ticks = 0
         self.launches = 0
-        self.workspaces = {}
+        self.sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+        self.plans = {}        # (scalars, ((job, parity), ...)) -> (Batch, workspace, staging), most recent last
+        self.plan_builds = 0
+        self.inflight = []     # (event, plans used, jobs finishing at this tick)
 
     # -- job lifetime ---------------------------------------------------------------------------
     def _admit(self, job: Job, now: float) -> None:
@@ -111,6 +146,7 @@ class Server:
         job.grid = native.make_grid(geo.nx, geo.ny, geo.nz, geo.halo, geo.dx, geo.dy, geo.dz)
         kinds = [0, 0, 1] + [0] * job.nscalar
         native.halo_fill(job.grid, [t.data_ptr() for t in first], kinds, stream=self.stream.cuda_stream)
+        self.launches += 1
         job.buffers = [first, second]
         job.admitted = now
         self.claimed += job.device_bytes()
@@ -129,14 +165,12 @@ class Server:
     def fits(self, job: Job) -> bool:
         return len(self.active) < self.max_active and self.claimed + job.device_bytes() <= self.budget
 
-    # -- one tick: every active job advances one step --------------------------------------------
-    def tick(self) -> None:
-        torch = self.torch
-        groups = {}
-        for job in self.active:
-            groups.setdefault(job.nscalar, []).append(job)
-        s = self.stream.cuda_stream
-        for nscalar, jobs in sorted(groups.items()):
+    def _plan(self, nscalar: int, jobs: list[Job]):
+        """The cached plan of one group's step (built on first use; the 16 most recent are kept)."""
+        key = (nscalar, tuple((job.ident, job.done % 2) for job in jobs))
+        plan = self.plans.pop(key, None)
+        if plan is None:
+            torch = self.torch
             grids, fields = [], []
             for job in jobs:
                 src, dst = job.buffers[job.done % 2], job.buffers[1 - job.done % 2]
@@ -144,21 +178,53 @@ class Server:
                 grids.append(job.grid)
                 fields.append(native.make_fields(*p[:3], *q[:3], scalars=p[3:], scalar_out=q[3:],
                                                  mode=native.ADVANCE, dt=DT))
-            batch = native.Batch(grids, fields)
+            kz = tick_chunk_depth([(j.nx, j.ny, j.nz) for j in jobs], self.sms)
+            batch = native.Batch(grids, fields, kz=[kz] * len(jobs))
             need = batch.workspace_bytes()
-            ws = self.workspaces.get(nscalar)
-            if ws is None or ws.numel() < need:
-                ws = torch.empty(max(need, 1 << 20) * 2, dtype=torch.uint8, device="cuda")
-                self.workspaces[nscalar] = ws
-            batch.prepare(ws.data_ptr(), ws.numel(), s)
-            batch.step(s)
-            self.launches += 1
-        for job in self.active:
-            dst = job.buffers[1 - job.done % 2]
-            native.halo_fill(job.grid, [t.data_ptr() for t in dst], [0, 0, 1] + [0] * job.nscalar, stream=s)
-            self.launches += 1
+            workspace = torch.empty(need, dtype=torch.uint8, device="cuda")
+            staging = torch.empty(need, dtype=torch.uint8, pin_memory=True)
+            batch.prepare_async(workspace.data_ptr(), need, staging.data_ptr(), self.stream.cuda_stream)
+            plan = (batch, workspace, staging)
+            self.plan_builds += 1
+        self.plans[key] = plan
+        while len(self.plans) > 16:  # ticks still in flight hold their own references
+            self.plans.pop(next(iter(self.plans)))
+        return plan
+
+    # -- one tick: every active job advances one step --------------------------------------------
+    def select(self) -> list[Job]:
+        """The jobs that step in the next tick."""
+        if self.tick_points is None:
+            return list(self.active)
+        chosen, total = [], 0
+        for job in sorted(self.active, key=lambda j: ((j.steps - j.done) * j.points, j.ident)):
+            if chosen and total >= self.tick_points:
+                break
+            chosen.append(job)
+            total += job.points
+        return chosen
+
+    def tick(self):
+        """Issue one step of the selected jobs; returns (the plans used, the jobs whose last step this was)."""
+        stepping = self.select()
+        groups = {}
+        for job in stepping:
+            groups.setdefault(job.nscalar, []).append(job)
+        s = self.stream.cuda_stream
+        used = []
+        for nscalar, jobs in sorted(groups.items()):
+            plan = self._plan(nscalar, jobs)
+            plan[0].step(s)
+            plan[0].halo(s)
+            used.append(plan)
+            self.launches += 2
+        finishing = []
+        for job in stepping:
             job.done += 1
+            if job.done >= job.steps:
+                finishing.append(job)
         self.ticks += 1
+        return used, finishing
 
     # -- the open-loop run ------------------------------------------------------------------------
     def run(self, jobs: list[Job]) -> dict:
@@ -168,7 +234,23 @@ class Server:
         start = time.perf_counter()
         i = 0
         finished = []
-        while i < len(pending) or waiting or self.active:
+
+        def drain(block: bool) -> None:
+            # retire the jobs of completed ticks, oldest first; `block` waits for the oldest one
+            while self.inflight:
+                event, _, done = self.inflight[0]
+                if block:
+                    event.synchronize()
+                    block = False
+                elif not event.query():
+                    return
+                now = time.perf_counter() - start
+                for job in done:
+                    self._retire(job, now)
+                    finished.append(job)
+                self.inflight.pop(0)
+
+        while i < len(pending) or waiting or self.active or self.inflight:
             now = time.perf_counter() - start
             while i < len(pending) and pending[i].arrival <= now:
                 waiting.append(pending[i])
@@ -176,6 +258,9 @@ class Server:
             while waiting and self.fits(waiting[0]):
                 self._admit(waiting.pop(0), now)
             if not self.active:
+                if self.inflight:
+                    drain(True)
+                    continue
                 if i < len(pending):  # idle until the next arrival
                     delay = pending[i].arrival - (time.perf_counter() - start)
                     if delay > 0:
@@ -184,20 +269,65 @@ class Server:
                 if waiting:
                     raise RuntimeError("a job does not fit the device budget on its own")
                 break
-            self.tick()
-            torch.cuda.current_stream().wait_stream(self.stream)
-            self.stream.synchronize()
-            now = time.perf_counter() - start
-            still = []
-            for job in self.active:
-                if job.done >= job.steps:
-                    self._retire(job, now)
-                    finished.append(job)
-                else:
-                    still.append(job)
-            self.active = still
+            if len(self.inflight) >= self.depth:
+                drain(True)
+            used, done = self.tick()
+            event = torch.cuda.Event()
+            event.record(self.stream)
+            self.inflight.append((event, used, done))
+            if done:
+                self.active = [j for j in self.active if j.done < j.steps]
+            drain(False)
         wall = time.perf_counter() - start
-        return summarise(finished, wall, self.ticks, self.launches)
+        out = summarise(finished, wall, self.ticks, self.launches)
+        out["plan_builds"] = self.plan_builds
+        return out
+
+
+class SerialServer:
+    """The same open-loop stream served one job at a time through the single-instance path.
+
+    A job is admitted when the previous one has finished (and it has arrived): its fields are generated on the
+    device as the continuous server does, each step is one advection launch and one boundary fill, and the job
+    is retired (one value read back) when its last step completes. Wall-clock, like ``Server.run``.
+    """
+
+    def __init__(self, torch):
+        self.torch = torch
+        self.stream = torch.cuda.Stream()
+        self.launches = 0
+
+    def run(self, jobs: list[Job]) -> dict:
+        torch = self.torch
+        start = time.perf_counter()
+        finished = []
+        for job in sorted(jobs, key=lambda j: j.arrival):
+            delay = job.arrival - (time.perf_counter() - start)
+            if delay > 0:
+                time.sleep(delay)
+            geo = job.geometry
+            with torch.cuda.stream(self.stream):
+                a = wl.advection_fields_device(geo, job.seed, job.nscalar, torch)
+                b = [torch.empty_like(t) for t in a]
+            grid = native.make_grid(geo.nx, geo.ny, geo.nz, geo.halo, geo.dx, geo.dy, geo.dz)
+            kinds = [0, 0, 1] + [0] * job.nscalar
+            s = self.stream.cuda_stream
+            native.halo_fill(grid, [t.data_ptr() for t in a], kinds, stream=s)
+            job.admitted = time.perf_counter() - start
+            bufs = [a, b]
+            for n in range(job.steps):
+                src, dst = bufs[n % 2], bufs[1 - n % 2]
+                p, q = [t.data_ptr() for t in src], [t.data_ptr() for t in dst]
+                native.advection(grid, *p[:3], *q[:3], scalars=p[3:], scalar_out=q[3:], mode=native.ADVANCE,
+                                 dt=DT, stream=s)
+                native.halo_fill(grid, q, kinds, stream=s)
+            self.launches += 1 + 2 * job.steps
+            with torch.cuda.stream(self.stream):
+                bufs[job.steps % 2][0].view(-1)[:1].cpu()
+            job.finished = time.perf_counter() - start
+            finished.append(job)
+        wall = time.perf_counter() - start
+        return summarise(finished, wall, 0, self.launches)
 
 
 def summarise(jobs: list[Job], wall: float, ticks: int = 0, launches: int = 0) -> dict:
@@ -248,7 +378,12 @@ def serial_timeline(jobs: list[Job], solo: dict) -> dict:
 
 
 def bench_main(args) -> None:
-    """``bench.py --workload serving``: rates swept over {50, ..., 2000} jobs/s; continuous batching vs serial."""
+    """``bench.py --workload serving``: rates swept over {50, ..., 2000} jobs/s; continuous batching vs serial.
+
+    Both servers run the same open-loop stream in wall-clock time with the same per-job work (fields generated
+    on the device at admission, one value read back at retirement); ``serial_device_model`` adds the
+    device-time-only FIFO model of the serial server (no host work at all) for reference.
+    """
     import json
 
     import torch
@@ -257,21 +392,28 @@ def bench_main(args) -> None:
     count = max(20, args.steps)
     results = []
     for rate in rates:
-        jobs = poisson_jobs(count, rate, seed=int(rate))
-        solo = {j.ident: solo_seconds(torch, j) for j in jobs}
-        torch.cuda.synchronize()
         served = Server(torch).run(poisson_jobs(count, rate, seed=int(rate)))
-        serial = serial_timeline(jobs, solo)
-        results.append({"rate_jobs_per_s": rate, "continuous_batching": served, "serial_plain": serial,
-                        "throughput_ratio": served["gpts_per_s"] / serial["gpts_per_s"] if serial["gpts_per_s"]
-                        else None})
+        torch.cuda.synchronize()
+        every = Server(torch, tick_points=None).run(poisson_jobs(count, rate, seed=int(rate)))
+        torch.cuda.synchronize()
+        serial = SerialServer(torch).run(poisson_jobs(count, rate, seed=int(rate)))
+        torch.cuda.synchronize()
+        jobs = poisson_jobs(count, rate, seed=int(rate))
+        model = serial_timeline(jobs, {j.ident: solo_seconds(torch, j) for j in jobs})
+        results.append({"rate_jobs_per_s": rate, "continuous_batching": served, "every_job_every_tick": every,
+                        "serial_plain": serial,
+                         "serial_device_model": model,
+                         "throughput_ratio": served["gpts_per_s"] / serial["gpts_per_s"] if serial["gpts_per_s"]
+                         else None,
+                         "p99_ratio": served["p99_ms"] / serial["p99_ms"] if serial["p99_ms"] else None})
         torch.cuda.empty_cache()
     print(json.dumps({"metric": "serving: jobs/s, Gpts/s and p50/p99 job latency (continuous batching vs serial)",
                       "unit": "Gpts/s", "jobs_per_rate": count, "dtype": "f64",
                       "config": {"workload": "Poisson arrivals; nx,ny log-uniform [48,320] (independent draws), "
                                              "nz log-uniform [24,128], 0-3 scalars, 1-100 Euler steps",
-                                 "budget_bytes": BUDGET_BYTES},
+                                 "budget_bytes": BUDGET_BYTES,
+                                 "policy": f"shortest remaining work first, {TICK_POINTS} points per tick"},
                       "results": results}), flush=True)
 
 
-__all__ = ["Job", "Server", "poisson_jobs", "serial_timeline", "solo_seconds", "bench_main", "summarise"]
+__all__ = ["Job", "Server", "SerialServer", "poisson_jobs", "serial_timeline", "solo_seconds", "bench_main", "summarise"]

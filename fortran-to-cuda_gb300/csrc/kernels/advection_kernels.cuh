@@ -78,42 +78,55 @@ __global__ void __launch_bounds__(BX *BY) advection_direct_kernel(const AdvArgs 
 // vertical walls over whole planes) would copy into it. Periodic maps compose,
 // and each vertical mirror source is an interior, non-wall level (nz > halo),
 // so no ghost reads another ghost and the pass order is free.
-static __global__ void __launch_bounds__(256) halo_fill_kernel(const HaloArgs a) {
-    const int ex = a.nx + 2 * a.h, ey = a.ny + 2 * a.h, ez = a.nz + 2 * a.h;
-    const long long row = blockIdx.x;          // j + ey*k
-    const int fidx = blockIdx.y;
-    const int j = (int)(row % ey), k = (int)(row / ey);
-    if (k >= ez || fidx >= a.count) return;
-    double *__restrict__ f = a.f[fidx];
-    const int kind = a.kind[fidx];
-    const int h = a.h;
-    const bool jin = j >= h && j < h + a.ny;
-    const bool kwall = kind == 1 && (k == h - 1 || k == h + a.nz - 1);
-    const bool kin = k >= h && k < h + a.nz && !kwall;
-    const int jj = j < h ? j + a.ny : (j >= h + a.ny ? j - a.ny : j);
+//
+// halo_row fills the ghosts of row (j, k) of one field (kind 0: periodic x/y,
+// mirrored z; kind 1: the W rule, zero walls at h-1 and h+nz-1 and sign-flipped
+// mirrors beyond); threads `lane` = 0.. stride `lanes` across the row. A row
+// inside the interior in j and k has only its 2h x-ghosts to fill.
+__device__ __forceinline__ void halo_row(double *__restrict__ f, int kind, int nx, int ny, int nz, int h, long long sx,
+                                         long long plane, int j, int k, int lane, int lanes) {
+    const int ex = nx + 2 * h;
+    const bool jin = j >= h && j < h + ny;
+    const bool kwall = kind == 1 && (k == h - 1 || k == h + nz - 1);
+    const bool kin = k >= h && k < h + nz && !kwall;
+    const int jj = j < h ? j + ny : (j >= h + ny ? j - ny : j);
     int kk = k;
     double sign = 1.0;
     if (kind == 0) {
         if (k < h) kk = 2 * h - 1 - k;
-        else if (k >= h + a.nz) kk = 2 * (h + a.nz) - 1 - k;
+        else if (k >= h + nz) kk = 2 * (h + nz) - 1 - k;
     } else if (!kwall) {
         if (k < h - 1) { kk = 2 * (h - 1) - k; sign = -1.0; }
-        else if (k >= h + a.nz) { kk = 2 * (h + a.nz - 1) - k; sign = -1.0; }
+        else if (k >= h + nz) { kk = 2 * (h + nz - 1) - k; sign = -1.0; }
     }
-    const long long dst_row = a.sx * (long long)j + a.plane * (long long)k;
-    const long long src_row = a.sx * (long long)jj + a.plane * (long long)kk;
-    const bool row_interior = jin && kin;
-    for (int i = threadIdx.x; i < ex; i += blockDim.x) {
-        const bool iin = i >= h && i < h + a.nx;
-        if (row_interior && iin) continue;
+    const long long dst_row = sx * (long long)j + plane * (long long)k;
+    const long long src_row = sx * (long long)jj + plane * (long long)kk;
+    if (jin && kin) {
+        for (int t = lane; t < 2 * h; t += lanes) {
+            const int i = t < h ? t : nx + t;
+            const int ii = i < h ? i + nx : i - nx;
+            f[dst_row + i] = f[src_row + ii];
+        }
+        return;
+    }
+    for (int i = lane; i < ex; i += lanes) {
         if (kwall) {
             f[dst_row + i] = 0.0;
             continue;
         }
-        const int ii = i < h ? i + a.nx : (i >= h + a.nx ? i - a.nx : i);
+        const int ii = i < h ? i + nx : (i >= h + nx ? i - nx : i);
         const double v = f[src_row + ii];
         f[dst_row + i] = sign < 0.0 ? -v : v;
     }
+}
+
+static __global__ void __launch_bounds__(256) halo_fill_kernel(const HaloArgs a) {
+    const int ey = a.ny + 2 * a.h, ez = a.nz + 2 * a.h;
+    const long long row = blockIdx.x;          // j + ey*k
+    const int fidx = blockIdx.y;
+    const int j = (int)(row % ey), k = (int)(row / ey);
+    if (k >= ez || fidx >= a.count) return;
+    halo_row(a.f[fidx], a.kind[fidx], a.nx, a.ny, a.nz, a.h, a.sx, a.plane, j, k, threadIdx.x, blockDim.x);
 }
 
 inline cudaError_t launch_advection(const AdvArgs &a, cudaStream_t stream) {

@@ -107,13 +107,20 @@ extern "C" size_t f2c_batch_workspace_bytes_v1(const f2c_grid_v1 *grids, const i
            align_up(sizeof(BatchItem) * item_count(grids, kz, count));
 }
 
-extern "C" int f2c_batch_prepare_v1(const f2c_grid_v1 *grids, const f2c_fields_v1 *fields, const int32_t *kz,
-                                    int32_t count, void *workspace, size_t workspace_bytes, void *stream,
-                                    f2c_batch_plan_v1 *plan) {
-    if (!grids || !fields || count <= 0 || !plan) return fail(1, "empty batch");
-    if (!workspace) return fail(1, "null batch workspace");
-    if (workspace_bytes < f2c_batch_workspace_bytes_v1(grids, kz, count)) return fail(4, "batch workspace too small");
-    std::vector<AdvArgs> descs((size_t)count);
+namespace f2c {
+namespace {
+// Descriptors and the flattened item queue of a batch, built and checked on the host.
+struct Built {
+    std::vector<AdvArgs> descs;
+    std::vector<BatchItem> items;
+    int ns = -1, mask = -1;
+    bool halo_ok = true; // every instance admits the boundary fill (nz > halo, nx and ny >= halo)
+};
+
+int build(const f2c_grid_v1 *grids, const f2c_fields_v1 *fields, const int32_t *kz, int32_t count, Built &out) {
+    if (!grids || !fields || count <= 0) return fail(1, "empty batch");
+    std::vector<AdvArgs> &descs = out.descs;
+    descs.assign((size_t)count, AdvArgs{});
     int ns = -1, mask = -1;
     for (int n = 0; n < count; ++n) {
         if (int s = check_grid(&grids[n])) return s;
@@ -145,11 +152,13 @@ extern "C" int f2c_batch_prepare_v1(const f2c_grid_v1 *grids, const f2c_fields_v
         a.sx = g.sx;
         a.plane = g.sx * g.sy;
         a.c = make_coefficients(g.dx, g.dy, g.dz);
+        if (g.nz < g.halo + 1 || g.nx < g.halo || g.ny < g.halo) out.halo_ok = false;
     }
     if (mask != 7 && mask != 1 && mask != 2 && mask != 4 && mask != 0) mask = 7;
     if (mask == 0 && ns == 0) return fail(1, "batch computes nothing");
     // the flattened queue: full-depth items first (largest first), then the partial ones
-    std::vector<BatchItem> items;
+    std::vector<BatchItem> &items = out.items;
+    items.clear();
     items.reserve(item_count(grids, kz, count));
     for (int n = 0; n < count; ++n) {
         const f2c_grid_v1 &g = grids[n];
@@ -169,30 +178,129 @@ extern "C" int f2c_batch_prepare_v1(const f2c_grid_v1 *grids, const f2c_fields_v
     };
     std::stable_sort(items.begin(), items.end(),
                      [&](const BatchItem &a, const BatchItem &b) { return cost(a) > cost(b); });
-    char *base = static_cast<char *>(workspace);
-    const size_t desc_off = align_up(sizeof(BatchHeader));
-    const size_t item_off = desc_off + align_up(sizeof(AdvArgs) * (size_t)count);
-    const cudaStream_t s = static_cast<cudaStream_t>(stream);
-    cudaError_t e = cudaMemcpyAsync(base + desc_off, descs.data(), sizeof(AdvArgs) * descs.size(),
-                                    cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync(base + item_off, items.data(), sizeof(BatchItem) * items.size(), cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess) return fail(6, std::string("batch prepare: ") + cudaGetErrorString(e));
-    const Kernel k = kernel_for(ns, mask);
+    out.ns = ns;
+    out.mask = mask;
+    return 0;
+}
+
+size_t descs_offset() { return align_up(sizeof(BatchHeader)); }
+size_t items_offset(int count) { return descs_offset() + align_up(sizeof(AdvArgs) * (size_t)count); }
+
+// The plan of a built batch whose descriptors and items are (being) copied into `workspace`.
+int finish(const Built &b, int32_t count, void *workspace, size_t workspace_bytes, f2c_batch_plan_v1 *plan) {
+    const Kernel k = kernel_for(b.ns, b.mask);
     int device = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&device);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k.fn, kFaceThreads, k.smem);
+    const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k.fn, kFaceThreads, k.smem);
     if (e != cudaSuccess || per_sm < 1) return fail(6, "batch kernel does not fit on an SM");
     plan->workspace = workspace;
     plan->workspace_bytes = workspace_bytes;
     plan->count = count;
-    plan->nscalar = ns;
-    plan->mask = mask;
-    plan->items = (int32_t)items.size();
-    plan->ctas = (uint32_t)std::min<size_t>((size_t)sms * per_sm, items.size());
-    plan->reserved = 0;
+    plan->nscalar = b.ns;
+    plan->mask = b.mask;
+    plan->items = (int32_t)b.items.size();
+    plan->ctas = (uint32_t)std::min<size_t>((size_t)sms * per_sm, b.items.size());
+    plan->reserved = b.halo_ok ? 1u : 0u;
+    return 0;
+}
+
+// Halo fill of every instance's outputs: one warp per (instance, field, row) unit,
+// instances found by a binary search over their first units (shared memory).
+constexpr int kBatchHaloThreads = 256;
+constexpr int kBatchHaloMaxInstances = 4096;
+
+__global__ void __launch_bounds__(kBatchHaloThreads) batch_halo_kernel(const AdvArgs *__restrict__ inst, int count,
+                                                                      int nfields) {
+    extern __shared__ long long first[]; // first[n]: first unit of instance n; first[count]: all units
+    for (int n = threadIdx.x; n < count; n += blockDim.x) {
+        const AdvArgs &a = inst[n];
+        first[n + 1] = (long long)(a.ny + 2 * a.h) * (a.nz + 2 * a.h) * nfields;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        first[0] = 0;
+        for (int n = 1; n <= count; ++n) first[n] += first[n - 1];
+    }
+    __syncthreads();
+    const long long total = first[count];
+    const int lane = threadIdx.x & 31, warps = blockDim.x >> 5;
+    for (long long u = (long long)blockIdx.x * warps + (threadIdx.x >> 5); u < total;
+         u += (long long)gridDim.x * warps) {
+        int lo = 0, hi = count - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (first[mid] <= u) lo = mid;
+            else hi = mid - 1;
+        }
+        const AdvArgs &a = inst[lo];
+        const int ey = a.ny + 2 * a.h;
+        const long long rows = (long long)ey * (a.nz + 2 * a.h);
+        const long long local = u - first[lo];
+        const int fidx = (int)(local / rows);
+        const long long row = local - (long long)fidx * rows;
+        double *f = fidx < 3 ? a.out[fidx] : a.st[fidx - 3];
+        if (!f) continue;
+        halo_row(f, fidx == 2 ? 1 : 0, a.nx, a.ny, a.nz, a.h, a.sx, a.plane, (int)(row % ey), (int)(row / ey), lane,
+                 32);
+    }
+}
+}  // namespace
+}  // namespace f2c
+
+extern "C" int f2c_batch_prepare_v1(const f2c_grid_v1 *grids, const f2c_fields_v1 *fields, const int32_t *kz,
+                                    int32_t count, void *workspace, size_t workspace_bytes, void *stream,
+                                    f2c_batch_plan_v1 *plan) {
+    if (!grids || !fields || count <= 0 || !plan) return fail(1, "empty batch");
+    if (!workspace) return fail(1, "null batch workspace");
+    if (workspace_bytes < f2c_batch_workspace_bytes_v1(grids, kz, count)) return fail(4, "batch workspace too small");
+    Built b;
+    if (int s = build(grids, fields, kz, count, b)) return s;
+    char *base = static_cast<char *>(workspace);
+    const cudaStream_t s = static_cast<cudaStream_t>(stream);
+    cudaError_t e = cudaMemcpyAsync(base + descs_offset(), b.descs.data(), sizeof(AdvArgs) * b.descs.size(),
+                                    cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(base + items_offset(count), b.items.data(), sizeof(BatchItem) * b.items.size(),
+                            cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return fail(6, std::string("batch prepare: ") + cudaGetErrorString(e));
+    return finish(b, count, workspace, workspace_bytes, plan);
+}
+
+extern "C" int f2c_batch_prepare_async_v1(const f2c_grid_v1 *grids, const f2c_fields_v1 *fields, const int32_t *kz,
+                                          int32_t count, void *workspace, size_t workspace_bytes, void *staging,
+                                          void *stream, f2c_batch_plan_v1 *plan) {
+    if (!grids || !fields || count <= 0 || !plan) return fail(1, "empty batch");
+    if (!workspace || !staging) return fail(1, "null batch workspace or staging");
+    if (workspace_bytes < f2c_batch_workspace_bytes_v1(grids, kz, count)) return fail(4, "batch workspace too small");
+    Built b;
+    if (int s = build(grids, fields, kz, count, b)) return s;
+    char *host = static_cast<char *>(staging);
+    const size_t descs = descs_offset(), items = items_offset(count);
+    std::memcpy(host + descs, b.descs.data(), sizeof(AdvArgs) * b.descs.size());
+    std::memcpy(host + items, b.items.data(), sizeof(BatchItem) * b.items.size());
+    const size_t bytes = items + sizeof(BatchItem) * b.items.size() - descs;
+    const cudaError_t e = cudaMemcpyAsync(static_cast<char *>(workspace) + descs, host + descs, bytes,
+                                          cudaMemcpyHostToDevice, static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return fail(6, std::string("batch prepare: ") + cudaGetErrorString(e));
+    return finish(b, count, workspace, workspace_bytes, plan);
+}
+
+extern "C" int f2c_batch_halo_v1(const f2c_batch_plan_v1 *plan, void *stream) {
+    if (!plan || !plan->workspace || plan->count <= 0) return fail(1, "batch plan not prepared");
+    if (plan->count > kBatchHaloMaxInstances) return fail(1, "batch halo fill takes at most 4096 instances");
+    if (!(plan->reserved & 1u)) return fail(1, "halo fill needs nz > halo, nx >= halo and ny >= halo in every instance");
+    const AdvArgs *descs = reinterpret_cast<const AdvArgs *>(static_cast<char *>(plan->workspace) + descs_offset());
+    int device = 0, sms = 0;
+    cudaGetDevice(&device);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    const int count = plan->count, nfields = 3 + plan->nscalar;
+    const size_t shared = sizeof(long long) * (size_t)(count + 1);
+    batch_halo_kernel<<<(unsigned)(sms > 0 ? sms * 8 : 1216), kBatchHaloThreads, shared,
+                        static_cast<cudaStream_t>(stream)>>>(descs, count, nfields);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(6, std::string("batch halo launch: ") + cudaGetErrorString(e));
     return 0;
 }
 
@@ -200,11 +308,9 @@ extern "C" int f2c_batch_step_v1(const f2c_batch_plan_v1 *plan, void *stream) {
     if (!plan || !plan->workspace || plan->items <= 0) return fail(1, "batch plan not prepared");
     const cudaStream_t s = static_cast<cudaStream_t>(stream);
     char *base = static_cast<char *>(plan->workspace);
-    const size_t desc_off = align_up(sizeof(BatchHeader));
-    const size_t item_off = desc_off + align_up(sizeof(AdvArgs) * (size_t)plan->count);
     unsigned *counter = reinterpret_cast<unsigned *>(base);
-    const AdvArgs *descs = reinterpret_cast<const AdvArgs *>(base + desc_off);
-    const BatchItem *items = reinterpret_cast<const BatchItem *>(base + item_off);
+    const AdvArgs *descs = reinterpret_cast<const AdvArgs *>(base + descs_offset());
+    const BatchItem *items = reinterpret_cast<const BatchItem *>(base + items_offset(plan->count));
     cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(unsigned), s);
     if (e != cudaSuccess) return fail(6, std::string("batch counter reset: ") + cudaGetErrorString(e));
     const Kernel k = kernel_for(plan->nscalar, plan->mask);

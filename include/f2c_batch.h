@@ -34,7 +34,7 @@ typedef struct f2c_batch_plan_v1 {
     size_t workspace_bytes;
     int32_t count, nscalar, mask, items;
     uint32_t ctas;             /* persistent grid size */
-    uint32_t reserved;
+    uint32_t reserved;         /* bit 0: every instance admits f2c_batch_halo_v1 */
 } f2c_batch_plan_v1;
 
 /* Bytes of workspace for `count` instances cut into z-chunks of kz[i] levels (kz NULL: 32). */
@@ -44,6 +44,24 @@ int f2c_batch_prepare_v1(const f2c_grid_v1 *grids, const f2c_fields_v1 *fields, 
                          void *workspace, size_t workspace_bytes, void *stream, f2c_batch_plan_v1 *plan);
 /* One step of every instance: counter reset + one persistent launch on `stream`. */
 int f2c_batch_step_v1(const f2c_batch_plan_v1 *plan, void *stream);
+
+/* f2c_batch_prepare_v1 without waiting, for a caller that re-plans every step
+ * (a server whose set of instances changes between steps): descriptors and
+ * queue are written into `staging` (host memory of f2c_batch_workspace_bytes_v1
+ * bytes or more; pinned memory keeps the copy asynchronous) and copied to the
+ * workspace on `stream`. Neither `staging` nor the workspace may be reused
+ * until the stream has passed the steps that use this plan (an event recorded
+ * after them tells). */
+int f2c_batch_prepare_async_v1(const f2c_grid_v1 *grids, const f2c_fields_v1 *fields, const int32_t *kz,
+                               int32_t count, void *workspace, size_t workspace_bytes, void *staging, void *stream,
+                               f2c_batch_plan_v1 *plan);
+
+/* Boundary fill of every instance's outputs in one launch on `stream` (the
+ * per-instance rule of f2c_halo_fill_v1: U, V and scalars periodic in x and y
+ * and mirrored in z, W with zero walls): after a forward-Euler step it
+ * completes each instance's new fields. At most 4096 instances, each with
+ * nz > halo, nx >= halo and ny >= halo (as f2c_halo_fill_v1 requires). */
+int f2c_batch_halo_v1(const f2c_batch_plan_v1 *plan, void *stream);
 
 /* The same batched step for callers that cannot allocate device memory. It has
  * no counterpart in the reference.

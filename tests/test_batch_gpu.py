@@ -79,3 +79,46 @@ def test_batch_rejects_mixed_instances(cuda):
         batch.prepare(ws.data_ptr(), ws.numel())
     with pytest.raises(native.NativeError):
         native.Batch([x[4] for x in inst], [x[5] for x in inst]).prepare(ws.data_ptr(), 64)
+
+
+def test_async_prepare_and_batched_halo_equal_the_single_instance_path(cuda):
+    """prepare_async (through pinned staging) plans what prepare does, and one batched boundary fill writes
+    every instance's ghosts exactly as one f2c_halo_fill_v1 per instance."""
+    nscalar = 2
+    inst = _setup(cuda, nscalar, mode=native.ADVANCE, dt=0.1)
+    ref = _setup(cuda, nscalar, mode=native.ADVANCE, dt=0.1)
+    batch = native.Batch([x[4] for x in inst], [x[5] for x in inst])
+    ws = cuda.empty(batch.workspace_bytes(), dtype=cuda.uint8, device="cuda")
+    staging = cuda.empty(batch.workspace_bytes(), dtype=cuda.uint8, pin_memory=True)
+    stream = cuda.cuda.Stream()
+    batch.prepare_async(ws.data_ptr(), ws.numel(), staging.data_ptr(), stream.cuda_stream)
+    batch.step(stream.cuda_stream)
+    batch.halo(stream.cuda_stream)
+    stream.synchronize()
+    single = native.Batch([x[4] for x in ref], [x[5] for x in ref])
+    ws2 = cuda.empty(single.workspace_bytes(), dtype=cuda.uint8, device="cuda")
+    single.prepare(ws2.data_ptr(), ws2.numel())
+    assert (batch.plan.items, batch.plan.ctas, batch.plan.count) == (single.plan.items, single.plan.ctas,
+                                                                     single.plan.count)
+    single.step()
+    for geo, f, ins, outs, grid, fields in ref:
+        native.halo_fill(grid, [t.data_ptr() for t in outs], [0, 0, 1] + [0] * nscalar)
+    cuda.cuda.synchronize()
+    for a, b in zip(inst, ref):
+        for x, y in zip(a[3], b[3]):
+            assert np.array_equal(_bits(x.cpu().numpy()), _bits(y.cpu().numpy()))
+
+
+def test_batched_halo_refuses_instances_too_small_for_the_fill(cuda):
+    geo = wl.Geometry(16, 16, 2, halo=2)  # nz must exceed the halo
+    f = wl.advection_fields(geo, seed=1, nscalar=0)
+    ins = [cuda.from_numpy(a).cuda() for a in f.arrays()]
+    outs = [cuda.zeros_like(t) for t in ins]
+    grid = native.make_grid(16, 16, 2, 2, geo.dx, geo.dy, geo.dz)
+    fields = native.make_fields(*[t.data_ptr() for t in ins], *[t.data_ptr() for t in outs], mode=native.ADVANCE,
+                                dt=0.1)
+    batch = native.Batch([grid], [fields])
+    ws = cuda.empty(batch.workspace_bytes(), dtype=cuda.uint8, device="cuda")
+    batch.prepare(ws.data_ptr(), ws.numel())
+    with pytest.raises(native.NativeError, match="halo fill needs"):
+        batch.halo()

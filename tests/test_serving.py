@@ -63,3 +63,29 @@ def test_each_job_is_the_same_alone_and_in_the_mix(cuda):
         state = [api.halo(x, 1 if n == 2 else 0, geo.halo) for n, x in enumerate(new)]
     for got, want in zip(in_mix[job.ident], state):
         assert np.array_equal(got.view(np.int64), want.view(np.int64))
+
+
+def test_tick_selection_takes_shortest_remaining_work_first():
+    class Stub(serving.Server):
+        def __init__(self, tick_points):  # no device: only the selection rule
+            self.tick_points = tick_points
+            self.active = []
+
+    jobs = [serving.Job(n, 0.0, nx, 100, 10, 0, steps, seed=n)
+            for n, (nx, steps) in enumerate([(100, 50), (100, 5), (200, 5), (100, 6)])]
+    jobs[0].done = 48  # 2 steps left
+    server = Stub(tick_points=250_000)
+    server.active = jobs
+    # remaining work: job0 2x1e5, job1 5x1e5, job3 6x1e5, job2 5x2e5: the first three fill 3e5 >= 2.5e5 points
+    assert [j.ident for j in server.select()] == [0, 1, 3]
+    server.tick_points = None
+    assert [j.ident for j in server.select()] == [0, 1, 2, 3]
+    server.tick_points = 1
+    assert [j.ident for j in server.select()] == [0]  # always at least one job
+
+
+def test_tick_chunk_depth_spreads_small_ticks():
+    assert serving.tick_chunk_depth([(512, 512, 128)] * 4, 152) == 32
+    # one 64x64x32 job: 16 column tiles x 32 levels = 512 tile-levels over 608 CTAs: the shallowest chunks
+    assert serving.tick_chunk_depth([(64, 64, 32)], 152) == 2
+    assert serving.tick_chunk_depth([(160, 160, 64)], 152) == 11  # 100 tiles x 64 levels / 608
