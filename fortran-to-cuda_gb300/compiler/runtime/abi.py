@@ -87,6 +87,29 @@ class TraceState(c.Structure):
         (n, c.c_char * 65) for n in ("owner", "procedure", "segment", "operation", "implementation", "boundary")]
 
 
+class ExternalBinding(c.Structure):
+    _fields_ = [("buffer", U64), ("type", c.c_uint32), ("rank", c.c_uint32), ("element_bytes", SIZE),
+                ("access", Access)]
+
+
+class ExternalView(c.Structure):
+    _fields_ = [("buffer", U64), ("generation", U64), ("type", c.c_uint32), ("rank", c.c_uint32),
+                ("element_bytes", SIZE), ("bytes", SIZE), ("extents", c.POINTER(SIZE)), ("strides", c.POINTER(SIZE)),
+                ("lower_bounds", c.POINTER(c.c_int64)), ("device", c.c_void_p)]
+
+
+class ExternalCall(c.Structure):
+    _fields_ = [("version", c.c_uint32), ("reserved", c.c_uint32), ("bindings", c.POINTER(ExternalBinding)),
+                ("binding_count", SIZE), ("workspace_lease", U64), ("workspace_bytes", SIZE)]
+
+
+class ExternalReport(c.Structure):
+    _fields_ = [("version", c.c_uint32), ("status", c.c_int32), ("started", c.c_uint32), ("committed", c.c_uint32)]
+
+
+# int worker(void *user, const fort_scope_external_view_v1 *views, size_t count, void *stream, int *started)
+EXTERNAL_WORKER = c.CFUNCTYPE(c.c_int, c.c_void_p, c.POINTER(ExternalView), SIZE, c.c_void_p, c.POINTER(c.c_int))
+
 P = c.POINTER
 SIGNATURES = {
     "abi_version": ([], c.c_uint32),
@@ -145,6 +168,11 @@ SIGNATURES = {
     "graph_stats_get_v1": ([U64, P(GraphStats)], c.c_int),
     "device_reserve_slabs_v1": ([U64, P(U64), SIZE, P(c.c_void_p), P(c.c_int)], c.c_int),
     "slab_enqueue_v1": ([U64, U64, P(Task), SIZE, P(SIZE)], c.c_int),
+    "domain_workspace_reserve_v1": ([U64, SIZE, P(U64)], c.c_int),
+    "domain_workspace_resize_v1": ([U64, U64, SIZE], c.c_int),
+    "domain_workspace_release_v1": ([U64, U64], c.c_int),
+    "identity_swap_v1": ([U64, U64, U64, P(Layout), P(Layout), P(U64), P(U64)], c.c_int),
+    "external_execute_v1": ([U64, P(ExternalCall), EXTERNAL_WORKER, c.c_void_p, P(ExternalReport)], c.c_int),
 }
 
 

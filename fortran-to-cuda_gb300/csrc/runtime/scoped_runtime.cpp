@@ -137,6 +137,9 @@ struct Domain {
     std::map<uint64_t, std::unique_ptr<Buffer>> buffers;
     std::map<uint64_t, uint64_t> by_identity;
     size_t device_bytes = 0, scratch_bytes = 0;
+    // device memory external providers allocated themselves, claimed against the same budget
+    std::map<uint64_t, size_t> workspaces;
+    size_t workspace_bytes = 0;
     fort_scope_stats stats{};
     fort_scope_residency_stats_v1 residency{};
     uint64_t tick = 0;
@@ -432,7 +435,7 @@ void release_mirror(Context *c, Buffer *b) {
     b->device_valid.clear();
 }
 
-size_t claimed(const Domain *d) { return d->device_bytes + d->scratch_bytes; }
+size_t claimed(const Domain *d) { return d->device_bytes + d->scratch_bytes + d->workspace_bytes; }
 
 // Make room for `bytes` more, evicting least recently used mirrors that are not
 // in `keep`, not prepared and not used by queued tasks.
@@ -799,6 +802,11 @@ void accept(Context *c, Task &&task, std::vector<Bound> &bound) {
     if (c->pending.size() > c->queue_stats.peak_pending_tasks) c->queue_stats.peak_pending_tasks = c->pending.size();
     trace_line(c, "queue_enqueue", 0, bytes);
     if (!c->queue_enabled || (c->queue_work_limit && c->pending_threads >= c->queue_work_limit)) flush(c);
+}
+
+void count_external_launch(Context *c) {
+    c->domain->stats.launches++;
+    c->queue_stats.direct_submissions++;
 }
 
 // ---- slab pipelines -------------------------------------------------------------------------
@@ -1171,19 +1179,70 @@ int fort_scope_domain_abandon_v1(fort_scope_domain_t domain) {
     });
 }
 
-int fort_scope_domain_workspace_reserve_v1(fort_scope_domain_t, size_t, uint64_t *) {
-    return fail(FORT_SCOPE_RESOURCE, "external workspace claims are not provided by the GB300 advection runtime");
+// Workspace claims: bytes an external provider allocated on its own, counted
+// against the domain's budget like mirrors and scratch (no memory is allocated
+// here). A claim that does not fit evicts unprepared, idle mirrors (publishing
+// dirty values first) through the domain's context, or fails with RESOURCE and
+// changes nothing.
+void fit_workspace(Domain *d, size_t after) {
+    if (!d->budget_set || after <= d->workspace_bytes) return;
+    const size_t growth = after - d->workspace_bytes;
+    if (claimed(d) + growth <= d->budget) return;
+    Context *c = d->borrower;
+    if (!c || c->poisoned) raise(FORT_SCOPE_RESOURCE, "workspace claim exceeds the device budget");
+    ensure_stream(c);
+    make_room(c, growth, {});
 }
-int fort_scope_domain_workspace_resize_v1(fort_scope_domain_t, uint64_t, size_t) {
-    return fail(FORT_SCOPE_RESOURCE, "external workspace claims are not provided by the GB300 advection runtime");
+
+Domain *live_domain(fort_scope_domain_t handle) {
+    Domain *d = find_domain(handle);
+    if (d->poisoned) raise(FORT_SCOPE_EXECUTION, "residency domain has failed");
+    return d;
 }
-int fort_scope_domain_workspace_release_v1(fort_scope_domain_t, uint64_t) {
-    return fail(FORT_SCOPE_RESOURCE, "external workspace claims are not provided by the GB300 advection runtime");
+
+int fort_scope_domain_workspace_reserve_v1(fort_scope_domain_t domain, size_t bytes, uint64_t *lease) {
+    return guarded([&] {
+        if (!lease) raise(FORT_SCOPE_ARGUMENT, "null workspace lease output");
+        Domain *d = live_domain(domain);
+        if (bytes > SIZE_MAX - d->workspace_bytes) raise(FORT_SCOPE_RESOURCE, "workspace byte overflow");
+        fit_workspace(d, d->workspace_bytes + bytes);
+        const uint64_t token = new_handle();
+        d->workspaces[token] = bytes;
+        d->workspace_bytes += bytes;
+        *lease = token;
+        return FORT_SCOPE_OK;
+    });
+}
+
+int fort_scope_domain_workspace_resize_v1(fort_scope_domain_t domain, uint64_t lease, size_t bytes) {
+    return guarded([&] {
+        Domain *d = live_domain(domain);
+        auto it = d->workspaces.find(lease);
+        if (it == d->workspaces.end()) raise(FORT_SCOPE_STALE, "foreign or stale workspace lease");
+        const size_t others = d->workspace_bytes - it->second;
+        if (bytes > SIZE_MAX - others) raise(FORT_SCOPE_RESOURCE, "workspace byte overflow");
+        fit_workspace(d, others + bytes);
+        d->workspace_bytes = others + bytes;
+        it->second = bytes;
+        return FORT_SCOPE_OK;
+    });
+}
+
+int fort_scope_domain_workspace_release_v1(fort_scope_domain_t domain, uint64_t lease) {
+    return guarded([&] {
+        Domain *d = find_domain(domain);
+        auto it = d->workspaces.find(lease);
+        if (it == d->workspaces.end()) raise(FORT_SCOPE_STALE, "foreign or stale workspace lease");
+        d->workspace_bytes -= it->second;
+        d->workspaces.erase(it);
+        return FORT_SCOPE_OK;
+    });
 }
 
 int fort_scope_set_device_budget(fort_scope_t context, size_t bytes) {
     return guarded([&] {
         Context *c = live_context(context);
+        if (bytes < c->domain->workspace_bytes) raise(FORT_SCOPE_STATE, "the device budget must cover the workspace claims");
         c->domain->budget = bytes;
         c->domain->budget_set = true;
         return FORT_SCOPE_OK;
@@ -1388,15 +1447,53 @@ int fort_scope_admit_source_reads_v1(fort_scope_t context, fort_buffer_t buffer,
     });
 }
 
-int fort_scope_identity_swap_v1(fort_scope_t context, fort_buffer_t, fort_buffer_t, const fort_scope_layout *,
-                                const fort_scope_layout *, fort_buffer_t *, fort_buffer_t *) {
-    std::lock_guard<std::recursive_mutex> lock(g_mutex);
-    auto it = g_contexts.find(context);
-    if (it != g_contexts.end()) {
-        it->second->poisoned = true;
-        it->second->domain->poisoned = true;
-    }
-    return fail(FORT_SCOPE_EXECUTION, "identity swap is not provided by the GB300 advection runtime; unsafe replay prohibited");
+// Commit a descriptor exchange the program has already made (a MOVE_ALLOC
+// swap): the two registered identities trade the arrays they name. Nothing
+// physical moves; only the identity map changes and the caller is told which
+// array each identity now names. Because the exchange already happened, every
+// failed check poisons the context (EXECUTION): continuing under the old names
+// could publish into the wrong array.
+int fort_scope_identity_swap_v1(fort_scope_t context, fort_buffer_t first, fort_buffer_t second,
+                                const fort_scope_layout *first_after, const fort_scope_layout *second_after,
+                                fort_buffer_t *first_current, fort_buffer_t *second_current) {
+    return guarded([&] {
+        Context *c = live_context(context);
+        try {
+            if (first == second || !first_current || !second_current || first_current == second_current)
+                raise(FORT_SCOPE_ARGUMENT, "identity exchange needs two distinct arrays and output slots");
+            Buffer *a = find_buffer(c, first);
+            Buffer *b = find_buffer(c, second);
+            if (a->prepared != Buffer::NONE || b->prepared != Buffer::NONE)
+                raise(FORT_SCOPE_STATE, "identity exchange during a prepared access");
+            Domain *d = c->domain;
+            auto ai = d->by_identity.find(a->identity), bi = d->by_identity.find(b->identity);
+            if (a->identity == b->identity || ai == d->by_identity.end() || bi == d->by_identity.end() ||
+                ai->second != first || bi->second != second)
+                raise(FORT_SCOPE_STALE, "identity exchange names stale identities");
+            auto describes = [](const fort_scope_layout *after, const Buffer *x) {
+                if (!after || (int)after->rank != x->rank || !after->extents || !after->lower_bounds ||
+                    after->host != x->host || after->type != x->type || after->element_bytes != x->elem ||
+                    after->generation != x->generation)
+                    return false;
+                for (int r = 0; r < x->rank; ++r)
+                    if (after->extents[r] != x->extents[r] || after->lower_bounds[r] != x->lower[r]) return false;
+                return true;
+            };
+            if (!describes(first_after, b) || !describes(second_after, a))
+                raise(FORT_SCOPE_STALE, "a post-exchange layout does not describe the other array");
+            ai->second = second;
+            bi->second = first;
+            std::swap(a->identity, b->identity);
+            *first_current = second;
+            *second_current = first;
+            trace_line(c, "identity_swap", first, second);
+        } catch (Failure &f) {
+            c->poisoned = true;
+            c->domain->poisoned = true;
+            raise(FORT_SCOPE_EXECUTION, f.message + "; unsafe replay prohibited");
+        }
+        return FORT_SCOPE_OK;
+    });
 }
 
 int fort_scope_forget_definition(fort_scope_t context, fort_buffer_t buffer) {
@@ -1922,15 +2019,86 @@ int fort_scope_graph_stats_get_v1(fort_scope_t context, fort_scope_graph_stats_v
     });
 }
 
-int fort_scope_external_execute_v1(fort_scope_t, const fort_scope_external_call_v1 *, fort_scope_external_worker_v1,
-                                   void *, fort_scope_external_report_v1 *report) {
+// A checked opaque device transaction: the bindings are validated (known,
+// distinct, of the declared type, rank and element size, not under a prepared
+// access, reads defined) before anything moves; storage is reserved and what
+// the bindings read is uploaded after every queued task; the worker gets views
+// of the device copies and the context stream. It must report started = 0 when
+// it rejects the call before enqueuing anything, and started = 1 before its
+// first enqueue. Success (with started = 1) commits the bindings' exact effects;
+// a rejection before start changes no value; anything else after start poisons
+// the context, since the device may hold half-done work.
+int fort_scope_external_execute_v1(fort_scope_t context, const fort_scope_external_call_v1 *call,
+                                   fort_scope_external_worker_v1 worker, void *user,
+                                   fort_scope_external_report_v1 *report) {
     if (report) {
         report->version = FORT_SCOPE_EXTERNAL_ABI_VERSION;
-        report->status = FORT_SCOPE_RESOURCE;
+        report->status = FORT_SCOPE_OK;
         report->started = 0;
         report->committed = 0;
     }
-    return fail(FORT_SCOPE_RESOURCE, "external providers are not provided by the GB300 advection runtime");
+    const int status = guarded([&] {
+        if (!call || !report || call->version != FORT_SCOPE_EXTERNAL_ABI_VERSION || call->reserved ||
+            (call->binding_count && (!call->bindings || !worker)))
+            raise(FORT_SCOPE_ARGUMENT, "invalid external transaction");
+        Context *c = live_context(context);
+        if (!call->binding_count) return FORT_SCOPE_OK;
+        if (call->workspace_lease) {
+            auto lease = c->domain->workspaces.find(call->workspace_lease);
+            if (lease == c->domain->workspaces.end()) raise(FORT_SCOPE_STALE, "foreign or stale external workspace lease");
+            if (call->workspace_bytes > lease->second) raise(FORT_SCOPE_RESOURCE, "external workspace claim is too small");
+        } else if (call->workspace_bytes) {
+            raise(FORT_SCOPE_ARGUMENT, "an external workspace needs a workspace lease");
+        }
+        const size_t n = call->binding_count;
+        std::vector<fort_scope_plan_binding> plan(n);
+        std::set<uint64_t> seen;
+        for (size_t i = 0; i < n; ++i) {
+            const fort_scope_external_binding_v1 &x = call->bindings[i];
+            Buffer *b = find_buffer(c, x.buffer);
+            if (!seen.insert(b->handle).second) raise(FORT_SCOPE_ALIAS, "external transaction repeats an array");
+            if (x.type != b->type || (int)x.rank != b->rank || x.element_bytes != b->elem)
+                raise(FORT_SCOPE_ARGUMENT, "external transaction type or rank mismatch");
+            plan[i] = {x.buffer, x.access};
+        }
+        std::vector<Bound> bound = bind_all(c, plan.data(), n);
+        std::vector<Buffer *> list;
+        for (auto &x : bound) list.push_back(x.buffer);
+        flush(c);
+        reserve(c, list, false);
+        device_acquire(c, bound);
+        std::vector<fort_scope_external_view_v1> views(n);
+        std::vector<std::vector<size_t>> strides(n);
+        for (size_t i = 0; i < n; ++i) {
+            Buffer *b = bound[i].buffer;
+            strides[i].resize((size_t)b->rank);
+            size_t stride = b->elem;
+            for (int d = 0; d < b->rank; ++d) {
+                strides[i][(size_t)d] = stride;
+                stride *= b->extents[d];
+            }
+            views[i] = {b->handle, b->generation, b->type, (uint32_t)b->rank, b->elem, b->bytes, b->extents,
+                        strides[i].data(), b->lower, b->device};
+        }
+        int started = -1;
+        const int result = worker(user, views.data(), n, Backend::cpu ? nullptr : (void *)c->stream, &started);
+        report->started = started == 0 ? 0u : 1u;
+        const bool known = result >= FORT_SCOPE_ARGUMENT && result <= FORT_SCOPE_STATE && result != FORT_SCOPE_EXECUTION;
+        if ((started != 0 && started != 1) || (result == FORT_SCOPE_OK && started != 1) ||
+            (result != FORT_SCOPE_OK && (started != 0 || !known)))
+            poison(c, "external execution failed or did not report its submission state");
+        if (result != FORT_SCOPE_OK) raise(result, "external provider rejected the call before submission");
+        for (auto &x : bound) {
+            device_commit(c, x.buffer, x.effects.writes, x.effects.overwrites);
+            note_device_use(x.buffer);
+        }
+        count_external_launch(c);
+        report->committed = 1;
+        trace_line(c, "external_commit", 0, n);
+        return FORT_SCOPE_OK;
+    });
+    if (report) report->status = status;
+    return status;
 }
 
 } // extern "C"

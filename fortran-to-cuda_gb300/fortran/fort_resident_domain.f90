@@ -9,8 +9,10 @@
 ! tolerant binding answers 0 for an empty or non-contiguous array); observe
 ! publishes named arrays; publish observes and unregisters every non-persistent
 ! array; end_epoch publishes and ends the epoch; close releases the context and
-! the domain. resident_require stops the program on a nonzero status: work that
-! failed after it started is never replayed.
+! the domain. held answers the handle of the storage an array lies in (0 when
+! the domain keeps none); host_modify hands arrays to host code that may change
+! them and host_done hands them back. resident_require stops the program on a
+! nonzero status: work that failed after it started is never replayed.
 module fort_resident_domain
   use, intrinsic :: iso_c_binding
   use, intrinsic :: iso_fortran_env, only: error_unit
@@ -37,6 +39,8 @@ module fort_resident_domain
     procedure :: bind_real64
     generic :: bind => bind_real64
     procedure :: held
+    procedure :: host_modify
+    procedure :: host_done
     procedure :: release
     procedure :: observe
     procedure :: publish
@@ -161,12 +165,38 @@ contains
     if (.not. self%active .or. size(values) == 0) return
     identity = transfer(c_loc(values), identity)
     do i = 1, size(self%storage)
-      if (self%storage(i)%identity == identity) then
-        handle = self%storage(i)%handle
-        return
-      endif
+      ! the storage whose bytes contain the array's first element
+      if (identity < self%storage(i)%identity) cycle
+      if (identity >= self%storage(i)%identity + 8_c_int64_t * int(product(self%storage(i)%extents), c_int64_t)) cycle
+      handle = self%storage(i)%handle
+      return
     enddo
   end function
+
+  ! Hand arrays (by handle; 0 and repeats ignored) to host code that may change them.
+  subroutine host_modify(self, handles)
+    class(resident_domain), intent(inout) :: self
+    integer(c_int64_t), intent(in) :: handles(:)
+    type(fort_scope_access), target :: access
+    integer :: i
+    access%flags = ior(FORT_SCOPE_READ_ALL, FORT_SCOPE_WRITE_ALL)
+    do i = 1, size(handles)
+      if (handles(i) == 0 .or. any(handles(:i - 1) == handles(i))) cycle
+      call resident_require(fort_scope_host_begin(self%context, handles(i), access))
+    enddo
+  end subroutine
+
+  ! Hand them back, in reverse order, after the host code.
+  subroutine host_done(self, handles)
+    class(resident_domain), intent(inout) :: self
+    integer(c_int64_t), intent(in) :: handles(:)
+    integer :: i
+    do i = size(handles), 1, -1
+      if (handles(i) == 0 .or. any(handles(:i - 1) == handles(i))) cycle
+      call resident_require(fort_scope_host_end(self%context, handles(i)))
+    enddo
+    self%stamp = self%stamp + 1
+  end subroutine
 
   ! Retire an array's device state without bringing its values home: for a
   ! temporary about to be deallocated.

@@ -667,3 +667,171 @@ def test_reserve_many_hands_host_round_arrays_out_in_place(monkeypatch):
         assert _enqueue(scope, fn, hx, 8, 1.0, 1.0) == abi.OK
         assert lib.fort_scope_observe_v1(scope.handle, (abi.U64 * 1)(hx), 1) == abi.OK
     assert lib.fort_scope_close(scope.handle) == abi.OK
+
+
+# ------------------------------------------------------------------------------- external providers
+
+
+def _external(lib, scope, handle, worker, *, type_=abi.REAL64, rank=1, flags=abi.READ_ALL | abi.WRITE_ALL):
+    acc = abi.access(flags=flags)
+    binding = (abi.ExternalBinding * 1)(abi.ExternalBinding(handle, type_, rank, 8, acc))
+    call = abi.ExternalCall(1, 0, binding, 1, 0, 0)
+    report = abi.ExternalReport()
+    status = lib.fort_scope_external_execute_v1(scope.handle, c.byref(call), worker, None, c.byref(report))
+    return status, report
+
+
+def _worker(log, *, started, result, scale=2.0):
+    def run(user, views, count, stream, flag):
+        v = views[0]
+        log.append((count, v.rank, v.extents[0], v.strides[0], v.element_bytes))
+        flag[0] = started
+        if started == 1 and result == abi.OK:
+            _dev(v.device, v.extents[0])[:] *= scale
+        return result
+
+    return abi.EXTERNAL_WORKER(run)
+
+
+def test_external_transaction_commits_its_effects(both):
+    scope = abi.Scope(both)
+    host, address = _array(np.arange(6.0))
+    _, h = scope.register(address, [6])
+    log = []
+    status, report = _external(both, scope, h, _worker(log, started=1, result=abi.OK))
+    assert status == abi.OK
+    assert (report.status, report.started, report.committed) == (abi.OK, 1, 1)
+    assert log == [(1, 1, 6, 8, 8)]  # one view: rank 1, extent 6, byte stride 8
+    assert both.fort_scope_host_begin(scope.handle, h, c.byref(abi.access(flags=abi.READ_ALL))) == abi.OK
+    assert host.tolist() == [2.0 * i for i in range(6)]
+    assert both.fort_scope_host_end(scope.handle, h) == abi.OK
+    assert both.fort_scope_close(scope.handle) == abi.OK
+
+
+def test_external_rejection_before_start_changes_nothing(both):
+    scope = abi.Scope(both)
+    host, address = _array(np.arange(4.0))
+    _, h = scope.register(address, [4])
+    status, report = _external(both, scope, h, _worker([], started=0, result=abi.RESOURCE))
+    assert status == abi.RESOURCE
+    assert (report.started, report.committed) == (0, 0)
+    # the context stays usable and the values are those of the host
+    assert both.fort_scope_host_begin(scope.handle, h, c.byref(abi.access(flags=abi.READ_ALL))) == abi.OK
+    assert host.tolist() == [0.0, 1.0, 2.0, 3.0]
+    assert both.fort_scope_host_end(scope.handle, h) == abi.OK
+    assert both.fort_scope_close(scope.handle) == abi.OK
+
+
+@pytest.mark.parametrize("started, result", [(1, abi.ARGUMENT), (-1, abi.OK), (0, abi.OK), (0, abi.EXECUTION)])
+def test_external_failure_after_start_or_without_a_report_poisons(both, started, result):
+    scope = abi.Scope(both)
+    _, address = _array(np.zeros(4))
+    _, h = scope.register(address, [4])
+    status, report = _external(both, scope, h, _worker([], started=started, result=result))
+    assert status == abi.EXECUTION
+    # nothing is replayed: the context refuses further work
+    assert both.fort_scope_host_begin(scope.handle, h, c.byref(abi.access(flags=abi.READ_ALL))) == abi.EXECUTION
+    both.fort_scope_abandon(scope.handle)
+
+
+def test_external_bindings_are_checked_before_the_worker_runs(both):
+    scope = abi.Scope(both)
+    _, address = _array(np.zeros(4))
+    _, h = scope.register(address, [4])
+    log = []
+    status, _ = _external(both, scope, h, _worker(log, started=1, result=abi.OK), type_=abi.REAL32)
+    assert status == abi.ARGUMENT
+    status, _ = _external(both, scope, h, _worker(log, started=1, result=abi.OK), rank=2)
+    assert status == abi.ARGUMENT
+    assert log == []
+    # no bindings: nothing is called
+    call = abi.ExternalCall(1, 0, None, 0, 0, 0)
+    report = abi.ExternalReport()
+    assert both.fort_scope_external_execute_v1(scope.handle, c.byref(call), _worker(log, started=1, result=abi.OK),
+                                               None, c.byref(report)) == abi.OK
+    assert log == []
+    assert both.fort_scope_close(scope.handle) == abi.OK
+
+
+# ------------------------------------------------------------------------------- identity exchange
+
+
+def _layout(address, shape, generation=1, lower=None):
+    extents = (abi.SIZE * len(shape))(*shape)
+    bounds = (c.c_int64 * len(shape))(*(lower or [1] * len(shape)))
+    layout = abi.Layout(len(shape), abi.REAL64, 8, address, extents, bounds, generation)
+    layout.keep = (extents, bounds)
+    return layout
+
+
+def test_identity_swap_exchanges_names_not_storage(both):
+    scope = abi.Scope(both)
+    x, xa = _array(np.arange(4.0))
+    y, ya = _array(np.arange(4.0) + 10)
+    _, hx = scope.register(xa, [4], identity=1001)
+    _, hy = scope.register(ya, [4], identity=1002)
+    now_x, now_y = abi.U64(), abi.U64()
+    status = both.fort_scope_identity_swap_v1(scope.handle, hx, hy, c.byref(_layout(ya, [4])), c.byref(_layout(xa, [4])),
+                                              c.byref(now_x), c.byref(now_y))
+    assert status == abi.OK
+    assert (now_x.value, now_y.value) == (hy, hx)
+    # each identity now names the other array: registering it again finds that array's handle
+    status, again = scope.register(ya, [4], identity=1001)
+    assert (status, again) == (abi.OK, hy)
+    assert both.fort_scope_close(scope.handle) == abi.OK
+
+
+def test_identity_swap_with_a_wrong_layout_poisons(both):
+    scope = abi.Scope(both)
+    _, xa = _array(np.zeros(4))
+    _, ya = _array(np.zeros(4))
+    _, hx = scope.register(xa, [4], identity=2001)
+    _, hy = scope.register(ya, [4], identity=2002)
+    now_x, now_y = abi.U64(), abi.U64()
+    # the first layout describes its own array instead of the other one
+    status = both.fort_scope_identity_swap_v1(scope.handle, hx, hy, c.byref(_layout(xa, [4])), c.byref(_layout(xa, [4])),
+                                              c.byref(now_x), c.byref(now_y))
+    assert status == abi.EXECUTION
+    assert both.fort_scope_host_begin(scope.handle, hx, c.byref(abi.access(flags=abi.READ_ALL))) == abi.EXECUTION
+    both.fort_scope_abandon(scope.handle)
+
+
+# ------------------------------------------------------------------------------- workspace claims
+
+
+def test_workspace_claims_count_against_the_budget(both):
+    dom = abi.U64()
+    assert both.fort_scope_domain_create_v1(0, c.byref(dom)) == abi.OK
+    scope = abi.Scope(both, domain=dom.value)
+    assert both.fort_scope_set_device_budget(scope.handle, 1 << 20) == abi.OK
+    budget, free = abi.SIZE(), abi.SIZE()
+    lease = abi.U64()
+    assert both.fort_scope_domain_workspace_reserve_v1(dom.value, 4096, c.byref(lease)) == abi.OK
+    assert both.fort_scope_domain_budget_get_v1(dom.value, c.byref(budget), c.byref(free)) == abi.OK
+    assert (budget.value, free.value) == (1 << 20, (1 << 20) - 4096)
+    assert both.fort_scope_domain_workspace_resize_v1(dom.value, lease.value, 1024) == abi.OK
+    assert both.fort_scope_domain_budget_get_v1(dom.value, c.byref(budget), c.byref(free)) == abi.OK
+    assert free.value == (1 << 20) - 1024
+    # a claim beyond the budget fails and changes nothing
+    assert both.fort_scope_domain_workspace_resize_v1(dom.value, lease.value, 2 << 20) == abi.RESOURCE
+    assert both.fort_scope_domain_budget_get_v1(dom.value, c.byref(budget), c.byref(free)) == abi.OK
+    assert free.value == (1 << 20) - 1024
+    # an external call may use the lease up to its size
+    _, address = _array(np.zeros(4))
+    _, h = scope.register(address, [4])
+    binding = (abi.ExternalBinding * 1)(abi.ExternalBinding(h, abi.REAL64, 1, 8,
+                                                           abi.access(flags=abi.READ_ALL | abi.WRITE_ALL)))
+    worker = _worker([], started=1, result=abi.OK)
+    report = abi.ExternalReport()
+    call = abi.ExternalCall(1, 0, binding, 1, lease.value, 2048)
+    assert both.fort_scope_external_execute_v1(scope.handle, c.byref(call), worker, None, c.byref(report)) == \
+        abi.RESOURCE
+    call = abi.ExternalCall(1, 0, binding, 1, lease.value, 1024)
+    assert both.fort_scope_external_execute_v1(scope.handle, c.byref(call), worker, None, c.byref(report)) == abi.OK
+    assert both.fort_scope_domain_workspace_release_v1(dom.value, lease.value) == abi.OK
+    assert both.fort_scope_domain_workspace_release_v1(dom.value, lease.value) == abi.STALE
+    call = abi.ExternalCall(1, 0, binding, 1, lease.value, 0)
+    assert both.fort_scope_external_execute_v1(scope.handle, c.byref(call), worker, None, c.byref(report)) == \
+        abi.STALE
+    assert both.fort_scope_close(scope.handle) == abi.OK
+    assert both.fort_scope_domain_close_v1(dom.value) == abi.OK
