@@ -2007,8 +2007,89 @@ int fort_scope_graph_submit_v1(fort_scope_t context, uint64_t group_key, const f
     });
 }
 
-int fort_scope_graph_execute_v1(fort_scope_t, uint64_t, const fort_scope_graph_task_v1 *, size_t) {
-    return fail(FORT_SCOPE_RESOURCE, "checked graph execution is not provided; use fort_scope_graph_enqueue_v1");
+// Checked graph execution: the tasks' effects are simulated in order on
+// private copies of each array's definition and device coherence, so a task
+// may read what an earlier task of the group defines. Only what the group
+// needs from the host (reads not defined inside the group and not current on
+// the device) is uploaded, after every queued task; then the kernels launch in
+// order on the context stream (their argument values are read as each launch is
+// made, so the records need no argument sizes), and the final definitions and
+// coherence are committed. Nothing changes unless every task validates. Every
+// array needs reserved device storage; none may be under a prepared access.
+int fort_scope_graph_execute_v1(fort_scope_t context, uint64_t group_key, const fort_scope_graph_task_v1 *tasks,
+                                size_t count) {
+    return guarded([&] {
+        Context *c = live_context(context);
+        if (count && !tasks) raise(FORT_SCOPE_ARGUMENT, "null tasks");
+        if (!count) return FORT_SCOPE_OK;
+        if (!group_key) raise(FORT_SCOPE_ARGUMENT, "a graph group needs a stable key");
+        struct Sim {
+            Region defined, device, upload;
+        };
+        std::map<Buffer *, Sim> sim;
+        std::vector<LaunchSpec> list;
+        std::vector<std::vector<Bound>> bound(count);
+        for (size_t n = 0; n < count; ++n) {
+            const fort_scope_graph_task_v1 &t = tasks[n];
+            list.push_back(spec_of(t.kernel));
+            for (size_t a = 0; a < t.kernel.argument_count; ++a) {
+                if (!t.kernel.arguments[a]) raise(FORT_SCOPE_ARGUMENT, "empty kernel argument");
+                list.back().arguments.push_back(t.kernel.arguments[a]);
+            }
+            if (t.binding_count && !t.bindings) raise(FORT_SCOPE_ARGUMENT, "null bindings");
+            std::set<uint64_t> seen;
+            for (size_t i = 0; i < t.binding_count; ++i) {
+                Buffer *b = find_buffer(c, t.bindings[i].buffer);
+                if (!seen.insert(b->handle).second) raise(FORT_SCOPE_ALIAS, "a task binds one array twice");
+                if (b->prepared != Buffer::NONE) raise(FORT_SCOPE_STATE, "array already has a prepared access");
+                if (!b->device || b->in_place) raise(FORT_SCOPE_STATE, "task binds an array whose device storage is not reserved");
+                Effects e = effects_of(b, t.bindings[i].access);
+                auto it = sim.find(b);
+                if (it == sim.end()) it = sim.emplace(b, Sim{b->defined, b->device_valid, Region{}}).first;
+                Sim &st = it->second;
+                for (const auto &box : e.reads.boxes)
+                    if (!st.defined.covers(box))
+                        raise(FORT_SCOPE_UNINITIALIZED, "a task reads array values that were never defined");
+                Region need = e.reads;
+                Region partial = e.writes;
+                partial.remove(e.overwrites);
+                need.add(partial);
+                need = st.defined.clip(need);
+                need.remove(st.device);
+                st.upload.add(need);
+                st.device.add(need);
+                st.device.add(e.writes);
+                st.defined.add(e.overwrites);
+                bound[n].push_back({b, std::move(e)});
+            }
+        }
+        flush(c);
+        ensure_stream(c);
+        for (auto &kv : sim) {
+            Buffer *b = kv.first;
+            Region up = kv.second.upload;
+            up.remove(b->device_valid);
+            if (up.empty()) continue;
+            const Region moved = widened(b, up, true);
+            copy_region(c, b, moved, true);
+            Region device = b->device_valid;
+            device.add(up);
+            device.add(b->host_valid.clip(moved));
+            settle(c, b, b->defined, b->host_valid, device);
+        }
+        for (const LaunchSpec &k : list) {
+            trace_line(c, "launch", 0, 0);
+            if (!Backend::launch(k, c->stream)) poison(c, std::string("kernel launch failed: ") + Backend::last_error());
+        }
+        c->domain->stats.launches += count;
+        c->queue_stats.direct_submissions++;
+        c->queue_stats.direct_kernels += count;
+        for (auto &tb : bound)
+            for (auto &x : tb) device_commit(c, x.buffer, x.effects.writes, x.effects.overwrites);
+        for (auto &kv : sim) note_device_use(kv.first);
+        c->queue_stats.accepted_tasks += count;
+        return FORT_SCOPE_OK;
+    });
 }
 
 int fort_scope_graph_stats_get_v1(fort_scope_t context, fort_scope_graph_stats_v1 *stats) {

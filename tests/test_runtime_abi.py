@@ -835,3 +835,61 @@ def test_workspace_claims_count_against_the_budget(both):
         abi.STALE
     assert both.fort_scope_close(scope.handle) == abi.OK
     assert both.fort_scope_domain_close_v1(dom.value) == abi.OK
+
+
+# ------------------------------------------------------------------------------- checked graph execution
+
+
+def _scale_kernel(log):
+    """dst[i] = 2 * src[i] for i < n; arguments (double *src, double *dst, int n)."""
+
+    def run(args):
+        src = _dev(c.cast(args[0], c.POINTER(c.c_void_p))[0], 8)
+        dst = _dev(c.cast(args[1], c.POINTER(c.c_void_p))[0], 8)
+        n = c.cast(args[2], c.POINTER(c.c_int))[0]
+        dst[:n] = 2.0 * src[:n]
+        log.append("scale")
+
+    return KERNEL(run)
+
+
+def _task(fn, values, bindings):
+    argv = (c.c_void_p * len(values))(*[c.cast(c.pointer(v), c.c_void_p) for v in values])
+    kernel = abi.Kernel(1, 0, c.cast(fn, c.c_void_p), (c.c_uint32 * 3)(1, 1, 1), (c.c_uint32 * 3)(32, 1, 1), 0,
+                        argv, len(values))
+    packed = (abi.Binding * len(bindings))(*[abi.Binding(h, acc) for h, acc in bindings])
+    task = abi.Task(kernel, packed, len(bindings))
+    task.keep = (values, argv, bindings, packed)
+    return task
+
+
+def test_graph_group_may_read_what_an_earlier_task_defines(ours):
+    scope = abi.Scope(ours)
+    x, xa = _array(np.arange(8.0))
+    y, ya = _array(np.full(8, -1.0))
+    _, hx = scope.register(xa, [8])
+    _, hy = scope.register(ya, [8], initialized=False)
+    devices = (c.c_void_p * 2)()
+    assert ours.fort_scope_device_reserve_many_v1(scope.handle, (abi.U64 * 2)(hx, hy), 2, devices) == abi.OK
+    log = []
+    scale, axpy = _scale_kernel(log), _axpy_kernel(log)
+    produce = _task(scale, [c.c_void_p(devices[0]), c.c_void_p(devices[1]), c.c_int(8)],
+                    [(hx, abi.access(flags=abi.READ_ALL)), (hy, abi.access(flags=abi.WRITE_ALL | abi.OVERWRITE_ALL))])
+    consume = _task(axpy, [c.c_void_p(devices[1]), c.c_int(8), c.c_double(1.0), c.c_double(1.0)],
+                    [(hy, abi.access(flags=abi.READ_ALL | abi.WRITE_ALL))])
+    group = (abi.Task * 2)(produce, consume)
+    before = scope.stats()
+    assert ours.fort_scope_graph_execute_v1(scope.handle, 77, group, 2) == abi.OK
+    assert log == ["scale", (8, 1.0, 1.0)]
+    assert scope.stats().uploads - before.uploads == 1  # x only: y is defined inside the group
+    assert ours.fort_scope_host_begin(scope.handle, hy, c.byref(abi.access(flags=abi.READ_ALL))) == abi.OK
+    assert y.tolist() == [2.0 * i + 1.0 for i in range(8)]
+    assert ours.fort_scope_host_end(scope.handle, hy) == abi.OK
+    # in the other order the first task reads y before anything defines it: refused, nothing runs
+    log.clear()
+    assert ours.fort_scope_forget_definition(scope.handle, hy) == abi.OK
+    group = (abi.Task * 2)(consume, produce)
+    assert ours.fort_scope_graph_execute_v1(scope.handle, 78, group, 2) == abi.UNINITIALIZED
+    assert ours.fort_scope_graph_execute_v1(scope.handle, 0, group, 2) == abi.ARGUMENT
+    assert log == []
+    assert ours.fort_scope_close(scope.handle) == abi.OK
