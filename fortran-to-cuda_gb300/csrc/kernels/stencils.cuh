@@ -18,12 +18,17 @@ namespace f2c {
 // x * 2^e for an exact power-of-two factor, on the integer pipe when the
 // result stays normal (the same bits as the correctly rounded product);
 // the FP64 multiply otherwise.
+// The multiplication for the rare operands the exponent shift cannot take. Out
+// of line, so that the common path issues no FP64 instruction (an inline
+// fallback is evaluated alongside and costs one FP64 multiply per point).
+static __device__ __noinline__ double scale_by(double x, double factor) { return x * factor; }
+
 __device__ __forceinline__ double scale_pow2(double x, int e, double factor) {
     const long long b = __double_as_longlong(x);
     const int ex = (int)((unsigned long long)b >> 52) & 0x7ff;
     const int r = ex + e;
     if (ex != 0 && ex != 0x7ff && r >= 1 && r <= 0x7fe) return __longlong_as_double(b + ((long long)e << 52));
-    return x * factor;
+    return scale_by(x, factor);
 }
 
 struct DiffusionArgs {
