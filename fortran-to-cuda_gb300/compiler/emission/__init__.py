@@ -27,6 +27,7 @@ from __future__ import annotations
 
 import json
 from dataclasses import dataclass, field
+from functools import lru_cache
 from hashlib import sha256
 from pathlib import Path
 
@@ -145,6 +146,11 @@ def _step_entries():
 
 def registry() -> list[Entry]:
     """Every entry this build emits, in a fixed order."""
+    return list(_registry())
+
+
+@lru_cache(maxsize=1)
+def _registry() -> tuple:
     cdu = "benchmarks/cdu/src/cdu.f90"
     stencils = "compiler/tests/fixtures/stencils"
     entries = [
@@ -168,11 +174,12 @@ def registry() -> list[Entry]:
                _i("halo")),
               source="2-D TM Yee leapfrog (no reference source in the mount)", notes="H task then E task"),
     ]
-    return entries
+    return tuple(entries)
 
 
+@lru_cache(maxsize=None)
 def entry_for(procedure: str) -> Entry:
-    for entry in registry():
+    for entry in _registry():
         if entry.procedure == procedure.lower():
             return entry
     raise KeyError(procedure)
