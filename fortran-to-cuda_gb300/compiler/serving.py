@@ -3,20 +3,22 @@
 A job asks for ``steps`` forward-Euler steps (dt = 0.1, with the boundary fill
 after each) of an advection instance: seeded sine-mode U, V, W and 0-3
 scalars on an nx x ny x nz grid. The server keeps every admitted job's fields
-resident on the device (two buffer sets, ping-pong) until its last step, and
-advances ALL admitted jobs by one step per tick: one persistent batched launch
-per scalar count over the union of their tiles (``f2c_batch_*``), then each
-job's boundary fill. Jobs that arrive while others run are admitted at the
-next tick as slots and memory allow (a device-memory budget, 150 GB by
-default), so their steps overlap on the device with the running jobs' steps.
-Every job's arithmetic is the single-instance kernel's, so a job's result is
-the same alone and in any mix, bit for bit.
+resident on the device (two buffer sets, ping-pong) until its last step. Each
+tick advances the jobs with the least remaining work, up to about 4 M grid
+points, by one step: per scalar count one persistent batched launch over the
+union of their tiles (``f2c_batch_*``) and one batched boundary fill. Jobs are
+admitted as they arrive while slots and memory allow (a device-memory budget,
+150 GB by default); their fields are generated on a side stream and they join
+the ticks once ready, so their steps overlap on the device with the running
+jobs' steps. Every job's arithmetic is the single-instance kernel's, so a job's
+result is the same alone and in any mix, bit for bit.
 
 The open-loop arrival stream and the job sizes follow the serving
 configuration: Poisson arrivals at a given rate; nx and ny drawn independently
 log-uniform in [48, 320], nz log-uniform in [24, 128]; 0-3 scalars and 1-100
-steps uniform. ``serial_timeline`` gives the comparison: the same stream served
-one job at a time through the single-instance path.
+steps uniform. ``SerialServer`` gives the comparison: the same stream served
+one job at a time through the single-instance path, in wall-clock time with
+the same per-job work; ``serial_timeline`` models it from device times alone.
 """
 
 from __future__ import annotations
