@@ -570,7 +570,7 @@ def run_stencils(args):
 def main():
     parser = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     parser.add_argument("--gpus", type=int, default=1)
-    parser.add_argument("--steps", type=int, default=50)
+    parser.add_argument("--steps", type=int, default=200)
     parser.add_argument("--warmup", type=int, default=3)
     parser.add_argument("--impl", choices=("gb300", "reference"), default="gb300")
     parser.add_argument("--no-cpu-baseline", action="store_true")
@@ -580,6 +580,7 @@ def main():
                         default="advection", help="the headline step (default) or another configuration")
     parser.add_argument("--tune", action="store_true", help="batched: run the z-chunk autotuner first")
     parser.add_argument("--instances", type=int, default=64, help="batched: the first N instances of the ensemble")
+    parser.add_argument("--jobs", type=int, default=50, help="serving: jobs per arrival rate")
     args = parser.parse_args()
     args.warmup = max(3, args.warmup)
     if args.size:

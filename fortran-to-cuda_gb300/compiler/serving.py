@@ -421,7 +421,7 @@ def bench_main(args) -> None:
     import torch
 
     rates = (50, 100, 200, 500, 1000, 2000)
-    count = max(20, args.steps)
+    count = max(20, getattr(args, "jobs", 50))
     # untimed warm-up of both servers (module loading, first allocations, plan building)
     Server(torch).run(poisson_jobs(8, 2000.0, seed=1))
     SerialServer(torch).run(poisson_jobs(8, 2000.0, seed=1))
