@@ -31,7 +31,7 @@ constexpr size_t kAlign = 256;
 size_t align_up(size_t v) { return (v + kAlign - 1) / kAlign * kAlign; }
 
 template <int NS, int MASK>
-__global__ void __launch_bounds__(kFaceThreads, 1)
+__global__ void __launch_bounds__(kFaceThreads, kFaceCtasPerSM)
     advection_batched_kernel(const AdvArgs *__restrict__ instances, const BatchItem *__restrict__ items, int nitems,
                              unsigned *counter) {
     extern __shared__ double smem[];
