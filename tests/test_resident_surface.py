@@ -247,7 +247,24 @@ def test_cli_prepare_only(tmp_path, capsys):
     assert line == {"application": "Synthetic", "entries": 1, "nests": {"advection": 1}, "directives": 2,
                     "outcome": "prepared"}
     (tmp_path / "bad").mkdir()
-    assert cli.main([str(_write_app(tmp_path / "bad", minimum=5)), "--output", str(tmp_path / "o2")]) == 2
+    assert cli.main([str(_write_app(tmp_path / "bad", minimum=5)), "--output", str(tmp_path / "o2")]) == 1
+
+
+def test_cli_takes_the_reference_command_line(tmp_path, capsys):
+    app = str(_write_app(tmp_path))
+    out = str(tmp_path / "out")
+    # the reference's full argument list, preparing only
+    assert cli.main([app, "--output", out, "--fortran", "gfortran", "--cxx", "g++", "--architecture", "103a",
+                     "--jobs", "2", "--prepare-only"]) == 0
+    capsys.readouterr()
+    # building what was prepared: no Fortran compiler here, so it stops after the preparation it finds
+    assert cli.main([app, "--output", out, "--build-prepared"]) == 0
+    assert json.loads(capsys.readouterr().out)["application"] == "Synthetic"
+    for extra, message in ((["--architecture", "86"], "built for sm_103a"), (["--fast-fp"], "strict"),
+                           (["--input", "elmm=/tmp"], "outside the advection path"),
+                           (["--prepare-only", "--build-prepared"], "choose preparation")):
+        assert cli.main([app, "--output", out, *extra]) == 1
+        assert message in capsys.readouterr().err
 
 
 @pytest.mark.skipif(not CDU_TOML.exists(), reason="the reference's cdu benchmark is not on this machine")
