@@ -208,7 +208,7 @@ def run_e2e(fields, steps, dist, torch):
 
     for _ in range(2):
         step()
-    n = max(1, min(steps, 5))
+    n = max(1, min(steps, 10))
     barrier(dist, torch)
     t0 = time.perf_counter()
     for _ in range(n):

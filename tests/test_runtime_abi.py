@@ -893,3 +893,31 @@ def test_graph_group_may_read_what_an_earlier_task_defines(ours):
     assert ours.fort_scope_graph_execute_v1(scope.handle, 0, group, 2) == abi.ARGUMENT
     assert log == []
     assert ours.fort_scope_close(scope.handle) == abi.OK
+
+
+def test_slab_pipeline_keeps_coherence_compact(monkeypatch):
+    """Ten slabs publish ten interior boxes that merge back into one: no reconciliation is ever needed."""
+    monkeypatch.setenv("F2C_TEST_MAPPED", "1")
+    lib = _ours()
+    scope = abi.Scope(lib)
+    x, xa = _array(np.arange(NX_S * NY_S * NZ_S, dtype=np.float64))
+    y, ya = _array(np.zeros(NX_S * NY_S * NZ_S))
+    _, hx = scope.register(xa, [NX_S, NY_S, NZ_S])
+    _, hy = scope.register(ya, [NX_S, NY_S, NZ_S])
+    log = []
+    fn = _plane_sum_kernel(log)
+    bounds = [(k, k + 1) for k in range(1, 9)]  # one level per slab: eight slabs
+    for round_ in range(4):
+        status, devices, pipelined = _reserve_slabs(lib, scope, [hx, hy])
+        assert status == abi.OK
+        tasks, sizes, keep = _slab_tasks(fn, devices, hx, hy, bounds)
+        assert lib.fort_scope_slab_enqueue_v1(scope.handle, 11, tasks, len(bounds), sizes) == abi.OK
+        assert lib.fort_scope_observe_v1(scope.handle, (abi.U64 * 1)(hy), 1) == abi.OK
+        assert lib.fort_scope_host_begin(scope.handle, hx, c.byref(abi.access(flags=abi.WRITE_ALL))) == abi.OK
+        assert lib.fort_scope_host_end(scope.handle, hx) == abi.OK
+    p = x.reshape(NZ_S, -1)
+    want = np.zeros_like(p)
+    want[1:9] = p[0:8] + p[1:9] + p[2:10]
+    assert np.array_equal(y, want.ravel())
+    assert scope.stats().reconciliations == 0
+    assert lib.fort_scope_close(scope.handle) == abi.OK
