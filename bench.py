@@ -272,6 +272,21 @@ def run_gb300(args):
     points = geo.points
     value = whole_job_value(points, world, args.steps, elapsed_ms)
 
+    # The reference's emitted structure on the same GPU: per momentum component the set, flux-form,
+    # advective-form and halving procedures as separate grid-stride launches, the scalars as one more launch.
+    u_, v_, w_ = p[:3]
+
+    def reference_structure(s):
+        ops = ((native.CDU_DIV, native.CDU_ADV), (native.CDV_DIV, native.CDV_ADV), (native.CDW_DIV, native.CDW_ADV))
+        for o, (div, adv) in zip(q[:3], ops):
+            native.procedure(native.SET, grid, o, value=0.0, stream=s)
+            native.procedure(div, grid, o, u_, v_, w_, stream=s)
+            native.procedure(adv, grid, o, u_, v_, w_, stream=s)
+            native.procedure(native.MULTIPLY, grid, o, value=0.5, stream=s)
+        native.advection(grid, u_, v_, w_, scalars=p[3:], scalar_out=q[3:], stream=s)
+
+    reference_ms = _graph_time(torch, stream, reference_structure, max(3, min(args.steps, 20)), args.warmup)
+
     # FP64 pipe rate of this GPU (the roofline that binds first on GB300)
     scratch = torch.empty(8 * torch.cuda.get_device_properties(local).multi_processor_count * 256,
                           dtype=torch.float64, device="cuda")
@@ -317,6 +332,10 @@ def run_gb300(args):
                         "in place, copies by DMA over NVLink-C2C"},
         "gpu_launches": args.steps,
         "clocks": sampler.summary(),
+        "reference_structure": {"value": whole_job_value(points, world, 1, reference_ms), "ms_per_step": reference_ms,
+                                "how": "the reference's emitted structure on this GPU: set, flux form, advective form "
+                                       "and halving as separate launches per momentum component, plus one launch "
+                                       "for the scalars; graph-replayed"},
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         v, cores, sample = cpu_oracle_sample(fields)
