@@ -58,6 +58,17 @@ __device__ __forceinline__ double exact_half(double x) {
     return __longlong_as_double(r);
 }
 
+// IEEE negation (the sign bit flipped, exact for every value) on the integer
+// pipe. Written as inline PTX so that it stays an integer operation: a plain
+// `-x`, or a sign flip written in C++, becomes a floating negation that the
+// compiler issues on the FP64 pipe here (measured: three FP64 additions per
+// point fewer, 2 % faster, results unchanged).
+__device__ __forceinline__ double opaque_negate(double x) {
+    unsigned long long r;
+    asm("xor.b64 %0, %1, 0x8000000000000000;" : "=l"(r) : "l"((unsigned long long)__double_as_longlong(x)));
+    return __longlong_as_double((long long)r);
+}
+
 template <int NS, int MASK>
 struct FaceSmem {
     static constexpr int NF = 3 + NS;
@@ -253,7 +264,7 @@ __device__ __forceinline__ void faces_tile(const AdvArgs &a, int tile_x, int til
             const double Vw = LD(V, p, -1, 0, 0), Vs = LD(V, p, 0, -1, 0), Vm = LD(V, p, 0, 0, -1);
             const double Ww = LD(W, p, -1, 0, 0), Ws = LD(W, p, 0, -1, 0), Wm = LD(W, p, 0, 0, -1);
             if (DO_U) {
-                const double r = -(((FUx - xf[0 * Smem::XF + xw]) + (FUy - yf[0 * Smem::YF + ys])) + (FUz - FUzb));
+                const double r = opaque_negate(((FUx - xf[0 * Smem::XF + xw]) + (FUy - yf[0 * Smem::YF + ys])) + (FUz - FUzb));
                 const double Vadv = (sVx + Vs) + LD(V, p, 1, -1, 0);
                 const double Wadv = (sWx + Wm) + LD(W, p, 1, 0, -1);
                 const double adv = ((c.Bux * (Ue - Uw)) * U0 + (c.Buy * (Un - Us)) * Vadv) + (c.Buz * (Up - Um)) * Wadv;
@@ -261,7 +272,7 @@ __device__ __forceinline__ void faces_tile(const AdvArgs &a, int tile_x, int til
                 FUzb = FUz;
             }
             if (DO_V) {
-                const double r = -(((FVy - yf[1 * Smem::YF + ys]) + (FVx - xf[1 * Smem::XF + xw])) + (FVz - FVzb));
+                const double r = opaque_negate(((FVy - yf[1 * Smem::YF + ys]) + (FVx - xf[1 * Smem::XF + xw])) + (FVz - FVzb));
                 const double Uadv = (sUy + Uw) + LD(U, p, -1, 1, 0);
                 const double Wadv = (sWy + Wm) + LD(W, p, 0, 1, -1);
                 const double adv = ((c.Bvx * (Ve - Vw)) * Uadv + (c.Bvy * (Vn - Vs)) * V0) + (c.Bvz * (Vp - Vm)) * Wadv;
@@ -269,7 +280,7 @@ __device__ __forceinline__ void faces_tile(const AdvArgs &a, int tile_x, int til
                 FVzb = FVz;
             }
             if (DO_W) {
-                const double r = -(((FWz - FWzb) + (FWy - yf[2 * Smem::YF + ys])) + (FWx - xf[2 * Smem::XF + xw]));
+                const double r = opaque_negate(((FWz - FWzb) + (FWy - yf[2 * Smem::YF + ys])) + (FWx - xf[2 * Smem::XF + xw]));
                 const double Uadv = (sUz + Uw) + LD(U, p, -1, 0, 1);
                 const double Vadv = (sVz + Vs) + LD(V, p, 0, -1, 1);
                 const double adv = ((c.Bwx * (We - Ww)) * Uadv + (c.Bwy * (Wn - Ws)) * Vadv) + (c.Bwz * (Wp - Wm)) * W0;
@@ -278,7 +289,7 @@ __device__ __forceinline__ void faces_tile(const AdvArgs &a, int tile_x, int til
             }
 #pragma unroll
             for (int n = 0; n < NS; ++n) {
-                const double st = -(((fe[n] - xf[(3 + n) * Smem::XF + xw]) + (fn[n] - yf[(3 + n) * Smem::YF + ys])) +
+                const double st = opaque_negate(((fe[n] - xf[(3 + n) * Smem::XF + xw]) + (fn[n] - yf[(3 + n) * Smem::YF + ys])) +
                                     (ft[n] - ftb[n]));
                 if (a.st[n]) store_result(a.st[n], a.s[n], p, st, a.mode, a.dt);
                 ftb[n] = ft[n];
