@@ -161,16 +161,21 @@ void faces_spec_ns(int ns, const AdvArgs &a, fort_scope_kernel_v1 &k) {
     }
 }
 
-// Planes per slab when a step is cut into slabs to overlap host transfers with
-// the kernels (F2C_SLAB_PLANES overrides, read once per process).
-constexpr int kSlabPlanes = 12;
-int slab_planes() {
-    static const int planes = [] {
+// Levels per slab when a step is cut into slabs to overlap host transfers with
+// the kernels: about 2.5 M points a slab (measured on GB300 over plane sizes
+// from 160 x 160 to 1024 x 512: thinner slabs pay per-copy and per-launch
+// costs, thicker ones a longer pipeline fill and drain), at least 4 levels.
+// F2C_SLAB_PLANES fixes the depth instead (read once per process).
+constexpr long long kSlabPoints = 2500000;
+int slab_planes(long long nx, long long ny) {
+    static const int fixed = [] {
         const char *v = std::getenv("F2C_SLAB_PLANES");
         const int p = v ? std::atoi(v) : 0;
-        return p >= 2 ? p : kSlabPlanes;
+        return p >= 2 ? p : 0;
     }();
-    return planes;
+    if (fixed) return fixed;
+    const long long plane = std::max(1LL, nx * ny);
+    return (int)std::max(4LL, (kSlabPoints + plane - 1) / plane);
 }
 
 // Slab boundaries along z: slabs of `planes` levels between a first and a last
@@ -198,7 +203,7 @@ std::vector<int> slab_bounds(int nz, int planes) {
 // planes relative to its interior start and reads one plane either side).
 int enqueue_step_slabs(const EntryCall &call, const Geometry &g, const std::deque<Use> &roles, const AdvArgs &whole,
                        int ns) {
-    const std::vector<int> bounds = slab_bounds((int)g.n[2], slab_planes());
+    const std::vector<int> bounds = slab_bounds((int)g.n[2], slab_planes(g.n[0], g.n[1]));
     const int count = (int)bounds.size() - 1;
     std::vector<AdvArgs> args(count);
     std::vector<void *> argument_of(count);
@@ -484,7 +489,7 @@ int run(const EntryCall &call) {
     for (auto &u : uses) handles.push_back(u.handle);
     std::vector<void *> devices(handles.size(), nullptr);
     // a deep step may run as slabs, its host transfers overlapped with the kernels
-    const bool sliceable = step && g.n[2] >= 2 * slab_planes();
+    const bool sliceable = step && g.n[2] >= 2 * slab_planes(g.n[0], g.n[1]);
     int pipelined = 0;
     {
         const int s = sliceable ? fort_scope_device_reserve_slabs_v1(call.context, handles.data(), handles.size(),

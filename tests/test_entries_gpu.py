@@ -175,14 +175,16 @@ def test_budget_too_small_declines_before_any_work(cuda, capfd):
     assert capfd.readouterr().err.count("budget_warning") == 1
 
 
-@pytest.mark.parametrize("nz, path", [(16, "in place"), (48, "slabs")])
-def test_arrays_the_host_rewrites_every_step_are_streamed(resident, nz, path):
+@pytest.mark.parametrize("nx, ny, nz, path", [(96, 64, 16, "in place"), (96, 64, 48, "in place"),
+                                              (512, 512, 24, "slabs")])
+def test_arrays_the_host_rewrites_every_step_are_streamed(resident, nx, ny, nz, path):
     """Host writes the inputs and reads the outputs between every step. After two such rounds the runtime
-    either hands the kernel the mapped host arrays (a shallow step: no copies at all) or, for a step of 24
-    levels or more, cuts it into slabs of about 12 levels whose uploads, kernels and publications overlap
-    on three streams. Results stay bit-identical to the oracle either way."""
+    either hands the kernel the mapped host arrays (a step less than two slabs deep: no copies at all) or
+    cuts the step into slabs of about 2.5 M points (10 levels of 512 x 512, thin first and last slabs)
+    whose uploads, kernels and publications overlap on three streams. Results stay bit-identical to the
+    oracle either way."""
     dom, fns = resident
-    geo = wl.Geometry(96, 64, nz, halo=2)  # arrays of 1 MiB or more are pinned
+    geo = wl.Geometry(nx, ny, nz, halo=2)  # arrays of 1 MiB or more are pinned
     f = wl.advection_fields(geo, seed=8, nscalar=1)
     ins = [a.copy() for a in f.arrays()]
     outs = [np.zeros_like(a) for a in ins]
