@@ -15,7 +15,9 @@ application such as ``benchmarks/cdu/cdu.toml``:
 
 Preparation copies the sources, splices a call block into every selected
 procedure that has a template (compiler.emission), applies the edits (which
-may add residency directives), expands the directives, and writes the build.
+may add residency directives), wraps the host statements that touch arrays the
+entries keep on the device (compiler.resident.host_access), expands the
+directives, and writes the build.
 Keys of the full format that describe multi-tree applications (``inputs``,
 ``patch``, ``rewrite``, ``held``, ``domain``, ``rewrites``) are refused with a
 clear message: the procedures they serve are outside the advection path.
@@ -28,7 +30,8 @@ import tomllib
 from dataclasses import dataclass, field
 from pathlib import Path
 
-from . import directives, splice
+from .. import emission
+from . import directives, host_access, splice
 
 SUPPORTED = {"name", "sources", "program", "variants", "selection", "edit", "build", "executable", "addressable"}
 UNSUPPORTED = {"inputs", "patch", "rewrite", "held", "domain", "rewrites", "program_edit"}
@@ -149,6 +152,7 @@ def prepare(app: Application, output) -> Application:
     patterns = [p for s in app.selections for p in s.procedures]
     report = {"application": app.name, "variant": app.variant, "entries": [], "directives": []}
     nests = {s.label: 0 for s in app.selections}
+    texts, spliced_units, entry_arrays = {}, set(), {}
     for src in app.sources:
         text = src.read_text()
         (native_dir / src.name).write_text(text)
@@ -156,13 +160,24 @@ def prepare(app: Application, output) -> Application:
         for d in done:
             report["entries"].append({"procedure": d.procedure, "entry": d.entry, "module": d.module,
                                       "nests": d.nests, "file": src.name})
+            spliced_units.add(d.procedure)
+            entry = emission.entry_for(d.procedure)
+            entry_arrays[d.procedure.split("::")[-1]] = [(n, p.name.lower()) for n, p in enumerate(entry.params)
+                                                         if p.kind == "array"]
             for s in app.selections:
                 if any(splice.matches(p, d.procedure) for p in s.procedures):
                     nests[s.label] += d.nests
         for edit in app.edits:
             if edit.file == src.name:
                 spliced = apply_edit(spliced, edit)
-        expanded, records = directives.expand(spliced, origin=src.stem)
+        texts[src.name] = spliced
+    # host statements that touch arrays the entries keep on the device
+    try:
+        texts, report["host_blocks"] = host_access.wrap(texts, entry_arrays, spliced_units)
+    except host_access.HostAccessError as error:
+        raise DescriptionError(str(error)) from None
+    for src in app.sources:
+        expanded, records = directives.expand(texts[src.name], origin=src.stem)
         report["directives"] += [{"file": src.name, **r} for r in records]
         (resident_dir / src.name).write_text(expanded)
     for s in app.selections:

@@ -1,11 +1,12 @@
 """Just enough of free-form Fortran to find procedures and their executable parts.
 
 The reference locates procedures with fparser (compiler/frontend). The resident
-build here only needs, for each selected procedure, where its executable
-statements start and end, so this module scans the text: ``module`` blocks,
-``subroutine`` / ``function`` headers (with prefixes, continuation lines and
+build here only needs, for each program unit, where its executable statements
+start and end, so this module scans the text: ``module`` blocks, ``program``,
+``subroutine`` and ``function`` headers (with prefixes, continuation lines and
 matching ``end``), the specification part (declarations, ``use``,
-``implicit``), and an internal ``contains`` section.
+``implicit``), and ``contains`` sections, whose internal procedures are
+reported as procedures of their own.
 """
 
 from __future__ import annotations
@@ -19,7 +20,8 @@ _HEADER = re.compile(
     r"^\s*(?:(?:pure|elemental|impure|recursive|module|non_recursive)\s+)*"
     r"(?:(?:integer|real|logical|complex|character|double\s+precision|type\s*\([^)]*\))(?:\s*\([^)]*\))?\s+)?"
     r"(subroutine|function)\s+([A-Za-z]\w*)", re.I)
-_END_PROC = re.compile(r"^\s*end\s*(subroutine|function)?\s*([A-Za-z]\w*)?\s*(?:!.*)?$", re.I)
+_PROGRAM = re.compile(r"^\s*program\s+([A-Za-z]\w*)", re.I)
+_END_PROC = re.compile(r"^\s*end\s*(subroutine|function|program)?\s*([A-Za-z]\w*)?\s*(?:!.*)?$", re.I)
 _END_GENERIC = re.compile(r"^\s*end\s*(?:!.*)?$", re.I)
 _CONTAINS = re.compile(r"^\s*contains\s*(?:!.*)?$", re.I)
 _DECLARATION = re.compile(
@@ -32,7 +34,7 @@ _DECLARATION = re.compile(
 class Procedure:
     module: str            # lower case, "" outside a module
     name: str              # as written
-    kind: str              # "subroutine" or "function"
+    kind: str              # "subroutine", "function" or "program"
     header: int            # line index of the header
     body: int              # first line index of the executable part
     end: int               # line index of the END statement (exclusive end of the executable part)
@@ -72,8 +74,9 @@ def procedures(text: str) -> list[Procedure]:
             i += 1
             continue
         h = _HEADER.match(line)
-        if h and not line.strip().lower().startswith("end"):
-            kind, name = h.group(1).lower(), h.group(2)
+        p = _PROGRAM.match(line)
+        if (h or p) and not line.strip().lower().startswith("end"):
+            kind, name = ("program", p.group(1)) if p else (h.group(1).lower(), h.group(2))
             header = i
             while _continued(lines[i]):
                 i += 1
@@ -100,15 +103,9 @@ def procedures(text: str) -> list[Procedure]:
                         break
                     depth -= 1
                 elif _CONTAINS.match(cur) and depth == 0 and end is None:
-                    # internal procedures follow: the executable part ends here
-                    contains_at = i
-                    i += 1
-                    while i < len(lines):
-                        e = _END_PROC.match(lines[i])
-                        if e and e.group(1) and (not e.group(2) or e.group(2).lower() == name.lower()):
-                            break
-                        i += 1
-                    out.append(Procedure(module, name, kind, header, body, contains_at))
+                    # internal procedures follow: the executable part ends here, and the scan goes on
+                    # into them (the unit's own END is passed over like any other line)
+                    out.append(Procedure(module, name, kind, header, body, i))
                     end = -1
                     break
                 i += 1

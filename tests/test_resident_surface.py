@@ -76,7 +76,7 @@ def _balanced(text: str):
 
 def test_procedure_finder_locates_executable_parts():
     found = {p.qualified: p for p in fortran.procedures(SYNTHETIC)}
-    assert set(found) == {"momentumadvection::set", "momentumadvection::helper"}
+    assert set(found) == {"momentumadvection::set", "momentumadvection::helper", "momentumadvection::inner"}
     lines = SYNTHETIC.splitlines()
     s = found["momentumadvection::set"]
     assert lines[s.header].strip().startswith("subroutine set(")
@@ -85,6 +85,8 @@ def test_procedure_finder_locates_executable_parts():
     h = found["momentumadvection::helper"]
     assert lines[h.body].strip() == "r = n + 1"
     assert lines[h.end].strip() == "contains"
+    inner = found["momentumadvection::inner"]                # an internal procedure is a unit of its own
+    assert (lines[inner.body].strip(), lines[inner.end].strip()) == ("y = x", "end function inner")
 
 
 @pytest.mark.parametrize("line, call", [
@@ -280,6 +282,10 @@ def test_reference_cdu_description_prepares(tmp_path):
     assert main.index("begin_epoch") < main.index("! ---- warm-up ----")
     assert main.index("end_epoch") < main.index("call system_clock(t_end)")
     assert main.index("call resident%close()") < main.index("deallocate(U, V, W, U2)")
+    # host statements on the fields: the initialisation is handed over, the checksum observed, the
+    # deallocation released
+    assert [(b["block"], b["arrays"]) for b in report["host_blocks"]] == [
+        ("hand-over", ["u", "u2", "v", "w"]), ("observe", ["u2"]), ("release", ["u", "u2", "v", "w"])]
     kernels = (tmp_path / "resident" / "cdu.f90").read_text()
     _balanced(kernels)
     _balanced(main)
