@@ -83,6 +83,7 @@ class Unit:
     attrs: dict          # declared name -> set of attributes
     stmts: list
     host: "Unit | None" = None
+    terminals: set = field(default_factory=set)   # statements that end labelled DO loops
     calls: list = field(default_factory=list)   # (callee, [actual argument code])
 
     @property
@@ -241,17 +242,16 @@ def statements(lines: list, start: int, end: int) -> list:
 
 def _terminals(stmts: list) -> set:
     """Indices of the statements that end labelled DO loops (an END DO there closes no other construct)."""
-    return {_close_of(stmts, j) for j, s in enumerate(stmts) if s.role == "open" and s.target}
+    return {_close_of(stmts, j, set()) for j, s in enumerate(stmts) if s.role == "open" and s.target}
 
 
-def _close_of(stmts: list, k: int) -> int:
+def _close_of(stmts: list, k: int, terminals: set) -> int:
     """Index of the statement that closes the construct opened at k."""
     if stmts[k].target:
         for j in range(k + 1, len(stmts)):
             if stmts[j].label == stmts[k].target:
                 return j
         raise HostAccessError(f"line {stmts[k].first + 1}: no statement labelled {stmts[k].target}")
-    terminals = _terminals(stmts)
     depth = 0
     for j in range(k, len(stmts)):
         s = stmts[j]
@@ -329,8 +329,8 @@ def _units(files: dict) -> list:
             attrs = {}
             for st in statements(lines, proc.header + 1, proc.body):
                 _declare(st.code, attrs)
-            units.append(Unit(proc, name, lines, _dummies(lines, proc), attrs,
-                              statements(lines, proc.body, proc.end)))
+            stmts = statements(lines, proc.body, proc.end)
+            units.append(Unit(proc, name, lines, _dummies(lines, proc), attrs, stmts, terminals=_terminals(stmts)))
     # an internal procedure's host: the innermost unit whose CONTAINS section holds its header
     for u in units:
         hosts = [h for h in units if h is not u and h.file == u.file and h.proc.end < u.proc.header
@@ -746,7 +746,7 @@ def _walk(an, u, bound, labels, lo, hi, out, dom):
     while k < hi:
         st = stmts[k]
         if st.role == "open":
-            e = _close_of(stmts, k)
+            e = _close_of(stmts, k, u.terminals)
             span = stmts[k:e + 1]
             if any(an.calls_entry(x) for x in span):
                 flush()
@@ -795,7 +795,7 @@ def _enter(an, u, bound, labels, k, e, out, dom):
     """A construct inside which entries run: its own conditions first, then its bodies."""
     stmts = u.stmts
     opener = stmts[k]
-    heads = [opener] + [stmts[j] for j in _middles(stmts, k, e)]
+    heads = [opener] + [stmts[j] for j in _middles(stmts, k, e, u.terminals)]
     modes, _, _ = _touches(an, u, heads, bound)
     ind = _indent(u.lines[opener.first])
     if modes:
@@ -808,14 +808,13 @@ def _enter(an, u, bound, labels, k, e, out, dom):
         else:
             kind, before, _ = _precise(an, u, ind, modes, dom)
             out.append(Block(u.file, opener.first, opener.first, kind, sorted(modes), before + f"{ind}end block\n"))
-    cut = [k] + _middles(stmts, k, e) + [e]
+    cut = [k] + _middles(stmts, k, e, u.terminals) + [e]
     for a, b in zip(cut, cut[1:]):
         _walk(an, u, bound, labels, a + 1, b, out, dom)
 
 
-def _middles(stmts, k, e):
+def _middles(stmts, k, e, terminals):
     out, depth = [], 0
-    terminals = _terminals(stmts)
     for j in range(k, e + 1):
         s = stmts[j]
         if s.role == "open" and not s.target:

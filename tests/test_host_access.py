@@ -240,3 +240,31 @@ library = "resident"
     _balanced(resident)
     # the directives' own expansions are not wrapped again
     assert resident.count("call resident%end_epoch()") == 2     # the leave directive and the do-while block
+
+
+def test_labelled_loops_and_select_constructs():
+    """An old-style labelled DO is one construct up to its terminal statement; SELECT CASE around an entry call
+    is entered and each CASE body gets its own blocks."""
+    text = MAIN.replace("  call smooth(V)\n", """  do 30 it = 1, n
+    U(1,1,it) = 2
+30 continue
+  select case (n)
+  case (1)
+    call CDU(U2, U, V, W, 1d0, 1d0, 1d0, n, n, n)
+  case default
+    V = 0
+  end select
+  call smooth(V)
+""")
+    files, records = _wrap({"kernels.f90": KERNELS, "main.f90": text})
+    lines = text.splitlines()
+    at = {r["line"]: r for r in records}
+    loop = lines.index("  do 30 it = 1, n") + 1
+    assert at[loop]["block"] == "hand-over" and at[loop]["arrays"] == ["u"]
+    assert lines.index("  select case (n)") + 1 not in at         # the selector names no array
+    assert at[lines.index("    V = 0") + 1]["arrays"] == ["v"]    # inside CASE DEFAULT
+    out = files["main.f90"]
+    _balanced(out)
+    # the labelled terminal stays inside the block around its loop
+    wrapped = out[out.index("do 30 it = 1, n"):]
+    assert wrapped.index("30 continue") < wrapped.index("call resident%host_done")
