@@ -114,6 +114,11 @@ struct Backend {
         return *p != nullptr;
     }
     static void free(void *p, Stream) { std::free(p); }
+    // `bytes` contiguous bytes between the host array and its device copy.
+    static bool linear(void *dst, const void *src, size_t bytes, bool, const void *, Stream) {
+        std::memcpy(dst, src, bytes);
+        return true;
+    }
     static bool copy(void *dst, const void *src, const CopyPlan &plan, const Box &box, bool, Stream) {
         for_each_run(plan, box, [&](size_t off, size_t width, size_t rows, size_t pitch) {
             for (size_t r = 0; r < rows; ++r)
@@ -199,6 +204,11 @@ struct Backend {
         const size_t head = (kAlign - reinterpret_cast<uintptr_t>(host) % kAlign) % kAlign;
         if (bytes < 4 * kAlign || head == 0) return ok(cudaMemcpyAsync(d, sp, bytes, kind, s));
         return ok(cudaMemcpyAsync(d, sp, head, kind, s)) && ok(cudaMemcpyAsync(d + head, sp + head, bytes - head, kind, s));
+    }
+    static bool linear(void *dst, const void *src, size_t bytes, bool to_device, const void *host, Stream s) {
+        return contiguous(static_cast<char *>(dst), static_cast<const char *>(src), bytes,
+                          to_device ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost, static_cast<const char *>(host),
+                          s);
     }
     static bool copy(void *dst, const void *src, const CopyPlan &plan, const Box &box, bool to_device, Stream s) {
         const cudaMemcpyKind kind = to_device ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost;

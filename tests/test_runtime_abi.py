@@ -558,15 +558,15 @@ def _plane_sum_kernel(log):
     return KERNEL(run)
 
 
-def _slab_tasks(fn, devices, hx, hy, bounds):
+def _slab_tasks(fn, devices, hx, hy, bounds, nx=NX_S, ny=NY_S, reads=None):
     keep, tasks, sizes = [], [], []
     for k0, k1 in bounds:
         values = [c.c_void_p(devices[0]), c.c_void_p(devices[1]), c.c_int(k0), c.c_int(k1)]
         argv = (c.c_void_p * 4)(*[c.cast(c.pointer(v), c.c_void_p) for v in values])
         kernel = abi.Kernel(1, 0, c.cast(fn, c.c_void_p), (c.c_uint32 * 3)(1, 1, 1), (c.c_uint32 * 3)(32, 1, 1), 0,
                             argv, 4)
-        read = abi.access(read=[((0, 0, k0 - 1), (NX_S, NY_S, k1 + 1))])
-        write = abi.access(write=[((0, 0, k0), (NX_S, NY_S, k1))], overwrite=[((0, 0, k0), (NX_S, NY_S, k1))])
+        read = abi.access(read=reads(k0, k1) if reads else [((0, 0, k0 - 1), (nx, ny, k1 + 1))])
+        write = abi.access(write=[((0, 0, k0), (nx, ny, k1))], overwrite=[((0, 0, k0), (nx, ny, k1))])
         binding = (abi.Binding * 2)(abi.Binding(hx, read), abi.Binding(hy, write))
         keep += [values, argv, read, write, binding]
         tasks.append(abi.Task(kernel, binding, 2))
@@ -624,6 +624,119 @@ def test_slab_pipeline_publishes_host_round_writes(monkeypatch):
         assert lib.fort_scope_host_end(scope.handle, hx) == abi.OK
         if round_ == 1:
             assert after.uploads - before.uploads == len(bounds)
+    assert lib.fort_scope_close(scope.handle) == abi.OK
+
+
+def test_slab_uploads_end_on_host_boundaries(monkeypatch):
+    """A slab upload of 8 MiB or more runs on to the next 2 MiB boundary of the host array (where the host is
+    current), so the next slab's upload starts on one; results and the total moved are unchanged."""
+    monkeypatch.setenv("F2C_TEST_MAPPED", "1")
+    nx, ny, nz = 256, 256, 82                       # planes of 512 KiB, slabs of 20 planes
+    plane, n = nx * ny, nx * ny * nz
+    lib = _ours()
+    scope = abi.Scope(lib)
+    x, xa = _array(np.arange(n, dtype=np.float64))
+    y, ya = _array(np.zeros(n))
+    _, hx = scope.register(xa, [nx, ny, nz])
+    _, hy = scope.register(ya, [nx, ny, nz])
+    log = []
+
+    def run(args):
+        xd = _dev(c.cast(args[0], c.POINTER(c.c_void_p))[0], n)
+        yd = _dev(c.cast(args[1], c.POINTER(c.c_void_p))[0], n)
+        k0 = c.cast(args[2], c.POINTER(c.c_int))[0]
+        k1 = c.cast(args[3], c.POINTER(c.c_int))[0]
+        unfilled = np.isnan(xd)
+        log.append((k0, k1, int(unfilled.argmax()) if unfilled.any() else n))
+        xp, yp = xd.reshape(nz, plane), yd.reshape(nz, plane)
+        yp[k0:k1] = xp[k0 - 1:k1 - 1] + xp[k0:k1] + xp[k0 + 1:k1 + 1]
+
+    fn = KERNEL(run)
+    bounds = [(1, 21), (21, 41), (41, 61), (61, 81)]
+
+    def reads(k0, k1):
+        # overlapping boxes whose union is the planes read, as the entries' cross-shaped stencils give
+        return [((0, 0, k0 - 1), (nx - 1, ny, k1 + 1)), ((1, 0, k0 - 1), (nx, ny, k1 + 1)),
+                ((0, 1, k0), (nx, ny - 1, k1))]
+
+    for round_ in range(3):
+        status, devices, pipelined = _reserve_slabs(lib, scope, [hx, hy])
+        assert status == abi.OK and pipelined == (0 if round_ == 0 else 1)
+        if pipelined:
+            _dev(devices[0], n)[:] = np.nan                        # nothing of x on the device yet
+        tasks, sizes, keep = _slab_tasks(fn, devices, hx, hy, bounds, nx, ny, reads)
+        before = scope.stats()
+        assert lib.fort_scope_slab_enqueue_v1(scope.handle, 11, tasks, len(bounds), sizes) == abi.OK
+        after = scope.stats()
+        if pipelined:
+            filled = [f for _, _, f in log[-len(bounds):]]
+            for (k0, k1), f in zip(bounds[:-1], filled[:-1]):
+                assert f >= (k1 + 1) * plane                       # what the slab reads is there
+                assert (xa + 8 * f) % (2 << 20) == 0               # and the upload ended on a host boundary
+            assert filled[-1] == n
+            assert after.uploads - before.uploads == len(bounds)   # one copy a slab
+            assert after.upload_bytes - before.upload_bytes == x.nbytes
+            assert after.reconciliations == before.reconciliations  # the valid sections stay a few boxes
+        assert lib.fort_scope_observe_v1(scope.handle, (abi.U64 * 1)(hy), 1) == abi.OK
+        p = x.reshape(nz, plane)
+        assert np.array_equal(y.reshape(nz, plane)[1:81], p[0:80] + p[1:81] + p[2:82])
+        assert lib.fort_scope_host_begin(scope.handle, hx, c.byref(abi.access(flags=abi.WRITE_ALL))) == abi.OK
+        x[:] = x * 0.5 + round_
+        assert lib.fort_scope_host_end(scope.handle, hx) == abi.OK
+    assert lib.fort_scope_close(scope.handle) == abi.OK
+
+
+def test_slab_uploads_of_the_advection_step_stay_few(monkeypatch):
+    """The 512 x 512 x 128 step (halo 2) in its 14 slabs, with the read sections the advection entries declare
+    for U (interior plus one cell, cross-shaped): one upload a slab and no reconciliation. Marking the upload's
+    cross-shaped pieces valid before the whole run splintered the valid sections past their limit at slab 11,
+    and the runtime then reconciled synchronously."""
+    monkeypatch.setenv("F2C_TEST_MAPPED", "1")
+    n_in, nz, h = 512, 128, 2
+    ex, ez = n_in + 2 * h, nz + 2 * h
+    lib = _ours()
+    scope = abi.Scope(lib)
+    _, xa = _array(np.zeros(ex * ex * ez))
+    _, ya = _array(np.zeros(ex * ex * ez))
+    _, hx = scope.register(xa, [ex, ex, ez])
+    _, hy = scope.register(ya, [ex, ex, ez])
+    fn = KERNEL(lambda args: None)
+    edges = [0, 5, 14, 24, 34, 44, 54, 64, 73, 83, 93, 103, 113, 123, 128]
+    i0, i1 = h, h + n_in
+
+    def reads(k0, k1):
+        z0, z1 = k0 + h, k1 + h
+        return [((i0 - 1, i0, z0), (i1 + 1, i1, z1)), ((i0, i0 - 1, z0), (i1, i1 + 1, z1)),
+                ((i0, i0, z0 - 1), (i1, i1, z1 + 1)), ((i0 - 1, i0, z0), (i1, i1 + 1, z1)),
+                ((i0 - 1, i0, z0), (i1, i1, z1 + 1))]
+
+    keep = []
+    for round_ in range(3):
+        status, devices, pipelined = _reserve_slabs(lib, scope, [hx, hy])
+        assert status == abi.OK and pipelined == (0 if round_ == 0 else 1)
+        tasks, sizes = [], []
+        for k0, k1 in zip(edges, edges[1:]):
+            values = [c.c_void_p(devices[0]), c.c_void_p(devices[1])]
+            argv = (c.c_void_p * 2)(*[c.cast(c.pointer(v), c.c_void_p) for v in values])
+            kernel = abi.Kernel(1, 0, c.cast(fn, c.c_void_p), (c.c_uint32 * 3)(1, 1, 1), (c.c_uint32 * 3)(32, 1, 1),
+                                0, argv, 2)
+            read = abi.access(read=reads(k0, k1))
+            box = [((i0, i0, k0 + h), (i1, i1, k1 + h))]
+            write = abi.access(write=box, overwrite=box)
+            binding = (abi.Binding * 2)(abi.Binding(hx, read), abi.Binding(hy, write))
+            keep += [values, argv, read, write, binding]
+            tasks.append(abi.Task(kernel, binding, 2))
+            sizes += [8, 8]
+        before = scope.stats()
+        assert lib.fort_scope_slab_enqueue_v1(scope.handle, 11, (abi.Task * len(tasks))(*tasks), len(tasks),
+                                              (c.c_size_t * len(sizes))(*sizes)) == abi.OK
+        after = scope.stats()
+        if pipelined:
+            assert after.uploads - before.uploads == len(tasks)
+            assert after.reconciliations == before.reconciliations
+        assert lib.fort_scope_observe_v1(scope.handle, (abi.U64 * 1)(hy), 1) == abi.OK
+        assert lib.fort_scope_host_begin(scope.handle, hx, c.byref(abi.access(flags=abi.WRITE_ALL))) == abi.OK
+        assert lib.fort_scope_host_end(scope.handle, hx) == abi.OK
     assert lib.fort_scope_close(scope.handle) == abi.OK
 
 
