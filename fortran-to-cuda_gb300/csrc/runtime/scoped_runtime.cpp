@@ -971,13 +971,23 @@ void run_slabs(Context *c, std::vector<Task> &tasks, std::vector<std::vector<Bou
             Region up = needed(b, x.effects);
             up.remove(b->device_valid);
             if (up.empty()) continue;
-            Region moved = publish.count(b) ? up : widened(b, up, true);
+            Region moved = up;
             if (!publish.count(b)) {
-                // what the device does not hold yet of the widened region, as one run up to a host boundary
-                Region rest = moved;
+                // the whole planes spanning the need, less what the device holds: one run (up to a host
+                // boundary) when it moves at most a quarter more than the need; else the usual widening
+                Box planes = bounding(up);
+                for (int d = 0; d + 1 < planes.rank; ++d) {
+                    planes.lo[d] = 0;
+                    planes.hi[d] = b->extents[d];
+                }
+                Region rest;
+                rest.add(planes);
                 rest.remove(b->device_valid);
                 size_t lo, hi;
-                if (!rest.empty() && as_interval(b, rest, lo, hi)) moved = to_host_boundary(b, rest);
+                if (as_interval(b, rest, lo, hi) && (double)rest.volume() <= 1.25 * (double)up.volume())
+                    moved = to_host_boundary(b, rest);
+                else
+                    moved = widened(b, up, true);
             }
             copy_run(c, b, moved, true, c->copy_in);
             Region device = b->device_valid;
