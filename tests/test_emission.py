@@ -1,6 +1,5 @@
 """Entry emission and the exported C ABI (CPU only: no GPU call is made)."""
 
-import ctypes as c
 import re
 import subprocess
 

@@ -176,7 +176,7 @@ def test_budget_too_small_declines_before_any_work(cuda, capfd):
 
 
 @pytest.mark.parametrize("nx, ny, nz, path", [(96, 64, 16, "in place"), (96, 64, 48, "in place"),
-                                              (512, 512, 24, "slabs")])
+                                              (512, 512, 24, "slabs"), (300, 200, 90, "slabs")])
 def test_arrays_the_host_rewrites_every_step_are_streamed(resident, nx, ny, nz, path):
     """Host writes the inputs and reads the outputs between every step. After two such rounds the runtime
     either hands the kernel the mapped host arrays (a step less than two slabs deep: no copies at all) or
