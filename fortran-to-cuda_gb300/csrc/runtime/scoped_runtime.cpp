@@ -215,10 +215,8 @@ Domain *find_domain(fort_scope_domain_t handle) {
 
 Buffer *find_buffer(Context *c, fort_buffer_t handle) {
     auto it = c->domain->buffers.find(handle);
-    if (it == c->domain->buffers.end()) {
-        if (g_retired.count(handle)) raise(FORT_SCOPE_STALE, "stale buffer handle");
-        raise(FORT_SCOPE_ARGUMENT, "unknown buffer handle");
-    }
+    if (it == c->domain->buffers.end())
+        raise(FORT_SCOPE_STALE, g_retired.count(handle) ? "stale buffer handle" : "unknown or foreign buffer handle");
     return it->second.get();
 }
 
@@ -548,6 +546,7 @@ void release_mirror(Context *c, Buffer *b) {
     Backend::free(b->device, c->stream);
     b->device = nullptr;
     c->domain->device_bytes -= b->bytes;
+    c->domain->stats.allocated_bytes -= b->bytes;  // the bytes mirrors hold now; the peak keeps the maximum
     b->device_valid.clear();
 }
 
@@ -1804,6 +1803,9 @@ int fort_scope_observe_v1(fort_scope_t context, const fort_buffer_t *buffers, si
             if (b->prepared != Buffer::NONE) raise(FORT_SCOPE_STATE, "cannot observe under a prepared access");
             list.push_back(b);
         }
+        for (size_t n = 0; n < list.size(); ++n)  // all checks before any publication
+            for (size_t m = 0; m < n; ++m)
+                if (list[m] == list[n]) raise(FORT_SCOPE_ALIAS, "a buffer is named twice in one observation");
         if (list.empty()) return FORT_SCOPE_OK;
         flush(c);
         bool any = false;

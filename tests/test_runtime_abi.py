@@ -214,6 +214,99 @@ def test_unregister_publishes_device_values(both):
     assert both.fort_scope_close(scope.handle) == abi.OK
 
 
+def test_observation_publishes_each_array_once_in_one_wait(both):
+    """Observing three arrays whose middle a device task defined: one wait, one download each, and the
+    undefined ends stay undefined on the host (reference: test_scoped_graph_replay.py:83-104)."""
+    scope = abi.Scope(both)
+    middle = [((2,), (6,))]
+    arrays = []
+    for n in range(1, 4):
+        host, address = _array(np.arange(8, dtype=np.float64))
+        status, h = scope.register(address, [8], identity=n, initialized=False)
+        assert status == abi.OK
+        status, dev = _device_begin(scope, h, abi.access(write=middle, overwrite=middle))
+        assert status == abi.OK
+        _dev(dev, 8)[2:6] = [100.0 * n + i for i in range(2, 6)]
+        assert both.fort_scope_device_end(scope.handle, h) == abi.OK
+        arrays.append((host, h))
+    before = scope.stats()
+    assert both.fort_scope_observe_v1(scope.handle, (abi.U64 * 3)(*[h for _, h in arrays]), 3) == abi.OK
+    after = scope.stats()
+    assert (after.waits, after.downloads) == (before.waits + 1, before.downloads + 3)
+    for n, (host, h) in enumerate(arrays, 1):
+        assert host.tolist() == [0, 1, *[100.0 * n + i for i in range(2, 6)], 6, 7]
+        assert both.fort_scope_host_begin(scope.handle, h, c.byref(abi.access(flags=abi.READ_ALL))) == \
+            abi.UNINITIALIZED
+    assert both.fort_scope_close(scope.handle) == abi.OK
+
+
+def test_an_invalid_observation_publishes_nothing(both):
+    """A batch naming an unknown handle, or one handle twice, is refused before any array is published
+    (reference: test_scoped_graph_replay.py:108-123)."""
+    scope = abi.Scope(both)
+    host, address = _array(np.arange(8, dtype=np.float64))
+    _, h = scope.register(address, [8])
+    status, dev = _device_begin(scope, h, abi.access(flags=abi.READ_ALL | abi.WRITE_ALL))
+    assert status == abi.OK
+    _dev(dev, 8)[0] = 1000.0
+    assert both.fort_scope_device_end(scope.handle, h) == abi.OK
+    before = bytes(scope.stats())
+    for other, status in ((2**63, abi.STALE), (h, abi.ALIAS)):
+        assert both.fort_scope_observe_v1(scope.handle, (abi.U64 * 2)(h, other), 2) == status
+        assert bytes(scope.stats()) == before and host[0] == 0.0
+    assert both.fort_scope_observe_v1(scope.handle, (abi.U64 * 1)(h), 1) == abi.OK
+    assert host[0] == 1000.0
+    assert both.fort_scope_close(scope.handle) == abi.OK
+
+
+def test_discard_and_retire_publish_no_dead_values(both):
+    """Discard drops the device's values without a transfer (the host may not read them any more); retire
+    frees the storage without publishing and the handle goes stale (reference:
+    test_scoped_graph_replay.py:127-150)."""
+    scope = abi.Scope(both)
+    host, address = _array(np.arange(8, dtype=np.float64))
+    _, h = scope.register(address, [8])
+    status, dev = _device_begin(scope, h, abi.access(flags=abi.READ_ALL | abi.WRITE_ALL))
+    assert status == abi.OK
+    _dev(dev, 8)[0] = 1000.0
+    assert both.fort_scope_device_end(scope.handle, h) == abi.OK
+    before = scope.stats()
+    assert both.fort_scope_discard_v1(scope.handle, h) == abi.OK
+    after = scope.stats()
+    assert (after.downloads, after.waits) == (before.downloads, before.waits)
+    assert both.fort_scope_host_begin(scope.handle, h, c.byref(abi.access(flags=abi.READ_ALL))) == abi.UNINITIALIZED
+    status, dev = _device_begin(scope, h, abi.access(flags=abi.WRITE_ALL | abi.OVERWRITE_ALL))
+    assert status == abi.OK
+    _dev(dev, 8)[:] = 2000.0 + np.arange(8)
+    assert both.fort_scope_device_end(scope.handle, h) == abi.OK
+    assert scope.stats().allocations == 1                    # the discarded storage was reused
+    assert both.fort_scope_retire_v1(scope.handle, h) == abi.OK
+    final = scope.stats()
+    assert (final.downloads, final.allocated_bytes) == (0, 0)
+    assert host.tolist() == list(range(8))
+    assert both.fort_scope_host_begin(scope.handle, h, c.byref(abi.access(flags=abi.READ_ALL))) == abi.STALE
+    assert both.fort_scope_close(scope.handle) == abi.OK
+
+
+def test_retire_and_discard_refuse_an_open_access(both):
+    """Neither drops an array a device access still holds; an empty observation waits for nothing, a retirement
+    for the array's work (reference: test_scoped_graph_replay.py:154-168)."""
+    scope = abi.Scope(both)
+    host, address = _array(np.arange(8, dtype=np.float64))
+    _, h = scope.register(address, [8])
+    status, _ = _device_begin(scope, h, abi.access(flags=abi.READ_ALL))
+    assert status == abi.OK
+    assert both.fort_scope_discard_v1(scope.handle, h) == abi.STATE
+    assert both.fort_scope_retire_v1(scope.handle, h) == abi.STATE
+    assert both.fort_scope_device_end(scope.handle, h) == abi.OK
+    waits = scope.stats().waits
+    assert both.fort_scope_observe_v1(scope.handle, None, 0) == abi.OK
+    assert scope.stats().waits == waits
+    assert both.fort_scope_retire_v1(scope.handle, h) == abi.OK
+    assert scope.stats().waits == waits + 1
+    assert both.fort_scope_close(scope.handle) == abi.OK
+
+
 def test_budget_eviction_publishes_dirty_values(both):
     scope = abi.Scope(both)
     a, pa = _array(np.zeros(128))
