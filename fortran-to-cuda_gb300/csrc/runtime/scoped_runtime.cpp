@@ -1512,7 +1512,8 @@ static int register_impl(fort_scope_t context, uint64_t identity, uint64_t gener
                         b->host == layout->host;
             for (int r = 0; same && r < b->rank; ++r) same = b->extents[r] == layout->extents[r];
             if (!same) raise(FORT_SCOPE_ALIAS, "identity already registered with another layout");
-            b->generation = generation;
+            if (b->generation != generation)
+                raise(FORT_SCOPE_STALE, "allocation generation changed: unregister before changing storage");
             for (int r = 0; r < b->rank; ++r) b->lower[r] = layout->lower_bounds[r];
             *out = b->handle;
             return FORT_SCOPE_OK;

@@ -307,6 +307,70 @@ def test_retire_and_discard_refuse_an_open_access(both):
     assert both.fort_scope_close(scope.handle) == abi.OK
 
 
+def _domain(lib, device=0):
+    handle = abi.U64()
+    assert lib.fort_scope_domain_create_v1(device, c.byref(handle)) == abi.OK
+    return handle.value
+
+
+def test_domain_ordinal_is_metadata_and_stale_after_close(both):
+    """The device ordinal of a domain is a query that allocates nothing; after close the handle is stale
+    (reference: test_scoped_domains.py:188-195)."""
+    domain = _domain(both, 3)
+    ordinal = c.c_int(-1)
+    assert both.fort_scope_domain_device_get_v1(domain, c.byref(ordinal)) == abi.OK and ordinal.value == 3
+    stats = abi.Stats()
+    assert both.fort_scope_domain_stats_get_v1(domain, c.byref(stats)) == abi.OK
+    assert bytes(stats) == bytes(abi.Stats())
+    assert both.fort_scope_domain_close_v1(domain) == abi.OK
+    assert both.fort_scope_domain_device_get_v1(domain, c.byref(ordinal)) == abi.STALE
+
+
+def test_retired_storage_never_lends_its_handle_or_definition(both):
+    """After retirement a new registration of the same host array gets a new handle, the old one is stale, and a
+    later context of the same domain finds the new storage (with its definition) and refuses an older allocation
+    generation (reference: test_scoped_domains.py:198-219)."""
+    domain = _domain(both)
+    host, address = _array([1.0, 2.0, 3.0, 4.0])
+    scope = abi.Scope(both, domain=domain)
+    status, old = scope.register(address, [4])
+    assert status == abi.OK
+    assert both.fort_scope_retire_v1(scope.handle, old) == abi.OK
+    status, new = scope.register(address, [4], generation=2, initialized=False)
+    assert status == abi.OK and new != old
+    out = c.c_void_p()
+    read = abi.access(flags=abi.READ_ALL)
+    assert both.fort_scope_device_begin(scope.handle, old, c.byref(read), c.byref(out)) == abi.STALE
+    assert both.fort_scope_device_begin(scope.handle, new, c.byref(read), c.byref(out)) == abi.UNINITIALIZED
+    assert both.fort_scope_close(scope.handle) == abi.OK
+    again = abi.Scope(both, domain=domain)
+    assert again.register(address, [4], generation=1)[0] == abi.STALE
+    status, same = again.register(address, [4], generation=2, initialized=True)
+    assert status == abi.OK and same == new
+    assert both.fort_scope_device_begin(again.handle, same, c.byref(read), c.byref(out)) == abi.UNINITIALIZED
+    assert both.fort_scope_close(again.handle) == abi.OK
+    assert both.fort_scope_domain_close_v1(domain) == abi.OK
+
+
+def test_contexts_never_adopt_foreign_handles(both):
+    """The same host array registered in another domain, or in a private context, gets its own handle, and
+    neither context accepts the other's (reference: test_scoped_domains.py:297-316)."""
+    first, second = _domain(both), _domain(both)
+    owner, foreign, private = abi.Scope(both, domain=first), abi.Scope(both, domain=second), abi.Scope(both)
+    host, address = _array([7.0, 9.0])
+    status, owned = owner.register(address, [2])
+    assert status == abi.OK
+    read = abi.access(flags=abi.READ_ALL)
+    for scope in (foreign, private):
+        status, handle = scope.register(address, [2])
+        assert status == abi.OK and handle != owned
+        assert both.fort_scope_host_begin(scope.handle, owned, c.byref(read)) == abi.STALE
+        assert both.fort_scope_host_begin(owner.handle, handle, c.byref(read)) == abi.STALE
+    for scope in (owner, foreign, private):
+        assert both.fort_scope_close(scope.handle) == abi.OK
+    assert both.fort_scope_domain_close_v1(first) == abi.OK and both.fort_scope_domain_close_v1(second) == abi.OK
+
+
 def test_budget_eviction_publishes_dirty_values(both):
     scope = abi.Scope(both)
     a, pa = _array(np.zeros(128))
