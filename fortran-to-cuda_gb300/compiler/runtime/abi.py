@@ -57,6 +57,12 @@ class GraphStats(c.Structure):
                            "logical_kernels", "live_graphs", "destructions")]
 
 
+class CompletionStats(c.Structure):
+    _fields_ = [("version", c.c_uint32), ("reserved", c.c_uint32)] + [
+        (n, U64) for n in ("event_records", "event_queries", "event_waits", "stream_waits", "created_events",
+                           "reused_events", "independent_host_tasks")]
+
+
 class QueueStats(c.Structure):
     _fields_ = [("version", c.c_uint32), ("queue_enabled", c.c_uint32), ("graphs_enabled", c.c_uint32),
                 ("reserved", c.c_uint32)] + [
@@ -166,6 +172,7 @@ SIGNATURES = {
     "graph_queue_cancel_v1": ([U64], c.c_int),
     "graph_queue_stats_get_v1": ([U64, P(QueueStats)], c.c_int),
     "graph_stats_get_v1": ([U64, P(GraphStats)], c.c_int),
+    "completion_stats_get_v1": ([U64, P(CompletionStats)], c.c_int),
     "graph_execute_v1": ([U64, U64, P(Task), SIZE], c.c_int),
     "device_reserve_slabs_v1": ([U64, P(U64), SIZE, P(c.c_void_p), P(c.c_int)], c.c_int),
     "slab_enqueue_v1": ([U64, U64, P(Task), SIZE, P(SIZE)], c.c_int),

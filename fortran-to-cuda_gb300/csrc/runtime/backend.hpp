@@ -128,6 +128,18 @@ struct Backend {
         return true;
     }
     static bool sync(Stream) { return !std::getenv("F2C_TEST_FAIL_WAIT"); }
+    // Completion events. Work here is synchronous, but an event reads as pending
+    // until it is waited for, so that the runtime's bookkeeping of what is still
+    // in flight is exercised as on a device.
+    using Event = int;
+    static bool make_event(Event *e) {
+        *e = 1;
+        return true;
+    }
+    static void destroy_event(Event) {}
+    static bool record(Event, Stream) { return true; }
+    static bool query(Event) { return false; }
+    static bool wait_event(Event) { return !std::getenv("F2C_TEST_FAIL_WAIT"); }
     // Host arrays are never pinned here, unless a test asks for the mapped
     // case (F2C_TEST_MAPPED): then the "device-usable" address is the array.
     static bool pin(void *p, size_t, void **mapped) {
@@ -240,6 +252,21 @@ struct Backend {
         return good;
     }
     static bool sync(Stream s) { return ok(cudaStreamSynchronize(s)); }
+    using Event = cudaEvent_t;
+    static bool make_event(Event *e) { return ok(cudaEventCreateWithFlags(e, cudaEventDisableTiming)); }
+    static void destroy_event(Event e) {
+        if (e) cudaEventDestroy(e);
+    }
+    static bool record(Event e, Stream s) { return ok(cudaEventRecord(e, s)); }
+    // Complete or not; a failure of the work shows at the wait. "Not ready" is an
+    // answer, not an error: should it be left as the last error, it is cleared so
+    // that no later launch check reads it.
+    static bool query(Event e) {
+        const cudaError_t r = cudaEventQuery(e);
+        if (r == cudaErrorNotReady && cudaPeekAtLastError() == cudaErrorNotReady) (void)cudaGetLastError();
+        return r == cudaSuccess;
+    }
+    static bool wait_event(Event e) { return ok(cudaEventSynchronize(e)); }
     // `waiter` runs its later work after everything queued so far on `signaller`.
     static bool join(Stream waiter, Stream signaller) {
         cudaEvent_t e;

@@ -33,6 +33,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <deque>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -99,6 +100,12 @@ struct Buffer {
     Region prep_writes, prep_overwrites;
     uint64_t last_use = 0;
     int queued = 0; // accepted tasks not yet submitted that use this buffer
+    // Host sections that device-side work still in flight reads (uploads, kernels
+    // on the mapped array) or writes (publications, kernels on the mapped array),
+    // and the completion token recorded after that work (0: none).
+    Region host_reading, host_writing;
+    uint64_t host_token = 0;
+    bool awaits_token = false;  // queued in-place work: its token is recorded when it is submitted
 
     Box full() const { return whole(rank, extents); }
     CopyPlan plan() const {
@@ -163,6 +170,16 @@ struct Context {
     fort_scope_graph_stats_v1 graph_stats{};
     fort_scope_graph_queue_stats_v1 queue_stats{};
     fort_scope_completion_stats_v1 completion{};
+    // completion tokens: events recorded on the context stream, oldest first
+    struct Token {
+        uint64_t serial;
+        Backend::Event event;
+    };
+    std::deque<Token> tokens;
+    std::vector<Backend::Event> spare_events;
+    uint64_t token_serial = 0, complete_serial = 0;
+    std::vector<uint64_t> awaiting_token;  // handles of arrays with in-place work not yet submitted
+    bool untracked = false;                // device work whose host accesses no token records
     char trace[6][65] = {};
     // scratch arena
     void *scratch = nullptr;
@@ -473,6 +490,83 @@ void wait_stream(Context *c) {
     c->domain->stats.waits++;
     c->completion.stream_waits++;
     if (!Backend::sync(c->stream)) poison(c, std::string("device work failed: ") + Backend::last_error());
+    c->complete_serial = c->token_serial;
+    for (auto &t : c->tokens) c->spare_events.push_back(t.event);
+    c->tokens.clear();
+    c->untracked = false;
+}
+
+// ---- completion tokens ----------------------------------------------------------------------
+// A token is an event recorded on the context stream after work that reads or
+// writes host memory. Host accesses wait on the token of the arrays they touch,
+// and only where they overlap what that work reads or writes, instead of on the
+// whole stream.
+
+uint64_t record_token(Context *c) {
+    ensure_stream(c);
+    Backend::Event e;
+    if (!c->spare_events.empty()) {
+        e = c->spare_events.back();
+        c->spare_events.pop_back();
+        c->completion.reused_events++;
+    } else {
+        if (!Backend::make_event(&e)) poison(c, std::string("event creation failed: ") + Backend::last_error());
+        c->completion.created_events++;
+    }
+    if (!Backend::record(e, c->stream)) poison(c, std::string("event record failed: ") + Backend::last_error());
+    c->completion.event_records++;
+    c->tokens.push_back({++c->token_serial, e});
+    return c->token_serial;
+}
+
+bool token_done(Context *c, uint64_t serial) {
+    while (serial > c->complete_serial && !c->tokens.empty() && c->tokens.front().serial <= serial) {
+        c->completion.event_queries++;
+        if (!Backend::query(c->tokens.front().event)) return false;
+        c->complete_serial = c->tokens.front().serial;
+        c->spare_events.push_back(c->tokens.front().event);
+        c->tokens.pop_front();
+    }
+    return serial <= c->complete_serial;
+}
+
+void wait_token(Context *c, uint64_t serial) {
+    c->domain->stats.waits++;
+    c->completion.event_waits++;
+    for (auto &t : c->tokens)
+        if (t.serial == serial && !Backend::wait_event(t.event))
+            poison(c, std::string("device work failed: ") + Backend::last_error());
+    while (!c->tokens.empty() && c->tokens.front().serial <= serial) {
+        c->spare_events.push_back(c->tokens.front().event);
+        c->tokens.pop_front();
+    }
+    if (serial > c->complete_serial) c->complete_serial = serial;
+}
+
+// Record that work up to `serial` reads / writes these host sections of `b`.
+void hold_host(Buffer *b, const Region &reading, const Region &writing, uint64_t serial) {
+    b->host_reading.add(reading);
+    b->host_writing.add(writing);
+    b->host_token = serial;
+    if (!b->host_reading.fits() || !b->host_writing.fits()) {  // keep the bookkeeping small: the whole array
+        b->host_reading.clear();
+        b->host_reading.add(b->full());
+        b->host_writing.clear();
+        b->host_writing.add(b->full());
+    }
+}
+
+void free_host(Buffer *b) {
+    b->host_reading.clear();
+    b->host_writing.clear();
+    b->host_token = 0;
+}
+
+void release_events(Context *c) {
+    for (auto &t : c->tokens) Backend::destroy_event(t.event);
+    for (auto e : c->spare_events) Backend::destroy_event(e);
+    c->tokens.clear();
+    c->spare_events.clear();
 }
 
 Box bounding(const Region &r) {
@@ -754,6 +848,19 @@ void flush(Context *c) {
     c->queue_stats.pending_tasks = 0;
     trace_line(c, "flush", 0, tasks.size());
     submit(c, tasks, key);
+    if (!c->awaiting_token.empty()) {  // kernels on mapped host arrays read and write them in place
+        const uint64_t token = record_token(c);
+        for (uint64_t h : c->awaiting_token) {
+            auto it = c->domain->buffers.find(h);
+            if (it == c->domain->buffers.end()) continue;
+            Buffer *b = it->second.get();
+            Region whole;
+            whole.add(b->full());
+            hold_host(b, whole, whole, token);
+            b->awaits_token = false;
+        }
+        c->awaiting_token.clear();
+    }
 }
 
 // Validate and apply the effects of one device task transactionally: nothing is
@@ -779,6 +886,7 @@ std::vector<Bound> bind_all(Context *c, const fort_scope_plan_binding *bindings,
 }
 
 void device_acquire(Context *c, std::vector<Bound> &bound) {
+    std::vector<std::pair<Buffer *, Region>> uploads;
     for (auto &x : bound) {
         Buffer *b = x.buffer;
         Region up = needed(b, x.effects);
@@ -790,8 +898,12 @@ void device_acquire(Context *c, std::vector<Bound> &bound) {
             device.add(up);
             device.add(b->host_valid.clip(moved));
             settle(c, b, b->defined, b->host_valid, device);
+            uploads.emplace_back(b, moved);
         }
     }
+    if (uploads.empty()) return;
+    const uint64_t token = record_token(c);  // one token for the whole batch
+    for (auto &u : uploads) hold_host(u.first, u.second, Region{}, token);
 }
 
 void device_commit(Context *c, Buffer *b, const Region &writes, const Region &overwrites) {
@@ -803,10 +915,20 @@ void device_commit(Context *c, Buffer *b, const Region &writes, const Region &ov
     b->last_use = ++c->domain->tick;
 }
 
+// A host access orders after the work it conflicts with and nothing else:
+// queued tasks on its arrays are submitted first (they may write what it
+// reads); values it reads that only the device holds are downloaded and waited
+// for; otherwise it waits on an array's completion token only where it writes
+// what in-flight work reads from the host copy, or touches what in-flight work
+// writes into it. Work without tokens (kernels launched without bindings) is
+// waited for as a whole.
 void host_acquire(Context *c, std::vector<Bound> &bound) {
-    // A host access orders after every queued task (they may write what it
-    // reads) and after in-flight uploads (they read the host copy).
-    flush(c);
+    for (auto &x : bound)
+        if (x.buffer->queued || x.buffer->awaits_token) {
+            flush(c);
+            break;
+        }
+    bool downloaded = false;
     for (auto &x : bound) {
         Region down = needed(x.buffer, x.effects);
         down.remove(x.buffer->host_valid);
@@ -818,9 +940,33 @@ void host_acquire(Context *c, std::vector<Bound> &bound) {
             host.add(down);
             host.add(x.buffer->device_valid.clip(moved));
             settle(c, x.buffer, x.buffer->defined, host, x.buffer->device_valid);
+            downloaded = true;
         }
     }
-    wait_stream(c);
+    if (downloaded || c->untracked) {
+        wait_stream(c);
+        for (auto &x : bound) free_host(x.buffer);
+        return;
+    }
+    bool waited = false;
+    for (auto &x : bound) {
+        Buffer *b = x.buffer;
+        if (!b->host_token) continue;
+        if (token_done(c, b->host_token)) {
+            free_host(b);
+            continue;
+        }
+        Region touched = needed(b, x.effects);
+        touched.add(x.effects.writes);
+        bool conflict = !b->host_writing.clip(touched).empty();
+        for (const Box &w : x.effects.writes.boxes) conflict = conflict || b->host_reading.intersects(w);
+        if (conflict) {
+            wait_token(c, b->host_token);
+            free_host(b);
+            waited = true;
+        }
+    }
+    if (!waited) c->completion.independent_host_tasks++;
 }
 
 void host_commit(Context *c, Buffer *b, const Region &writes, const Region &overwrites) {
@@ -901,6 +1047,10 @@ void accept(Context *c, Task &&task, std::vector<Bound> &bound) {
     for (auto &x : in_place) {
         host_commit(c, x.buffer, x.effects.writes, x.effects.overwrites);
         trace_line(c, "in_place", x.buffer->handle, x.buffer->bytes);
+        if (!x.buffer->awaits_token) {
+            x.buffer->awaits_token = true;
+            c->awaiting_token.push_back(x.buffer->handle);
+        }
     }
     for (auto &x : bound) {
         note_device_use(x.buffer);
@@ -962,7 +1112,7 @@ void run_slabs(Context *c, std::vector<Task> &tasks, std::vector<std::vector<Bou
     };
     join(c->copy_in, c->stream);
     join(c->copy_out, c->stream);
-    std::map<Buffer *, Region> publishing;
+    std::map<Buffer *, Region> publishing, uploading;
     for (size_t n = 0; n < tasks.size(); ++n) {
         bool uploaded = false;
         for (auto &x : bound[n]) {
@@ -989,6 +1139,7 @@ void run_slabs(Context *c, std::vector<Task> &tasks, std::vector<std::vector<Bou
                     moved = widened(b, up, true);
             }
             copy_run(c, b, moved, true, c->copy_in);
+            uploading[b].add(moved);
             Region device = b->device_valid;
             Region unheld = moved;
             unheld.remove(b->host_valid);
@@ -1032,6 +1183,15 @@ void run_slabs(Context *c, std::vector<Task> &tasks, std::vector<std::vector<Bou
     }
     join(c->stream, c->copy_in);
     join(c->stream, c->copy_out);
+    if (!uploading.empty() || !publishing.empty()) {
+        const uint64_t token = record_token(c);
+        for (Buffer *b : all) {
+            auto up = uploading.find(b), down = publishing.find(b);
+            if (up != uploading.end() || down != publishing.end())
+                hold_host(b, up != uploading.end() ? up->second : Region{},
+                          down != publishing.end() ? down->second : Region{}, token);
+        }
+    }
     for (Buffer *b : all) note_device_use(b);
     Domain *d = c->domain;
     d->stats.launches += tasks.size();
@@ -1102,6 +1262,7 @@ void detach(Context *c) {
         Backend::sync(c->stream);
         for (auto &kv : c->graphs)
             if (kv.second.graph) Backend::graph_destroy(kv.second.graph);
+        release_events(c);
         Backend::destroy_stream(c->stream);
     }
     if (c->domain->borrower == c) c->domain->borrower = nullptr;
@@ -2140,6 +2301,7 @@ int fort_scope_graph_submit_v1(fort_scope_t context, uint64_t group_key, const f
         flush(c);
         // arguments are borrowed for this call only: launch them from caller storage
         ensure_stream(c);
+        c->untracked = true;  // kernels without bindings: host accesses wait for the stream
         c->domain->stats.launches += count;
         c->graph_stats.submissions++;
         c->graph_stats.logical_kernels += count;
@@ -2219,6 +2381,7 @@ int fort_scope_graph_execute_v1(fort_scope_t context, uint64_t group_key, const 
             device.add(b->host_valid.clip(moved));
             settle(c, b, b->defined, b->host_valid, device);
         }
+        c->untracked = true;  // host accesses after a checked group wait for the stream
         for (const LaunchSpec &k : list) {
             trace_line(c, "launch", 0, 0);
             if (!Backend::launch(k, c->stream)) poison(c, std::string("kernel launch failed: ") + Backend::last_error());

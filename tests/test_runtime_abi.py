@@ -371,6 +371,110 @@ def test_contexts_never_adopt_foreign_handles(both):
     assert both.fort_scope_domain_close_v1(first) == abi.OK and both.fort_scope_domain_close_v1(second) == abi.OK
 
 
+def _completion(scope):
+    out = abi.CompletionStats()
+    assert scope.lib.fort_scope_completion_stats_get_v1(scope.handle, c.byref(out)) == abi.OK
+    assert out.version == 1
+    return out
+
+
+def test_host_access_to_an_untouched_array_waits_for_nothing(both):
+    """Device work on one array does not make host work on another wait (reference:
+    test_scoped_host_completion.py:40-54)."""
+    scope = abi.Scope(both)
+    _, a = _array(np.arange(8, dtype=np.float64))
+    host, b = _array(np.arange(8, dtype=np.float64))
+    _, on_device = scope.register(a, [8], identity=1)
+    _, on_host = scope.register(b, [8], identity=2)
+    status, dev = _device_begin(scope, on_device, abi.access(flags=abi.WRITE_ALL | abi.OVERWRITE_ALL))
+    assert status == abi.OK
+    _dev(dev, 8)[0] = 100.0
+    assert both.fort_scope_device_end(scope.handle, on_device) == abi.OK
+    waits = scope.stats().waits
+    assert both.fort_scope_host_begin(scope.handle, on_host, c.byref(abi.access(flags=abi.READ_ALL | abi.WRITE_ALL))) \
+        == abi.OK
+    host[0] = 999.0
+    assert both.fort_scope_host_end(scope.handle, on_host) == abi.OK
+    assert scope.stats().waits == waits
+    assert _completion(scope).independent_host_tasks == 1
+    assert both.fort_scope_close(scope.handle) == abi.OK
+
+
+def test_an_upload_in_flight_fences_only_overlapping_host_writes(both):
+    """While an upload reads part of the host copy, host reads and writes elsewhere go ahead; a write over it
+    waits on its event. A cancelled write leaves the device copy valid (reference:
+    test_scoped_host_completion.py:57-85)."""
+    scope = abi.Scope(both)
+    host, address = _array(np.arange(8, dtype=np.float64))
+    _, h = scope.register(address, [8], identity=1)
+    middle = [((2,), (6,))]
+    status, _ = _device_begin(scope, h, abi.access(read=middle))
+    assert status == abi.OK
+    assert both.fort_scope_device_end(scope.handle, h) == abi.OK
+    waits = scope.stats().waits
+    assert both.fort_scope_host_begin(scope.handle, h, c.byref(abi.access(flags=abi.READ_ALL))) == abi.OK
+    assert host.tolist() == list(range(8))
+    assert both.fort_scope_host_end(scope.handle, h) == abi.OK
+    first = [((0,), (2,))]
+    assert both.fort_scope_host_begin(scope.handle, h, c.byref(abi.access(write=first, overwrite=first))) == abi.OK
+    host[0], host[1] = -1.0, -2.0
+    assert both.fort_scope_host_end(scope.handle, h) == abi.OK
+    assert scope.stats().waits == waits
+    assert both.fort_scope_host_begin(scope.handle, h, c.byref(abi.access(write=middle, overwrite=middle))) == abi.OK
+    assert scope.stats().waits == waits + 1
+    assert both.fort_scope_cancel_access(scope.handle, h) == abi.OK
+    uploads = scope.stats().uploads
+    status, dev = _device_begin(scope, h, abi.access(read=middle))
+    assert status == abi.OK and _dev(dev, 8)[2:6].tolist() == [2.0, 3.0, 4.0, 5.0]
+    assert both.fort_scope_device_end(scope.handle, h) == abi.OK
+    assert scope.stats().uploads == uploads
+    assert _completion(scope).event_waits == 1
+    assert both.fort_scope_close(scope.handle) == abi.OK
+
+
+def test_one_upload_batch_shares_one_event(both):
+    """A device access over five arrays records one event for its uploads, and a host write over all five waits
+    on it once (reference: test_scoped_host_completion.py:88-104)."""
+    scope = abi.Scope(both)
+    handles, keep = [], []
+    for n in range(1, 6):
+        host, address = _array(np.arange(8, dtype=np.float64))
+        keep.append(host)
+        handles.append(scope.register(address, [8], identity=n)[1])
+    reads = [abi.access(flags=abi.READ_ALL) for _ in handles]
+    bindings = (abi.Binding * 5)(*[abi.Binding(h, r) for h, r in zip(handles, reads)])
+    pointers = (c.c_void_p * 5)()
+    assert both.fort_scope_access_begin_v1(scope.handle, bindings, 5, 1, pointers) == abi.OK
+    for h in handles:
+        assert both.fort_scope_device_end(scope.handle, h) == abi.OK
+    assert _completion(scope).event_records == 1
+    writes = [abi.access(flags=abi.WRITE_ALL | abi.OVERWRITE_ALL) for _ in handles]
+    bindings = (abi.Binding * 5)(*[abi.Binding(h, w) for h, w in zip(handles, writes)])
+    waits = scope.stats().waits
+    assert both.fort_scope_access_begin_v1(scope.handle, bindings, 5, 0, None) == abi.OK
+    assert scope.stats().waits == waits + 1 and _completion(scope).event_waits == 1
+    for h in handles:
+        assert both.fort_scope_cancel_access(scope.handle, h) == abi.OK
+    assert both.fort_scope_close(scope.handle) == abi.OK
+
+
+def test_host_only_work_records_no_events(both):
+    """Host accesses with no device work behind them need no event and no wait (reference:
+    test_scoped_host_completion.py:107-118)."""
+    scope = abi.Scope(both)
+    host, address = _array(np.arange(8, dtype=np.float64))
+    _, h = scope.register(address, [8], identity=1)
+    for _ in range(5):
+        assert both.fort_scope_host_begin(scope.handle, h, c.byref(abi.access(flags=abi.READ_ALL | abi.WRITE_ALL))) \
+            == abi.OK
+        host[0] += 1.0
+        assert both.fort_scope_host_end(scope.handle, h) == abi.OK
+    done = _completion(scope)
+    assert (done.event_records, done.created_events, done.event_waits, done.stream_waits) == (0, 0, 0, 0)
+    assert done.independent_host_tasks == 5
+    assert both.fort_scope_close(scope.handle) == abi.OK
+
+
 def test_budget_eviction_publishes_dirty_values(both):
     scope = abi.Scope(both)
     a, pa = _array(np.zeros(128))
