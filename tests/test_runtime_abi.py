@@ -475,6 +475,63 @@ def test_host_only_work_records_no_events(both):
     assert both.fort_scope_close(scope.handle) == abi.OK
 
 
+def test_a_detached_context_leaves_values_to_the_domain(both):
+    """Closing a context of a domain publishes nothing; the next context finds the same storage, downloads only
+    what the host reads and re-uploads nothing; closing the domain publishes (reference:
+    test_scoped_domains.py:130-163)."""
+    domain = _domain(both)
+    host, address = _array(np.arange(8, dtype=np.float64))
+    first = abi.Scope(both, domain=domain)
+    _, h = first.register(address, [8], lower=[-2])
+    interior = [((1,), (7,))]
+    status, dev = _device_begin(first, h, abi.access(read=interior, write=interior))
+    assert status == abi.OK
+    _dev(dev, 8)[1:7] += 100.0
+    assert both.fort_scope_device_end(first.handle, h) == abi.OK
+    assert both.fort_scope_close(first.handle) == abi.OK
+    assert host.tolist() == list(range(8))                       # not published at detach
+    stats = abi.Stats()
+    assert both.fort_scope_domain_stats_get_v1(domain, c.byref(stats)) == abi.OK and stats.download_bytes == 0
+    second = abi.Scope(both, domain=domain)
+    status, same = second.register(address, [8], lower=[-2], initialized=False)
+    assert status == abi.OK and same == h
+    assert both.fort_scope_host_begin(second.handle, same, c.byref(abi.access(read=[((3,), (4,))]))) == abi.OK
+    assert (host[3], host[2]) == (103.0, 2.0)                    # only the element read came home
+    assert both.fort_scope_host_end(second.handle, same) == abi.OK
+    status, dev = _device_begin(second, same, abi.access(read=interior))
+    assert status == abi.OK and _dev(dev, 8)[1:7].tolist() == [100.0 + i for i in range(1, 7)]
+    assert both.fort_scope_device_end(second.handle, same) == abi.OK
+    after = second.stats()
+    assert (after.upload_bytes, after.download_bytes) == (48, 8)
+    assert both.fort_scope_close(second.handle) == abi.OK
+    assert both.fort_scope_domain_close_v1(domain) == abi.OK
+    assert host.tolist() == [0.0, *[100.0 + i for i in range(1, 7)], 7.0]
+    assert both.fort_scope_wait(first.handle) == abi.STALE
+    assert both.fort_scope_create_in_domain_v1(domain, c.byref(abi.U64())) == abi.STALE
+
+
+def test_one_context_at_a_time_and_no_detach_under_an_access(both):
+    """A domain lends itself to one context at a time and cannot close while lent; a context cannot close while
+    an access is prepared; a private context has no domain to report (reference: test_scoped_domains.py:166-185)."""
+    domain = _domain(both)
+    scope = abi.Scope(both, domain=domain)
+    assert both.fort_scope_create_in_domain_v1(domain, c.byref(abi.U64())) == abi.STATE
+    assert both.fort_scope_domain_close_v1(domain) == abi.STATE
+    found = abi.U64()
+    assert both.fort_scope_domain_get_v1(scope.handle, c.byref(found)) == abi.OK and found.value == domain
+    host, address = _array([1.0, 2.0])
+    _, h = scope.register(address, [2])
+    status, _ = _device_begin(scope, h, abi.access(flags=abi.READ_ALL))
+    assert status == abi.OK
+    assert both.fort_scope_close(scope.handle) == abi.STATE
+    assert both.fort_scope_device_end(scope.handle, h) == abi.OK
+    assert both.fort_scope_close(scope.handle) == abi.OK
+    assert both.fort_scope_domain_close_v1(domain) == abi.OK
+    private = abi.Scope(both)
+    assert both.fort_scope_domain_get_v1(private.handle, c.byref(found)) == abi.OK and found.value == 0
+    assert both.fort_scope_close(private.handle) == abi.OK
+
+
 def test_budget_eviction_publishes_dirty_values(both):
     scope = abi.Scope(both)
     a, pa = _array(np.zeros(128))
