@@ -1293,6 +1293,10 @@ int guarded(F &&f) {
         return fail(e.status, e.message);
     } catch (std::bad_alloc &) {
         return fail(FORT_SCOPE_RESOURCE, "host memory exhausted");
+    } catch (std::exception &e) {  // nothing thrown crosses the C boundary
+        return fail(FORT_SCOPE_EXECUTION, std::string("unexpected exception: ") + e.what());
+    } catch (...) {
+        return fail(FORT_SCOPE_EXECUTION, "unexpected exception");
     }
 }
 
@@ -1448,6 +1452,7 @@ int fort_scope_domain_close_v1(fort_scope_domain_t domain) {
         Domain *d = find_domain(domain);
         if (d->borrower) raise(FORT_SCOPE_STATE, "domain still borrowed by a context");
         if (d->poisoned) raise(FORT_SCOPE_EXECUTION, "domain poisoned; abandon it instead");
+        if (!d->workspaces.empty()) raise(FORT_SCOPE_STATE, "provider workspace leases are still held");
         for (auto &kv : d->buffers)
             if (kv.second->prepared != Buffer::NONE) raise(FORT_SCOPE_STATE, "domain has a prepared access");
         Context *c = make_context(d, false);
@@ -1468,6 +1473,8 @@ int fort_scope_domain_abandon_v1(fort_scope_domain_t domain) {
     return guarded([&] {
         Domain *d = find_domain(domain);
         if (d->borrower) raise(FORT_SCOPE_STATE, "domain still borrowed by a context");
+        // the provider destroys what it owns and releases its leases first: the runtime cannot free its bytes
+        if (!d->workspaces.empty()) raise(FORT_SCOPE_STATE, "release the provider's workspace leases first");
         d->poisoned = false;
         Context *c = make_context(d, false);
         close_domain_through(c, false);
@@ -2466,8 +2473,13 @@ int fort_scope_external_execute_v1(fort_scope_t context, const fort_scope_extern
             views[i] = {b->handle, b->generation, b->type, (uint32_t)b->rank, b->elem, b->bytes, b->extents,
                         strides[i].data(), b->lower, b->device};
         }
-        int started = -1;
-        const int result = worker(user, views.data(), n, Backend::cpu ? nullptr : (void *)c->stream, &started);
+        int started = -1, result = FORT_SCOPE_EXECUTION;
+        try {
+            result = worker(user, views.data(), n, Backend::cpu ? nullptr : (void *)c->stream, &started);
+        } catch (...) {  // a provider that throws may have submitted work: contained, and never replayed
+            report->started = 1;
+            poison(c, "external provider threw an exception");
+        }
         report->started = started == 0 ? 0u : 1u;
         const bool known = result >= FORT_SCOPE_ARGUMENT && result <= FORT_SCOPE_STATE && result != FORT_SCOPE_EXECUTION;
         if ((started != 0 && started != 1) || (result == FORT_SCOPE_OK && started != 1) ||

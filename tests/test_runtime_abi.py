@@ -11,6 +11,7 @@ test_scoped_graph_queue.py, test_scoped_scratch.py, test_scoped_access_batch.py)
 
 import ctypes as c
 import os
+import shutil
 import subprocess
 import sys
 
@@ -1163,6 +1164,100 @@ def test_external_failure_after_start_or_without_a_report_poisons(both, started,
     # nothing is replayed: the context refuses further work
     assert both.fort_scope_host_begin(scope.handle, h, c.byref(abi.access(flags=abi.READ_ALL))) == abi.EXECUTION
     both.fort_scope_abandon(scope.handle)
+
+
+def test_an_empty_external_request_touches_nothing(both):
+    """No bindings: the worker is not called, nothing is reported as started or committed, no statistic moves
+    (reference: test_scoped_domains.py:607-623)."""
+    domain = _domain(both)
+    scope = abi.Scope(both, domain=domain)
+    calls = []
+
+    def run(user, views, count, stream, flag):
+        calls.append(count)
+        return abi.OK
+
+    worker = abi.EXTERNAL_WORKER(run)
+    call = abi.ExternalCall(1, 0, None, 0, 0, 0)
+    report = abi.ExternalReport()
+    assert both.fort_scope_external_execute_v1(scope.handle, c.byref(call), worker, None, c.byref(report)) == abi.OK
+    assert (report.status, report.started, report.committed) == (abi.OK, 0, 0) and calls == []
+    assert bytes(scope.stats()) == bytes(abi.Stats())
+    assert both.fort_scope_close(scope.handle) == abi.OK
+    stats = abi.Stats()
+    assert both.fort_scope_domain_stats_get_v1(domain, c.byref(stats)) == abi.OK
+    assert bytes(stats) == bytes(abi.Stats())
+    assert both.fort_scope_domain_close_v1(domain) == abi.OK
+
+
+def test_a_failed_domain_is_abandoned_only_after_its_provider_workspace(both):
+    """After a provider failed mid-transaction the context is abandoned; the domain refuses abandonment while the
+    provider's workspace lease is held, and accepts it once the lease is released; nothing is published
+    (reference: test_scoped_domains.py:582-604)."""
+    domain = _domain(both)
+    lease = abi.U64()
+    assert both.fort_scope_domain_workspace_reserve_v1(domain, 16, c.byref(lease)) == abi.OK
+    scope = abi.Scope(both, domain=domain)
+    host, address = _array([1.0, 2.0])
+    _, h = scope.register(address, [2])
+    binding = (abi.ExternalBinding * 1)(abi.ExternalBinding(h, abi.REAL64, 1, 8,
+                                                            abi.access(flags=abi.READ_ALL | abi.WRITE_ALL)))
+    call = abi.ExternalCall(1, 0, binding, 1, lease.value, 16)
+    report = abi.ExternalReport()
+    worker = _worker([], started=1, result=abi.EXECUTION)
+    assert both.fort_scope_external_execute_v1(scope.handle, c.byref(call), worker, None, c.byref(report)) == \
+        abi.EXECUTION
+    assert both.fort_scope_abandon(scope.handle) == abi.OK
+    assert both.fort_scope_domain_abandon_v1(domain) == abi.STATE
+    assert both.fort_scope_domain_workspace_release_v1(domain, lease.value) == abi.OK
+    assert both.fort_scope_domain_abandon_v1(domain) == abi.OK
+    assert host.tolist() == [1.0, 2.0]
+
+
+CALLBACK_THROWS = r"""
+#include <cassert>
+#include <stdexcept>
+#include "scoped_runtime.h"
+static int worker(void *, const fort_scope_external_view_v1 *, size_t, void *, int *) {
+    throw std::runtime_error("provider exception");
+}
+int main() {
+    fort_scope_domain_t domain = 0;
+    fort_scope_t context = 0;
+    fort_buffer_t buffer = 0;
+    if (fort_scope_domain_create_v1(0, &domain) || fort_scope_create_in_domain_v1(domain, &context)) return 2;
+    double host[2] = {3, 5};
+    size_t extents[1] = {2};
+    int64_t lower[1] = {-1};
+    fort_scope_layout layout{1, FORT_SCOPE_REAL64, 8, host, extents, lower, 1};
+    if (fort_scope_register(context, 1, 1, &layout, 1, &buffer)) return 3;
+    fort_scope_access access{};
+    access.flags = FORT_SCOPE_READ_ALL | FORT_SCOPE_WRITE_ALL;
+    fort_scope_external_binding_v1 binding{buffer, FORT_SCOPE_REAL64, 1, 8, access};
+    fort_scope_external_call_v1 call{1, 0, &binding, 1, 0, 0};
+    fort_scope_external_report_v1 report{};
+    if (fort_scope_external_execute_v1(context, &call, worker, nullptr, &report) != FORT_SCOPE_EXECUTION) return 4;
+    if (report.started != 1 || report.committed) return 5;
+    if (fort_scope_close(context) != FORT_SCOPE_EXECUTION) return 6;   // poisoned: no publication, no replay
+    if (fort_scope_abandon(context) || fort_scope_domain_abandon_v1(domain)) return 7;
+    return host[0] == 3 && host[1] == 5 ? 0 : 8;
+}
+"""
+
+
+def test_a_throwing_provider_is_contained(both, tmp_path):
+    """A provider callback that throws a C++ exception is caught at the C boundary: the call fails as an execution
+    error, the context is poisoned, nothing is published (reference: test_scoped_domains.py:671-706)."""
+    compiler = shutil.which("g++")
+    if compiler is None:
+        pytest.skip("no C++ compiler")
+    source, exe = tmp_path / "throws.cpp", tmp_path / "throws"
+    source.write_text(CALLBACK_THROWS)
+    built = subprocess.run([compiler, "-std=c++17", f"-I{os.path.join(ROOT, 'include')}", str(source), both._name,
+                            "-o", str(exe)], capture_output=True, text=True, timeout=120)
+    assert built.returncode == 0, built.stderr
+    run = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
+    assert run.returncode == 0, (run.returncode, run.stderr)
 
 
 def test_external_bindings_are_checked_before_the_worker_runs(both):
