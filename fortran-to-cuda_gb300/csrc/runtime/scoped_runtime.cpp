@@ -319,8 +319,8 @@ Box bounding(const Region &r);
 // The region actually moved for a needed transfer `r`: the whole array, the
 // whole planes (every dimension but the last complete) spanning `r`, or the
 // bounding box of `r`, the first of these that moves at most a quarter more
-// bytes and cannot overwrite values only the destination holds; `r` itself
-// otherwise. Fewer, larger (and, for whole planes, contiguous) copies keep the
+// bytes, holds only defined cells and cannot overwrite values only the
+// destination holds; `r` itself otherwise. Fewer, larger (and, for whole planes, contiguous) copies keep the
 // copy engines busy instead of the host.
 Region widened(const Buffer *b, const Region &r, bool to_device) {
     if (r.boxes.size() <= 1) return r;
@@ -336,6 +336,7 @@ Region widened(const Buffer *b, const Region &r, bool to_device) {
     const Box candidates[3] = {b->full(), planes, bounding(r)};
     for (const Box &cand : candidates) {
         if ((double)cand.volume() > 1.25 * (double)need) continue;
+        if (!b->defined.covers(cand)) continue;  // undefined cells are never moved
         Region clash = only_destination.clip(cand);
         clash.remove(r);
         if (!clash.empty()) continue;
@@ -457,7 +458,9 @@ Region to_host_boundary(const Buffer *b, const Region &r) {
     const Region more = interval_region(b, hi, top);
     Region stale = more;
     stale.remove(b->host_valid);
-    if (!stale.empty()) return r;
+    Region undefined = more;
+    undefined.remove(b->defined);
+    if (!stale.empty() || !undefined.empty()) return r;
     Region out = r;
     out.boxes.insert(out.boxes.end(), more.boxes.begin(), more.boxes.end());
     return out;
@@ -718,7 +721,7 @@ void reserve(Context *c, const std::vector<Buffer *> &list, bool allow_in_place)
     }
     for (Buffer *b : list) {
         b->last_use = ++d->tick;
-        if (b->in_place) continue;
+        if (b->in_place || !b->bytes) continue;  // mapped host array, or an empty one: no storage
         if (b->device) {
             d->residency.reuse_hits++;
             continue;
@@ -1022,7 +1025,7 @@ void note_device_use(Buffer *b) {
 
 void accept(Context *c, Task &&task, std::vector<Bound> &bound) {
     for (auto &x : bound)
-        if (!x.buffer->device && !x.buffer->in_place)
+        if (!x.buffer->device && !x.buffer->in_place && x.buffer->bytes)
             raise(FORT_SCOPE_STATE, "task binds an array whose device storage is not reserved");
     ensure_stream(c);
     std::vector<Bound> mirrored, in_place;
@@ -1132,8 +1135,11 @@ void run_slabs(Context *c, std::vector<Task> &tasks, std::vector<std::vector<Bou
                 Region rest;
                 rest.add(planes);
                 rest.remove(b->device_valid);
+                Region undefined = rest;
+                undefined.remove(b->defined);
                 size_t lo, hi;
-                if (as_interval(b, rest, lo, hi) && (double)rest.volume() <= 1.25 * (double)up.volume())
+                if (undefined.empty() && as_interval(b, rest, lo, hi) &&
+                    (double)rest.volume() <= 1.25 * (double)up.volume())
                     moved = to_host_boundary(b, rest);
                 else
                     moved = widened(b, up, true);
@@ -1671,8 +1677,7 @@ static int register_impl(fort_scope_t context, uint64_t identity, uint64_t gener
         }
         if (count && count > SIZE_MAX / layout->element_bytes) raise(FORT_SCOPE_ARGUMENT, "array size overflows");
         const size_t bytes = count * layout->element_bytes;
-        if (!bytes) raise(FORT_SCOPE_ARGUMENT, "empty arrays cannot be registered");
-        if (!layout->host) raise(FORT_SCOPE_ARGUMENT, "null host storage");
+        if (bytes && !layout->host) raise(FORT_SCOPE_ARGUMENT, "null host storage");
         auto existing = d->by_identity.find(identity);
         if (existing != d->by_identity.end()) {
             Buffer *b = d->buffers.at(existing->second).get();
@@ -1688,6 +1693,7 @@ static int register_impl(fort_scope_t context, uint64_t identity, uint64_t gener
         }
         const char *lo = static_cast<const char *>(layout->host);
         for (auto &kv : d->buffers) {
+            if (!bytes) break;  // an empty array occupies no host storage
             const Buffer *o = kv.second.get();
             const char *olo = static_cast<const char *>(o->host);
             if (lo < olo + o->bytes && olo < lo + bytes)
@@ -2217,7 +2223,7 @@ int fort_scope_slab_enqueue_v1(fort_scope_t context, uint64_t code_key, const fo
             offset += tasks[n].kernel.argument_count;
             bound.push_back(bind_all(c, tasks[n].bindings, tasks[n].binding_count));
             for (auto &x : bound.back())
-                if (!x.buffer->device || x.buffer->in_place)
+                if ((!x.buffer->device && x.buffer->bytes) || x.buffer->in_place)
                     raise(FORT_SCOPE_STATE, "a slab task binds an array without reserved device storage");
         }
         run_slabs(c, list, bound);
@@ -2353,7 +2359,8 @@ int fort_scope_graph_execute_v1(fort_scope_t context, uint64_t group_key, const 
                 Buffer *b = find_buffer(c, t.bindings[i].buffer);
                 if (!seen.insert(b->handle).second) raise(FORT_SCOPE_ALIAS, "a task binds one array twice");
                 if (b->prepared != Buffer::NONE) raise(FORT_SCOPE_STATE, "array already has a prepared access");
-                if (!b->device || b->in_place) raise(FORT_SCOPE_STATE, "task binds an array whose device storage is not reserved");
+                if ((!b->device && b->bytes) || b->in_place)
+                    raise(FORT_SCOPE_STATE, "task binds an array whose device storage is not reserved");
                 Effects e = effects_of(b, t.bindings[i].access);
                 auto it = sim.find(b);
                 if (it == sim.end()) it = sim.emplace(b, Sim{b->defined, b->device_valid, Region{}}).first;

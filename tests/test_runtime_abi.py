@@ -533,6 +533,96 @@ def test_one_context_at_a_time_and_no_detach_under_an_access(both):
     assert both.fort_scope_close(private.handle) == abi.OK
 
 
+def test_stencil_sections_move_exactly_their_cells(both):
+    """An array defined only on a stencil's ten shifted footprints (negative lower bounds) moves exactly those
+    cells, coalesced into three transfers each way; a read of the whole array is refused as uninitialized and moves
+    nothing (reference: test_scoped_runtime.py:228-261)."""
+    scope = abi.Scope(both)
+    shape, interior = (8, 7, 6), (5, 4, 3)
+    host, address = _array(np.arange(8 * 7 * 6, dtype=np.float64))
+    shifts = [(0, 0, 0), (-1, 0, 0), (0, 1, 0), (-1, 1, 0), (0, -1, 0), (-1, -1, 0), (0, 0, 1), (-1, 0, 1),
+              (0, 0, -1), (-1, 0, -1)]
+    boxes = [(tuple(1 + d for d in s), tuple(n + 1 + d for n, d in zip(interior, s))) for s in shifts]
+    cells = {i + 8 * (j + 7 * k) for lo, hi in boxes for k in range(lo[2], hi[2]) for j in range(lo[1], hi[1])
+             for i in range(lo[0], hi[0])}
+    status, h = scope.register(address, list(shape), lower=[-2, -5, -9], defined=boxes)
+    assert status == abi.OK
+    status, dev = _device_begin(scope, h, abi.access(read=boxes, write=boxes))
+    assert status == abi.OK
+    stats = scope.stats()
+    assert (stats.uploads, stats.upload_bytes) == (3, 8 * len(cells))
+    view = _dev(dev, 8 * 7 * 6)
+    assert all(view[o] == o for o in cells)
+    for o in cells:
+        view[o] += 1000.0
+    assert both.fort_scope_device_end(scope.handle, h) == abi.OK
+    before = bytes(scope.stats())
+    assert both.fort_scope_host_begin(scope.handle, h, c.byref(abi.access(flags=abi.READ_ALL))) == abi.UNINITIALIZED
+    assert bytes(scope.stats()) == before
+    assert both.fort_scope_host_begin(scope.handle, h, c.byref(abi.access(read=boxes))) == abi.OK
+    assert both.fort_scope_host_end(scope.handle, h) == abi.OK
+    stats = scope.stats()
+    assert (stats.downloads, stats.download_bytes) == (3, 8 * len(cells))
+    assert all(host[o] == o + 1000.0 for o in cells)
+    assert both.fort_scope_close(scope.handle) == abi.OK
+
+
+def test_a_partial_device_write_keeps_the_host_values_around_it(both):
+    """A device write that need not cover its section first brings the section's host values along, so cells it
+    skips keep them; an uninitialized array cannot be read, and a complete overwrite uploads nothing (reference:
+    test_scoped_runtime.py:264-291)."""
+    scope = abi.Scope(both)
+    host, address = _array(np.arange(8, dtype=np.float64))
+    _, h = scope.register(address, [8])
+    status, dev = _device_begin(scope, h, abi.access(write=[((2,), (6,))]))
+    assert status == abi.OK
+    _dev(dev, 8)[2], _dev(dev, 8)[4] = 102.0, 104.0
+    assert both.fort_scope_device_end(scope.handle, h) == abi.OK
+    assert both.fort_scope_host_begin(scope.handle, h, c.byref(abi.access(read=[((1,), (7,))]))) == abi.OK
+    assert host.tolist() == [0, 1, 102, 3, 104, 5, 6, 7]
+    assert both.fort_scope_host_end(scope.handle, h) == abi.OK
+    stats = scope.stats()
+    assert stats.upload_bytes == stats.download_bytes == 32
+    assert both.fort_scope_close(scope.handle) == abi.OK
+    scope = abi.Scope(both)
+    out, address = _array(np.zeros(8))
+    _, h = scope.register(address, [8], initialized=False)
+    status, _ = _device_begin(scope, h, abi.access(flags=abi.READ_ALL))
+    assert status == abi.UNINITIALIZED
+    status, dev = _device_begin(scope, h, abi.access(flags=abi.WRITE_ALL | abi.OVERWRITE_ALL))
+    assert status == abi.OK
+    _dev(dev, 8)[:] = 2.0 * np.arange(8)
+    assert both.fort_scope_device_end(scope.handle, h) == abi.OK
+    assert scope.stats().upload_bytes == 0
+    assert both.fort_scope_close(scope.handle) == abi.OK
+    assert out.tolist() == [2.0 * i for i in range(8)]
+
+
+def test_registration_aliases_generations_sizes_and_empty_arrays(both):
+    """Another identity over the same host storage is an alias; the same identity with another allocation
+    generation is stale until it is unregistered; an array whose size overflows is an argument error; an empty
+    array registers without storage and allocates nothing (reference: test_scoped_runtime.py:322-342)."""
+    scope = abi.Scope(both)
+    host, address = _array(np.arange(8, dtype=np.float64))
+    status, first = scope.register(address, [8])
+    assert status == abi.OK
+    assert scope.register(address, [8], identity=2)[0] == abi.ALIAS
+    assert scope.register(address, [8], generation=2)[0] == abi.STALE
+    assert both.fort_scope_unregister(scope.handle, first) == abi.OK
+    status, second = scope.register(address, [8], generation=2)
+    assert status == abi.OK and second != first
+    assert both.fort_scope_host_begin(scope.handle, first, c.byref(abi.access(flags=abi.READ_ALL))) == abi.STALE
+    huge = (1 << (8 * c.sizeof(abi.SIZE))) - 1
+    assert scope.register(address, [huge], identity=3)[0] == abi.ARGUMENT
+    status, empty = scope.register(None, [huge, 0], identity=3)
+    assert status == abi.OK
+    status, dev = _device_begin(scope, empty, abi.access(flags=abi.READ_ALL))
+    assert status == abi.OK and not dev
+    assert both.fort_scope_device_end(scope.handle, empty) == abi.OK
+    assert scope.stats().allocations == 0
+    assert both.fort_scope_close(scope.handle) == abi.OK
+
+
 def test_budget_eviction_publishes_dirty_values(both):
     scope = abi.Scope(both)
     a, pa = _array(np.zeros(128))
