@@ -293,6 +293,12 @@ Effects effects_of(const Buffer *b, const fort_scope_access &a) {
     if (a.flags & FORT_SCOPE_OVERWRITE_ALL) e.overwrites.add(b->full());
     else list(a.overwrite_count, a.overwrites, e.overwrites);
     e.writes.add(e.overwrites);
+    if (!e.overwrites.empty()) {
+        // the definition the access would leave must stay exact: refused here, before anything changes
+        Region defined = b->defined;
+        defined.add(e.overwrites);
+        if (!defined.fits()) raise(FORT_SCOPE_BOUNDARY, "the array's defined sections would exceed the tracked limit");
+    }
     return e;
 }
 

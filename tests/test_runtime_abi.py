@@ -623,6 +623,97 @@ def test_registration_aliases_generations_sizes_and_empty_arrays(both):
     assert both.fort_scope_close(scope.handle) == abi.OK
 
 
+def _inject(monkeypatch, what):
+    """Turn on a host-side failure in both runtimes (each reads its own switch)."""
+    monkeypatch.setenv(f"F2C_TEST_FAIL_{what}", "1")
+    monkeypatch.setenv(f"FORT_SCOPE_TEST_FAIL_{what}", "1")
+
+
+def test_definitions_past_the_section_limit_are_refused_before_the_access(both):
+    """A host write that would need a 129th defined section is refused at preparation, with nothing committed and
+    no access left open (reference: test_scoped_runtime.py:345-360)."""
+    scope = abi.Scope(both)
+    limit = 128
+    host, address = _array(np.zeros(2 * limit + 16))
+    _, h = scope.register(address, [2 * limit + 16], initialized=False)
+    for i in range(limit):
+        box = [((2 * i,), (2 * i + 1,))]
+        assert both.fort_scope_host_begin(scope.handle, h, c.byref(abi.access(write=box, overwrite=box))) == abi.OK
+        host[2 * i] = i + 10.0
+        assert both.fort_scope_host_end(scope.handle, h) == abi.OK
+    box = [((2 * limit,), (2 * limit + 1,))]
+    assert both.fort_scope_host_begin(scope.handle, h, c.byref(abi.access(write=box, overwrite=box))) == \
+        abi.BOUNDARY
+    assert both.fort_scope_close(scope.handle) == abi.OK
+    assert [host[2 * i] for i in range(limit)] == [i + 10.0 for i in range(limit)]
+
+
+def test_an_allocation_failure_keeps_earlier_work_and_the_context(both, monkeypatch):
+    """A device access that cannot allocate fails with RESOURCE before any change; earlier results stay
+    reachable and the host can carry on where the device could not (reference: test_scoped_runtime.py:363-386)."""
+    scope = abi.Scope(both)
+    host, a = _array(np.arange(8, dtype=np.float64))
+    other, b = _array(np.zeros(8))
+    _, h = scope.register(a, [8])
+    status, dev = _device_begin(scope, h, abi.access(flags=abi.READ_ALL | abi.WRITE_ALL))
+    assert status == abi.OK
+    _dev(dev, 8)[:] += 10.0
+    assert both.fort_scope_device_end(scope.handle, h) == abi.OK
+    _, unused = scope.register(b, [8], identity=2, initialized=False)
+    _inject(monkeypatch, "ALLOC")
+    status, _ = _device_begin(scope, unused, abi.access(flags=abi.WRITE_ALL | abi.OVERWRITE_ALL))
+    assert status == abi.RESOURCE
+    assert both.fort_scope_host_begin(scope.handle, h, c.byref(abi.access(flags=abi.READ_ALL))) == abi.OK
+    assert host.tolist() == [i + 10.0 for i in range(8)]
+    assert both.fort_scope_host_end(scope.handle, h) == abi.OK
+    assert both.fort_scope_host_begin(scope.handle, unused,
+                                      c.byref(abi.access(flags=abi.WRITE_ALL | abi.OVERWRITE_ALL))) == abi.OK
+    other[:] = host * 2
+    assert both.fort_scope_host_end(scope.handle, unused) == abi.OK
+    assert both.fort_scope_close(scope.handle) == abi.OK
+    assert other.tolist() == [2 * (i + 10.0) for i in range(8)]
+
+
+def test_a_failed_completion_poisons_the_context(both, monkeypatch):
+    """When waiting for device work fails, the context refuses everything after (no replay) until it is
+    abandoned (reference: test_scoped_runtime.py:389-403)."""
+    scope = abi.Scope(both)
+    host, address = _array(np.arange(8, dtype=np.float64))
+    _, h = scope.register(address, [8])
+    status, dev = _device_begin(scope, h, abi.access(flags=abi.READ_ALL | abi.WRITE_ALL))
+    assert status == abi.OK
+    _dev(dev, 8)[0] = 100.0
+    assert both.fort_scope_device_end(scope.handle, h) == abi.OK
+    _inject(monkeypatch, "WAIT")
+    assert both.fort_scope_host_begin(scope.handle, h, c.byref(abi.access(flags=abi.READ_ALL))) == abi.EXECUTION
+    assert both.fort_scope_close(scope.handle) == abi.EXECUTION
+    status, _ = _device_begin(scope, h, abi.access(flags=abi.READ_ALL))
+    assert status == abi.EXECUTION
+    assert both.fort_scope_abandon(scope.handle) == abi.OK
+    assert both.fort_scope_wait(scope.handle) == abi.STALE
+
+
+def test_contexts_on_several_threads_stay_independent(both):
+    """Twelve contexts on four threads, each doubling its own array on the device (reference:
+    test_scoped_runtime.py:406-425)."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    def run(seed):
+        scope = abi.Scope(both)
+        host, address = _array(seed + np.arange(32, dtype=np.float64))
+        _, h = scope.register(address, [32])
+        status, dev = _device_begin(scope, h, abi.access(flags=abi.READ_ALL | abi.WRITE_ALL))
+        assert status == abi.OK
+        _dev(dev, 32)[:] *= 2.0
+        assert both.fort_scope_device_end(scope.handle, h) == abi.OK
+        assert both.fort_scope_close(scope.handle) == abi.OK
+        return host.tolist()
+
+    with ThreadPoolExecutor(max_workers=4) as pool:
+        results = list(pool.map(run, range(12)))
+    assert results == [[2.0 * (seed + i) for i in range(32)] for seed in range(12)]
+
+
 def test_budget_eviction_publishes_dirty_values(both):
     scope = abi.Scope(both)
     a, pa = _array(np.zeros(128))
