@@ -96,6 +96,10 @@ struct Buffer {
     int host_rounds = 0;         // consecutive device uses, each preceded by host access
     bool in_place = false;       // the pending reservation hands out `mapped`
     Region defined, host_valid, device_valid;
+    // Cells whose values are real: every definition since the values were last
+    // discarded. Forgetting a definition makes reads illegal but keeps these,
+    // so what the device already wrote still reaches the host.
+    Region physical;
     enum { NONE, HOST, DEVICE } prepared = NONE;
     Region prep_writes, prep_overwrites;
     uint64_t last_use = 0;
@@ -332,7 +336,7 @@ Region widened(const Buffer *b, const Region &r, bool to_device) {
     if (r.boxes.size() <= 1) return r;
     Region only_destination = to_device ? b->device_valid : b->host_valid;
     only_destination.remove(to_device ? b->host_valid : b->device_valid);
-    only_destination = b->defined.clip(only_destination);
+    only_destination = b->physical.clip(only_destination);
     const size_t need = r.volume();
     Box planes = bounding(r);
     for (int d = 0; d + 1 < planes.rank; ++d) {
@@ -596,6 +600,14 @@ void flush(Context *c);
 // sets), then track each side as the whole array. A definition set that is
 // still too fragmented is widened to its bounding box.
 void settle(Context *c, Buffer *b, Region defined, Region host, Region device) {
+    Region physical = b->physical;
+    physical.add(defined);
+    if (!physical.fits()) {  // only publication reads it: a hull over-approximates harmlessly
+        const Box hull = bounding(physical);
+        physical.clear();
+        physical.add(hull);
+    }
+    b->physical = std::move(physical);
     if (defined.fits() && host.fits() && device.fits()) {
         b->defined = std::move(defined);
         b->host_valid = std::move(host);
@@ -605,10 +617,10 @@ void settle(Context *c, Buffer *b, Region defined, Region host, Region device) {
     flush(c);
     if (b->device) {
         ensure_stream(c);
-        Region down = defined.clip(device);
+        Region down = b->physical.clip(device);
         down.remove(host);
         copy_region(c, b, down, false);
-        Region up = defined.clip(host);
+        Region up = b->physical.clip(host);
         up.remove(device);
         copy_region(c, b, up, true);
         wait_stream(c);
@@ -632,7 +644,7 @@ void settle(Context *c, Buffer *b, Region defined, Region host, Region device) {
 
 void publish_buffer(Context *c, Buffer *b) {
     if (!b->device) return;
-    Region dirty = b->defined.clip(b->device_valid);
+    Region dirty = b->physical.clip(b->device_valid);
     dirty.remove(b->host_valid);
     if (dirty.empty()) return;
     ensure_stream(c);
@@ -689,7 +701,7 @@ void make_room(Context *c, size_t bytes, const std::set<uint64_t> &keep) {
             if (!victim || b->last_use < victim->last_use) victim = b;
         }
         if (!victim) raise(FORT_SCOPE_RESOURCE, "device budget exhausted by arrays in use");
-        Region dirty = victim->defined.clip(victim->device_valid);
+        Region dirty = victim->physical.clip(victim->device_valid);
         dirty.remove(victim->host_valid);
         if (!dirty.empty()) {
             d->residency.dirty_evictions++;
@@ -1179,7 +1191,7 @@ void run_slabs(Context *c, std::vector<Task> &tasks, std::vector<std::vector<Bou
         for (auto &x : bound[n]) {
             Buffer *b = x.buffer;
             if (!publish.count(b)) continue;
-            Region down = b->defined.clip(x.effects.writes);
+            Region down = b->physical.clip(x.effects.writes);
             down.remove(b->host_valid);
             if (down.empty()) continue;
             if (!ordered) {
@@ -1726,6 +1738,7 @@ static int register_impl(fort_scope_t context, uint64_t identity, uint64_t gener
                 raise(FORT_SCOPE_ARGUMENT, "initialized section list exceeds the bounded interface");
             for (size_t n = 0; n < initialized_count; ++n) b->defined.add(section_box(b.get(), initialized[n]));
         }
+        b->physical = b->defined;
         // arrays of 1 MiB or more are pinned in place (the CPU test backend pins only when a test asks)
         if (bytes >= (Backend::cpu ? size_t(0) : size_t(1) << 20) && env_flag("FORT_SCOPE_PIN_HOST", true))
             b->pinned_host = Backend::pin(b->host, bytes, &b->mapped);
@@ -1993,7 +2006,7 @@ int fort_scope_observe_v1(fort_scope_t context, const fort_buffer_t *buffers, si
         for (Buffer *b : list) {
             b->host_touched = true;
             if (!b->device) continue;
-            Region dirty = b->defined.clip(b->device_valid);
+            Region dirty = b->physical.clip(b->device_valid);
             dirty.remove(b->host_valid);
             if (!dirty.empty()) any = true;
             publish_buffer(c, b);
@@ -2022,6 +2035,7 @@ static int drop_values(fort_scope_t context, fort_buffer_t buffer, bool recycle)
         if (recycle && b->queued) return FORT_SCOPE_OK; // the new definition replaces the values
         if (b->queued) flush(c);
         b->defined.clear();
+        b->physical.clear();  // dead values: nothing of them is published
         return FORT_SCOPE_OK;
     });
 }

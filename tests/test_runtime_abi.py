@@ -714,6 +714,72 @@ def test_contexts_on_several_threads_stay_independent(both):
     assert results == [[2.0 * (seed + i) for i in range(32)] for seed in range(12)]
 
 
+def test_undefined_halos_are_never_moved_or_read(both):
+    """An array defined only in its middle uploads only the middle; a read of its undefined halo is refused, even
+    after a re-registration that claims the array initialized (reference: test_scoped_runtime.py:486-506)."""
+    scope = abi.Scope(both)
+    host, address = _array(101.0 + np.arange(8))
+    middle = [((2,), (6,))]
+    status, h = scope.register(address, [8], defined=middle, lower=[-2])
+    assert status == abi.OK
+    status, dev = _device_begin(scope, h, abi.access(read=middle, write=middle))
+    assert status == abi.OK
+    _dev(dev, 8)[2:6] += 10.0
+    assert both.fort_scope_device_end(scope.handle, h) == abi.OK
+    assert scope.stats().upload_bytes == 32
+    halo = abi.access(read=[((0,), (1,))])
+    assert both.fort_scope_host_begin(scope.handle, h, c.byref(halo)) == abi.UNINITIALIZED
+    status, again = scope.register(address, [8], lower=[-2], initialized=True)
+    assert status == abi.OK and again == h
+    assert both.fort_scope_host_begin(scope.handle, h, c.byref(halo)) == abi.UNINITIALIZED
+    assert both.fort_scope_close(scope.handle) == abi.OK
+    assert host.tolist() == [101, 102, 113, 114, 115, 116, 107, 108]
+
+
+def test_forgetting_a_definition_keeps_the_values_already_written(both):
+    """forget_definition makes reads illegal without moving anything, but what the device already wrote still
+    reaches the host at close, and the allocation is reused (reference: test_scoped_runtime.py:509-530)."""
+    scope = abi.Scope(both)
+    host, address = _array(np.arange(8, dtype=np.float64))
+    _, h = scope.register(address, [8])
+    status, dev = _device_begin(scope, h, abi.access(flags=abi.WRITE_ALL | abi.OVERWRITE_ALL))
+    assert status == abi.OK
+    _dev(dev, 8)[:] = 1000.0 + np.arange(8)
+    assert both.fort_scope_device_end(scope.handle, h) == abi.OK
+    assert both.fort_scope_forget_definition(scope.handle, h) == abi.OK
+    assert scope.stats().downloads == 0
+    assert both.fort_scope_host_begin(scope.handle, h, c.byref(abi.access(flags=abi.READ_ALL))) == abi.UNINITIALIZED
+    middle = [((2,), (6,))]
+    status, dev = _device_begin(scope, h, abi.access(write=middle, overwrite=middle))
+    assert status == abi.OK
+    _dev(dev, 8)[2:6] = 2000.0 + np.arange(2, 6)
+    assert both.fort_scope_device_end(scope.handle, h) == abi.OK
+    assert scope.stats().allocations == 1
+    assert both.fort_scope_close(scope.handle) == abi.OK
+    assert host.tolist() == [1000, 1001, 2002, 2003, 2004, 2005, 1006, 1007]
+
+
+def test_forgetting_a_definition_cannot_lose_executed_device_writes(both):
+    """After forget_definition a read is refused, nothing moves and nothing waits, yet closing publishes the
+    device's writes exactly (reference: test_scoped_runtime.py:533-557)."""
+    scope = abi.Scope(both)
+    host, address = _array(np.arange(8, dtype=np.float64))
+    _, h = scope.register(address, [8])
+    written = [((1,), (7,))]
+    status, dev = _device_begin(scope, h, abi.access(write=written, overwrite=written))
+    assert status == abi.OK
+    _dev(dev, 8)[1:7] = 3000.0 + np.arange(1, 7)
+    assert both.fort_scope_device_end(scope.handle, h) == abi.OK
+    before = scope.stats()
+    assert both.fort_scope_forget_definition(scope.handle, h) == abi.OK
+    after = scope.stats()
+    assert (after.download_bytes, after.waits) == (before.download_bytes, before.waits)
+    assert both.fort_scope_host_begin(scope.handle, h, c.byref(abi.access(read=[((3,), (4,))]))) == \
+        abi.UNINITIALIZED
+    assert both.fort_scope_close(scope.handle) == abi.OK
+    assert host.tolist() == [0, 3001, 3002, 3003, 3004, 3005, 3006, 7]
+
+
 def test_budget_eviction_publishes_dirty_values(both):
     scope = abi.Scope(both)
     a, pa = _array(np.zeros(128))
