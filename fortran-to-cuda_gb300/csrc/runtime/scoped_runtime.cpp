@@ -1572,7 +1572,12 @@ int fort_scope_domain_workspace_release_v1(fort_scope_domain_t domain, uint64_t 
 int fort_scope_set_device_budget(fort_scope_t context, size_t bytes) {
     return guarded([&] {
         Context *c = live_context(context);
-        if (bytes < c->domain->workspace_bytes) raise(FORT_SCOPE_STATE, "the device budget must cover the workspace claims");
+        Domain *d = c->domain;
+        if (c->stream_ready || d->device_bytes) {  // the device is in use: the budget is fixed
+            if (!d->budget_set || bytes != d->budget) raise(FORT_SCOPE_STATE, "cannot change a live device budget");
+            return FORT_SCOPE_OK;
+        }
+        if (bytes < d->workspace_bytes) raise(FORT_SCOPE_STATE, "the device budget must cover the workspace claims");
         c->domain->budget = bytes;
         c->domain->budget_set = true;
         return FORT_SCOPE_OK;

@@ -780,6 +780,115 @@ def test_forgetting_a_definition_cannot_lose_executed_device_writes(both):
     assert host.tolist() == [0, 3001, 3002, 3003, 3004, 3005, 3006, 7]
 
 
+@pytest.mark.parametrize("source", ["host", "device"])
+def test_reconciling_fragmented_reads_keeps_the_current_copy(both, source):
+    """129 single-cell reads fragment the current sections past the limit; the reconciliation brings the other copy
+    up to date once, so a later whole-array access moves nothing more (reference: test_scoped_runtime.py:563-601)."""
+    scope = abi.Scope(both)
+    size = 2 * 128 + 16
+    host, address = _array(np.arange(size, dtype=np.float64))
+    _, h = scope.register(address, [size])
+    if source == "device":
+        status, dev = _device_begin(scope, h, abi.access(flags=abi.WRITE_ALL | abi.OVERWRITE_ALL))
+        assert status == abi.OK
+        _dev(dev, size)[:] = np.arange(size) + 100.0
+        assert both.fort_scope_device_end(scope.handle, h) == abi.OK
+    else:
+        status, _ = _device_begin(scope, h, abi.access())  # storage without values
+        assert status == abi.OK
+        assert both.fort_scope_device_end(scope.handle, h) == abi.OK
+    for i in range(128 + 1):
+        cell = abi.access(read=[((2 * i,), (2 * i + 1,))])
+        if source == "device":
+            assert both.fort_scope_host_begin(scope.handle, h, c.byref(cell)) == abi.OK
+            assert host[2 * i] == 2 * i + 100.0
+            assert both.fort_scope_host_end(scope.handle, h) == abi.OK
+        else:
+            status, dev = _device_begin(scope, h, cell)
+            assert status == abi.OK and _dev(dev, size)[2 * i] == 2 * i
+            assert both.fort_scope_device_end(scope.handle, h) == abi.OK
+    assert scope.stats().reconciliations
+    before = scope.stats()
+    if source == "device":
+        status, dev = _device_begin(scope, h, abi.access(flags=abi.READ_ALL))
+        assert status == abi.OK and _dev(dev, size).tolist() == [i + 100.0 for i in range(size)]
+        assert both.fort_scope_device_end(scope.handle, h) == abi.OK
+        assert scope.stats().upload_bytes == before.upload_bytes
+    else:
+        assert both.fort_scope_host_begin(scope.handle, h, c.byref(abi.access(flags=abi.READ_ALL))) == abi.OK
+        assert both.fort_scope_host_end(scope.handle, h) == abi.OK
+        assert scope.stats().download_bytes == before.download_bytes
+    assert both.fort_scope_close(scope.handle) == abi.OK
+    assert both.fort_scope_wait(scope.handle) == abi.STALE
+
+
+def test_definitions_cannot_change_under_a_prepared_access(both):
+    """(reference: test_scoped_runtime.py:604-613)"""
+    scope = abi.Scope(both)
+    _, address = _array(np.arange(8, dtype=np.float64))
+    _, h = scope.register(address, [8])
+    assert both.fort_scope_host_begin(scope.handle, h, c.byref(abi.access(flags=abi.READ_ALL | abi.WRITE_ALL))) == \
+        abi.OK
+    assert both.fort_scope_forget_definition(scope.handle, h) == abi.STATE
+    assert both.fort_scope_host_end(scope.handle, h) == abi.OK
+    assert both.fort_scope_close(scope.handle) == abi.OK
+
+
+def test_initialized_sections_are_checked_before_registration(both):
+    """A section outside the array is refused; an empty list registers an array with nothing defined (reference:
+    test_scoped_runtime.py:616-625)."""
+    scope = abi.Scope(both)
+    _, address = _array(np.arange(8, dtype=np.float64))
+    assert scope.register(address, [8], defined=[((0,), (9,))])[0] == abi.ARGUMENT
+    status, h = scope.register(address, [8], defined=[])
+    assert status == abi.OK
+    assert both.fort_scope_host_begin(scope.handle, h, c.byref(abi.access(flags=abi.READ_ALL))) == abi.UNINITIALIZED
+    assert both.fort_scope_close(scope.handle) == abi.OK
+
+
+def test_a_declared_budget_evicts_and_the_host_carries_on(both):
+    """Under a budget of one array the second array's device access evicts the first, publishing its device values;
+    the budget cannot be declared again; the host finishes the work (reference: test_scoped_runtime.py:628-653)."""
+    scope = abi.Scope(both)
+    host, a = _array(np.arange(8, dtype=np.float64))
+    other, b = _array(np.zeros(8))
+    _, first = scope.register(a, [8])
+    _, second = scope.register(b, [8], identity=2, initialized=False)
+    assert both.fort_scope_set_device_budget(scope.handle, 64) == abi.OK
+    status, dev = _device_begin(scope, first, abi.access(flags=abi.READ_ALL | abi.WRITE_ALL))
+    assert status == abi.OK
+    _dev(dev, 8)[:] += 100.0
+    assert both.fort_scope_device_end(scope.handle, first) == abi.OK
+    assert both.fort_scope_set_device_budget(scope.handle, 128) == abi.STATE
+    status, _ = _device_begin(scope, second, abi.access(flags=abi.WRITE_ALL | abi.OVERWRITE_ALL))
+    assert status == abi.OK
+    stats = scope.stats()
+    assert stats.allocated_bytes == stats.peak_device_bytes == 64
+    assert host.tolist() == [i + 100.0 for i in range(8)]
+    assert both.fort_scope_cancel_access(scope.handle, second) == abi.OK
+    assert both.fort_scope_host_begin(scope.handle, first, c.byref(abi.access(flags=abi.READ_ALL))) == abi.OK
+    assert both.fort_scope_host_end(scope.handle, first) == abi.OK
+    assert both.fort_scope_host_begin(scope.handle, second,
+                                      c.byref(abi.access(flags=abi.WRITE_ALL | abi.OVERWRITE_ALL))) == abi.OK
+    other[:] = host * 2
+    assert both.fort_scope_host_end(scope.handle, second) == abi.OK
+    assert both.fort_scope_close(scope.handle) == abi.OK
+    assert other.tolist() == [2 * (i + 100.0) for i in range(8)]
+
+
+def test_a_zero_budget_allocates_nothing(both):
+    """(reference: test_scoped_runtime.py:656-667)"""
+    scope = abi.Scope(both)
+    _, address = _array(np.arange(8, dtype=np.float64))
+    _, h = scope.register(address, [8])
+    assert both.fort_scope_set_device_budget(scope.handle, 0) == abi.OK
+    status, _ = _device_begin(scope, h, abi.access(flags=abi.READ_ALL))
+    assert status == abi.RESOURCE and scope.stats().allocations == 0
+    assert both.fort_scope_host_begin(scope.handle, h, c.byref(abi.access(flags=abi.READ_ALL))) == abi.OK
+    assert both.fort_scope_host_end(scope.handle, h) == abi.OK
+    assert both.fort_scope_close(scope.handle) == abi.OK
+
+
 def test_budget_eviction_publishes_dirty_values(both):
     scope = abi.Scope(both)
     a, pa = _array(np.zeros(128))
