@@ -1511,17 +1511,12 @@ int fort_scope_domain_abandon_v1(fort_scope_domain_t domain) {
 
 // Workspace claims: bytes an external provider allocated on its own, counted
 // against the domain's budget like mirrors and scratch (no memory is allocated
-// here). A claim that does not fit evicts unprepared, idle mirrors (publishing
-// dirty values first) through the domain's context, or fails with RESOURCE and
-// changes nothing.
+// here). A claim that does not fit beside what the domain already holds fails
+// with RESOURCE and changes nothing: mirrors are not evicted for a provider.
 void fit_workspace(Domain *d, size_t after) {
     if (!d->budget_set || after <= d->workspace_bytes) return;
     const size_t growth = after - d->workspace_bytes;
-    if (claimed(d) + growth <= d->budget) return;
-    Context *c = d->borrower;
-    if (!c || c->poisoned) raise(FORT_SCOPE_RESOURCE, "workspace claim exceeds the device budget");
-    ensure_stream(c);
-    make_room(c, growth, {});
+    if (claimed(d) + growth > d->budget) raise(FORT_SCOPE_RESOURCE, "workspace claim exceeds the free device budget");
 }
 
 Domain *live_domain(fort_scope_domain_t handle) {
@@ -1707,7 +1702,7 @@ static int register_impl(fort_scope_t context, uint64_t identity, uint64_t gener
             bool same = b->rank == (int)layout->rank && b->type == layout->type && b->elem == layout->element_bytes &&
                         b->host == layout->host;
             for (int r = 0; same && r < b->rank; ++r) same = b->extents[r] == layout->extents[r];
-            if (!same) raise(FORT_SCOPE_ALIAS, "identity already registered with another layout");
+            if (!same) raise(FORT_SCOPE_ARGUMENT, "identity already registered with another layout or storage");
             if (b->generation != generation)
                 raise(FORT_SCOPE_STALE, "allocation generation changed: unregister before changing storage");
             for (int r = 0; r < b->rank; ++r) b->lower[r] = layout->lower_bounds[r];

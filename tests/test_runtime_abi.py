@@ -889,6 +889,79 @@ def test_a_zero_budget_allocates_nothing(both):
     assert both.fort_scope_close(scope.handle) == abi.OK
 
 
+def test_workspace_leases_share_the_budget_and_outlive_the_context(both):
+    """A provider's workspace lease counts against the domain's budget exactly, can shrink to make room, survives
+    the context, holds the domain open, and belongs to its domain alone (reference:
+    test_scoped_domains.py:222-245)."""
+    domain = _domain(both)
+    scope = abi.Scope(both, domain=domain)
+    assert both.fort_scope_set_device_budget(scope.handle, 96) == abi.OK
+    lease = abi.U64()
+    assert both.fort_scope_domain_workspace_reserve_v1(domain, 64, c.byref(lease)) == abi.OK
+    _, address = _array(np.arange(8, dtype=np.float64))
+    _, h = scope.register(address, [8])
+    status, _ = _device_begin(scope, h, abi.access(flags=abi.READ_ALL))
+    assert status == abi.RESOURCE and scope.stats().allocations == 0
+    assert both.fort_scope_domain_workspace_resize_v1(domain, lease.value, 32) == abi.OK
+    status, _ = _device_begin(scope, h, abi.access(flags=abi.READ_ALL))
+    assert status == abi.OK
+    assert both.fort_scope_device_end(scope.handle, h) == abi.OK
+    assert both.fort_scope_domain_workspace_resize_v1(domain, lease.value, 33) == abi.RESOURCE
+    assert both.fort_scope_close(scope.handle) == abi.OK
+    assert both.fort_scope_domain_close_v1(domain) == abi.STATE
+    other = _domain(both)
+    assert both.fort_scope_domain_workspace_release_v1(other, lease.value) == abi.STALE
+    assert both.fort_scope_domain_close_v1(other) == abi.OK
+    assert both.fort_scope_domain_workspace_release_v1(domain, lease.value) == abi.OK
+    assert both.fort_scope_domain_workspace_release_v1(domain, lease.value) == abi.STALE
+    assert both.fort_scope_domain_close_v1(domain) == abi.OK
+
+
+def test_after_a_storage_cut_identities_bind_to_their_new_arrays(both):
+    """Closing a domain publishes and cuts storage; a new domain binds each identity to whatever array it now
+    names, at a new generation, with fresh handles; an identity cannot be moved to other storage or back to an old
+    generation while registered (reference: test_scoped_domains.py:248-296)."""
+    left, la = _array([1.0, 2.0])
+    right, ra = _array([3.0, 4.0])
+    first = _domain(both)
+    before = abi.Scope(both, domain=first)
+    old = []
+    for identity, address, increment in ((1, la, 10.0), (2, ra, 20.0)):
+        _, h = before.register(address, [2], identity=identity)
+        old.append(h)
+        status, dev = _device_begin(before, h, abi.access(flags=abi.READ_ALL | abi.WRITE_ALL))
+        assert status == abi.OK
+        _dev(dev, 2)[:] += increment
+        assert both.fort_scope_device_end(before.handle, h) == abi.OK
+    assert both.fort_scope_close(before.handle) == abi.OK
+    assert (left.tolist(), right.tolist()) == ([1.0, 2.0], [3.0, 4.0])
+    assert both.fort_scope_domain_close_v1(first) == abi.OK
+    assert (left.tolist(), right.tolist()) == ([11.0, 12.0], [23.0, 24.0])
+    second = _domain(both)
+    after = abi.Scope(both, domain=second)
+    current = []
+    for identity, address, expected in ((1, ra, [23.0, 24.0]), (2, la, [11.0, 12.0])):
+        status, h = after.register(address, [2], identity=identity, generation=2)
+        assert status == abi.OK
+        current.append(h)
+        status, dev = _device_begin(after, h, abi.access(flags=abi.READ_ALL))
+        assert status == abi.OK and _dev(dev, 2).tolist() == expected
+        assert both.fort_scope_device_end(after.handle, h) == abi.OK
+    for h in old:
+        assert _device_begin(after, h, abi.access(flags=abi.READ_ALL))[0] == abi.STALE
+    assert not set(old) & set(current)
+    assert after.register(la, [2], identity=1, generation=2)[0] == abi.ARGUMENT   # other storage
+    assert after.register(ra, [2], identity=1, generation=1)[0] == abi.STALE      # an older generation
+    assert both.fort_scope_close(after.handle) == abi.OK
+    again = abi.Scope(both, domain=second)
+    for identity, address, h in ((1, ra, current[0]), (2, la, current[1])):
+        status, same = again.register(address, [2], identity=identity, generation=2, initialized=False)
+        assert status == abi.OK and same == h
+    assert both.fort_scope_host_begin(after.handle, current[0], c.byref(abi.access(flags=abi.READ_ALL))) == abi.STALE
+    assert both.fort_scope_close(again.handle) == abi.OK
+    assert both.fort_scope_domain_close_v1(second) == abi.OK
+
+
 def test_budget_eviction_publishes_dirty_values(both):
     scope = abi.Scope(both)
     a, pa = _array(np.zeros(128))
