@@ -128,6 +128,8 @@ struct Backend {
         return true;
     }
     static bool sync(Stream) { return !std::getenv("F2C_TEST_FAIL_WAIT"); }
+    // An external provider's effects fail to commit after it ran (tests only).
+    static bool external_commit_fails() { return std::getenv("F2C_TEST_FAIL_EXTERNAL_COMMIT") != nullptr; }
     // Completion events. Work here is synchronous, but an event reads as pending
     // until it is waited for, so that the runtime's bookkeeping of what is still
     // in flight is exercised as on a device.
@@ -252,6 +254,7 @@ struct Backend {
         return good;
     }
     static bool sync(Stream s) { return ok(cudaStreamSynchronize(s)); }
+    static bool external_commit_fails() { return false; }
     using Event = cudaEvent_t;
     static bool make_event(Event *e) { return ok(cudaEventCreateWithFlags(e, cudaEventDisableTiming)); }
     static void destroy_event(Event e) {

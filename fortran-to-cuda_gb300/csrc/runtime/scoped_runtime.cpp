@@ -1090,10 +1090,8 @@ void accept(Context *c, Task &&task, std::vector<Bound> &bound) {
     if (!c->queue_enabled || (c->queue_work_limit && c->pending_threads >= c->queue_work_limit)) flush(c);
 }
 
-void count_external_launch(Context *c) {
-    c->domain->stats.launches++;
-    c->queue_stats.direct_submissions++;
-}
+// A provider's kernels are opaque: its submission is counted, its launches are not invented.
+void count_external_launch(Context *c) { c->queue_stats.direct_submissions++; }
 
 // ---- slab pipelines -------------------------------------------------------------------------
 
@@ -1474,8 +1472,8 @@ int fort_scope_domain_stats_get_v1(fort_scope_domain_t domain, fort_scope_stats 
 int fort_scope_domain_close_v1(fort_scope_domain_t domain) {
     return guarded([&] {
         Domain *d = find_domain(domain);
-        if (d->borrower) raise(FORT_SCOPE_STATE, "domain still borrowed by a context");
         if (d->poisoned) raise(FORT_SCOPE_EXECUTION, "domain poisoned; abandon it instead");
+        if (d->borrower) raise(FORT_SCOPE_STATE, "domain still borrowed by a context");
         if (!d->workspaces.empty()) raise(FORT_SCOPE_STATE, "provider workspace leases are still held");
         for (auto &kv : d->buffers)
             if (kv.second->prepared != Buffer::NONE) raise(FORT_SCOPE_STATE, "domain has a prepared access");
@@ -2513,6 +2511,7 @@ int fort_scope_external_execute_v1(fort_scope_t context, const fort_scope_extern
             (result != FORT_SCOPE_OK && (started != 0 || !known)))
             poison(c, "external execution failed or did not report its submission state");
         if (result != FORT_SCOPE_OK) raise(result, "external provider rejected the call before submission");
+        if (Backend::external_commit_fails()) poison(c, "external provider effects could not be committed");
         for (auto &x : bound) {
             device_commit(c, x.buffer, x.effects.writes, x.effects.overwrites);
             note_device_use(x.buffer);

@@ -1689,6 +1689,163 @@ def test_a_throwing_provider_is_contained(both, tmp_path):
     assert run.returncode == 0, (run.returncode, run.stderr)
 
 
+def _execute(lib, scope, bindings, worker, *, lease=0, workspace=0):
+    """bindings: (handle, access, type, rank) tuples."""
+    items = (abi.ExternalBinding * max(1, len(bindings)))(
+        *[abi.ExternalBinding(h, t, r, 8, acc) for h, acc, t, r in bindings])
+    call = abi.ExternalCall(1, 0, items if bindings else None, len(bindings), lease, workspace)
+    report = abi.ExternalReport()
+    status = lib.fort_scope_external_execute_v1(scope.handle, c.byref(call), worker, None, c.byref(report))
+    return status, report
+
+
+def test_external_views_partial_effects_and_workspace(both):
+    """The provider sees each array's generation, extents, byte strides and lower bounds; a workspace beyond its
+    lease is refused before the call; a partial overwrite defines exactly its section, which the host gets when it
+    reads it; the provider's kernels are not counted as launches (reference: test_scoped_domains.py:433-470)."""
+    domain = _domain(both)
+    scope = abi.Scope(both, domain=domain)
+    source, sa = _array(np.arange(6, dtype=np.float64))
+    output, oa = _array(np.full(6, -99.0))
+    _, a = scope.register(sa, [6], lower=[-3], generation=11)
+    _, b = scope.register(oa, [6], identity=2, initialized=False)
+    box = [((1,), (5,))]
+    bindings = [(a, abi.access(read=box), abi.REAL64, 1), (b, abi.access(write=box, overwrite=box), abi.REAL64, 1)]
+    seen = []
+
+    def run(user, views, count, stream, started):
+        v = views
+        seen.append((count, stream, v[0].generation, v[0].extents[0], v[0].strides[0], v[0].lower_bounds[0],
+                     v[1].bytes))
+        started[0] = 1
+        av, bv = _dev(v[0].device, 6), _dev(v[1].device, 6)
+        bv[1:5] = 3 * av[1:5]
+        return abi.OK
+
+    worker = abi.EXTERNAL_WORKER(run)
+    lease = abi.U64()
+    assert both.fort_scope_domain_workspace_reserve_v1(domain, 24, c.byref(lease)) == abi.OK
+    status, _ = _execute(both, scope, bindings, worker, lease=lease.value, workspace=25)
+    assert status == abi.RESOURCE and seen == []
+    status, report = _execute(both, scope, bindings, worker, lease=lease.value, workspace=24)
+    assert status == abi.OK
+    assert (report.version, report.status, report.started, report.committed) == (1, abi.OK, 1, 1)
+    assert seen == [(2, None, 11, 6, 8, -3, 48)]
+    assert output.tolist() == [-99.0] * 6
+    assert both.fort_scope_host_begin(scope.handle, b, c.byref(abi.access(read=box))) == abi.OK
+    assert both.fort_scope_host_end(scope.handle, b) == abi.OK
+    assert output.tolist() == [-99.0, 3.0, 6.0, 9.0, 12.0, -99.0]
+    stats = scope.stats()
+    assert (stats.upload_bytes, stats.download_bytes, stats.launches) == (32, 32, 0)
+    assert both.fort_scope_close(scope.handle) == abi.OK
+    assert both.fort_scope_domain_workspace_release_v1(domain, lease.value) == abi.OK
+    assert both.fort_scope_domain_close_v1(domain) == abi.OK
+
+
+@pytest.mark.parametrize("invalid", ["type", "rank", "duplicate", "undefined"])
+def test_external_preflight_refuses_before_the_provider(both, invalid):
+    """A wrong type or rank, an array bound twice, or a read of undefined values is refused before the provider
+    runs and before storage is allocated; a call under a prepared access is refused, and so is closing the context
+    (reference: test_scoped_domains.py:473-511)."""
+    domain = _domain(both)
+    scope = abi.Scope(both, domain=domain)
+    _, address = _array([1.0, 2.0, 3.0, 4.0])
+    _, h = scope.register(address, [4], initialized=invalid != "undefined")
+    read = abi.access(flags=abi.READ_ALL)
+    item = (h, read, abi.REAL32 if invalid == "type" else abi.REAL64, 2 if invalid == "rank" else 1)
+    bindings = [item, item] if invalid == "duplicate" else [item]
+    expected = {"type": abi.ARGUMENT, "rank": abi.ARGUMENT, "duplicate": abi.ALIAS, "undefined": abi.UNINITIALIZED}
+    calls = []
+
+    def run(user, views, count, stream, started):
+        calls.append(count)
+        started[0] = 1
+        return abi.OK
+
+    worker = abi.EXTERNAL_WORKER(run)
+    status, report = _execute(both, scope, bindings, worker)
+    assert status == expected[invalid]
+    assert (report.started, report.committed) == (0, 0) and calls == []
+    assert scope.stats().allocations == 0
+    if invalid != "undefined":
+        status, _ = _device_begin(scope, h, read)
+        assert status == abi.OK
+        status, _ = _execute(both, scope, [(h, read, abi.REAL64, 1)], worker)
+        assert status == abi.STATE
+        assert both.fort_scope_close(scope.handle) == abi.STATE
+        assert both.fort_scope_device_end(scope.handle, h) == abi.OK
+    assert both.fort_scope_close(scope.handle) == abi.OK
+    assert both.fort_scope_domain_close_v1(domain) == abi.OK
+
+
+def test_a_rejecting_provider_defines_nothing_and_the_host_recovers(both):
+    """A provider that rejects before starting grants no definitions; the host then writes the values itself
+    (reference: test_scoped_domains.py:514-536)."""
+    domain = _domain(both)
+    scope = abi.Scope(both, domain=domain)
+    host, address = _array(np.full(4, -8.0))
+    _, h = scope.register(address, [4], initialized=False)
+
+    def reject(user, views, count, stream, started):
+        started[0] = 0
+        return abi.RESOURCE
+
+    worker = abi.EXTERNAL_WORKER(reject)
+    status, report = _execute(both, scope, [(h, abi.access(flags=abi.WRITE_ALL | abi.OVERWRITE_ALL), abi.REAL64, 1)],
+                              worker)
+    assert status == report.status == abi.RESOURCE and (report.started, report.committed) == (0, 0)
+    assert both.fort_scope_host_begin(scope.handle, h, c.byref(abi.access(flags=abi.READ_ALL))) == abi.UNINITIALIZED
+    assert both.fort_scope_host_begin(scope.handle, h,
+                                      c.byref(abi.access(flags=abi.WRITE_ALL | abi.OVERWRITE_ALL))) == abi.OK
+    host[:] = 2.0 * np.arange(4)
+    assert both.fort_scope_host_end(scope.handle, h) == abi.OK
+    assert both.fort_scope_close(scope.handle) == abi.OK
+    assert both.fort_scope_domain_close_v1(domain) == abi.OK
+    assert host.tolist() == [0.0, 2.0, 4.0, 6.0]
+
+
+@pytest.mark.parametrize("mode", ["submitted_failure", "missing_marker", "success_without_submission",
+                                  "execution_failure", "commit_failure"])
+def test_an_uncertain_provider_outcome_poisons_the_domain(both, monkeypatch, mode):
+    """A failure after submission, a missing submission marker, success without submission, an execution failure
+    or a failed commit poison context and domain: nothing is published or replayed, and only abandonment ends them
+    (reference: test_scoped_domains.py:539-579)."""
+    domain = _domain(both)
+    scope = abi.Scope(both, domain=domain)
+    host, address = _array([1.0, 2.0, 3.0, 4.0])
+    _, h = scope.register(address, [4])
+    calls = []
+
+    def run(user, views, count, stream, started):
+        calls.append(count)
+        if mode in ("submitted_failure", "commit_failure"):
+            started[0] = 1
+            _dev(views[0].device, 4)[0] = 1000.0
+            return abi.RESOURCE if mode == "submitted_failure" else abi.OK
+        if mode == "missing_marker":
+            return abi.OK
+        started[0] = 0
+        return abi.OK if mode == "success_without_submission" else abi.EXECUTION
+
+    if mode == "commit_failure":
+        _inject(monkeypatch, "EXTERNAL_COMMIT")
+    worker = abi.EXTERNAL_WORKER(run)
+    binding = [(h, abi.access(flags=abi.READ_ALL | abi.WRITE_ALL), abi.REAL64, 1)]
+    status, report = _execute(both, scope, binding, worker)
+    assert status == report.status == abi.EXECUTION and report.committed == 0 and len(calls) == 1
+    assert both.fort_scope_wait(scope.handle) == abi.EXECUTION
+    assert both.fort_scope_domain_close_v1(domain) == abi.EXECUTION
+    assert both.fort_scope_create_in_domain_v1(domain, c.byref(abi.U64())) == abi.EXECUTION
+    status, _ = _execute(both, scope, binding, worker)
+    assert status == abi.EXECUTION and len(calls) == 1
+    found = abi.U64()
+    assert both.fort_scope_domain_get_v1(scope.handle, c.byref(found)) == abi.OK and found.value == domain
+    assert both.fort_scope_domain_abandon_v1(domain) == abi.STATE
+    assert both.fort_scope_abandon(scope.handle) == abi.OK
+    assert both.fort_scope_domain_abandon_v1(domain) == abi.OK
+    assert host.tolist() == [1.0, 2.0, 3.0, 4.0]
+
+
 def test_external_bindings_are_checked_before_the_worker_runs(both):
     scope = abi.Scope(both)
     _, address = _array(np.zeros(4))
