@@ -962,6 +962,122 @@ def test_after_a_storage_cut_identities_bind_to_their_new_arrays(both):
     assert both.fort_scope_domain_close_v1(second) == abi.OK
 
 
+def _descriptor(address, shape, generation, lower, keep):
+    extents = (abi.SIZE * len(shape))(*shape)
+    bounds = (c.c_int64 * len(shape))(*lower)
+    keep += [extents, bounds]
+    return abi.Layout(len(shape), abi.REAL64, 8, address, extents, bounds, generation)
+
+
+def _swap(lib, scope, first, second, after_first, after_second):
+    now_first, now_second = abi.U64(111), abi.U64(222)
+    status = lib.fort_scope_identity_swap_v1(scope.handle, first, second, c.byref(after_first), c.byref(after_second),
+                                             c.byref(now_first), c.byref(now_second))
+    return status, now_first.value, now_second.value
+
+
+def test_an_exchange_renames_storage_without_moving_it(both):
+    """After the host swapped two arrays' descriptors, the exchange tells each identity which storage it now names:
+    no copy, allocation, wait or replay; each name finds its dirty device values, generation and layout; the
+    domain publishes them to the right arrays (reference: test_scoped_domains.py:319-371)."""
+    domain = _domain(both)
+    scope = abi.Scope(both, domain=domain)
+    a, pa = _array([1.0, 2.0, 3.0, 4.0])
+    b, pb = _array([11.0, 12.0, 13.0, 14.0, 15.0, 16.0])
+    handles = []
+    for identity, address, shape, lower, generation, n in ((1, pa, [2, 2], [-2, 3], 11, 4), (2, pb, [3, 2], [-7, 9], 27, 6)):
+        status, h = scope.register(address, shape, identity=identity, lower=lower, generation=generation)
+        assert status == abi.OK
+        handles.append(h)
+        status, dev = _device_begin(scope, h, abi.access(flags=abi.READ_ALL | abi.WRITE_ALL))
+        assert status == abi.OK
+        _dev(dev, n)[:] += 100.0 * identity
+        assert both.fort_scope_device_end(scope.handle, h) == abi.OK
+    assert both.fort_scope_close(scope.handle) == abi.OK
+    again = abi.Scope(both, domain=domain)
+    before = bytes(again.stats())
+    keep = []
+    status, now_a, now_b = _swap(both, again, handles[0], handles[1], _descriptor(pb, [3, 2], 27, [-7, 9], keep),
+                                 _descriptor(pa, [2, 2], 11, [-2, 3], keep))
+    assert status == abi.OK and (now_a, now_b) == (handles[1], handles[0])
+    assert bytes(again.stats()) == before
+    for identity, address, shape, lower, generation, expected_handle, expected in (
+            (1, pb, [3, 2], [-7, 9], 27, now_a, [211.0 + i for i in range(6)]),
+            (2, pa, [2, 2], [-2, 3], 11, now_b, [101.0 + i for i in range(4)])):
+        status, h = again.register(address, shape, identity=identity, lower=lower, generation=generation)
+        assert status == abi.OK and h == expected_handle
+        layout = abi.Layout()
+        assert both.fort_scope_layout_get(again.handle, h, c.byref(layout)) == abi.OK
+        assert layout.generation == generation
+        status, dev = _device_begin(again, h, abi.access(flags=abi.READ_ALL))
+        assert status == abi.OK and _dev(dev, len(expected)).tolist() == expected
+        assert both.fort_scope_device_end(again.handle, h) == abi.OK
+    assert (again.stats().upload_bytes, again.stats().download_bytes) == (80, 0)
+    assert both.fort_scope_close(again.handle) == abi.OK
+    assert (a.tolist(), b.tolist()) == ([1.0, 2.0, 3.0, 4.0], [11.0 + i for i in range(6)])
+    assert both.fort_scope_domain_close_v1(domain) == abi.OK
+    assert (a.tolist(), b.tolist()) == ([101.0 + i for i in range(4)], [211.0 + i for i in range(6)])
+
+
+def test_an_exchange_never_defines_from_the_new_name(both):
+    """A name that moves to undefined storage stays undefined even when re-registered as initialized (reference:
+    test_scoped_domains.py:374-394)."""
+    domain = _domain(both)
+    scope = abi.Scope(both, domain=domain)
+    a, pa = _array([-9.0, -8.0])
+    b, pb = _array([3.0, 5.0])
+    _, old_a = scope.register(pa, [2], initialized=False, generation=2, lower=[0])
+    _, old_b = scope.register(pb, [2], identity=2, generation=7, lower=[0])
+    keep = []
+    status, new_a, new_b = _swap(both, scope, old_a, old_b, _descriptor(pb, [2], 7, [0], keep), _descriptor(pa, [2], 2, [0], keep))
+    assert status == abi.OK
+    assert scope.register(pa, [2], identity=2, generation=2, initialized=True, lower=[0])[1] == new_b
+    assert _device_begin(scope, new_b, abi.access(flags=abi.READ_ALL))[0] == abi.UNINITIALIZED
+    status, dev = _device_begin(scope, new_a, abi.access(flags=abi.READ_ALL))
+    assert status == abi.OK and _dev(dev, 2).tolist() == [3.0, 5.0]
+    assert both.fort_scope_device_end(scope.handle, new_a) == abi.OK
+    assert both.fort_scope_close(scope.handle) == abi.OK
+    assert both.fort_scope_domain_close_v1(domain) == abi.OK
+    assert a.tolist() == [-9.0, -8.0]
+
+
+@pytest.mark.parametrize("invalid", ["host", "generation", "extent", "lower", "same_handle", "prepared"])
+def test_an_inconsistent_exchange_is_fatal(both, invalid):
+    """The exchange reports a mutation that already happened, so an inconsistent report cannot be refused and
+    retried: it poisons context and domain without publishing (reference: test_scoped_domains.py:397-430)."""
+    domain = _domain(both)
+    scope = abi.Scope(both, domain=domain)
+    a, pa = _array([1.0, 2.0])
+    b, pb = _array([3.0, 4.0])
+    _, old_a = scope.register(pa, [2], generation=2, lower=[0])
+    _, old_b = scope.register(pb, [2], identity=2, generation=7, lower=[0])
+    status, dev = _device_begin(scope, old_a, abi.access(flags=abi.READ_ALL | abi.WRITE_ALL))
+    assert status == abi.OK
+    _dev(dev, 2)[0] = 1000.0
+    assert both.fort_scope_device_end(scope.handle, old_a) == abi.OK
+    keep = []
+    after_a, after_b = _descriptor(pb, [2], 7, [0], keep), _descriptor(pa, [2], 2, [0], keep)
+    if invalid == "host":
+        after_a.host = pa
+    elif invalid == "generation":
+        after_a.generation = 2
+    elif invalid == "extent":
+        after_a = _descriptor(pb, [1], 7, [0], keep)
+    elif invalid == "lower":
+        after_a = _descriptor(pb, [2], 7, [-1], keep)
+    elif invalid == "same_handle":
+        old_b = old_a
+    elif invalid == "prepared":
+        assert _device_begin(scope, old_b, abi.access(flags=abi.READ_ALL))[0] == abi.OK
+    status, now_a, now_b = _swap(both, scope, old_a, old_b, after_a, after_b)
+    assert status == abi.EXECUTION and (now_a, now_b) == (111, 222)
+    assert both.fort_scope_wait(scope.handle) == abi.EXECUTION
+    assert both.fort_scope_close(scope.handle) == abi.EXECUTION
+    assert both.fort_scope_abandon(scope.handle) == abi.OK
+    assert both.fort_scope_domain_abandon_v1(domain) == abi.OK
+    assert (a.tolist(), b.tolist()) == ([1.0, 2.0], [3.0, 4.0])
+
+
 def test_budget_eviction_publishes_dirty_values(both):
     scope = abi.Scope(both)
     a, pa = _array(np.zeros(128))
