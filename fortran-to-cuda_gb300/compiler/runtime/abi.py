@@ -174,6 +174,7 @@ SIGNATURES = {
     "graph_stats_get_v1": ([U64, P(GraphStats)], c.c_int),
     "completion_stats_get_v1": ([U64, P(CompletionStats)], c.c_int),
     "graph_execute_v1": ([U64, U64, P(Task), SIZE], c.c_int),
+    "graph_submit_v1": ([U64, U64, P(Kernel), SIZE], c.c_int),
     "device_reserve_slabs_v1": ([U64, P(U64), SIZE, P(c.c_void_p), P(c.c_int)], c.c_int),
     "slab_enqueue_v1": ([U64, U64, P(Task), SIZE, P(SIZE)], c.c_int),
     "domain_workspace_reserve_v1": ([U64, SIZE, P(U64)], c.c_int),

@@ -1000,6 +1000,7 @@ void host_commit(Context *c, Buffer *b, const Region &writes, const Region &over
 
 LaunchSpec spec_of(const fort_scope_kernel_v1 &k) {
     if (k.version != FORT_SCOPE_GRAPH_ABI_VERSION) raise(FORT_SCOPE_ARGUMENT, "unknown kernel record version");
+    if (k.reserved) raise(FORT_SCOPE_ARGUMENT, "reserved kernel record field is not zero");
     if (!k.function) raise(FORT_SCOPE_ARGUMENT, "null kernel function");
     if (k.argument_count > 384) raise(FORT_SCOPE_ARGUMENT, "too many kernel arguments");
     if (k.argument_count && !k.arguments) raise(FORT_SCOPE_ARGUMENT, "null kernel arguments");
@@ -2322,6 +2323,7 @@ int fort_scope_graph_submit_v1(fort_scope_t context, uint64_t group_key, const f
         Context *c = live_context(context);
         if (count && !kernels) raise(FORT_SCOPE_ARGUMENT, "null kernels");
         if (!count) return FORT_SCOPE_OK;
+        if (!group_key) raise(FORT_SCOPE_ARGUMENT, "a kernel group needs a nonzero key");
         std::vector<Task> tasks;
         for (size_t n = 0; n < count; ++n) {
             Task t;

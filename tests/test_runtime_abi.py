@@ -1078,6 +1078,56 @@ def test_an_inconsistent_exchange_is_fatal(both, invalid):
     assert (a.tolist(), b.tolist()) == ([1.0, 2.0], [3.0, 4.0])
 
 
+@pytest.mark.parametrize("invalid", ["key", "version", "reserved", "function", "grid", "block", "arguments"])
+def test_invalid_kernel_groups_fail_before_any_launch(both, invalid):
+    """A zero group key, an unknown record version, a nonzero reserved field, no function, an empty launch
+    dimension or arguments without storage are refused, with nothing built or launched (reference:
+    test_scoped_graph_replay.py:64-79)."""
+    scope = abi.Scope(both)
+    kernel = abi.Kernel(1, 0, 1, (c.c_uint32 * 3)(1, 1, 1), (c.c_uint32 * 3)(32, 1, 1), 0, None, 0)
+    key = 0 if invalid == "key" else 1
+    if invalid == "version":
+        kernel.version = 0
+    elif invalid == "reserved":
+        kernel.reserved = 1
+    elif invalid == "function":
+        kernel.function = None
+    elif invalid in ("grid", "block"):
+        getattr(kernel, invalid)[0] = 0
+    elif invalid == "arguments":
+        kernel.argument_count = 1
+    assert both.fort_scope_graph_submit_v1(scope.handle, key, c.byref(kernel), 1) == abi.ARGUMENT
+    graphs = abi.GraphStats()
+    assert both.fort_scope_graph_stats_get_v1(scope.handle, c.byref(graphs)) == abi.OK
+    assert graphs.creations == scope.stats().launches == 0
+    assert both.fort_scope_close(scope.handle) == abi.OK
+
+
+def test_a_reservation_changes_only_storage_and_a_bad_group_commits_nothing(both):
+    """Reserving twice allocates once and moves nothing; a group whose second task names a stale array is refused
+    as a whole, so the first task defines nothing (reference: test_scoped_graph_replay.py:197-218)."""
+    scope = abi.Scope(both)
+    _, address = _array(np.zeros(8))
+    _, h = scope.register(address, [8], initialized=False)
+    first, second = c.c_void_p(), c.c_void_p()
+    assert both.fort_scope_device_reserve_v1(scope.handle, h, c.byref(first)) == abi.OK
+    assert both.fort_scope_device_reserve_v1(scope.handle, h, c.byref(second)) == abi.OK
+    assert first.value == second.value
+    stats = scope.stats()
+    assert (stats.allocations, stats.uploads, stats.downloads) == (1, 0, 0)
+    assert both.fort_scope_host_begin(scope.handle, h, c.byref(abi.access(flags=abi.READ_ALL))) == abi.UNINITIALIZED
+    produce = abi.access(flags=abi.WRITE_ALL | abi.OVERWRITE_ALL)
+    stale = abi.access(flags=abi.READ_ALL)
+    kernel = abi.Kernel(1, 0, 1, (c.c_uint32 * 3)(1, 1, 1), (c.c_uint32 * 3)(32, 1, 1), 0, None, 0)
+    one, two = (abi.Binding * 1)(abi.Binding(h, produce)), (abi.Binding * 1)(abi.Binding(2**63, stale))
+    tasks = (abi.Task * 2)(abi.Task(kernel, one, 1), abi.Task(kernel, two, 1))
+    before = bytes(scope.stats())
+    assert both.fort_scope_graph_execute_v1(scope.handle, 9, tasks, 2) == abi.STALE
+    assert bytes(scope.stats()) == before
+    assert both.fort_scope_host_begin(scope.handle, h, c.byref(abi.access(flags=abi.READ_ALL))) == abi.UNINITIALIZED
+    assert both.fort_scope_close(scope.handle) == abi.OK
+
+
 def test_budget_eviction_publishes_dirty_values(both):
     scope = abi.Scope(both)
     a, pa = _array(np.zeros(128))
