@@ -110,6 +110,14 @@ struct Backend {
     static void destroy_stream(Stream) {}
     static bool alloc(void **p, size_t bytes, Stream) {
         if (std::getenv("F2C_TEST_FAIL_ALLOC")) return false;
+        // F2C_TEST_FAIL_ALLOC_AFTER=n: the allocations after the first n fail (counted while it is set)
+        static int granted = 0;
+        if (const char *after = std::getenv("F2C_TEST_FAIL_ALLOC_AFTER")) {
+            if (granted >= std::atoi(after)) return false;
+            ++granted;
+        } else {
+            granted = 0;
+        }
         *p = std::malloc(bytes ? bytes : 1);
         return *p != nullptr;
     }

@@ -1128,6 +1128,201 @@ def test_a_reservation_changes_only_storage_and_a_bad_group_commits_nothing(both
     assert both.fort_scope_close(scope.handle) == abi.OK
 
 
+def _batch(lib, scope, items, *, device=False, outputs=None):
+    bindings = (abi.Binding * max(1, len(items)))(*[abi.Binding(h, acc) for h, acc in items])
+    return lib.fort_scope_access_begin_v1(scope.handle, bindings if items else None, len(items), int(device),
+                                          outputs)
+
+
+def _counted(scope, identity, *, initialized=True, count=8):
+    host, address = _array(identity * 10.0 + np.arange(count))
+    status, h = scope.register(address, [count], identity=identity, initialized=initialized)
+    assert status == abi.OK
+    return host, h
+
+
+@pytest.mark.parametrize("device", [False, True])
+@pytest.mark.parametrize("failure", ["stale", "effects", "undefined", "duplicate"])
+def test_a_bad_late_binding_changes_nothing(both, device, failure):
+    """A batch whose last binding is stale, out of bounds, reads undefined values or repeats an array is refused
+    before anything is published, prepared or written out (reference: test_scoped_access_batch.py:130-166)."""
+    scope = abi.Scope(both)
+    values, first = _counted(scope, 1)
+    _, second = _counted(scope, 2, initialized=False)
+    status, dev = _device_begin(scope, first, abi.access(flags=abi.READ_ALL | abi.WRITE_ALL))
+    assert status == abi.OK
+    _dev(dev, 8)[0] = 987.0
+    assert both.fort_scope_device_end(scope.handle, first) == abi.OK
+    read = abi.access(flags=abi.READ_ALL)
+    final, expected = {"stale": ((2**63, abi.access(flags=abi.READ_ALL)), abi.STALE),
+                       "effects": ((second, abi.access(write=[((0,), (9,))])), abi.ARGUMENT),
+                       "undefined": ((second, abi.access(flags=abi.READ_ALL)), abi.UNINITIALIZED),
+                       "duplicate": ((first, abi.access(flags=abi.READ_ALL)), abi.ALIAS)}[failure]
+    outputs = (c.c_void_p * 2)(123, 456)
+    before = bytes(scope.stats())
+    assert _batch(both, scope, [(first, read), final], device=device, outputs=outputs) == expected
+    assert bytes(scope.stats()) == before and list(outputs) == [123, 456]
+    assert values[0] == 10.0
+    assert both.fort_scope_host_begin(scope.handle, first, c.byref(read)) == abi.OK
+    assert values[0] == 987.0
+    assert both.fort_scope_host_end(scope.handle, first) == abi.OK
+    assert both.fort_scope_host_begin(scope.handle, second, c.byref(read)) == abi.UNINITIALIZED
+    assert both.fort_scope_close(scope.handle) == abi.OK
+
+
+def test_a_failed_allocation_leaves_the_batch_unprepared(both, monkeypatch):
+    """When the second allocation of a device batch fails, nothing is prepared, uploaded or defined; the first
+    storage stays allocated (reference: test_scoped_access_batch.py:169-184)."""
+    scope = abi.Scope(both)
+    _, first = _counted(scope, 1, initialized=False)
+    _, second = _counted(scope, 2, initialized=False)
+    write = abi.access(flags=abi.WRITE_ALL | abi.OVERWRITE_ALL)
+    outputs = (c.c_void_p * 2)(123, 456)
+    monkeypatch.setenv("F2C_TEST_FAIL_ALLOC_AFTER", "1")
+    monkeypatch.setenv("FORT_SCOPE_TEST_FAIL_ALLOC_AFTER", "1")
+    assert _batch(both, scope, [(first, write), (second, write)], device=True, outputs=outputs) == abi.RESOURCE
+    monkeypatch.delenv("F2C_TEST_FAIL_ALLOC_AFTER")
+    monkeypatch.delenv("FORT_SCOPE_TEST_FAIL_ALLOC_AFTER")
+    assert list(outputs) == [123, 456]
+    assert (scope.stats().uploads, scope.stats().allocations) == (0, 1)
+    for h in (first, second):
+        assert both.fort_scope_host_begin(scope.handle, h, c.byref(abi.access(flags=abi.READ_ALL))) == \
+            abi.UNINITIALIZED
+        assert both.fort_scope_host_begin(scope.handle, h, c.byref(write)) == abi.OK
+        assert both.fort_scope_cancel_access(scope.handle, h) == abi.OK
+    assert both.fort_scope_close(scope.handle) == abi.OK
+
+
+def test_a_batch_over_the_budget_allocates_nothing(both):
+    """(reference: test_scoped_access_batch.py:187-197)"""
+    scope = abi.Scope(both)
+    _, first = _counted(scope, 1)
+    _, second = _counted(scope, 2)
+    assert both.fort_scope_set_device_budget(scope.handle, 64) == abi.OK
+    outputs = (c.c_void_p * 2)(123, 456)
+    read = abi.access(flags=abi.READ_ALL)
+    assert _batch(both, scope, [(first, read), (second, read)], device=True, outputs=outputs) == abi.RESOURCE
+    assert list(outputs) == [123, 456]
+    assert (scope.stats().allocations, scope.stats().upload_bytes) == (0, 0)
+    assert both.fort_scope_close(scope.handle) == abi.OK
+
+
+def test_a_cancelled_batch_keeps_definitions_and_device_values(both):
+    """A host batch that may write part of an array brings that part home first; cancelling it defines nothing
+    new and leaves the device's latest values valid (reference: test_scoped_access_batch.py:200-225)."""
+    scope = abi.Scope(both)
+    values, first = _counted(scope, 1, initialized=False)
+    _, second = _counted(scope, 2, initialized=False)
+    middle = [((2,), (6,))]
+    status, dev = _device_begin(scope, first, abi.access(write=middle, overwrite=middle))
+    assert status == abi.OK
+    _dev(dev, 8)[2:6] = 1000.0 + np.arange(2, 6)
+    assert both.fort_scope_device_end(scope.handle, first) == abi.OK
+    assert _batch(both, scope, [(first, abi.access(write=middle)),
+                                (second, abi.access(flags=abi.WRITE_ALL | abi.OVERWRITE_ALL))]) == abi.OK
+    assert values.tolist()[2:6] == [1002.0, 1003.0, 1004.0, 1005.0]
+    for h in (first, second):
+        assert both.fort_scope_cancel_access(scope.handle, h) == abi.OK
+    for h in (first, second):
+        assert both.fort_scope_host_begin(scope.handle, h, c.byref(abi.access(flags=abi.READ_ALL))) == \
+            abi.UNINITIALIZED
+    status, dev = _device_begin(scope, first, abi.access(read=middle))
+    assert status == abi.OK and _dev(dev, 8)[2:6].tolist() == [1002.0, 1003.0, 1004.0, 1005.0]
+    assert both.fort_scope_device_end(scope.handle, first) == abi.OK
+    assert both.fort_scope_close(scope.handle) == abi.OK
+
+
+def test_an_empty_batch_waits_for_nothing_and_an_overwrite_fences_an_upload(both, monkeypatch):
+    """An empty batch neither waits nor fails; a host overwrite of an array whose upload may still be reading it
+    waits once, and the device then sees the new value (reference: test_scoped_access_batch.py:228-245)."""
+    scope = abi.Scope(both)
+    values, h = _counted(scope, 1)
+    status, _ = _device_begin(scope, h, abi.access(flags=abi.READ_ALL))
+    assert status == abi.OK
+    assert both.fort_scope_device_end(scope.handle, h) == abi.OK
+    waits = scope.stats().waits
+    _inject(monkeypatch, "WAIT")
+    assert _batch(both, scope, []) == abi.OK and scope.stats().waits == waits
+    monkeypatch.delenv("F2C_TEST_FAIL_WAIT")
+    monkeypatch.delenv("FORT_SCOPE_TEST_FAIL_WAIT")
+    assert _batch(both, scope, [(h, abi.access(flags=abi.WRITE_ALL | abi.OVERWRITE_ALL))]) == abi.OK
+    assert scope.stats().waits == waits + 1
+    values[0] = 555.0
+    assert both.fort_scope_host_end(scope.handle, h) == abi.OK
+    status, dev = _device_begin(scope, h, abi.access(flags=abi.READ_ALL))
+    assert status == abi.OK and _dev(dev, 8)[0] == 555.0
+    assert both.fort_scope_device_end(scope.handle, h) == abi.OK
+    assert both.fort_scope_close(scope.handle) == abi.OK
+
+
+def test_a_failed_wait_in_a_batch_poisons_without_replay(both, monkeypatch):
+    """(reference: test_scoped_access_batch.py:248-261)"""
+    scope = abi.Scope(both)
+    handles = [_counted(scope, identity)[1] for identity in (1, 2)]
+    for h in handles:
+        status, dev = _device_begin(scope, h, abi.access(flags=abi.READ_ALL | abi.WRITE_ALL))
+        assert status == abi.OK
+        _dev(dev, 8)[0] += 100.0
+        assert both.fort_scope_device_end(scope.handle, h) == abi.OK
+    _inject(monkeypatch, "WAIT")
+    items = [(h, abi.access(flags=abi.READ_ALL)) for h in handles]
+    assert _batch(both, scope, items) == abi.EXECUTION
+    assert _batch(both, scope, items) == abi.EXECUTION
+    assert both.fort_scope_close(scope.handle) == abi.EXECUTION
+    assert both.fort_scope_abandon(scope.handle) == abi.OK
+
+
+def test_a_refused_batch_leaves_an_existing_access_alone(both):
+    """A batch naming an array another access already holds is refused; that access stays valid and the batch's
+    other array was never prepared (reference: test_scoped_access_batch.py:275-287)."""
+    scope = abi.Scope(both)
+    _, first = _counted(scope, 1)
+    _, second = _counted(scope, 2)
+    read = abi.access(flags=abi.READ_ALL)
+    assert both.fort_scope_host_begin(scope.handle, first, c.byref(read)) == abi.OK
+    assert _batch(both, scope, [(second, read), (first, read)]) == abi.STATE
+    assert both.fort_scope_host_end(scope.handle, first) == abi.OK
+    assert both.fort_scope_host_begin(scope.handle, second, c.byref(read)) == abi.OK
+    assert both.fort_scope_host_end(scope.handle, second) == abi.OK
+    assert both.fort_scope_close(scope.handle) == abi.OK
+
+
+def test_a_retired_generation_is_refused_before_any_transfer(both):
+    """(reference: test_scoped_access_batch.py:290-307)"""
+    scope = abi.Scope(both)
+    _, first = _counted(scope, 1)
+    old_values, old = _counted(scope, 2)
+    assert both.fort_scope_unregister(scope.handle, old) == abi.OK
+    status, current = scope.register(old_values.ctypes.data, [8], identity=2, generation=2)
+    assert status == abi.OK
+    read = abi.access(flags=abi.READ_ALL)
+    outputs = (c.c_void_p * 2)()
+    before = bytes(scope.stats())
+    assert _batch(both, scope, [(first, read), (old, read)], device=True, outputs=outputs) == abi.STALE
+    assert bytes(scope.stats()) == before
+    assert _batch(both, scope, [(first, read), (current, read)], device=True, outputs=outputs) == abi.OK
+    for h in (first, current):
+        assert both.fort_scope_device_end(scope.handle, h) == abi.OK
+    assert both.fort_scope_close(scope.handle) == abi.OK
+
+
+def test_empty_arrays_and_empty_batches_allocate_and_wait_for_nothing(both, monkeypatch):
+    """(reference: test_scoped_access_batch.py:310-324)"""
+    scope = abi.Scope(both)
+    status, h = scope.register(None, [0], identity=5, initialized=False)
+    assert status == abi.OK
+    _inject(monkeypatch, "ALLOC")
+    assert both.fort_scope_access_begin_v1(scope.handle, None, 0, 1, None) == abi.OK
+    outputs = (c.c_void_p * 1)(123)
+    assert _batch(both, scope, [(h, abi.access(flags=7))], device=True, outputs=outputs) == abi.OK
+    assert outputs[0] is None
+    assert both.fort_scope_device_end(scope.handle, h) == abi.OK
+    assert _batch(both, scope, [(h, abi.access(flags=abi.READ_ALL))]) == abi.OK
+    assert both.fort_scope_host_end(scope.handle, h) == abi.OK
+    assert bytes(scope.stats()) == bytes(abi.Stats())
+    assert both.fort_scope_close(scope.handle) == abi.OK
+
+
 def test_budget_eviction_publishes_dirty_values(both):
     scope = abi.Scope(both)
     a, pa = _array(np.zeros(128))
