@@ -136,6 +136,8 @@ struct Backend {
         return true;
     }
     static bool sync(Stream) { return !std::getenv("F2C_TEST_FAIL_WAIT"); }
+    // A scratch arena cannot be allocated (tests only).
+    static bool scratch_alloc_fails() { return std::getenv("F2C_TEST_FAIL_SCRATCH_ALLOC") != nullptr; }
     // An external provider's effects fail to commit after it ran (tests only).
     static bool external_commit_fails() { return std::getenv("F2C_TEST_FAIL_EXTERNAL_COMMIT") != nullptr; }
     // Completion events. Work here is synchronous, but an event reads as pending
@@ -263,6 +265,7 @@ struct Backend {
     }
     static bool sync(Stream s) { return ok(cudaStreamSynchronize(s)); }
     static bool external_commit_fails() { return false; }
+    static bool scratch_alloc_fails() { return false; }
     using Event = cudaEvent_t;
     static bool make_event(Event *e) { return ok(cudaEventCreateWithFlags(e, cudaEventDisableTiming)); }
     static void destroy_event(Event e) {

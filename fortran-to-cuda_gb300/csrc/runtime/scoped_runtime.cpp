@@ -151,6 +151,7 @@ struct Domain {
     // device memory external providers allocated themselves, claimed against the same budget
     std::map<uint64_t, size_t> workspaces;
     size_t workspace_bytes = 0;
+    size_t peak_total_bytes = 0;  // the most mirrors, scratch and workspace held at once
     fort_scope_stats stats{};
     fort_scope_residency_stats_v1 residency{};
     uint64_t tick = 0;
@@ -751,7 +752,8 @@ void reserve(Context *c, const std::vector<Buffer *> &list, bool allow_in_place)
         d->device_bytes += b->bytes;
         d->stats.allocations++;
         d->stats.allocated_bytes += b->bytes;
-        if (claimed(d) > d->stats.peak_device_bytes) d->stats.peak_device_bytes = claimed(d);
+        if (d->device_bytes > d->stats.peak_device_bytes) d->stats.peak_device_bytes = d->device_bytes;
+        if (claimed(d) > d->peak_total_bytes) d->peak_total_bytes = claimed(d);
         b->device_valid.clear();
     }
 }
@@ -1533,6 +1535,7 @@ int fort_scope_domain_workspace_reserve_v1(fort_scope_domain_t domain, size_t by
         const uint64_t token = new_handle();
         d->workspaces[token] = bytes;
         d->workspace_bytes += bytes;
+        if (claimed(d) > d->peak_total_bytes) d->peak_total_bytes = claimed(d);
         *lease = token;
         return FORT_SCOPE_OK;
     });
@@ -1547,6 +1550,7 @@ int fort_scope_domain_workspace_resize_v1(fort_scope_domain_t domain, uint64_t l
         if (bytes > SIZE_MAX - others) raise(FORT_SCOPE_RESOURCE, "workspace byte overflow");
         fit_workspace(d, others + bytes);
         d->workspace_bytes = others + bytes;
+        if (claimed(d) > d->peak_total_bytes) d->peak_total_bytes = claimed(d);
         it->second = bytes;
         return FORT_SCOPE_OK;
     });
@@ -2096,26 +2100,31 @@ int fort_scope_completion_stats_get_v1(fort_scope_t context, fort_scope_completi
 int fort_scope_scratch_acquire_v1(fort_scope_t context, size_t bytes, fort_scope_scratch_lease_v1 *lease) {
     return guarded([&] {
         if (!lease) raise(FORT_SCOPE_ARGUMENT, "null lease output");
+        *lease = fort_scope_scratch_lease_v1{};  // a refused acquisition leaves a cleared lease
         Context *c = live_context(context);
         if (c->scratch_active) raise(FORT_SCOPE_STATE, "context already holds a scratch lease");
         if (bytes) {
             if (bytes > c->scratch_capacity) {
-                ensure_stream(c);
                 const size_t grow = bytes - c->scratch_capacity;
-                make_room(c, grow, {});
+                Domain *d = c->domain;
+                // the arena fits beside what the domain holds, mirrors included (it evicts none of them), or
+                // the lease is refused before the device is used
+                if (d->budget_set && (claimed(d) > d->budget || grow > d->budget - claimed(d)))
+                    raise(FORT_SCOPE_RESOURCE, "scratch lease exceeds the free device budget");
+                ensure_stream(c);
                 if (c->scratch) {
                     wait_stream(c); // complete earlier uses before the old arena is retired
                     release_scratch(c);
                     c->scratch_stats.grows++;
                 }
                 void *p = nullptr;
-                if (!Backend::alloc(&p, bytes, c->stream)) raise(FORT_SCOPE_RESOURCE, "scratch allocation failed");
+                if (Backend::scratch_alloc_fails() || !Backend::alloc(&p, bytes, c->stream))
+                    raise(FORT_SCOPE_RESOURCE, "scratch allocation failed");
                 c->scratch = p;
                 c->scratch_capacity = bytes;
                 c->domain->scratch_bytes += bytes;
                 c->scratch_stats.allocations++;
-                if (claimed(c->domain) > c->domain->stats.peak_device_bytes)
-                    c->domain->stats.peak_device_bytes = claimed(c->domain);
+                if (claimed(c->domain) > c->domain->peak_total_bytes) c->domain->peak_total_bytes = claimed(c->domain);
             } else {
                 c->scratch_stats.reuses++;
             }
@@ -2137,7 +2146,7 @@ int fort_scope_scratch_acquire_v1(fort_scope_t context, size_t bytes, fort_scope
 
 int fort_scope_scratch_release_v1(fort_scope_t context, uint64_t token) {
     return guarded([&] {
-        Context *c = find_context(context);
+        Context *c = live_context(context);
         if (!c->scratch_active || token != c->scratch_token) raise(FORT_SCOPE_STALE, "not the active scratch lease");
         c->scratch_active = false;
         c->scratch_active_bytes = 0;
@@ -2155,7 +2164,7 @@ int fort_scope_scratch_stats_get_v1(fort_scope_t context, fort_scope_scratch_sta
         stats->active = c->scratch_active;
         stats->capacity_bytes = c->scratch_capacity;
         stats->active_bytes = c->scratch_active_bytes;
-        stats->peak_total_device_bytes = c->domain->stats.peak_device_bytes;
+        stats->peak_total_device_bytes = c->domain->peak_total_bytes;
         return FORT_SCOPE_OK;
     });
 }

@@ -85,7 +85,7 @@ typedef struct fort_scope_layout {
 typedef struct fort_scope_stats {
     uint64_t uploads, downloads, upload_bytes, download_bytes;
     /* allocations: device mirrors allocated so far; allocated_bytes: the bytes mirrors hold now;
-     * peak_device_bytes: the most the domain held at once (mirrors, scratch and workspace) */
+     * peak_device_bytes: the most mirrors held at once (scratch has its own statistics) */
     uint64_t allocations, allocated_bytes, peak_device_bytes;
     uint64_t launches, waits, reconciliations;
 } fort_scope_stats;

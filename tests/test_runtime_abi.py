@@ -1377,6 +1377,280 @@ def test_scratch_leases(both):
     assert both.fort_scope_close(scope.handle) == abi.OK
 
 
+def _lease(lib, scope, size):
+    lease = abi.ScratchLease()
+    assert lib.fort_scope_scratch_acquire_v1(scope.handle, size, c.byref(lease)) == abi.OK
+    assert (lease.version, lease.reserved, lease.bytes) == (1, 0, size) and lease.token and lease.capacity >= size
+    return lease
+
+
+def _scratch(lib, scope):
+    out = abi.ScratchStats()
+    assert lib.fort_scope_scratch_stats_get_v1(scope.handle, c.byref(out)) == abi.OK and out.version == 1
+    return out
+
+
+def test_an_empty_lease_allocates_nothing(both, monkeypatch):
+    """A zero-byte lease has no storage, allocates nothing and leaves the budget open to change (reference:
+    test_scoped_scratch.py:89-105)."""
+    scope = abi.Scope(both)
+    _inject(monkeypatch, "ALLOC")
+    lease = _lease(both, scope, 0)
+    assert lease.device is None and lease.capacity == 0
+    assert both.fort_scope_set_device_budget(scope.handle, 0) == abi.OK
+    stats = _scratch(both, scope)
+    assert (stats.active, stats.acquisitions, stats.allocations, stats.capacity_bytes) == (1, 1, 0, 0)
+    assert both.fort_scope_scratch_release_v1(scope.handle, lease.token) == abi.OK
+    assert both.fort_scope_close(scope.handle) == abi.OK
+
+
+@pytest.mark.parametrize("budget, size", [(0, 1), (64, (1 << (8 * c.sizeof(abi.SIZE))) - 1)])
+def test_an_impossible_lease_fails_before_the_device_is_used(both, budget, size):
+    """(reference: test_scoped_scratch.py:108-121)"""
+    scope = abi.Scope(both)
+    assert both.fort_scope_set_device_budget(scope.handle, budget) == abi.OK
+    out = abi.ScratchLease()
+    assert both.fort_scope_scratch_acquire_v1(scope.handle, size, c.byref(out)) == abi.RESOURCE
+    assert bytes(out) == bytes(abi.ScratchLease())
+    assert both.fort_scope_set_device_budget(scope.handle, 0) == abi.OK     # still before any device use
+    assert both.fort_scope_close(scope.handle) == abi.OK
+
+
+def test_one_lease_at_a_time_and_tokens_never_return(both):
+    """One active lease per context; a second acquisition is refused and its output cleared; tokens are the
+    context's own and never reused; a closed context's tokens are stale (reference: test_scoped_scratch.py:124-146)."""
+    first, second = abi.Scope(both), abi.Scope(both)
+    assert both.fort_scope_scratch_acquire_v1(first.handle, 0, None) == abi.ARGUMENT
+    assert both.fort_scope_scratch_stats_get_v1(first.handle, None) == abi.ARGUMENT
+    lease, other = _lease(both, first, 0), _lease(both, second, 0)
+    rejected = abi.ScratchLease(9, 9, 99, 17, 23, 23)
+    assert both.fort_scope_scratch_acquire_v1(first.handle, 0, c.byref(rejected)) == abi.STATE
+    assert bytes(rejected) == bytes(abi.ScratchLease())
+    assert both.fort_scope_scratch_release_v1(second.handle, lease.token) == abi.STALE
+    assert both.fort_scope_scratch_release_v1(first.handle, 0) == abi.STALE
+    assert both.fort_scope_scratch_release_v1(first.handle, lease.token) == abi.OK
+    assert both.fort_scope_scratch_release_v1(first.handle, lease.token) == abi.STALE
+    renewed = _lease(both, first, 0)
+    assert len({lease.token, other.token, renewed.token}) == 3
+    assert both.fort_scope_scratch_release_v1(first.handle, lease.token) == abi.STALE
+    assert both.fort_scope_scratch_release_v1(first.handle, renewed.token) == abi.OK
+    assert both.fort_scope_scratch_release_v1(second.handle, other.token) == abi.OK
+    assert both.fort_scope_close(first.handle) == abi.OK and both.fort_scope_close(second.handle) == abi.OK
+    assert both.fort_scope_scratch_release_v1(first.handle, renewed.token) == abi.STALE
+    assert both.fort_scope_scratch_stats_get_v1(first.handle, c.byref(abi.ScratchStats())) == abi.STALE
+
+
+def test_a_reused_arena_keeps_its_capacity_without_waiting(both):
+    """A smaller lease reuses the arena and its contents; nothing waits, publishes or counts as a mirror
+    (reference: test_scoped_scratch.py:149-176)."""
+    scope = abi.Scope(both)
+    lease = _lease(both, scope, 64)
+    (c.c_uint64 * 8).from_address(lease.device)[:] = list(range(8))
+    assert both.fort_scope_note_launch(scope.handle) == abi.OK
+    assert both.fort_scope_scratch_release_v1(scope.handle, lease.token) == abi.OK
+    waits = scope.stats().waits
+    smaller = _lease(both, scope, 24)
+    assert (smaller.device, smaller.capacity) == (lease.device, 64)
+    assert list((c.c_uint64 * 8).from_address(smaller.device)) == list(range(8))
+    assert both.fort_scope_scratch_release_v1(scope.handle, smaller.token) == abi.OK
+    empty = _lease(both, scope, 0)
+    assert empty.device is None and empty.capacity == 64
+    assert both.fort_scope_scratch_release_v1(scope.handle, empty.token) == abi.OK
+    assert scope.stats().waits == waits == 0
+    stats = _scratch(both, scope)
+    assert (stats.acquisitions, stats.allocations, stats.reuses, stats.releases, stats.grows) == (3, 1, 1, 3, 0)
+    assert stats.capacity_bytes == stats.peak_scratch_bytes == stats.peak_total_device_bytes == 64
+    assert not stats.active and stats.active_bytes == 0
+    mirrors = scope.stats()
+    assert (mirrors.allocations, mirrors.allocated_bytes, mirrors.peak_device_bytes) == (0, 0, 0)
+    assert both.fort_scope_close(scope.handle) == abi.OK
+
+
+def test_a_growing_arena_waits_for_its_old_work(both):
+    """(reference: test_scoped_scratch.py:179-192)"""
+    scope = abi.Scope(both)
+    assert both.fort_scope_set_device_budget(scope.handle, 96) == abi.OK
+    initial = _lease(both, scope, 64)
+    assert both.fort_scope_note_launch(scope.handle) == abi.OK
+    assert both.fort_scope_scratch_release_v1(scope.handle, initial.token) == abi.OK
+    grown = _lease(both, scope, 96)
+    assert grown.capacity == 96
+    stats = _scratch(both, scope)
+    assert (stats.allocations, stats.grows, stats.capacity_bytes, stats.peak_total_device_bytes) == (2, 1, 96, 96)
+    assert scope.stats().waits == 1
+    assert both.fort_scope_scratch_release_v1(scope.handle, grown.token) == abi.OK
+    assert both.fort_scope_close(scope.handle) == abi.OK
+
+
+@pytest.mark.parametrize("scratch_first", [False, True])
+def test_scratch_and_mirrors_share_the_budget_without_evicting_each_other(both, scratch_first):
+    """(reference: test_scoped_scratch.py:195-223)"""
+    scope = abi.Scope(both)
+    assert both.fort_scope_set_device_budget(scope.handle, 160) == abi.OK
+    values, address = _array(np.arange(16, dtype=np.float64))
+    _, h = scope.register(address, [16])
+    if scratch_first:
+        lease = _lease(both, scope, 64)
+        assert both.fort_scope_scratch_release_v1(scope.handle, lease.token) == abi.OK
+        assert _device_begin(scope, h, abi.access(flags=abi.READ_ALL))[0] == abi.RESOURCE
+        assert scope.stats().allocations == 0 and _scratch(both, scope).capacity_bytes == 64
+    else:
+        assert _device_begin(scope, h, abi.access(flags=abi.READ_ALL))[0] == abi.OK
+        assert both.fort_scope_device_end(scope.handle, h) == abi.OK
+        rejected = abi.ScratchLease()
+        assert both.fort_scope_scratch_acquire_v1(scope.handle, 64, c.byref(rejected)) == abi.RESOURCE
+        assert bytes(rejected) == bytes(abi.ScratchLease()) and _scratch(both, scope).capacity_bytes == 0
+        lease = _lease(both, scope, 32)
+        assert both.fort_scope_scratch_release_v1(scope.handle, lease.token) == abi.OK
+        assert _scratch(both, scope).peak_total_device_bytes == 160
+        assert scope.stats().peak_device_bytes == 128
+    assert both.fort_scope_close(scope.handle) == abi.OK
+    assert values.tolist() == list(range(16))
+
+
+def test_releasing_a_mirror_makes_room_for_scratch(both):
+    """(reference: test_scoped_scratch.py:226-242)"""
+    scope = abi.Scope(both)
+    assert both.fort_scope_set_device_budget(scope.handle, 160) == abi.OK
+    _, address = _array(np.arange(16, dtype=np.float64))
+    _, h = scope.register(address, [16])
+    assert _device_begin(scope, h, abi.access(flags=abi.READ_ALL))[0] == abi.OK
+    assert both.fort_scope_device_end(scope.handle, h) == abi.OK
+    first = _lease(both, scope, 32)
+    assert both.fort_scope_scratch_release_v1(scope.handle, first.token) == abi.OK
+    assert both.fort_scope_unregister(scope.handle, h) == abi.OK
+    grown = _lease(both, scope, 160)
+    assert both.fort_scope_scratch_release_v1(scope.handle, grown.token) == abi.OK
+    assert scope.stats().allocated_bytes == 0 and _scratch(both, scope).peak_total_device_bytes == 160
+    assert both.fort_scope_close(scope.handle) == abi.OK
+
+
+def test_an_active_lease_blocks_close_before_publication(both):
+    """(reference: test_scoped_scratch.py:245-261)"""
+    scope = abi.Scope(both)
+    values, address = _array(np.arange(4, dtype=np.float64))
+    _, h = scope.register(address, [4])
+    status, dev = _device_begin(scope, h, abi.access(flags=abi.WRITE_ALL | abi.OVERWRITE_ALL))
+    assert status == abi.OK
+    _dev(dev, 4)[:] = 10.0 + np.arange(4)
+    assert both.fort_scope_device_end(scope.handle, h) == abi.OK
+    lease = _lease(both, scope, 32)
+    assert both.fort_scope_close(scope.handle) == abi.STATE
+    assert values.tolist() == list(range(4)) and scope.stats().downloads == 0
+    assert both.fort_scope_scratch_release_v1(scope.handle, lease.token) == abi.OK
+    assert both.fort_scope_close(scope.handle) == abi.OK
+    assert values.tolist() == [10.0, 11.0, 12.0, 13.0]
+
+
+@pytest.mark.parametrize("growing", [False, True])
+def test_a_failed_scratch_allocation_grants_nothing(both, monkeypatch, growing):
+    """(reference: test_scoped_scratch.py:264-280)"""
+    scope = abi.Scope(both)
+    if growing:
+        lease = _lease(both, scope, 32)
+        assert both.fort_scope_scratch_release_v1(scope.handle, lease.token) == abi.OK
+    _inject(monkeypatch, "SCRATCH_ALLOC")
+    failed = abi.ScratchLease(1, 0, 9, 1, 64, 64)
+    assert both.fort_scope_scratch_acquire_v1(scope.handle, 64, c.byref(failed)) == abi.RESOURCE
+    assert bytes(failed) == bytes(abi.ScratchLease())
+    stats = _scratch(both, scope)
+    assert stats.active == stats.capacity_bytes == 0
+    monkeypatch.delenv("F2C_TEST_FAIL_SCRATCH_ALLOC")
+    monkeypatch.delenv("FORT_SCOPE_TEST_FAIL_SCRATCH_ALLOC")
+    recovered = _lease(both, scope, 64)
+    assert both.fort_scope_scratch_release_v1(scope.handle, recovered.token) == abi.OK
+    assert both.fort_scope_close(scope.handle) == abi.OK
+
+
+def test_a_refused_growth_keeps_the_idle_arena(both):
+    """(reference: test_scoped_scratch.py:283-295)"""
+    scope = abi.Scope(both)
+    assert both.fort_scope_set_device_budget(scope.handle, 64) == abi.OK
+    initial = _lease(both, scope, 64)
+    assert both.fort_scope_scratch_release_v1(scope.handle, initial.token) == abi.OK
+    out = abi.ScratchLease()
+    assert both.fort_scope_scratch_acquire_v1(scope.handle, 65, c.byref(out)) == abi.RESOURCE
+    assert bytes(out) == bytes(abi.ScratchLease())
+    renewed = _lease(both, scope, 64)
+    assert renewed.device == initial.device
+    assert both.fort_scope_scratch_release_v1(scope.handle, renewed.token) == abi.OK
+    assert both.fort_scope_close(scope.handle) == abi.OK
+
+
+def test_a_failed_wait_while_growing_poisons(both, monkeypatch):
+    """(reference: test_scoped_scratch.py:298-311)"""
+    scope = abi.Scope(both)
+    lease = _lease(both, scope, 32)
+    assert both.fort_scope_note_launch(scope.handle) == abi.OK
+    assert both.fort_scope_scratch_release_v1(scope.handle, lease.token) == abi.OK
+    _inject(monkeypatch, "WAIT")
+    out = abi.ScratchLease()
+    assert both.fort_scope_scratch_acquire_v1(scope.handle, 64, c.byref(out)) == abi.EXECUTION
+    assert bytes(out) == bytes(abi.ScratchLease())
+    assert both.fort_scope_close(scope.handle) == abi.EXECUTION
+    assert both.fort_scope_scratch_acquire_v1(scope.handle, 0, c.byref(out)) == abi.EXECUTION
+    assert both.fort_scope_abandon(scope.handle) == abi.OK
+    assert both.fort_scope_scratch_release_v1(scope.handle, lease.token) == abi.STALE
+
+
+def test_close_publishes_fields_and_retires_the_idle_arena(both):
+    """(reference: test_scoped_scratch.py:314-329)"""
+    scope = abi.Scope(both)
+    fields = []
+    for identity in (1, 2):
+        host, address = _array(np.arange(8, dtype=np.float64))
+        fields.append(host)
+        _, h = scope.register(address, [8], identity=identity, lower=[-identity])
+        status, dev = _device_begin(scope, h, abi.access(flags=abi.READ_ALL | abi.WRITE_ALL))
+        assert status == abi.OK
+        _dev(dev, 8)[:] = 100.0 * identity + np.arange(8)
+        assert both.fort_scope_device_end(scope.handle, h) == abi.OK
+    lease = _lease(both, scope, 256)
+    assert both.fort_scope_scratch_release_v1(scope.handle, lease.token) == abi.OK
+    assert both.fort_scope_close(scope.handle) == abi.OK
+    assert [f.tolist() for f in fields] == [[100.0 * n + i for i in range(8)] for n in (1, 2)]
+    assert both.fort_scope_wait(scope.handle) == abi.STALE
+
+
+def test_a_failed_wait_at_close_poisons(both, monkeypatch):
+    """(reference: test_scoped_scratch.py:332-347)"""
+    scope = abi.Scope(both)
+    _, address = _array(np.arange(8, dtype=np.float64))
+    _, h = scope.register(address, [8])
+    status, dev = _device_begin(scope, h, abi.access(flags=abi.READ_ALL | abi.WRITE_ALL))
+    assert status == abi.OK
+    _dev(dev, 8)[0] = 100.0
+    assert both.fort_scope_device_end(scope.handle, h) == abi.OK
+    lease = _lease(both, scope, 256)
+    assert both.fort_scope_scratch_release_v1(scope.handle, lease.token) == abi.OK
+    _inject(monkeypatch, "WAIT")
+    assert both.fort_scope_close(scope.handle) == abi.EXECUTION
+    assert both.fort_scope_host_begin(scope.handle, h, c.byref(abi.access(flags=abi.READ_ALL))) == abi.EXECUTION
+    assert both.fort_scope_abandon(scope.handle) == abi.OK
+    assert both.fort_scope_wait(scope.handle) == abi.STALE
+
+
+@pytest.mark.parametrize("active", [False, True])
+def test_abandonment_is_for_failed_contexts_and_publishes_nothing(both, active):
+    """A healthy context cannot be abandoned; after an execution error it can, its scratch is retired and nothing
+    is published (reference: test_scoped_scratch.py:350-368)."""
+    scope = abi.Scope(both)
+    values, address = _array(np.arange(4, dtype=np.float64))
+    _, h = scope.register(address, [4])
+    status, dev = _device_begin(scope, h, abi.access(flags=abi.WRITE_ALL | abi.OVERWRITE_ALL))
+    assert status == abi.OK
+    _dev(dev, 4)[:] = 10.0 + np.arange(4)
+    assert both.fort_scope_device_end(scope.handle, h) == abi.OK
+    lease = _lease(both, scope, 32)
+    if not active:
+        assert both.fort_scope_scratch_release_v1(scope.handle, lease.token) == abi.OK
+    assert both.fort_scope_abandon(scope.handle) == abi.STATE
+    assert both.fort_scope_execution_error(scope.handle, b"injected numerical failure") == abi.EXECUTION
+    assert both.fort_scope_scratch_release_v1(scope.handle, lease.token) == abi.EXECUTION
+    assert both.fort_scope_abandon(scope.handle) == abi.OK
+    assert values.tolist() == list(range(4))
+
+
 def test_domain_outlives_borrowing_context(both):
     domain = abi.U64()
     assert both.fort_scope_domain_create_v1(0, c.byref(domain)) == abi.OK
