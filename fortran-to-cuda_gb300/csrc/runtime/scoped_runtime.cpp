@@ -171,6 +171,14 @@ struct Context {
     uint64_t queue_work_limit = uint64_t(1) << 18;
     std::vector<Task> pending;
     uint64_t pending_threads = 0;
+    // Each array's coherence state before the first queued task touched it: cancelling the queue restores
+    // them (queued tasks apply their effects when accepted, and a cancelled task must leave none).
+    struct Before {
+        Region defined, host_valid, device_valid, physical;
+        bool host_touched;
+        int host_rounds;
+    };
+    std::map<uint64_t, Before> queued_before;
     std::map<uint64_t, CachedGraph> graphs;
     fort_scope_graph_stats_v1 graph_stats{};
     fort_scope_graph_queue_stats_v1 queue_stats{};
@@ -856,6 +864,7 @@ void submit(Context *c, std::vector<Task> &tasks, uint64_t key) {
 }
 
 void flush(Context *c) {
+    c->queued_before.clear();
     if (c->pending.empty()) return;
     std::vector<Task> tasks;
     tasks.swap(c->pending);
@@ -1049,6 +1058,11 @@ void accept(Context *c, Task &&task, std::vector<Bound> &bound) {
         if (!x.buffer->device && !x.buffer->in_place && x.buffer->bytes)
             raise(FORT_SCOPE_STATE, "task binds an array whose device storage is not reserved");
     ensure_stream(c);
+    for (auto &x : bound) {
+        const Buffer *b = x.buffer;
+        c->queued_before.emplace(b->handle, Context::Before{b->defined, b->host_valid, b->device_valid, b->physical,
+                                                             b->host_touched, b->host_rounds});
+    }
     std::vector<Bound> mirrored, in_place;
     for (auto &x : bound) (x.buffer->in_place ? in_place : mirrored).push_back(x);
     device_acquire(c, mirrored);
@@ -2263,7 +2277,7 @@ int fort_scope_graph_enqueue_members_v1(fort_scope_t context, uint64_t code_key,
                                         const size_t *argument_sizes, const fort_scope_graph_member_v1 *members,
                                         size_t member_count) {
     return guarded([&] {
-        if (!kernel || (member_count && !members)) raise(FORT_SCOPE_ARGUMENT, "null merged launch");
+        if (!kernel || !member_count || !members) raise(FORT_SCOPE_ARGUMENT, "a merged launch needs members");
         Context *c = live_context(context);
         Task t = make_task(code_key, *kernel, argument_sizes);
         std::vector<std::vector<Bound>> each;
@@ -2312,8 +2326,26 @@ int fort_scope_graph_flush_v1(fort_scope_t context) {
 int fort_scope_graph_queue_cancel_v1(fort_scope_t context) {
     return guarded([&] {
         Context *c = live_context(context);
-        if (!c->pending.empty())
-            raise(FORT_SCOPE_STATE, "accepted tasks already committed their effects; flush them instead");
+        // the queued tasks never run: every array they touched gets back its state from before them (values
+        // their uploads already moved stay on the device, no longer counted as current there)
+        for (auto &kv : c->queued_before) {
+            auto it = c->domain->buffers.find(kv.first);
+            if (it == c->domain->buffers.end()) continue;
+            Buffer *b = it->second.get();
+            b->defined = kv.second.defined;
+            b->host_valid = kv.second.host_valid;
+            b->device_valid = kv.second.device_valid;
+            b->physical = kv.second.physical;
+            b->host_touched = kv.second.host_touched;
+            b->host_rounds = kv.second.host_rounds;
+            b->queued = 0;
+            b->awaits_token = false;
+        }
+        c->queued_before.clear();
+        c->awaiting_token.clear();
+        c->pending.clear();
+        c->pending_threads = 0;
+        c->queue_stats.pending_tasks = 0;
         return FORT_SCOPE_OK;
     });
 }

@@ -1651,6 +1651,68 @@ def test_abandonment_is_for_failed_contexts_and_publishes_nothing(both, active):
     assert values.tolist() == list(range(4))
 
 
+def _members(lib, scope, key, *members):
+    """Enqueue one launch of independent members (each a list of (handle, access)); never submitted here."""
+    value = c.c_int(7)
+    arguments = (c.c_void_p * 1)(c.addressof(value))
+    kernel = abi.Kernel(1, 0, 1, (c.c_uint32 * 3)(1, 1, 1), (c.c_uint32 * 3)(32, 1, 1), 0, arguments, 1)
+    packs = [(abi.Binding * len(m))(*[abi.Binding(h, acc) for h, acc in m]) for m in members]
+    packed = (abi.Member * max(1, len(members)))(*[abi.Member(p, len(m)) for p, m in zip(packs, members)])
+    return lib.fort_scope_graph_enqueue_members_v1(scope.handle, key, c.byref(kernel), (abi.SIZE * 1)(4),
+                                                    packed if members else None, len(members))
+
+
+def _reserved(lib, scope, identity, *, initialized=False):
+    host, address = _array(np.arange(8, dtype=np.float64))
+    scope.keep.append(host)                                   # the array outlives the registration
+    status, h = scope.register(address, [8], identity=identity, initialized=initialized)
+    assert status == abi.OK
+    assert lib.fort_scope_device_reserve_v1(scope.handle, h, c.byref(c.c_void_p())) == abi.OK
+    return h
+
+
+def _queue(lib, scope):
+    out = abi.QueueStats()
+    assert lib.fort_scope_graph_queue_stats_get_v1(scope.handle, c.byref(out)) == abi.OK
+    return out
+
+
+def test_members_of_one_array_are_judged_on_their_sections(both):
+    """Members may write disjoint halves of one array; overlapping writes, or a read of what another member
+    writes, refuse the whole launch and leave no trace (reference: test_scoped_graph_queue.py:93-110)."""
+    scope = abi.Scope(both)
+    a = _reserved(both, scope, 1, initialized=True)
+    halves = [abi.access(write=[((0,), (4,))], overwrite=[((0,), (4,))]),
+              abi.access(write=[((4,), (8,))], overwrite=[((4,), (8,))])]
+    assert _members(both, scope, 21, [(a, halves[0])], [(a, halves[1])]) == abi.OK
+    assert _queue(both, scope).pending_tasks == 1
+    before = bytes(_queue(both, scope))
+    overlap = abi.access(write=[((3,), (5,))], overwrite=[((3,), (5,))])
+    assert _members(both, scope, 22, [(a, halves[0])], [(a, overlap)]) == abi.BOUNDARY
+    assert _members(both, scope, 23, [(a, halves[0])], [(a, abi.access(read=[((2,), (3,))]))]) == abi.BOUNDARY
+    assert bytes(_queue(both, scope)) == before
+    assert _members(both, scope, 24, [(a, abi.access(read=[((0,), (8,))]))]) == abi.OK
+    assert _queue(both, scope).pending_tasks == 2
+    assert both.fort_scope_graph_queue_cancel_v1(scope.handle) == abi.OK
+    assert both.fort_scope_close(scope.handle) == abi.OK
+
+
+def test_a_member_launch_validates_like_a_single_task(both):
+    """No members, an array repeated within a member, or a read of undefined values: refused, nothing queued
+    (reference: test_scoped_graph_queue.py:113-123)."""
+    scope = abi.Scope(both)
+    a = _reserved(both, scope, 1)
+    b = _reserved(both, scope, 2)
+    write = abi.access(flags=abi.WRITE_ALL | abi.OVERWRITE_ALL)
+    read = abi.access(flags=abi.READ_ALL)
+    assert _members(both, scope, 31) == abi.ARGUMENT
+    assert _members(both, scope, 32, [(a, write), (a, read)]) == abi.ALIAS
+    assert _members(both, scope, 33, [(a, write)], [(b, read)]) == abi.UNINITIALIZED
+    queued = _queue(both, scope)
+    assert queued.pending_tasks == queued.accepted_tasks == 0
+    assert both.fort_scope_close(scope.handle) == abi.OK
+
+
 def test_domain_outlives_borrowing_context(both):
     domain = abi.U64()
     assert both.fort_scope_domain_create_v1(0, c.byref(domain)) == abi.OK
