@@ -1713,6 +1713,57 @@ def test_a_member_launch_validates_like_a_single_task(both):
     assert both.fort_scope_close(scope.handle) == abi.OK
 
 
+def _queued_task(lib, scope, key, items, *, scalar=7):
+    """Queue one task (never submitted here) over (handle, access) items."""
+    value = c.c_int(scalar)
+    arguments = (c.c_void_p * 1)(c.addressof(value))
+    kernel = abi.Kernel(1, 0, 1, (c.c_uint32 * 3)(1, 1, 1), (c.c_uint32 * 3)(32, 1, 1), 0, arguments, 1)
+    bindings = (abi.Binding * len(items))(*[abi.Binding(h, acc) for h, acc in items])
+    task = abi.Task(kernel, bindings, len(items))
+    return lib.fort_scope_graph_enqueue_v1(scope.handle, key, c.byref(task), (abi.SIZE * 1)(c.sizeof(value)))
+
+
+def test_a_refused_enqueue_keeps_the_queue_it_found(both):
+    """Refused enqueues change nothing queued; a later task may read what an earlier queued task defines; a
+    cancelled queue leaves those definitions undone (reference: test_scoped_graph_queue.py:158-174)."""
+    scope = abi.Scope(both)
+    a = _reserved(both, scope, 1)
+    b = _reserved(both, scope, 2)
+    write = abi.access(flags=abi.WRITE_ALL | abi.OVERWRITE_ALL)
+    read = abi.access(flags=abi.READ_ALL)
+    assert _queued_task(both, scope, 1, [(a, write)]) == abi.OK
+    before = bytes(_queue(both, scope))
+    assert _queued_task(both, scope, 2, [(b, read)]) == abi.UNINITIALIZED
+    assert bytes(_queue(both, scope)) == before
+    assert _queued_task(both, scope, 3, [(2**63, read)]) == abi.STALE
+    assert bytes(_queue(both, scope)) == before
+    assert _queued_task(both, scope, 4, [(a, read), (b, write)]) == abi.OK
+    assert _queue(both, scope).pending_tasks == 2
+    assert both.fort_scope_graph_queue_cancel_v1(scope.handle) == abi.OK
+    assert both.fort_scope_host_begin(scope.handle, a, c.byref(read)) == abi.UNINITIALIZED
+    assert both.fort_scope_close(scope.handle) == abi.OK
+
+
+def test_a_long_queued_chain_runs_nothing_until_submitted(both):
+    """A hundred dependent tasks queue without launching, their arguments copied; cancelled, they leave the
+    array untouched (reference: test_scoped_graph_queue.py:177-189)."""
+    scope = abi.Scope(both)
+    host, address = _array(np.arange(8, dtype=np.float64))
+    scope.keep.append(host)
+    _, h = scope.register(address, [8], identity=1, initialized=False)
+    assert both.fort_scope_device_reserve_v1(scope.handle, h, c.byref(c.c_void_p())) == abi.OK
+    for index in range(100):
+        flags = abi.WRITE_ALL | abi.OVERWRITE_ALL if index == 0 else abi.READ_ALL | abi.WRITE_ALL
+        assert _queued_task(both, scope, index + 1, [(h, abi.access(flags=flags))], scalar=index) == abi.OK
+    queued = _queue(both, scope)
+    assert queued.accepted_tasks == queued.pending_tasks == queued.peak_pending_tasks == 100
+    assert queued.copied_argument_bytes == 100 * c.sizeof(c.c_int)
+    assert scope.stats().launches == 0
+    assert both.fort_scope_graph_queue_cancel_v1(scope.handle) == abi.OK
+    assert both.fort_scope_close(scope.handle) == abi.OK
+    assert host.tolist() == list(range(8))
+
+
 def test_domain_outlives_borrowing_context(both):
     domain = abi.U64()
     assert both.fort_scope_domain_create_v1(0, c.byref(domain)) == abi.OK
