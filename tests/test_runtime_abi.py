@@ -1764,6 +1764,51 @@ def test_a_long_queued_chain_runs_nothing_until_submitted(both):
     assert host.tolist() == list(range(8))
 
 
+@pytest.mark.parametrize("exact_budget", [False, True])
+def test_faces_move_exactly_and_round_trips_move_nothing(both, exact_budget):
+    """The device wrote everything and the host then overwrote the interior: a host read moves just the six
+    halo faces home, a device read moves just the interior back as one copy, and further read-only round trips
+    move nothing (reference: test_scoped_direct_transport.py:13-58)."""
+    x, y, z = 134, 70, 70
+    count = x * y * z
+    scope = abi.Scope(both)
+    if exact_budget:
+        assert both.fort_scope_set_device_budget(scope.handle, count * 8) == abi.OK
+    host, address = _array(np.full(count, -7.0))
+    _, h = scope.register(address, [x, y, z], lower=[-10, 2, -100])
+    status, dev = _device_begin(scope, h, abi.access(flags=abi.WRITE_ALL | abi.OVERWRITE_ALL))
+    assert status == abi.OK
+    _dev(dev, count)[:] = 1000000.0 + np.arange(count)
+    assert both.fort_scope_device_end(scope.handle, h) == abi.OK
+    interior = [((3, 3, 2), (131, 67, 68))]
+    assert both.fort_scope_host_begin(scope.handle, h, c.byref(abi.access(write=interior, overwrite=interior))) == \
+        abi.OK
+    view = host.reshape(z, y, x)
+    view[2:68, 3:67, 3:131] = -42.0
+    assert both.fort_scope_host_end(scope.handle, h) == abi.OK
+    read = abi.access(flags=abi.READ_ALL)
+    assert both.fort_scope_host_begin(scope.handle, h, c.byref(read)) == abi.OK
+    assert both.fort_scope_host_end(scope.handle, h) == abi.OK
+    inner = 128 * 64 * 66
+    stats = scope.stats()
+    assert (stats.downloads, stats.download_bytes) == (6, (count - inner) * 8)
+    expected = 1000000.0 + np.arange(count).reshape(z, y, x)
+    expected[2:68, 3:67, 3:131] = -42.0
+    assert np.array_equal(view, expected)
+    assert _device_begin(scope, h, read)[0] == abi.OK
+    assert both.fort_scope_device_end(scope.handle, h) == abi.OK
+    mirrored = scope.stats()
+    assert (mirrored.uploads, mirrored.upload_bytes) == (1, inner * 8)
+    for _ in range(20):
+        assert both.fort_scope_host_begin(scope.handle, h, c.byref(read)) == abi.OK
+        assert both.fort_scope_host_end(scope.handle, h) == abi.OK
+        assert _device_begin(scope, h, read)[0] == abi.OK
+        assert both.fort_scope_device_end(scope.handle, h) == abi.OK
+    final = scope.stats()
+    assert (final.uploads, final.downloads, final.allocations) == (mirrored.uploads, mirrored.downloads, 1)
+    assert both.fort_scope_close(scope.handle) == abi.OK
+
+
 def test_domain_outlives_borrowing_context(both):
     domain = abi.U64()
     assert both.fort_scope_domain_create_v1(0, c.byref(domain)) == abi.OK
