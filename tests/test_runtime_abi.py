@@ -6,7 +6,11 @@ checkout is present on this machine, against the reference's own runtime built
 with its CPU test switch (oracle/build_ref.py): both must return the same
 statuses, host values and transfer counts. The behaviours restated here are
 those the reference's runtime tests exercise (compiler/tests/test_scoped_runtime.py,
-test_scoped_graph_queue.py, test_scoped_scratch.py, test_scoped_access_batch.py).
+test_scoped_domains.py, test_scoped_graph_replay.py, test_scoped_graph_queue.py,
+test_scoped_host_completion.py, test_scoped_access_batch.py, test_scoped_scratch.py,
+test_scoped_direct_transport.py), each citing the scenario it follows. Scenarios
+that need the reference's CPU build to leave device kernels unrun are not
+restated: this runtime's CPU backend runs test kernels as host functions.
 """
 
 import ctypes as c
