@@ -31,7 +31,7 @@ from dataclasses import dataclass, field
 from pathlib import Path
 
 from .. import emission
-from . import directives, host_access, splice
+from . import directives, fortran, host_access, splice
 
 SUPPORTED = {"name", "sources", "program", "variants", "selection", "edit", "build", "executable", "addressable"}
 UNSUPPORTED = {"inputs", "patch", "rewrite", "held", "domain", "rewrites", "program_edit"}
@@ -50,11 +50,19 @@ class Selection:
 
 @dataclass
 class Edit:
+    """One edit of a source (the reference's format, compiler/resident/application.py:49-57): a place found by
+    ``at`` (text found once, tolerant of layout), ``between`` (from the start of the first text to the end of the
+    second), ``call`` (the CALL statement of that subroutine, from the start of its line) or ``module_end`` (before
+    END MODULE of that module), or with none of them the whole ``procedure``; ``procedure`` also confines the
+    others to that procedure."""
     file: str
     action: str
     text: str
     at: str | None = None
     procedure: str | None = None
+    between: list | None = None
+    call: str | None = None
+    module_end: str | None = None
 
 
 @dataclass
@@ -105,12 +113,23 @@ def load(path, variant: str | None = None) -> Application:
     selections = [Selection(s["label"], list(s["procedures"]), int(s.get("minimum_nests", 0)))
                   for s in data.get("selection", [])]
     edits = []
+    edit_keys = {"file", "action", "text", "template", "at", "procedure", "function", "between", "call", "module_end"}
     for e in data.get("edit", []):
+        unknown_keys = set(e) - edit_keys
+        if unknown_keys:
+            raise DescriptionError(f"{path.name}: unknown keys in edit: {sorted(unknown_keys)}")
         if e.get("action") not in {"before", "after", "replace"}:
             raise DescriptionError(f"{path.name}: edit action must be before, after or replace")
-        if "text" not in e:
-            raise DescriptionError(f"{path.name}: an edit needs text")
-        edits.append(Edit(e["file"], e["action"], e["text"], e.get("at"), e.get("procedure")))
+        if ("text" in e) == ("template" in e):
+            raise DescriptionError(f"{path.name}: an edit needs text or a template, not both")
+        text = e["text"] if "text" in e else (path.parent / e["template"]).read_text()
+        if not any(k in e for k in ("at", "between", "call", "module_end", "procedure")):
+            raise DescriptionError(f"{path.name}: an edit of {e.get('file')!r} locates no place")
+        between = e.get("between")
+        if between is not None and (not isinstance(between, list) or len(between) != 2):
+            raise DescriptionError(f"{path.name}: between takes two pieces of text")
+        edits.append(Edit(e["file"], e["action"], text, e.get("at"), e.get("procedure"), between, e.get("call"),
+                          e.get("module_end")))
     executables = [Executable(x["name"], x.get("library", "resident")) for x in data.get("executable", [])]
     return Application(path, data["name"], sources, program, list(variants[chosen].get("defines", [])),
                        selections, edits, dict(data.get("build", {})), executables, chosen)
@@ -123,18 +142,73 @@ def _locate(text: str, at: str) -> tuple[int, int]:
         start = text.index(at)
         return start, start + len(at)
     if count > 1:
-        raise DescriptionError(f"edit anchor found {count} times: {at!r}")
+        raise DescriptionError(f"edit anchor found {count} times, expected one: {at!r}")
     pattern = re.compile(r"\s+".join(re.escape(w) for w in at.split()) + (r"\s*\n" if at.endswith("\n") else ""))
     found = list(pattern.finditer(text))
     if len(found) != 1:
-        raise DescriptionError(f"edit anchor found {len(found)} times: {at!r}")
+        raise DescriptionError(f"edit anchor found {len(found)} times, expected one: {at!r}")
     return found[0].start(), found[0].end()
 
 
+def _procedure_span(text: str, name: str) -> tuple[int, int]:
+    """Offsets of a procedure (``name`` or ``module::name``) from its header line to the end of its END line."""
+    module, _, proc = name.lower().rpartition("::")
+    lines = text.splitlines(keepends=True)
+    found = [p for p in fortran.procedures(text) if p.name.lower() == proc and (not module or p.module == module)]
+    if len(found) != 1:
+        raise DescriptionError(f"edit: procedure {name!r} found {len(found)} times, expected one")
+    p = found[0]
+    last = p.end
+    if re.match(r"\s*contains\b", lines[last], re.I):  # internal procedures follow: find the unit's own END
+        pattern = re.compile(rf"\s*end\s*(subroutine|function|program)?\s*{re.escape(p.name)}?\s*(!.*)?$", re.I)
+        last = next(i for i in range(last + 1, len(lines))
+                    if pattern.match(lines[i].rstrip("\n")) and re.match(r"\s*end\s*(subroutine|function|program)\b",
+                                                                         lines[i], re.I))
+    start = sum(len(x) for x in lines[:p.header])
+    return start, sum(len(x) for x in lines[:last + 1])
+
+
+def _line_bounds(text: str, at: int) -> tuple[int, int]:
+    """Start of the line holding offset ``at`` and the end of its statement (continuations), before the newline."""
+    start = text.rfind("\n", 0, at) + 1
+    end = text.find("\n", at)
+    end = len(text) if end < 0 else end
+    while text[start:end].split("!", 1)[0].rstrip().endswith("&"):
+        nxt = text.find("\n", end + 1)
+        end = len(text) if nxt < 0 else nxt
+    return start, end
+
+
+def _place(text: str, edit: Edit) -> tuple[int, int]:
+    """The span an edit acts on, as offsets into ``text``."""
+    lo, hi = (0, len(text)) if not edit.procedure else _procedure_span(text, edit.procedure)
+    region = text[lo:hi]
+    if edit.at is not None:
+        start, end = _locate(region, edit.at)
+    elif edit.between is not None:
+        first, _ = _locate(region, edit.between[0])
+        tail_start, end = _locate(region[first:], edit.between[1])
+        end += first
+        start = first
+    elif edit.call is not None:
+        calls = [m for m in re.finditer(rf"(?im)^[ \t]*call[ \t]+{re.escape(edit.call)}\b", region)]
+        if len(calls) != 1:
+            raise DescriptionError(f"edit: CALL {edit.call} found {len(calls)} times, expected one")
+        start, end = _line_bounds(region, calls[0].start())
+    elif edit.module_end is not None:
+        ends = [m for m in re.finditer(rf"(?im)^[ \t]*end[ \t]*module[ \t]+{re.escape(edit.module_end)}\b", region)]
+        if len(ends) != 1:
+            raise DescriptionError(f"edit: END MODULE {edit.module_end} found {len(ends)} times, expected one")
+        start = end = ends[0].start()
+    elif edit.procedure is not None:
+        return lo, hi
+    else:
+        raise DescriptionError("edit: locates no place")
+    return lo + start, lo + end
+
+
 def apply_edit(text: str, edit: Edit) -> str:
-    if edit.at is None:
-        raise DescriptionError("edits need an `at` anchor here")
-    start, end = _locate(text, edit.at)
+    start, end = _place(text, edit)
     if edit.action == "before":
         return text[:start] + edit.text + text[start:]
     if edit.action == "after":

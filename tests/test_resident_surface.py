@@ -299,3 +299,51 @@ def test_fortran_modules_bind_only_declared_c_entry_points():
     for source in (root / "fortran").glob("*.f90"):
         for name in re.findall(r"bind\(C,\s*name='(\w+)'\)", source.read_text()):
             assert re.search(rf"\b{name}\s*\(", headers), f"{source.name}: {name} is not in include/*.h"
+
+
+EDIT_SOURCE = """module m
+contains
+  subroutine first(a)
+    real :: a
+    call helper(a)
+    a = a + 1
+  end subroutine first
+
+  subroutine second(a)
+    real :: a
+    a = a + 1
+  end subroutine second
+end module m
+"""
+
+
+def _edited(**fields):
+    return application.apply_edit(EDIT_SOURCE, application.Edit(file="m.f90", **fields))
+
+
+def test_edits_locate_by_anchor_call_span_procedure_and_module_end():
+    """The reference's edit locators (compiler/resident/application.py:49-57; its tests in
+    test_resident_application_description.py:40-60): an anchor confined to a procedure, a CALL statement from the
+    start of its line, a span between two texts, a whole procedure, and the end of a module."""
+    text = _edited(procedure="second", at="    a = a + 1\n", action="after", text="    a = 2 * a\n")
+    assert "    a = a + 1\n    a = 2 * a\n  end subroutine second" in text
+    with pytest.raises(application.DescriptionError, match="expected one"):
+        _edited(at="    a = a + 1\n", action="after", text="x")
+    text = _edited(procedure="first", call="helper", action="replace", text="    if (on) then\n{original}\n    end if")
+    assert "    if (on) then\n    call helper(a)\n    end if\n" in text
+    text = _edited(procedure="first", between=["call helper", "a = a + 1"], action="replace", text="! gone")
+    assert "    ! gone\n  end subroutine first" in text
+    text = _edited(procedure="second", action="before", text="  subroutine third\n  end subroutine third\n\n")
+    assert text.index("subroutine third") < text.index("subroutine second(a)")
+    text = _edited(module_end="m", action="before", text="\n  ! last\n")
+    assert text.endswith("  end subroutine second\n\n  ! last\nend module m\n")
+
+
+@pytest.mark.parametrize("edit, message", [
+    ("[[edit]]\nfile = 'main.f90'\naction = 'after'\ntext = ''\n", "locates no place"),
+    ("[[edit]]\nfile = 'main.f90'\nat = 'x'\naction = 'after'\ntext = ''\nfloor = 3\n", "unknown keys in edit"),
+    ("[[edit]]\nfile = 'main.f90'\nbetween = ['a']\naction = 'replace'\ntext = ''\n", "two pieces of text"),
+])
+def test_edits_are_checked_where_the_description_is_read(tmp_path, edit, message):
+    with pytest.raises(application.DescriptionError, match=message):
+        application.load(_write_app(tmp_path, extra=edit))
