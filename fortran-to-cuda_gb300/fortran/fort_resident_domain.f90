@@ -11,7 +11,10 @@
 ! array; end_epoch publishes and ends the epoch; close releases the context and
 ! the domain. held answers the handle of the storage an array lies in (0 when
 ! the domain keeps none); host_modify hands arrays to host code that may change
-! them and host_done hands them back. resident_require stops the program on a
+! them and host_done hands them back. observe_field takes the address of one
+! field in the first element of an array of derived type; this domain keeps no
+! such field on the device, so the field is already current on the host and
+! nothing moves. resident_require stops the program on a
 ! nonzero status: work that failed after it started is never replayed.
 module fort_resident_domain
   use, intrinsic :: iso_c_binding
@@ -43,6 +46,7 @@ module fort_resident_domain
     procedure :: host_done
     procedure :: release
     procedure :: observe
+    procedure :: observe_field
     procedure :: publish
     procedure :: end_epoch
     procedure :: close
@@ -224,6 +228,12 @@ contains
     if (size(distinct) == 0) return
     call resident_require(fort_scope_observe_v1(self%context, c_loc(distinct), size(distinct, kind=c_size_t)))
     self%stamp = self%stamp + 1
+  end subroutine
+
+  subroutine observe_field(self, first)
+    class(resident_domain), intent(inout) :: self
+    type(c_ptr), intent(in) :: first
+    ! no field of an array of derived type is ever bound here: nothing to bring back
   end subroutine
 
   subroutine publish(self)

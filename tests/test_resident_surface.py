@@ -109,31 +109,123 @@ def test_directives_expand_to_residency_calls(line, call):
 def test_observe_binds_and_observes_named_arrays():
     text, _ = directives.expand("  !$fort observe(U, V) if(mod(step, 10) == 0)\n", origin="main")
     assert "integer(c_int64_t) :: fort_observed(2)" in text
-    assert "fort_observed(2) = resident%bind_real64(V, lbound(V), .true., origin='main::v')" in text
+    assert "fort_observed(2) = resident%bind(V, lbound(V), .true., origin='main::v')" in text
     assert "if (resident%active .and. (mod(step, 10) == 0)) then" in text
     assert "call resident%observe(fort_observed)" in text
 
 
-def test_annotations_generate_no_code():
-    text, records = directives.expand("  !$fort host\n  !$fort reduction(+: total)\n")
-    assert text.strip() == ""
+DOMAIN = directives.Domain("my_state", "flow", "require", prefix="app")
+
+
+def _expand(line):
+    """One directive between two statements, expanded on the domain ``flow`` of module ``my_state``."""
+    text, records = directives.expand("  x = 1\n" + line + "\n  y = 2\n", DOMAIN, origin="unit")
+    assert text.startswith("  x = 1\n") and text.endswith("  y = 2\n")
+    return text[len("  x = 1\n"):-len("  y = 2\n")], records
+
+
+def test_text_without_directives_is_unchanged():
+    source = "  !$omp parallel do\n  ! $fort is not a directive\n  a = '!$fort publish'\n  !$fortran x\n"
+    assert directives.expand(source, DOMAIN) == (source, [])
+
+
+def test_enter_starts_an_epoch_once_under_its_condition():
+    block, records = _expand("    !$FORT enter budget(2*1024**3) if(supported() .and. (n > 1)) device(gpu)")
+    assert block == ("    block\n"
+                     "      use, intrinsic :: iso_c_binding\n"
+                     "      use my_state, only: flow\n"
+                     "      if (.not. flow%active) then\n"
+                     "        if (supported() .and. (n > 1)) call flow%begin_epoch(int(gpu, c_int), "
+                     "int(2*1024**3, c_size_t))\n"
+                     "      endif\n"
+                     "    end block\n")
+    assert records == [{"line": 2, "directive": "enter", "arrays": [],
+                        "clauses": {"budget": "2*1024**3", "if": "supported() .and. (n > 1)", "device": "gpu"}}]
+    unconditional, _ = _expand("!$fort enter budget(1024)")
+    assert "  if (.not. flow%active) then\n    call flow%begin_epoch(int(0, c_int), int(1024, c_size_t))\n" \
+        in unconditional
+    assert "    call flow%begin_epoch(int(0, c_int))\n" in _expand("!$fort enter")[0]  # the free device memory
+
+
+def test_active_tells_the_source_and_annotations_generate_nothing():
+    block, records = _expand("    !$fort active(on_device)")
+    assert "      on_device = flow%active\n" in block
+    assert records[0]["directive"] == "active"
+    text, records = directives.expand("  do i = 1, n\n    !$fort host\n    s = s + a(i)\n  end do\n"
+                                      "  !$fort reduction(+: s) private(i)\n", DOMAIN)
+    assert text == "  do i = 1, n\n    s = s + a(i)\n  end do\n"
     assert [r["directive"] for r in records] == ["host", "reduction"]
 
 
+def test_leave_close_and_publish_act_on_the_whole_domain():
+    assert "if (flow%active) call flow%end_epoch()" in _expand("!$fort leave")[0]
+    assert "  call flow%close()\n" in _expand("!$fort close")[0]  # also valid when no epoch ever began
+    assert "if (flow%active) call flow%publish()" in _expand("!$fort publish")[0]
+    assert "if (flow%active .and. (count > 0)) call flow%publish()" in _expand("!$fort publish if(count > 0)")[0]
+
+
+def test_observe_binds_the_named_arrays_and_keeps_their_device_copies():
+    block, records = _expand("  !$fort observe(U, state%pressure) if(mode == 2)")
+    assert block == ("  block\n"
+                     "    use, intrinsic :: iso_c_binding\n"
+                     "    use my_state, only: flow\n"
+                     "    integer(c_int64_t) :: app_observed(2)\n"
+                     "    if (flow%active .and. (mode == 2)) then\n"
+                     "      app_observed(1) = flow%bind(U, lbound(U), .true., origin='unit::u')\n"
+                     "      app_observed(2) = flow%bind(state%pressure, lbound(state%pressure), .true., "
+                     "origin='unit::state%pressure')\n"
+                     "      call flow%observe(app_observed)\n"
+                     "    endif\n"
+                     "  end block\n")
+    assert records[0]["arrays"] == ["U", "state%pressure"]
+
+
+def test_observe_brings_one_field_of_an_array_of_derived_type_back():
+    block, records = _expand("!$fort observe(points(:)%seen, u) if(ready)")
+    assert block == ("block\n"
+                     "  use, intrinsic :: iso_c_binding\n"
+                     "  use my_state, only: flow\n"
+                     "  integer(c_int64_t) :: app_observed(1)\n"
+                     "  if (flow%active .and. (ready)) then\n"
+                     "    app_observed(1) = flow%bind(u, lbound(u), .true., origin='unit::u')\n"
+                     "    call flow%observe(app_observed)\n"
+                     "    if (size(points) > 0) call flow%observe_field(c_loc(points(lbound(points,1))%seen))\n"
+                     "  endif\n"
+                     "end block\n")
+    assert records[0]["arrays"] == ["points(:)%seen", "u"]
+    assert "app_observed" not in _expand("!$fort observe(points(:)%seen)")[0]
+    with pytest.raises(ValueError, match="takes array names, not expressions"):
+        directives.expand("!$fort release(points(:)%seen)\n", DOMAIN)
+
+
+def test_release_retires_temporaries_without_bringing_them_back():
+    block, _ = _expand("!$fort release(tmp, work)")
+    assert "if (flow%active) then\n    call flow%release(tmp)\n    call flow%release(work)\n  endif" in block
+
+
 @pytest.mark.parametrize("line, message", [
-    ("!$fort launch", "unknown residency directive"),
-    ("!$fort enter budget", "unsupported clause"),
-    ("!$fort leave if(x)", "unsupported clause"),
-    ("!$fort observe", "needs a list"),
-    ("!$fort close(U)", "takes no list"),
-    ("!$fort observe(U(1:3))", "array names"),
-    ("!$fort active(a, b)", "one logical variable"),
-    ("!$fort observe(U", "unbalanced"),
+    ("!$fort", "Empty residency directive on line 2"),
+    ("!$fort sync", "Unknown residency directive on line 2: sync"),
+    ("!$fort enter budget(1) when(x)", "Unsupported clause"),
+    ("!$fort enter budget(1) if(a", "Unbalanced parentheses"),
+    ("!$fort publish if", "Unsupported clause"),
+    ("!$fort leave(a)", "takes no arguments"),
+    ("!$fort leave if(x)", "Unsupported clause"),
+    ("!$fort close(U)", "takes no arguments"),
+    ("!$fort observe", "needs a list of arrays"),
+    ("!$fort observe(a(1:n))", "takes array names, not expressions"),
+    ("!$fort release(a+b)", "takes array names, not expressions"),
+    ("!$fort publish, if(x)", "Malformed residency directive"),
+    ("!$fort host(a)", "Malformed"),
+    ("!$fort reduction", "Malformed"),
+    ("!$fort reduction(s)", "Malformed"),
+    ("!$fort active", "needs a list"),
+    ("!$fort active(a, b)", "takes one logical variable"),
 ])
 def test_malformed_directives_are_refused_with_their_line(line, message):
     with pytest.raises(directives.DirectiveError, match=message) as info:
-        directives.expand("program p\n\n  " + line + "\nend program p\n")
-    assert "line 3" in str(info.value)
+        directives.expand("  x = 1\n" + line + "\n", DOMAIN)
+    assert "line 2" in str(info.value)
 
 
 def test_splice_calls_the_entry_and_keeps_the_original_statements():
