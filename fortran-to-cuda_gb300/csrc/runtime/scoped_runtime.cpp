@@ -39,6 +39,7 @@
 #include <mutex>
 #include <set>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "backend.hpp"
@@ -676,8 +677,17 @@ void release_mirror(Context *c, Buffer *b) {
 
 size_t claimed(const Domain *d) { return d->device_bytes + d->scratch_bytes + d->workspace_bytes; }
 
-// Make room for `bytes` more, evicting least recently used mirrors that are not
-// in `keep`, not prepared and not used by queued tasks.
+// Values on the device that the host does not hold: evicting the mirror costs a download.
+bool dirty_mirror(const Buffer *b) {
+    Region dirty = b->physical.clip(b->device_valid);
+    dirty.remove(b->host_valid);
+    return !dirty.empty();
+}
+
+// Make room for `bytes` more, evicting mirrors that are not in `keep`, not
+// prepared and not used by queued tasks: clean ones (dropped without a
+// download) before dirty ones, each kind least recently used first, ties by
+// handle.
 void make_room(Context *c, size_t bytes, const std::set<uint64_t> &keep) {
     Domain *d = c->domain;
     if (!d->budget_set) return;
@@ -704,15 +714,21 @@ void make_room(Context *c, size_t bytes, const std::set<uint64_t> &keep) {
     }
     while (claimed(d) + bytes > d->budget) {
         Buffer *victim = nullptr;
+        bool victim_dirty = false;
         for (auto &kv : d->buffers) {
             Buffer *b = kv.second.get();
             if (!b->device || keep.count(b->handle) || b->prepared != Buffer::NONE || b->queued) continue;
-            if (!victim || b->last_use < victim->last_use) victim = b;
+            const bool dirty = dirty_mirror(b);
+            if (!victim || std::make_tuple(dirty, b->last_use, b->handle) <
+                               std::make_tuple(victim_dirty, victim->last_use, victim->handle)) {
+                victim = b;
+                victim_dirty = dirty;
+            }
         }
         if (!victim) raise(FORT_SCOPE_RESOURCE, "device budget exhausted by arrays in use");
-        Region dirty = victim->physical.clip(victim->device_valid);
-        dirty.remove(victim->host_valid);
-        if (!dirty.empty()) {
+        if (victim_dirty) {
+            Region dirty = victim->physical.clip(victim->device_valid);
+            dirty.remove(victim->host_valid);
             d->residency.dirty_evictions++;
             d->residency.dirty_download_bytes += dirty.volume() * victim->elem;
             publish_buffer(c, victim);
@@ -740,17 +756,18 @@ void reserve(Context *c, const std::vector<Buffer *> &list, bool allow_in_place)
         if (!b->device && !b->in_place) need += b->bytes;
     }
     Domain *d = c->domain;
-    d->residency.reserve_batches++;
-    d->residency.requested_resources += list.size();
     if (need) {
         ensure_stream(c);
         make_room(c, need, keep);
     }
+    std::set<uint64_t> seen;
+    size_t reused = 0;
     for (Buffer *b : list) {
         b->last_use = ++d->tick;
+        if (!seen.insert(b->handle).second) continue;  // a repeated array is one resource
         if (b->in_place || !b->bytes) continue;  // mapped host array, or an empty one: no storage
         if (b->device) {
-            d->residency.reuse_hits++;
+            ++reused;
             continue;
         }
         if (!Backend::alloc(&b->device, b->bytes, c->stream)) {
@@ -764,6 +781,10 @@ void reserve(Context *c, const std::vector<Buffer *> &list, bool allow_in_place)
         if (claimed(d) > d->peak_total_bytes) d->peak_total_bytes = claimed(d);
         b->device_valid.clear();
     }
+    // counted once the batch holds its storage: a refused reservation changes no counter
+    d->residency.reserve_batches++;
+    d->residency.requested_resources += seen.size();
+    d->residency.reuse_hits += reused;
 }
 
 // ---- the task queue ------------------------------------------------------------------------
@@ -1990,6 +2011,7 @@ int fort_scope_device_reserve_many_v1(fort_scope_t context, const fort_buffer_t 
         std::set<uint64_t> seen;
         for (size_t n = 0; n < count; ++n) {
             Buffer *b = find_buffer(c, buffers[n]);
+            if (b->prepared != Buffer::NONE) raise(FORT_SCOPE_STATE, "reservation of an array inside an access");
             if (seen.insert(b->handle).second) list.push_back(b);
         }
         if (list.empty()) return FORT_SCOPE_OK;
@@ -2236,6 +2258,7 @@ int fort_scope_device_reserve_slabs_v1(fort_scope_t context, const fort_buffer_t
         std::set<uint64_t> seen;
         for (size_t n = 0; n < count; ++n) {
             Buffer *b = find_buffer(c, buffers[n]);
+            if (b->prepared != Buffer::NONE) raise(FORT_SCOPE_STATE, "reservation of an array inside an access");
             if (seen.insert(b->handle).second) list.push_back(b);
         }
         if (list.empty()) return FORT_SCOPE_OK;

@@ -8,7 +8,7 @@ statuses, host values and transfer counts. The behaviours restated here are
 those the reference's runtime tests exercise (compiler/tests/test_scoped_runtime.py,
 test_scoped_domains.py, test_scoped_graph_replay.py, test_scoped_graph_queue.py,
 test_scoped_host_completion.py, test_scoped_access_batch.py, test_scoped_scratch.py,
-test_scoped_direct_transport.py), each citing the scenario it follows. Scenarios
+test_scoped_direct_transport.py, test_scoped_residency.py), each citing the scenario it follows. Scenarios
 that need the reference's CPU build to leave device kernels unrun are not
 restated: this runtime's CPU backend runs test kernels as host functions.
 """
@@ -1355,6 +1355,237 @@ def test_oversized_footprint_fails_before_any_change(both):
     status, _ = _device_begin(scope, ha, abi.access(flags=abi.READ_ALL))
     assert status == abi.RESOURCE
     assert scope.stats().allocations == 0
+    assert both.fort_scope_close(scope.handle) == abi.OK
+
+
+def _resident(scope, identity, *, initialized=True, defined=None):
+    """Eight values identity*100 + i, kept alive with the scope."""
+    host, address = _array(identity * 100.0 + np.arange(8))
+    scope.keep.append(host)
+    status, h = scope.register(address, [8], identity=identity, initialized=initialized, defined=defined)
+    assert status == abi.OK
+    return host, h
+
+
+def _reserve_many(lib, scope, *handles, outputs=None):
+    outputs = outputs if outputs is not None else (c.c_void_p * len(handles))()
+    return lib.fort_scope_device_reserve_many_v1(scope.handle, (abi.U64 * len(handles))(*handles), len(handles),
+                                                 outputs), outputs
+
+
+def _residency(lib, scope):
+    out = abi.ResidencyStats()
+    assert lib.fort_scope_residency_stats_get_v1(scope.handle, c.byref(out)) == abi.OK
+    assert out.version == 1
+    return out
+
+
+def _on_device(lib, scope, h, acc, change=None):
+    status, dev = _device_begin(scope, h, acc)
+    assert status == abi.OK
+    if change is not None:
+        change(_dev(dev, 8))
+    assert lib.fort_scope_device_end(scope.handle, h) == abi.OK
+
+
+def _shift(amount):
+    def change(d):
+        d[:] += amount
+    return change
+
+
+def test_lru_dirty_eviction_publishes_once_and_reloads_exactly(both):
+    """Two mirrors fill a 128-byte budget; reserving a third next to the clean one evicts the dirty one, which is
+    published first and reloads exactly (reference: test_scoped_residency.py:49-72)."""
+    scope = abi.Scope(both)
+    assert both.fort_scope_set_device_budget(scope.handle, 128) == abi.OK
+    host_a, a = _resident(scope, 1)
+    _, b = _resident(scope, 2)
+    _, other = _resident(scope, 3)
+    _on_device(both, scope, a, abi.access(flags=abi.READ_ALL | abi.WRITE_ALL), _shift(1000.0))
+    _on_device(both, scope, b, abi.access(flags=abi.READ_ALL))
+    before = scope.stats()
+    assert _reserve_many(both, scope, other, b)[0] == abi.OK   # b pinned: only the dirty a can go
+    assert host_a.tolist() == [1100.0 + i for i in range(8)]
+    assert scope.stats().download_bytes - before.download_bytes == 64
+    r = _residency(both, scope)
+    assert (r.evictions, r.evicted_bytes, r.dirty_evictions, r.dirty_download_bytes) == (1, 64, 1, 64)
+    status, dev = _device_begin(scope, a, abi.access(flags=abi.READ_ALL))
+    assert status == abi.OK and _dev(dev, 8).tolist() == host_a.tolist()
+    assert both.fort_scope_device_end(scope.handle, a) == abi.OK
+    assert scope.stats().allocated_bytes == scope.stats().peak_device_bytes == 128
+    assert both.fort_scope_close(scope.handle) == abi.OK
+
+
+def test_a_clean_replica_goes_before_older_dirty_storage(both):
+    """Eviction takes the clean mirror before the older dirty one; when every alternative is pinned the dirty one
+    is published exactly once (reference: test_scoped_residency.py:75-104)."""
+    scope = abi.Scope(both)
+    assert both.fort_scope_set_device_budget(scope.handle, 128) == abi.OK
+    host_a, a = _resident(scope, 1)
+    _, b = _resident(scope, 2)
+    _, other = _resident(scope, 3)
+    _on_device(both, scope, a, abi.access(flags=abi.READ_ALL | abi.WRITE_ALL), _shift(1000.0))
+    _on_device(both, scope, b, abi.access(flags=abi.READ_ALL))
+    assert _reserve_many(both, scope, other)[0] == abi.OK
+    assert host_a.tolist() == [100.0 + i for i in range(8)]    # a stayed on the device, unpublished
+    assert scope.stats().download_bytes == 0
+    r = _residency(both, scope)
+    assert (r.evictions, r.dirty_evictions) == (1, 0)
+    allocations, uploads = scope.stats().allocations, scope.stats().upload_bytes
+    status, dev = _device_begin(scope, a, abi.access(flags=abi.READ_ALL))
+    assert status == abi.OK and _dev(dev, 8).tolist() == [1100.0 + i for i in range(8)]
+    assert both.fort_scope_device_end(scope.handle, a) == abi.OK
+    assert (scope.stats().allocations, scope.stats().upload_bytes) == (allocations, uploads)
+    assert _reserve_many(both, scope, b, other)[0] == abi.OK
+    assert host_a.tolist() == [1100.0 + i for i in range(8)]
+    assert scope.stats().download_bytes == 64
+    r = _residency(both, scope)
+    assert (r.evictions, r.dirty_evictions) == (2, 1)
+    assert both.fort_scope_close(scope.handle) == abi.OK
+
+
+def test_evicting_a_read_mirror_downloads_nothing(both):
+    """(reference: test_scoped_residency.py:107-122)"""
+    scope = abi.Scope(both)
+    assert both.fort_scope_set_device_budget(scope.handle, 64) == abi.OK
+    host, a = _resident(scope, 1)
+    _, b = _resident(scope, 2)
+    _on_device(both, scope, a, abi.access(flags=abi.READ_ALL))
+    assert _reserve_many(both, scope, b)[0] == abi.OK
+    assert both.fort_scope_host_begin(scope.handle, a, c.byref(abi.access(flags=abi.READ_ALL))) == abi.OK
+    assert host.tolist() == [100.0 + i for i in range(8)]
+    assert both.fort_scope_host_end(scope.handle, a) == abi.OK
+    assert scope.stats().download_bytes == 0
+    r = _residency(both, scope)
+    assert (r.evictions, r.dirty_evictions) == (1, 0)
+    assert both.fort_scope_close(scope.handle) == abi.OK
+
+
+def test_an_impossible_reservation_changes_nothing(both):
+    """Two 64-byte arrays cannot both be reserved in 64 bytes: RESOURCE before the dirty one is published, the
+    output slots untouched, every counter unchanged (reference: test_scoped_residency.py:125-146)."""
+    scope = abi.Scope(both)
+    assert both.fort_scope_set_device_budget(scope.handle, 64) == abi.OK
+    host, a = _resident(scope, 1)
+    _, b = _resident(scope, 2)
+
+    def fill(d):
+        d[:] = 999.0 + np.arange(8)
+    _on_device(both, scope, a, abi.access(flags=abi.WRITE_ALL | abi.OVERWRITE_ALL), fill)
+    before, metrics = bytes(scope.stats()), bytes(_residency(both, scope))
+    outputs = (c.c_void_p * 2)(0x1234, 0x5678)
+    assert _reserve_many(both, scope, a, b, outputs=outputs)[0] == abi.RESOURCE
+    assert list(outputs) == [0x1234, 0x5678]
+    assert bytes(scope.stats()) == before and bytes(_residency(both, scope)) == metrics
+    assert host[0] == 100.0
+    status, dev = _device_begin(scope, a, abi.access(flags=abi.READ_ALL))
+    assert status == abi.OK and _dev(dev, 8)[0] == 999.0
+    assert both.fort_scope_device_end(scope.handle, a) == abi.OK
+    assert both.fort_scope_close(scope.handle) == abi.OK
+    assert host[0] == 999.0
+
+
+def test_a_reservation_pins_duplicates_and_reuse_refreshes_the_lru(both):
+    """(reference: test_scoped_residency.py:149-165)"""
+    scope = abi.Scope(both)
+    assert both.fort_scope_set_device_budget(scope.handle, 128) == abi.OK
+    a, b, other = (_resident(scope, n)[1] for n in (1, 2, 3))
+    assert _reserve_many(both, scope, a, b)[0] == abi.OK
+    status, duplicate = _reserve_many(both, scope, a, a)
+    assert status == abi.OK and duplicate[0] == duplicate[1]
+    assert _reserve_many(both, scope, a, other)[0] == abi.OK
+    allocations = scope.stats().allocations
+    assert _reserve_many(both, scope, a)[0] == abi.OK
+    assert scope.stats().allocations == allocations          # the recently used a survived
+    assert _reserve_many(both, scope, b)[0] == abi.OK
+    assert scope.stats().allocations == allocations + 1      # the cold b was evicted
+    assert both.fort_scope_close(scope.handle) == abi.OK
+
+
+def test_eviction_publishes_exactly_the_defined_part_and_keeps_holes(both):
+    """(reference: test_scoped_residency.py:168-185)"""
+    scope = abi.Scope(both)
+    assert both.fort_scope_set_device_budget(scope.handle, 64) == abi.OK
+    host, a = _resident(scope, 1, defined=[((2,), (6,))])
+    _, b = _resident(scope, 2)
+    span = [((2,), (6,))]
+
+    def fill(d):
+        d[2:6] = 1000.0 + np.arange(2, 6)
+    _on_device(both, scope, a, abi.access(read=span, write=span, overwrite=[((3,), (4,))]), fill)
+    assert _reserve_many(both, scope, b)[0] == abi.OK
+    assert host.tolist() == [100, 101, 1002, 1003, 1004, 1005, 106, 107]
+    assert scope.stats().upload_bytes == scope.stats().download_bytes == 32
+    assert both.fort_scope_host_begin(scope.handle, a, c.byref(abi.access(flags=abi.READ_ALL))) \
+        == abi.UNINITIALIZED
+    assert both.fort_scope_host_begin(scope.handle, a, c.byref(abi.access(read=span))) == abi.OK
+    assert both.fort_scope_host_end(scope.handle, a) == abi.OK
+    assert both.fort_scope_close(scope.handle) == abi.OK
+
+
+def test_a_prepared_array_is_neither_evicted_nor_reserved(both):
+    """(reference: test_scoped_residency.py:188-204)"""
+    scope = abi.Scope(both)
+    assert both.fort_scope_set_device_budget(scope.handle, 64) == abi.OK
+    host, a = _resident(scope, 1)
+    _, b = _resident(scope, 2)
+    status, dev = _device_begin(scope, a, abi.access(flags=abi.READ_ALL | abi.WRITE_ALL))
+    assert status == abi.OK
+    assert _reserve_many(both, scope, a)[0] == abi.STATE
+    assert _reserve_many(both, scope, b)[0] == abi.RESOURCE
+    assert _residency(both, scope).evictions == 0
+    _dev(dev, 8)[0] = 987.0
+    assert both.fort_scope_device_end(scope.handle, a) == abi.OK
+    assert _reserve_many(both, scope, b)[0] == abi.OK
+    assert both.fort_scope_host_begin(scope.handle, a, c.byref(abi.access(flags=abi.READ_ALL))) == abi.OK
+    assert host[0] == 987.0
+    assert both.fort_scope_host_end(scope.handle, a) == abi.OK
+    assert both.fort_scope_close(scope.handle) == abi.OK
+
+
+def test_buffer_membership_is_per_context(both):
+    """A handle belongs to the context that registered it, even for the same identity in another context; a closed
+    context answers STALE (reference: test_scoped_residency.py:207-224)."""
+    first, second = abi.Scope(both), abi.Scope(both)
+    _, old = _resident(first, 1)
+    _, current = _resident(second, 1)
+    present = c.c_int(-1)
+    assert both.fort_scope_buffer_valid_v1(first.handle, old, c.byref(present)) == abi.OK and present.value == 1
+    assert both.fort_scope_buffer_valid_v1(second.handle, old, c.byref(present)) == abi.OK and present.value == 0
+    assert both.fort_scope_close(first.handle) == abi.OK
+    assert both.fort_scope_buffer_valid_v1(second.handle, old, c.byref(present)) == abi.OK and present.value == 0
+    assert both.fort_scope_buffer_valid_v1(second.handle, current, c.byref(present)) == abi.OK
+    assert present.value == 1
+    assert second.stats().allocations == 0
+    assert both.fort_scope_buffer_valid_v1(first.handle, old, c.byref(present)) == abi.STALE
+    assert both.fort_scope_close(second.handle) == abi.OK
+
+
+def test_eviction_keeps_device_values_whose_definition_was_forgotten(both):
+    """Forgetting the definition of device-written values does not lose them: eviction still publishes them, and
+    reads admitted afterwards see them without another download (reference: test_scoped_residency.py:227-249)."""
+    scope = abi.Scope(both)
+    assert both.fort_scope_set_device_budget(scope.handle, 64) == abi.OK
+    host, a = _resident(scope, 1)
+    _, b = _resident(scope, 2)
+
+    def fill(d):
+        d[:] = 5000.0 + np.arange(8)
+    _on_device(both, scope, a, abi.access(flags=abi.WRITE_ALL | abi.OVERWRITE_ALL), fill)
+    assert both.fort_scope_forget_definition(scope.handle, a) == abi.OK
+    assert scope.stats().download_bytes == 0
+    assert _reserve_many(both, scope, b)[0] == abi.OK
+    assert host.tolist() == [5000.0 + i for i in range(8)]
+    assert scope.stats().download_bytes == 64
+    assert both.fort_scope_host_begin(scope.handle, a, c.byref(abi.access(flags=abi.READ_ALL))) \
+        == abi.UNINITIALIZED
+    reads = abi.access(read=[((0,), (8,))])
+    assert both.fort_scope_admit_source_reads_v1(scope.handle, a, reads.reads, reads.read_count) == abi.OK
+    assert both.fort_scope_host_begin(scope.handle, a, c.byref(abi.access(flags=abi.READ_ALL))) == abi.OK
+    assert host.tolist() == [5000.0 + i for i in range(8)]
+    assert both.fort_scope_host_end(scope.handle, a) == abi.OK
+    assert scope.stats().download_bytes == 64
     assert both.fort_scope_close(scope.handle) == abi.OK
 
 
