@@ -226,7 +226,7 @@ def run_e2e(fields, steps, warmup, dist, torch):
     world = dist.get_world_size() if dist is not None else 1
     nbytes = sum(a.nbytes for a in inputs)
     spread = {"min": per_step[0], "median": per_step[len(per_step) // 2], "max": per_step[-1]}
-    return geo.points * world * n / elapsed / 1e9, n, nbytes, sum(a.nbytes for a in outputs), spread
+    return geo.points * world * n / elapsed / 1e9, n, nbytes, outputs, spread
 
 
 def run_gb300(args):
@@ -304,7 +304,13 @@ def run_gb300(args):
     # End to end through the reference-facing C ABI: a residency domain holds the host arrays (pinned in
     # place at registration), every step the host rewrites the inputs (their device copies go stale), the
     # generated entry advection::step3 runs (uploading what changed) and the outputs are published back.
-    e2e_value, e2e_steps, bytes_in, bytes_out, e2e_spread = run_e2e(fields, args.steps, args.warmup, dist, torch)
+    e2e_value, e2e_steps, bytes_in, e2e_outputs, e2e_spread = run_e2e(fields, args.steps, args.warmup, dist, torch)
+    bytes_out = sum(a.nbytes for a in e2e_outputs)
+    # the host arrays the end-to-end path published equal, bit for bit, what the graph-replayed launches left
+    # on the device from the same inputs: the end-to-end steps did the whole step
+    e2e_matches = all(np.array_equal(a.view(np.int64), t.cpu().numpy().view(np.int64))
+                      for a, t in zip(e2e_outputs, dev_out))
+    del e2e_outputs
 
     peak, peak_kind = hbm_peak()
     alg = algorithmic_bytes_per_point(NSCALAR) * points
@@ -333,6 +339,7 @@ def run_gb300(args):
                           "peak_add_rn": fp64_add, "peak_fma_rn": fp64_fma, "peak_source": "measured live"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": bytes_in,
                 "d2h_bytes_per_step": bytes_out, "steps": e2e_steps, "step_ms": e2e_spread,
+                "outputs_equal_device_path": e2e_matches,
                 "path": "fort_scope runtime + generated entry advection::step3; the host rewrites the inputs and reads "
                         "the outputs every step, so from the second round the step runs as z-slabs whose uploads "
                         "(copy stream), kernels and publications (second copy stream) overlap; host arrays pinned "
