@@ -92,6 +92,7 @@ struct Buffer {
     int64_t lower[kMaxRank] = {};
     void *device = nullptr;
     bool pinned_host = false;
+    bool pin_tried = false;      // pinning is tried once, at the array's first device use
     void *mapped = nullptr;      // device-usable address of the pinned host array
     bool host_touched = true;    // the host wrote or read it since its last device use
     int host_rounds = 0;         // consecutive device uses, each preceded by host access
@@ -257,11 +258,26 @@ void poison(Context *c, const std::string &message) {
     raise(FORT_SCOPE_EXECUTION, message + "; unsafe replay prohibited");
 }
 
+// The device is brought up the first time a context needs it: registration, host
+// access, observation of host-current arrays and closing never touch it.
 void ensure_stream(Context *c) {
     if (c->stream_ready) return;
+    trace_line(c, "initialize", 0, 0);
     if (!Backend::select(c->domain->device)) raise(FORT_SCOPE_RESOURCE, "cannot select device: " + Backend::last_error());
     if (!Backend::make_stream(&c->stream)) raise(FORT_SCOPE_RESOURCE, "cannot create stream: " + Backend::last_error());
     c->stream_ready = true;
+}
+
+// Arrays of 1 MiB or more are pinned in place (and mapped) the first time the
+// device is about to use them, so that their copies run at DMA speed; the CPU
+// test backend pins only when a test asks.
+void pin_for_device(Context *c, Buffer *b) {
+    if (b->pin_tried) return;
+    b->pin_tried = true;
+    if (b->bytes < (Backend::cpu ? size_t(0) : size_t(1) << 20) || !b->bytes || !env_flag("FORT_SCOPE_PIN_HOST", true))
+        return;
+    ensure_stream(c);
+    b->pinned_host = Backend::pin(b->host, b->bytes, &b->mapped);
 }
 
 void ensure_copy_streams(Context *c) {
@@ -751,6 +767,7 @@ void reserve(Context *c, const std::vector<Buffer *> &list, bool allow_in_place)
     size_t need = 0;
     for (Buffer *b : list) {
         keep.insert(b->handle);
+        pin_for_device(c, b);
         b->in_place = allow_in_place && in_place_allowed() && b->mapped && b->prepared == Buffer::NONE &&
                       b->host_touched && b->host_rounds >= 1;
         if (!b->device && !b->in_place) need += b->bytes;
@@ -1777,9 +1794,6 @@ static int register_impl(fort_scope_t context, uint64_t identity, uint64_t gener
             for (size_t n = 0; n < initialized_count; ++n) b->defined.add(section_box(b.get(), initialized[n]));
         }
         b->physical = b->defined;
-        // arrays of 1 MiB or more are pinned in place (the CPU test backend pins only when a test asks)
-        if (bytes >= (Backend::cpu ? size_t(0) : size_t(1) << 20) && env_flag("FORT_SCOPE_PIN_HOST", true))
-            b->pinned_host = Backend::pin(b->host, bytes, &b->mapped);
         *out = b->handle;
         trace_line(c, "register", b->handle, bytes);
         d->by_identity[identity] = b->handle;
@@ -2264,6 +2278,7 @@ int fort_scope_device_reserve_slabs_v1(fort_scope_t context, const fort_buffer_t
         if (list.empty()) return FORT_SCOPE_OK;
         const bool stream = streaming_allowed();
         bool any = false;
+        for (Buffer *b : list) pin_for_device(c, b);
         for (Buffer *b : list) any = any || (stream && host_round(b));
         reserve(c, list, !stream);
         for (size_t n = 0; n < count; ++n) {

@@ -219,3 +219,26 @@ def test_arrays_the_host_rewrites_every_step_are_streamed(resident, nx, ny, nz, 
     if path == "in place":
         # only the first two steps moved field data through copies
         assert stats.upload_bytes <= 2 * sum(a.nbytes for a in ins)
+
+
+@pytest.mark.parametrize("use, visible", [("host", None), ("host", ""), ("device", None)])
+def test_the_product_runtime_brings_the_device_up_only_for_device_work(use, visible, tmp_path):
+    """The CUDA build: host-only use of 2 MiB arrays creates no stream and pins nothing, also with every device
+    hidden; a device access brings the device up once (reference: test_scoped_runtime_cuda.py:404-410)."""
+    import os
+    import subprocess
+    import sys
+
+    from test_runtime_abi import HOST_ONLY
+
+    assert native.LIBRARY.exists()
+    script = tmp_path / "host_only.py"
+    script.write_text(HOST_ONLY)
+    env = {**os.environ, "FORT_RUNTIME_TRACE": "1"}
+    if visible is not None:
+        env["CUDA_VISIBLE_DEVICES"] = visible
+    run = subprocess.run([sys.executable, str(script), str(native.LIBRARY), use, str(native.PACKAGE_ROOT)],
+                         capture_output=True, text=True, timeout=120, env=env)
+    assert run.returncode == 0, run.stdout + run.stderr
+    initialized = [line for line in run.stderr.splitlines() if line.startswith("FORT_SCOPED initialize")]
+    assert len(initialized) == (use == "device")

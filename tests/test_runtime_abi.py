@@ -1589,6 +1589,47 @@ def test_eviction_keeps_device_values_whose_definition_was_forgotten(both):
     assert both.fort_scope_close(scope.handle) == abi.OK
 
 
+HOST_ONLY = r"""
+import ctypes as c, sys
+import numpy as np
+sys.path[:0] = sys.argv[3:]
+from compiler.runtime import abi
+lib = abi.bind(c.CDLL(sys.argv[1]))
+scope = abi.Scope(lib)
+arrays = [np.arange(1 << 18, dtype=np.float64) for _ in range(2)]     # 2 MiB each
+handles = [scope.register(a.ctypes.data, [a.size], identity=n + 1)[1] for n, a in enumerate(arrays)]
+assert all(handles)
+acc = abi.access(flags=abi.READ_ALL | abi.WRITE_ALL)
+assert lib.fort_scope_host_begin(scope.handle, handles[0], c.byref(acc)) == abi.OK
+arrays[0][:] += 1.0
+assert lib.fort_scope_host_end(scope.handle, handles[0]) == abi.OK
+assert lib.fort_scope_observe_v1(scope.handle, (abi.U64 * 2)(*handles), 2) == abi.OK
+assert lib.fort_scope_unregister(scope.handle, handles[1]) == abi.OK
+if sys.argv[2] == "device":
+    out = c.c_void_p()
+    assert lib.fort_scope_device_begin(scope.handle, handles[0], c.byref(abi.access(flags=abi.READ_ALL)),
+                                       c.byref(out)) == abi.OK
+    assert lib.fort_scope_device_end(scope.handle, handles[0]) == abi.OK
+assert lib.fort_scope_close(scope.handle) == abi.OK
+assert arrays[0][5] == 6.0
+"""
+
+
+@pytest.mark.parametrize("use", ["host", "device"])
+def test_host_only_use_never_initializes_the_device(both, use, tmp_path):
+    """Registration, host access, observation of host-current arrays, unregistration and close bring no device
+    up; the first device access does, once (reference: test_scoped_host_completion_cuda.py:205-210,
+    test_scoped_runtime_cuda.py:404-410, traced as ``FORT_SCOPED initialize``)."""
+    script = tmp_path / "host_only.py"
+    script.write_text(HOST_ONLY)
+    package = os.path.join(ROOT, "fortran-to-cuda_gb300")
+    run = subprocess.run([sys.executable, str(script), both._name, use, package], capture_output=True, text=True,
+                         timeout=120, env={**os.environ, "FORT_RUNTIME_TRACE": "1"})
+    assert run.returncode == 0, run.stdout + run.stderr
+    initialized = [line for line in run.stderr.splitlines() if line.startswith("FORT_SCOPED initialize")]
+    assert len(initialized) == (use == "device")
+
+
 def test_scratch_leases(both):
     scope = abi.Scope(both)
     lease = abi.ScratchLease()
