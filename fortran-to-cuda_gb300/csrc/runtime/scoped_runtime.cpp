@@ -182,6 +182,7 @@ struct Context {
     };
     std::map<uint64_t, Before> queued_before;
     std::map<uint64_t, CachedGraph> graphs;
+    std::map<uint64_t, CachedGraph> group_graphs;  // kernel groups and checked groups, by the caller's key
     fort_scope_graph_stats_v1 graph_stats{};
     fort_scope_graph_queue_stats_v1 queue_stats{};
     fort_scope_completion_stats_v1 completion{};
@@ -901,6 +902,74 @@ void submit(Context *c, std::vector<Task> &tasks, uint64_t key) {
         poison(c, std::string("graph launch failed: ") + Backend::last_error());
 }
 
+// A group of kernels whose argument values live in the caller's storage for
+// this call only (fort_scope_graph_submit_v1, fort_scope_graph_execute_v1):
+// cached by the caller's key like the queue's sequences. The first reach of a
+// sequence runs as direct launches, the second builds and instantiates its
+// graph (the node parameters are copied then), later reaches copy every
+// node's arguments into the instantiated graph again and replay it; a new
+// sequence of functions under the key replaces the graph.
+void submit_group(Context *c, const std::vector<LaunchSpec> &specs, uint64_t key) {
+    ensure_stream(c);
+    c->domain->stats.launches += specs.size();
+    c->graph_stats.submissions++;
+    c->graph_stats.logical_kernels += specs.size();
+    std::vector<Task> direct(specs.size());
+    for (size_t n = 0; n < specs.size(); ++n) direct[n].spec = specs[n];
+    if (!c->graphs_enabled) {
+        launch_direct(c, direct);
+        return;
+    }
+    CachedGraph &g = c->group_graphs[key];
+    bool same_topology = g.functions.size() == specs.size();
+    for (size_t n = 0; same_topology && n < specs.size(); ++n)
+        same_topology = g.functions[n] == specs[n].function && g.argument_counts[n] == specs[n].arguments.size();
+    if (!same_topology) {
+        if (g.graph) {
+            Backend::graph_destroy(g.graph);
+            g.graph = nullptr;
+            c->graph_stats.rebuilds++;
+            c->graph_stats.destructions++;
+            c->graph_stats.live_graphs--;
+        }
+        g.functions.clear();
+        g.argument_counts.clear();
+        for (const auto &k : specs) {
+            g.functions.push_back(k.function);
+            g.argument_counts.push_back(k.arguments.size());
+        }
+        g.reached = 0;
+    }
+    if (++g.reached == 1) {
+        trace_line(c, "graph_warmup_direct", 0, specs.size());
+        launch_direct(c, direct);
+        return;
+    }
+    if (!g.graph) {
+        Backend::Graph *built = nullptr;
+        if (!Backend::graph_build(&built, specs)) {
+            c->queue_stats.graph_resource_fallbacks++;
+            g.reached = 0;
+            launch_direct(c, direct);
+            return;
+        }
+        g.graph = built;
+        c->graph_stats.creations++;
+        c->graph_stats.instantiations++;
+        c->graph_stats.live_graphs++;
+    } else {
+        for (size_t n = 0; n < specs.size(); ++n) {
+            if (!Backend::graph_update(g.graph, n, specs[n]))
+                poison(c, std::string("graph update failed: ") + Backend::last_error());
+            c->graph_stats.parameter_updates++;
+        }
+        c->graph_stats.replays++;
+    }
+    for (size_t n = 0; n < specs.size(); ++n) trace_line(c, "graph_kernel", 0, 0);
+    if (!Backend::graph_launch(g.graph, specs, c->stream))
+        poison(c, std::string("graph launch failed: ") + Backend::last_error());
+}
+
 void flush(Context *c) {
     c->queued_before.clear();
     if (c->pending.empty()) return;
@@ -1337,8 +1406,9 @@ void detach(Context *c) {
     }
     if (c->stream_ready) {
         Backend::sync(c->stream);
-        for (auto &kv : c->graphs)
-            if (kv.second.graph) Backend::graph_destroy(kv.second.graph);
+        for (auto *cache : {&c->graphs, &c->group_graphs})
+            for (auto &kv : *cache)
+                if (kv.second.graph) Backend::graph_destroy(kv.second.graph);
         release_events(c);
         Backend::destroy_stream(c->stream);
     }
@@ -2411,14 +2481,10 @@ int fort_scope_graph_submit_v1(fort_scope_t context, uint64_t group_key, const f
             tasks.push_back(std::move(t));
         }
         flush(c);
-        // arguments are borrowed for this call only: launch them from caller storage
-        ensure_stream(c);
         c->untracked = true;  // kernels without bindings: host accesses wait for the stream
-        c->domain->stats.launches += count;
-        c->graph_stats.submissions++;
-        c->graph_stats.logical_kernels += count;
-        (void)group_key;
-        launch_direct(c, tasks);
+        std::vector<LaunchSpec> specs;
+        for (auto &t : tasks) specs.push_back(std::move(t.spec));
+        submit_group(c, specs, group_key);
         return FORT_SCOPE_OK;
     });
 }
@@ -2495,13 +2561,7 @@ int fort_scope_graph_execute_v1(fort_scope_t context, uint64_t group_key, const 
             settle(c, b, b->defined, b->host_valid, device);
         }
         c->untracked = true;  // host accesses after a checked group wait for the stream
-        for (const LaunchSpec &k : list) {
-            trace_line(c, "launch", 0, 0);
-            if (!Backend::launch(k, c->stream)) poison(c, std::string("kernel launch failed: ") + Backend::last_error());
-        }
-        c->domain->stats.launches += count;
-        c->queue_stats.direct_submissions++;
-        c->queue_stats.direct_kernels += count;
+        submit_group(c, list, group_key);
         for (auto &tb : bound)
             for (auto &x : tb) device_commit(c, x.buffer, x.effects.writes, x.effects.overwrites);
         for (auto &kv : sim) note_device_use(kv.first);

@@ -1,0 +1,285 @@
+"""The task queue and checked graph groups of the runtime with real kernels on the GPU.
+
+The CPU scenarios of the queue (tests/test_runtime_abi.py) run test kernels as
+host functions; here a CUDA client written against include/scoped_runtime.h
+passes the addresses of its own ``__global__`` functions, so the CUDA
+backend's graph construction, parameter updates, replays and direct launches
+run for real. The behaviours follow the reference's CUDA suites
+(compiler/tests/test_scoped_graph_replay_cuda.py:241-262: replay, rebinding,
+topology change, long groups; test_scoped_graph_queue_cuda.py:333-341: the
+deferred queue). The client checks every value it reads back and prints the
+runtime's statistics as one JSON line per scenario.
+"""
+
+import json
+import subprocess
+from pathlib import Path
+
+import pytest
+
+from compiler import native
+
+pytestmark = pytest.mark.gpu
+
+CLIENT = r"""
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include "scoped_runtime.h"
+
+#define CHECK(x)                                                                                 \
+    do {                                                                                         \
+        const int status_ = (x);                                                                 \
+        if (status_) {                                                                           \
+            std::fprintf(stderr, "%s: status %d: %s\n", #x, status_, fort_scope_error());        \
+            return 1;                                                                            \
+        }                                                                                        \
+    } while (0)
+
+constexpr int N = 1024;
+
+__global__ void axpy(double *x, int n, double a, double b) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) x[i] = x[i] * a + b;
+}
+__global__ void produce(const double *a, double *b, int n, double add) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) b[i] = a[i] + add;
+}
+__global__ void consume(const double *b, double *out, int n, double factor) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = factor * b[i];
+}
+__global__ void alternate(const double *b, double *out, int n, double factor) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = factor * b[i] + 1.0;
+}
+
+struct Array {
+    double host[N];
+    fort_buffer_t handle = 0;
+    double *device = nullptr;
+};
+
+static size_t g_extent[1] = {N};
+static int64_t g_lower[1] = {1};
+
+static int add_array(fort_scope_t ctx, Array &a, uint64_t identity, bool initialized) {
+    fort_scope_layout layout{1, FORT_SCOPE_REAL64, 8, a.host, g_extent, g_lower, 1};
+    CHECK(fort_scope_register(ctx, identity, 1, &layout, initialized ? 1 : 0, &a.handle));
+    CHECK(fort_scope_device_reserve_v1(ctx, a.handle, reinterpret_cast<void **>(&a.device)));
+    return 0;
+}
+
+static fort_scope_access whole(uint32_t flags) {
+    fort_scope_access acc;
+    std::memset(&acc, 0, sizeof acc);
+    acc.flags = flags;
+    return acc;
+}
+
+static fort_scope_kernel_v1 kernel(const void *fn, void *const *args, size_t count) {
+    fort_scope_kernel_v1 k;
+    std::memset(&k, 0, sizeof k);
+    k.version = 1;
+    k.function = fn;
+    k.grid[0] = N / 256; k.grid[1] = k.grid[2] = 1;
+    k.block[0] = 256; k.block[1] = k.block[2] = 1;
+    k.arguments = args;
+    k.argument_count = count;
+    return k;
+}
+
+static int observe(fort_scope_t ctx, fort_buffer_t h) { return fort_scope_observe_v1(ctx, &h, 1); }
+
+static void print_stats(fort_scope_t ctx, const char *scenario) {
+    fort_scope_graph_stats_v1 g{};
+    fort_scope_graph_queue_stats_v1 q{};
+    fort_scope_stats s{};
+    fort_scope_graph_stats_get_v1(ctx, &g);
+    fort_scope_graph_queue_stats_get_v1(ctx, &q);
+    fort_scope_stats_get(ctx, &s);
+    std::printf("{\"scenario\": \"%s\", \"creations\": %llu, \"instantiations\": %llu, \"rebuilds\": %llu, "
+                "\"submissions\": %llu, \"replays\": %llu, \"parameter_updates\": %llu, \"live_graphs\": %llu, "
+                "\"accepted_tasks\": %llu, \"direct_submissions\": %llu, \"pending_tasks\": %llu, "
+                "\"uploads\": %llu, \"downloads\": %llu}\n",
+                scenario, (unsigned long long)g.creations, (unsigned long long)g.instantiations,
+                (unsigned long long)g.rebuilds, (unsigned long long)g.submissions, (unsigned long long)g.replays,
+                (unsigned long long)g.parameter_updates, (unsigned long long)g.live_graphs,
+                (unsigned long long)q.accepted_tasks, (unsigned long long)q.direct_submissions,
+                (unsigned long long)q.pending_tasks, (unsigned long long)s.uploads, (unsigned long long)s.downloads);
+}
+
+static int expect(const Array &a, double (*value)(int), const char *what) {
+    for (int i = 0; i < N; ++i)
+        if (a.host[i] != value(i)) {
+            std::fprintf(stderr, "%s: element %d is %.17g, expected %.17g\n", what, i, a.host[i], value(i));
+            return 1;
+        }
+    return 0;
+}
+
+// four queued axpy steps, each flushed: the first runs directly, the second instantiates, the rest replay
+static int queue_replay() {
+    fort_scope_t ctx = 0;
+    CHECK(fort_scope_create(0, &ctx));
+    static Array x;
+    for (int i = 0; i < N; ++i) x.host[i] = 1.0 + i;
+    if (add_array(ctx, x, 1, true)) return 1;
+    int n = N;
+    double a = 2.0, b = 0.0;
+    void *args[4] = {&x.device, &n, &a, &b};
+    const size_t sizes[4] = {sizeof(double *), sizeof(int), sizeof(double), sizeof(double)};
+    fort_scope_plan_binding bind{x.handle, whole(FORT_SCOPE_READ_ALL | FORT_SCOPE_WRITE_ALL)};
+    for (int step = 0; step < 4; ++step) {
+        b = step;  // argument values are copied when the task is accepted
+        fort_scope_graph_task_v1 task{kernel((const void *)axpy, args, 4), &bind, 1};
+        CHECK(fort_scope_graph_enqueue_v1(ctx, 7, &task, sizes));
+        CHECK(fort_scope_graph_flush_v1(ctx));
+    }
+    CHECK(observe(ctx, x.handle));
+    print_stats(ctx, "queue");
+    CHECK(fort_scope_close(ctx));
+    return expect(x, [](int i) { return ((((1.0 + i) * 2 + 0) * 2 + 1) * 2 + 2) * 2 + 3; }, "queue");
+}
+
+// a checked group (producer then consumer) executed four times with a new factor each time, then once with
+// another consumer: replays with parameter updates, and a new graph for the new sequence
+static int group_replay() {
+    fort_scope_t ctx = 0;
+    CHECK(fort_scope_create(0, &ctx));
+    static Array a, b, out;
+    for (int i = 0; i < N; ++i) a.host[i] = 0.5 * i;
+    if (add_array(ctx, a, 1, true) || add_array(ctx, b, 2, false) || add_array(ctx, out, 3, false)) return 1;
+    int n = N;
+    double add = 2.0, factor = 1.0;
+    void *produce_args[4] = {&a.device, &b.device, &n, &add};
+    void *consume_args[4] = {&b.device, &out.device, &n, &factor};
+    fort_scope_plan_binding producer[2] = {{a.handle, whole(FORT_SCOPE_READ_ALL)},
+                                           {b.handle, whole(FORT_SCOPE_WRITE_ALL | FORT_SCOPE_OVERWRITE_ALL)}};
+    fort_scope_plan_binding consumer[2] = {{b.handle, whole(FORT_SCOPE_READ_ALL)},
+                                           {out.handle, whole(FORT_SCOPE_WRITE_ALL | FORT_SCOPE_OVERWRITE_ALL)}};
+    for (int round = 1; round <= 4; ++round) {
+        factor = round;
+        fort_scope_graph_task_v1 tasks[2] = {{kernel((const void *)produce, produce_args, 4), producer, 2},
+                                             {kernel((const void *)consume, consume_args, 4), consumer, 2}};
+        CHECK(fort_scope_graph_execute_v1(ctx, 21, tasks, 2));
+    }
+    CHECK(observe(ctx, out.handle));
+    if (expect(out, [](int i) { return 4.0 * (0.5 * i + 2.0); }, "group")) return 1;
+    print_stats(ctx, "group");
+    factor = 10.0;
+    fort_scope_graph_task_v1 other[2] = {{kernel((const void *)produce, produce_args, 4), producer, 2},
+                                         {kernel((const void *)alternate, consume_args, 4), consumer, 2}};
+    CHECK(fort_scope_graph_execute_v1(ctx, 22, other, 2));
+    CHECK(fort_scope_graph_execute_v1(ctx, 22, other, 2));
+    CHECK(observe(ctx, out.handle));
+    if (expect(out, [](int i) { return 10.0 * (0.5 * i + 2.0) + 1.0; }, "topology")) return 1;
+    print_stats(ctx, "topology");
+    CHECK(fort_scope_close(ctx));
+    return 0;
+}
+
+// queued tasks that are cancelled never run and leave the array as it was
+static int cancel() {
+    fort_scope_t ctx = 0;
+    CHECK(fort_scope_create(0, &ctx));
+    static Array x;
+    for (int i = 0; i < N; ++i) x.host[i] = 3.0 * i;
+    if (add_array(ctx, x, 1, true)) return 1;
+    int n = N;
+    double a = 5.0, b = 7.0;
+    void *args[4] = {&x.device, &n, &a, &b};
+    const size_t sizes[4] = {sizeof(double *), sizeof(int), sizeof(double), sizeof(double)};
+    fort_scope_plan_binding bind{x.handle, whole(FORT_SCOPE_READ_ALL | FORT_SCOPE_WRITE_ALL)};
+    for (int k = 0; k < 3; ++k) {
+        fort_scope_graph_task_v1 task{kernel((const void *)axpy, args, 4), &bind, 1};
+        CHECK(fort_scope_graph_enqueue_v1(ctx, 9, &task, sizes));
+    }
+    CHECK(fort_scope_graph_queue_cancel_v1(ctx));
+    CHECK(fort_scope_graph_flush_v1(ctx));
+    CHECK(observe(ctx, x.handle));
+    print_stats(ctx, "cancel");
+    CHECK(fort_scope_close(ctx));
+    return expect(x, [](int i) { return 3.0 * i; }, "cancel");
+}
+
+// a long chain of queued tasks goes as one submission, in order
+static int long_chain() {
+    fort_scope_t ctx = 0;
+    CHECK(fort_scope_create(0, &ctx));
+    static Array x;
+    for (int i = 0; i < N; ++i) x.host[i] = i;
+    if (add_array(ctx, x, 1, true)) return 1;
+    int n = N;
+    double a = 1.0, b = 0.0;
+    void *args[4] = {&x.device, &n, &a, &b};
+    const size_t sizes[4] = {sizeof(double *), sizeof(int), sizeof(double), sizeof(double)};
+    fort_scope_plan_binding bind{x.handle, whole(FORT_SCOPE_READ_ALL | FORT_SCOPE_WRITE_ALL)};
+    for (int k = 0; k < 64; ++k) {
+        b = k;
+        fort_scope_graph_task_v1 task{kernel((const void *)axpy, args, 4), &bind, 1};
+        CHECK(fort_scope_graph_enqueue_v1(ctx, 5, &task, sizes));
+    }
+    CHECK(observe(ctx, x.handle));  // host access drains the queue
+    print_stats(ctx, "long");
+    CHECK(fort_scope_close(ctx));
+    return expect(x, [](int i) { return i + 63.0 * 64.0 / 2.0; }, "long");
+}
+
+int main(int argc, char **argv) {
+    const std::string mode = argc > 1 ? argv[1] : "";
+    if (mode == "queue") return queue_replay();
+    if (mode == "group") return group_replay();
+    if (mode == "cancel") return cancel();
+    if (mode == "long") return long_chain();
+    return 2;
+}
+"""
+
+
+@pytest.fixture(scope="module")
+def client(tmp_path_factory):
+    library = native.build()
+    directory = tmp_path_factory.mktemp("graph_client")
+    source = directory / "client.cu"
+    source.write_text(CLIENT)
+    exe = directory / "client"
+    built = subprocess.run([native.nvcc(), *native.ARCH, "-std=c++17", "-O2", "-cudart", "shared",
+                            f"-I{native.INCLUDE}", str(source), "-o", str(exe), str(library),
+                            f"-Xlinker=-rpath,{library.parent}"], capture_output=True, text=True)
+    assert built.returncode == 0, built.stderr
+    return exe
+
+
+def _run(client: Path, mode: str):
+    run = subprocess.run([str(client), mode], capture_output=True, text=True, timeout=120)
+    assert run.returncode == 0, run.stdout + run.stderr
+    return {r["scenario"]: r for r in map(json.loads, run.stdout.splitlines())}
+
+
+def test_queued_steps_replay_one_graph_with_new_parameters(client):
+    q = _run(client, "queue")["queue"]
+    assert (q["creations"], q["instantiations"], q["replays"], q["parameter_updates"]) == (1, 1, 2, 2)
+    assert (q["accepted_tasks"], q["direct_submissions"], q["pending_tasks"]) == (4, 1, 0)
+    assert (q["uploads"], q["downloads"]) == (1, 1)
+
+
+def test_a_checked_group_replays_and_a_new_sequence_gets_its_own_graph(client):
+    runs = _run(client, "group")
+    group, topology = runs["group"], runs["topology"]
+    assert group["creations"] == group["instantiations"] == 1
+    assert group["replays"] >= 2 and group["parameter_updates"] >= 2
+    assert topology["creations"] == group["creations"] + 1
+    assert topology["live_graphs"] == 2
+
+
+def test_cancelled_tasks_never_run(client):
+    c = _run(client, "cancel")["cancel"]
+    assert (c["accepted_tasks"], c["pending_tasks"], c["submissions"]) == (3, 0, 0)
+
+
+def test_a_long_chain_goes_in_one_submission(client):
+    chain = _run(client, "long")["long"]
+    assert chain["accepted_tasks"] == 64 and chain["pending_tasks"] == 0
+    assert chain["submissions"] == 1

@@ -3076,6 +3076,46 @@ def test_graph_group_may_read_what_an_earlier_task_defines(ours):
     assert ours.fort_scope_close(scope.handle) == abi.OK
 
 
+def test_a_checked_group_warms_up_then_replays_its_graph(ours):
+    """Under one key the first execution runs the kernels directly, the second instantiates the group's graph,
+    later ones copy every node's arguments in again and replay it; another sequence of functions under the key
+    replaces the graph (the reference's submit_graph policy, compiler/runtime/scoped_runtime.cu:1046-1078)."""
+    scope = abi.Scope(ours)
+    x, xa = _array(np.ones(8))
+    _, hx = scope.register(xa, [8])
+    devices = (c.c_void_p * 1)()
+    assert ours.fort_scope_device_reserve_many_v1(scope.handle, (abi.U64 * 1)(hx), 1, devices) == abi.OK
+    log = []
+    axpy, scale = _axpy_kernel(log), _scale_kernel(log)
+    for step in range(4):
+        task = _task(axpy, [c.c_void_p(devices[0]), c.c_int(8), c.c_double(2.0), c.c_double(float(step))],
+                     [(hx, abi.access(flags=abi.READ_ALL | abi.WRITE_ALL))])
+        assert ours.fort_scope_graph_execute_v1(scope.handle, 31, (abi.Task * 1)(task), 1) == abi.OK
+    g, q = abi.GraphStats(), abi.QueueStats()
+    assert ours.fort_scope_graph_stats_get_v1(scope.handle, c.byref(g)) == abi.OK
+    assert ours.fort_scope_graph_queue_stats_get_v1(scope.handle, c.byref(q)) == abi.OK
+    assert (g.creations, g.instantiations, g.replays, g.parameter_updates, g.live_graphs) == (1, 1, 2, 2, 1)
+    assert q.direct_submissions == 1
+    assert [entry[2] for entry in log] == [0.0, 1.0, 2.0, 3.0]      # each replay saw its own arguments
+    y, ya = _array(np.zeros(8))
+    _, hy = scope.register(ya, [8], initialized=False)
+    assert ours.fort_scope_device_reserve_many_v1(scope.handle, (abi.U64 * 1)(hy), 1, devices) == abi.OK
+    dy = devices[0]
+    assert ours.fort_scope_device_reserve_many_v1(scope.handle, (abi.U64 * 1)(hx), 1, devices) == abi.OK
+    other = _task(scale, [c.c_void_p(devices[0]), c.c_void_p(dy), c.c_int(8)],
+                  [(hx, abi.access(flags=abi.READ_ALL)), (hy, abi.access(flags=abi.WRITE_ALL | abi.OVERWRITE_ALL))])
+    for _ in range(2):
+        assert ours.fort_scope_graph_execute_v1(scope.handle, 31, (abi.Task * 1)(other), 1) == abi.OK
+    assert ours.fort_scope_graph_stats_get_v1(scope.handle, c.byref(g)) == abi.OK
+    assert (g.rebuilds, g.creations, g.live_graphs) == (1, 2, 1)
+    assert ours.fort_scope_observe_v1(scope.handle, (abi.U64 * 2)(hx, hy), 2) == abi.OK
+    want = 1.0
+    for step in range(4):
+        want = want * 2.0 + step
+    assert x.tolist() == [want] * 8 and y.tolist() == [2.0 * want] * 8
+    assert ours.fort_scope_close(scope.handle) == abi.OK
+
+
 def test_slab_pipeline_keeps_coherence_compact(monkeypatch):
     """Ten slabs publish ten interior boxes that merge back into one: no reconciliation is ever needed."""
     monkeypatch.setenv("F2C_TEST_MAPPED", "1")
