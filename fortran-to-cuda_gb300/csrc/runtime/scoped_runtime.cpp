@@ -123,8 +123,15 @@ struct Buffer {
     }
 };
 
+// The trace state (owner, procedure, segment, operation, implementation,
+// boundary) a launch is reported under.
+struct Provenance {
+    char fields[6][65] = {};
+};
+
 struct Task {
     uint64_t code_key = 0;
+    Provenance origin;  // the trace state when the task was accepted: its launch reports it
     LaunchSpec spec;
     std::vector<std::vector<unsigned char>> values;
     std::vector<uint64_t> buffers;
@@ -212,13 +219,43 @@ std::set<uint64_t> g_retired;
 
 uint64_t new_handle() { return ++g_next_handle; }
 
-void trace_line(Context *c, const char *event, uint64_t buffer, uint64_t bytes) {
+// One trace line per runtime event, with the reference's keys: the array's
+// identity and generation when the event concerns one, the bytes moved, the
+// context and its domain (storage when the context owns a private domain),
+// and the provenance fields, `unknown` where unset. A launch of a queued task
+// reports the provenance the task was accepted under.
+void trace_line(Context *c, const char *event, uint64_t buffer, uint64_t bytes, const Provenance *origin = nullptr) {
     if (!tracing()) return;
-    std::fprintf(stderr,
-                 "FORT_SCOPED %s buffer=%" PRIu64 " bytes=%" PRIu64 " context=%" PRIu64
-                 " owner=%s procedure=%s implementation=%s\n",
-                 event, buffer, bytes, c ? c->handle : 0, c && c->trace[0][0] ? c->trace[0] : "unknown",
-                 c && c->trace[1][0] ? c->trace[1] : "unknown", c && c->trace[4][0] ? c->trace[4] : "unknown");
+    std::string line = std::string("FORT_SCOPED ") + event;
+    char text[160];
+    const Buffer *b = nullptr;
+    if (buffer && c && c->domain) {
+        auto it = c->domain->buffers.find(buffer);
+        if (it != c->domain->buffers.end()) b = it->second.get();
+    }
+    if (b) {
+        std::snprintf(text, sizeof text, " buffer=%" PRIu64 " generation=%" PRIu64, b->identity, b->generation);
+        line += text;
+    }
+    std::snprintf(text, sizeof text, " bytes=%" PRIu64 " provenance_version=1 context=%" PRIu64, bytes,
+                  c ? c->handle : 0);
+    line += text;
+    if (c && c->domain) {
+        std::snprintf(text, sizeof text, " domain_version=1 domain=%" PRIu64 " domain_role=%s", c->domain->handle,
+                      c->private_domain ? "storage" : "execution");
+        line += text;
+    }
+    if (b) {
+        std::snprintf(text, sizeof text, " buffer_handle=%" PRIu64, b->handle);
+        line += text;
+    }
+    static const char *const names[6] = {"owner", "procedure", "segment", "operation", "implementation", "boundary"};
+    for (int n = 0; n < 6; ++n) {
+        const char *value = origin ? origin->fields[n] : c ? c->trace[n] : "";
+        line += std::string(" ") + names[n] + "=" + (value[0] ? value : "unknown");
+    }
+    line += "\n";
+    std::fputs(line.c_str(), stderr);
 }
 
 Context *find_context(fort_scope_t handle) {
@@ -818,7 +855,7 @@ uint64_t fnv1a(uint64_t h, const void *data, size_t n) {
 
 void launch_direct(Context *c, std::vector<Task> &tasks) {
     for (auto &t : tasks) {
-        trace_line(c, "launch", 0, 0);
+        trace_line(c, "launch", 0, 0, &t.origin);
         if (!Backend::launch(t.spec, c->stream)) poison(c, std::string("kernel launch failed: ") + Backend::last_error());
     }
     c->queue_stats.direct_submissions++;
@@ -897,7 +934,7 @@ void submit(Context *c, std::vector<Task> &tasks, uint64_t key) {
         g.specs[n].arguments.clear();
         for (auto &v : g.values[n]) g.specs[n].arguments.push_back(v.data());
     }
-    for (size_t n = 0; n < tasks.size(); ++n) trace_line(c, "graph_kernel", 0, 0);
+    for (size_t n = 0; n < tasks.size(); ++n) trace_line(c, "graph_kernel", 0, 0, &tasks[n].origin);
     if (!Backend::graph_launch(g.graph, g.specs, c->stream))
         poison(c, std::string("graph launch failed: ") + Backend::last_error());
 }
@@ -1204,6 +1241,7 @@ void accept(Context *c, Task &&task, std::vector<Bound> &bound) {
     }
     size_t bytes = 0;
     for (auto &v : task.values) bytes += v.size();
+    std::memcpy(task.origin.fields, c->trace, sizeof task.origin.fields);
     c->queue_stats.accepted_tasks++;
     c->queue_stats.copied_argument_bytes += bytes;
     c->pending_threads += task.threads;
@@ -1865,9 +1903,10 @@ static int register_impl(fort_scope_t context, uint64_t identity, uint64_t gener
         }
         b->physical = b->defined;
         *out = b->handle;
-        trace_line(c, "register", b->handle, bytes);
-        d->by_identity[identity] = b->handle;
-        d->buffers[b->handle] = std::move(b);
+        const uint64_t handle = b->handle;
+        d->by_identity[identity] = handle;
+        d->buffers[handle] = std::move(b);
+        trace_line(c, "register", handle, bytes);
         return FORT_SCOPE_OK;
     });
 }

@@ -2356,6 +2356,68 @@ def test_trace_lines(tmp_path):
     assert events.count("upload") == 1 and events.count("download") == 1 and "register" in events
 
 
+PROVENANCE = r"""
+import ctypes as c, sys
+import numpy as np
+sys.path[:0] = sys.argv[1:2]
+from compiler import native
+from compiler.runtime import abi
+lib = abi.bind(c.CDLL(str(native.build_cpu_runtime())))
+KERNEL = c.CFUNCTYPE(None, c.POINTER(c.c_void_p))
+
+
+@KERNEL
+def axpy(args):
+    x = np.ctypeslib.as_array(c.cast(c.cast(args[0], c.POINTER(c.c_void_p))[0], c.POINTER(c.c_double)), shape=(8,))
+    x[:] = x * c.cast(args[2], c.POINTER(c.c_double))[0] + c.cast(args[3], c.POINTER(c.c_double))[0]
+
+
+scope = abi.Scope(lib)
+a = np.ones(8)
+_, h = scope.register(a.ctypes.data, [8])
+dev = (c.c_void_p * 1)()
+assert lib.fort_scope_device_reserve_many_v1(scope.handle, (abi.U64 * 1)(h), 1, dev) == 0
+lib.fort_scope_trace_set_v1(scope.handle, 0b1011, b"a" * 64, b"b" * 64, None, b"d" * 64, None, None, None)
+values = [c.c_void_p(dev[0]), c.c_int(8), c.c_double(1.0), c.c_double(1.0)]
+argv = (c.c_void_p * 4)(*[c.cast(c.pointer(v), c.c_void_p) for v in values])
+sizes = (c.c_size_t * 4)(8, 4, 8, 8)
+task = abi.Task(abi.Kernel(1, 0, c.cast(axpy, c.c_void_p), (c.c_uint32 * 3)(1, 1, 1), (c.c_uint32 * 3)(32, 1, 1), 0,
+                           argv, 4), (abi.Binding * 1)(abi.Binding(h, abi.access(flags=3))), 1)
+for round_ in range(3):
+    for label in (b"1", b"2", b"3"):
+        lib.fort_scope_trace_set_v1(scope.handle, 1 << 4, None, None, None, None, label * 64, None, None)
+        assert lib.fort_scope_graph_enqueue_v1(scope.handle, 7, c.byref(task), sizes) == 0
+    lib.fort_scope_trace_set_v1(scope.handle, 1 << 4, None, None, None, None, b"9" * 64, None, None)
+    assert lib.fort_scope_graph_flush_v1(scope.handle) == 0
+assert lib.fort_scope_close(scope.handle) == 0
+assert a.tolist() == [10.0] * 8
+"""
+
+
+def test_queued_launches_report_the_provenance_they_were_accepted_under(tmp_path):
+    """A queued task's launch, direct or as a graph node, carries the trace state of its acceptance, not the one
+    current at the flush; every line carries the reference's keys (reference:
+    test_scoped_graph_queue_cuda.py:343-372)."""
+    import re
+
+    script = tmp_path / "provenance.py"
+    script.write_text(PROVENANCE)
+    run = subprocess.run([sys.executable, str(script), os.path.join(ROOT, "fortran-to-cuda_gb300")],
+                         capture_output=True, text=True, timeout=120, env={**os.environ, "FORT_RUNTIME_TRACE": "1"})
+    assert run.returncode == 0, run.stdout + run.stderr
+    rows = [(m[1], dict(re.findall(r"(\w+)=([^\s]+)", m[2]))) for line in run.stderr.splitlines()
+            if (m := re.match(r"FORT_SCOPED (launch|graph_kernel|register) (.*)", line))]
+    launched = [row for event, row in rows if event in ("launch", "graph_kernel")]
+    assert [row["implementation"] for row in launched] == [d * 64 for d in "123123123"]
+    assert [event for event, _ in rows if event != "register"] == ["launch"] * 3 + ["graph_kernel"] * 6
+    assert all(row["owner"] == "a" * 64 and row["procedure"] == "b" * 64 and row["operation"] == "d" * 64
+               and row["segment"] == "unknown" and row["bytes"] == "0" and row["provenance_version"] == "1"
+               for row in launched)
+    (register,) = [row for event, row in rows if event == "register"]
+    assert register["bytes"] == "64" and "buffer" in register and register["generation"] == "1"
+    assert register["domain_role"] == "storage"
+
+
 # ------------------------------------------------------------------------------- slab pipelines
 
 NX_S, NY_S, NZ_S = 4, 3, 10  # extents; planes 1..8 are the interior along the last dimension
