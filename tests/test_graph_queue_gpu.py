@@ -7,8 +7,10 @@ backend's graph construction, parameter updates, replays and direct launches
 run for real. The behaviours follow the reference's CUDA suites
 (compiler/tests/test_scoped_graph_replay_cuda.py:241-262: replay, rebinding,
 topology change, long groups; test_scoped_graph_queue_cuda.py:333-341: the
-deferred queue). The client checks every value it reads back and prints the
-runtime's statistics as one JSON line per scenario.
+deferred queue). An external provider's kernel on the runtime's stream is ordered before
+the publication that follows it (test_scoped_domains_cuda.py:267-300). The
+client checks every value it reads back and prints the runtime's statistics
+as one JSON line per scenario.
 """
 
 import json
@@ -25,6 +27,7 @@ CLIENT = r"""
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <cuda_runtime.h>
 #include "scoped_runtime.h"
 
 #define CHECK(x)                                                                                 \
@@ -227,8 +230,67 @@ static int long_chain() {
     return expect(x, [](int i) { return i + 63.0 * 64.0 / 2.0; }, "long");
 }
 
+// an external provider's kernel, slowed down by a bounded spin on the clock, runs on the stream the runtime
+// hands it: the publication that follows must wait for it
+__global__ void slow_double(const double *a, double *b, int n, long long delay) {
+    const long long start = clock64();
+    while (clock64() - start < delay) {
+    }
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) b[i] = 2.0 * a[i];
+}
+
+static int provider(void *user, const fort_scope_external_view_v1 *views, size_t count, void *stream, int *started) {
+    if (count != 2 || !views[0].device || !views[1].device || views[1].bytes != N * sizeof(double)) return 1;
+    const long long delay = *static_cast<const long long *>(user);
+    slow_double<<<N / 256, 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        static_cast<const double *>(views[0].device), static_cast<double *>(views[1].device), N, delay);
+    *started = 1;
+    return cudaGetLastError() == cudaSuccess ? 0 : 1;
+}
+
+static int external() {
+    fort_scope_t ctx = 0;
+    CHECK(fort_scope_create(0, &ctx));
+    static Array a, b;
+    for (int i = 0; i < N; ++i) a.host[i] = 0.25 * i;
+    if (add_array(ctx, a, 1, true)) return 1;
+    fort_scope_layout layout{1, FORT_SCOPE_REAL64, 8, b.host, g_extent, g_lower, 1};
+    CHECK(fort_scope_register(ctx, 2, 1, &layout, 0, &b.handle));
+    fort_scope_external_binding_v1 bindings[2];
+    std::memset(bindings, 0, sizeof bindings);
+    bindings[0].buffer = a.handle;
+    bindings[0].access = whole(FORT_SCOPE_READ_ALL);
+    bindings[1].buffer = b.handle;
+    bindings[1].access = whole(FORT_SCOPE_WRITE_ALL | FORT_SCOPE_OVERWRITE_ALL);
+    for (auto &x : bindings) {
+        x.type = FORT_SCOPE_REAL64;
+        x.rank = 1;
+        x.element_bytes = 8;
+    }
+    fort_scope_external_call_v1 call;
+    std::memset(&call, 0, sizeof call);
+    call.version = FORT_SCOPE_EXTERNAL_ABI_VERSION;
+    call.bindings = bindings;
+    call.binding_count = 2;
+    long long delay = 4000000;  // about 2 ms of clock cycles
+    fort_scope_external_report_v1 report{};
+    CHECK(fort_scope_external_execute_v1(ctx, &call, provider, &delay, &report));
+    if (report.status != 0 || !report.started || !report.committed) {
+        std::fprintf(stderr, "report: status %d started %u committed %u\n", report.status, report.started,
+                     report.committed);
+        return 1;
+    }
+    CHECK(observe(ctx, b.handle));  // reads what the provider's kernel wrote, after it finished
+    if (expect(b, [](int i) { return 0.5 * i; }, "external")) return 1;
+    print_stats(ctx, "external");
+    CHECK(fort_scope_close(ctx));
+    return 0;
+}
+
 int main(int argc, char **argv) {
     const std::string mode = argc > 1 ? argv[1] : "";
+    if (mode == "external") return external();
     if (mode == "queue") return queue_replay();
     if (mode == "group") return group_replay();
     if (mode == "cancel") return cancel();
@@ -283,3 +345,12 @@ def test_a_long_chain_goes_in_one_submission(client):
     chain = _run(client, "long")["long"]
     assert chain["accepted_tasks"] == 64 and chain["pending_tasks"] == 0
     assert chain["submissions"] == 1
+
+
+def test_an_external_providers_kernel_is_ordered_before_the_publication(client):
+    """The provider launches a deliberately slow kernel on the stream the runtime hands it; observing its output
+    right after the call returns still sees every value it wrote (reference:
+    test_scoped_domains_cuda.py:267-300, actual stream ordering)."""
+    e = _run(client, "external")["external"]
+    assert e["downloads"] == 1 and e["uploads"] == 1
+
