@@ -934,6 +934,7 @@ void submit(Context *c, std::vector<Task> &tasks, uint64_t key) {
         g.specs[n].arguments.clear();
         for (auto &v : g.values[n]) g.specs[n].arguments.push_back(v.data());
     }
+    trace_line(c, "graph_submit", 0, tasks.size());
     for (size_t n = 0; n < tasks.size(); ++n) trace_line(c, "graph_kernel", 0, 0, &tasks[n].origin);
     if (!Backend::graph_launch(g.graph, g.specs, c->stream))
         poison(c, std::string("graph launch failed: ") + Backend::last_error());
@@ -1002,6 +1003,7 @@ void submit_group(Context *c, const std::vector<LaunchSpec> &specs, uint64_t key
         }
         c->graph_stats.replays++;
     }
+    trace_line(c, "graph_submit", 0, specs.size());
     for (size_t n = 0; n < specs.size(); ++n) trace_line(c, "graph_kernel", 0, 0);
     if (!Backend::graph_launch(g.graph, specs, c->stream))
         poison(c, std::string("graph launch failed: ") + Backend::last_error());

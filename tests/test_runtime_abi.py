@@ -2406,7 +2406,9 @@ def test_queued_launches_report_the_provenance_they_were_accepted_under(tmp_path
                          capture_output=True, text=True, timeout=120, env={**os.environ, "FORT_RUNTIME_TRACE": "1"})
     assert run.returncode == 0, run.stdout + run.stderr
     rows = [(m[1], dict(re.findall(r"(\w+)=([^\s]+)", m[2]))) for line in run.stderr.splitlines()
-            if (m := re.match(r"FORT_SCOPED (launch|graph_kernel|register) (.*)", line))]
+            if (m := re.match(r"FORT_SCOPED (launch|graph_kernel|graph_submit|register) (.*)", line))]
+    assert [row["bytes"] for event, row in rows if event == "graph_submit"] == ["3", "3"]
+    rows = [(event, row) for event, row in rows if event != "graph_submit"]
     launched = [row for event, row in rows if event in ("launch", "graph_kernel")]
     assert [row["implementation"] for row in launched] == [d * 64 for d in "123123123"]
     assert [event for event, _ in rows if event != "register"] == ["launch"] * 3 + ["graph_kernel"] * 6
