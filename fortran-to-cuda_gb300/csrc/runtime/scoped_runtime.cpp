@@ -738,6 +738,16 @@ bool dirty_mirror(const Buffer *b) {
     return !dirty.empty();
 }
 
+// Said once per shared domain (the resident application's), in the reference's
+// words: what exceeding the device budget costs from now on.
+void budget_warning(Context *c, const char *consequence) {
+    Domain *d = c->domain;
+    if (c->private_domain || d->budget_warned) return;
+    d->budget_warned = true;
+    std::fprintf(stderr, "Resident domain: the arrays in use exceed the device budget of %zu bytes; %s.\n", d->budget,
+                 consequence);
+}
+
 // Make room for `bytes` more, evicting mirrors that are not in `keep`, not
 // prepared and not used by queued tasks: clean ones (dropped without a
 // download) before dirty ones, each kind least recently used first, ties by
@@ -753,13 +763,7 @@ void make_room(Context *c, size_t bytes, const std::set<uint64_t> &keep) {
         if (b->device && !keep.count(b->handle) && b->prepared == Buffer::NONE) evictable += b->bytes;
     }
     if (claimed(d) - evictable + bytes > d->budget) {
-        if (!d->budget_warned) {
-            d->budget_warned = true;
-            std::fprintf(stderr,
-                         "FORT_SCOPED budget_warning domain=%" PRIu64 " budget=%zu requested=%zu claimed=%zu: the "
-                         "statements run natively where their arrays do not fit\n",
-                         d->handle, d->budget, bytes, claimed(d));
-        }
+        budget_warning(c, "loop nests whose arrays do not fit together run on the host");
         raise(FORT_SCOPE_RESOURCE, "device budget too small for the task footprint");
     }
     if (!c->pending.empty()) {
@@ -788,6 +792,7 @@ void make_room(Context *c, size_t bytes, const std::set<uint64_t> &keep) {
             publish_buffer(c, victim);
             wait_stream(c);
         }
+        budget_warning(c, "the least recently used ones now move back to the host");
         d->residency.evictions++;
         d->residency.evicted_bytes += victim->bytes;
         trace_line(c, "evict", victim->handle, victim->bytes);

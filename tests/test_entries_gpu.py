@@ -172,7 +172,9 @@ def test_budget_too_small_declines_before_any_work(cuda, capfd):
     dom.end_epoch()
     dom.close()
     assert (out == 3.0).all()
-    assert capfd.readouterr().err.count("budget_warning") == 1
+    assert capfd.readouterr().err.count("Resident domain: the arrays in use exceed the device budget of "
+                                        f"{2 * f.U.nbytes} bytes; loop nests whose arrays do not fit together run "
+                                        "on the host.") == 1
 
 
 @pytest.mark.parametrize("nx, ny, nz, path", [(96, 64, 16, "in place"), (96, 64, 48, "in place"),

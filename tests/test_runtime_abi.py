@@ -1630,6 +1630,26 @@ def test_host_only_use_never_initializes_the_device(both, use, tmp_path):
     assert len(initialized) == (use == "device")
 
 
+@pytest.mark.parametrize("shared", [False, True])
+def test_the_budget_warning_is_said_once_per_shared_domain(both, shared, capfd):
+    """An eviction in a context of a shared domain (the resident application's) says once what exceeding the
+    budget costs, in the reference's words; a private context says nothing (reference:
+    compiler/runtime/scoped_runtime.cu:535-543, test_resident_application_cuda.py:118-135)."""
+    domain = _domain(both) if shared else None
+    scope = abi.Scope(both, domain=domain)
+    assert both.fort_scope_set_device_budget(scope.handle, 64) == abi.OK
+    handles = [_resident(scope, n)[1] for n in (1, 2, 3)]
+    for h in handles * 2:
+        assert _reserve_many(both, scope, h)[0] == abi.OK
+    assert _residency(both, scope).evictions == 5
+    assert both.fort_scope_close(scope.handle) == abi.OK
+    if shared:
+        assert both.fort_scope_domain_close_v1(domain) == abi.OK
+    said = capfd.readouterr().err.count("Resident domain: the arrays in use exceed the device budget of 64 bytes; "
+                                        "the least recently used ones now move back to the host.")
+    assert said == (1 if shared else 0)
+
+
 def test_scratch_leases(both):
     scope = abi.Scope(both)
     lease = abi.ScratchLease()
