@@ -8,7 +8,9 @@ run for real. The behaviours follow the reference's CUDA suites
 (compiler/tests/test_scoped_graph_replay_cuda.py:241-262: replay, rebinding,
 topology change, long groups; test_scoped_graph_queue_cuda.py:333-341: the
 deferred queue). An external provider's kernel on the runtime's stream is ordered before
-the publication that follows it (test_scoped_domains_cuda.py:267-300). The
+the publication that follows it (test_scoped_domains_cuda.py:267-300), and
+host work waits only for the device work it conflicts with, checked against a
+kernel delayed by a bounded spin (test_scoped_host_completion_cuda.py). The
 client checks every value it reads back and prints the runtime's statistics
 as one JSON line per scenario.
 """
@@ -288,8 +290,74 @@ static int external() {
     return 0;
 }
 
+// a device write delayed by about 40 ms of clock cycles (a bounded spin), on the context's stream
+__global__ void delayed_fill(double *out, int n, double value, long long cycles) {
+    const long long start = clock64();
+    while (clock64() - start < cycles) {
+    }
+    for (int i = 0; i < n; ++i) out[i] = value;
+}
+
+static int completion() {
+    fort_scope_t ctx = 0;
+    CHECK(fort_scope_create(0, &ctx));
+    static Array a, x;
+    for (int i = 0; i < N; ++i) {
+        a.host[i] = 0.0;
+        x.host[i] = 10.0 + i;
+    }
+    fort_scope_layout la{1, FORT_SCOPE_REAL64, 8, a.host, g_extent, g_lower, 1};
+    fort_scope_layout lx{1, FORT_SCOPE_REAL64, 8, x.host, g_extent, g_lower, 1};
+    CHECK(fort_scope_register(ctx, 1, 1, &la, 1, &a.handle));
+    CHECK(fort_scope_register(ctx, 2, 1, &lx, 1, &x.handle));
+    int previous = 0;
+    void *raw = nullptr;
+    CHECK(fort_scope_gpu_enter(ctx, &previous, &raw));
+    cudaStream_t stream = static_cast<cudaStream_t>(raw);
+    int khz = 0;
+    if (cudaDeviceGetAttribute(&khz, cudaDevAttrClockRate, 0) != cudaSuccess || khz <= 0) return 1;
+    const long long cycles = static_cast<long long>(khz) * 40;
+    fort_scope_access write = whole(FORT_SCOPE_WRITE_ALL | FORT_SCOPE_OVERWRITE_ALL);
+    double *pa = nullptr;
+    CHECK(fort_scope_device_begin(ctx, a.handle, &write, reinterpret_cast<void **>(&pa)));
+    delayed_fill<<<1, 1, 0, stream>>>(pa, N, 1.0, cycles);
+    if (cudaGetLastError() != cudaSuccess) return 1;
+    CHECK(fort_scope_note_launch(ctx));
+    CHECK(fort_scope_device_end(ctx, a.handle));
+    cudaEvent_t marker;
+    if (cudaEventCreateWithFlags(&marker, cudaEventDisableTiming) != cudaSuccess) return 1;
+    if (cudaEventRecord(marker, stream) != cudaSuccess) return 1;
+    fort_scope_stats before{}, after{};
+    CHECK(fort_scope_stats_get(ctx, &before));
+    // host work on an array the pending kernel does not touch returns at once
+    fort_scope_access rw = whole(FORT_SCOPE_READ_ALL | FORT_SCOPE_WRITE_ALL);
+    CHECK(fort_scope_host_begin(ctx, x.handle, &rw));
+    x.host[0] = 99.0;
+    CHECK(fort_scope_host_end(ctx, x.handle));
+    const bool pending = cudaEventQuery(marker) == cudaErrorNotReady;
+    cudaGetLastError();
+    CHECK(fort_scope_stats_get(ctx, &after));
+    fort_scope_completion_stats_v1 cs{};
+    CHECK(fort_scope_completion_stats_get_v1(ctx, &cs));
+    // host work on the array it writes waits for it
+    fort_scope_access read = whole(FORT_SCOPE_READ_ALL);
+    CHECK(fort_scope_host_begin(ctx, a.handle, &read));
+    const bool seen = a.host[0] == 1.0 && a.host[N - 1] == 1.0;
+    CHECK(fort_scope_host_end(ctx, a.handle));
+    const bool done = cudaEventQuery(marker) == cudaSuccess;
+    cudaEventDestroy(marker);
+    std::printf("{\"scenario\": \"completion\", \"pending_after_independent\": %s, \"independent_waits\": %llu, "
+                "\"independent_host_tasks\": %llu, \"dependent_saw_kernel\": %s, \"done_after_dependent\": %s}\n",
+                pending ? "true" : "false", (unsigned long long)(after.waits - before.waits),
+                (unsigned long long)cs.independent_host_tasks, seen ? "true" : "false", done ? "true" : "false");
+    CHECK(fort_scope_gpu_leave(ctx, previous));
+    CHECK(fort_scope_close(ctx));
+    return 0;
+}
+
 int main(int argc, char **argv) {
     const std::string mode = argc > 1 ? argv[1] : "";
+    if (mode == "completion") return completion();
     if (mode == "external") return external();
     if (mode == "queue") return queue_replay();
     if (mode == "group") return group_replay();
@@ -353,4 +421,13 @@ def test_an_external_providers_kernel_is_ordered_before_the_publication(client):
     test_scoped_domains_cuda.py:267-300, actual stream ordering)."""
     e = _run(client, "external")["external"]
     assert e["downloads"] == 1 and e["uploads"] == 1
+
+
+def test_host_work_waits_only_for_the_device_work_it_conflicts_with(client):
+    """While a kernel delayed by about 40 ms writes one array, host work on another array returns at once with no
+    wait; host work on the written array waits for the kernel and sees its values (reference:
+    test_scoped_host_completion_cuda.py:197-203, the independent scenario)."""
+    r = _run(client, "completion")["completion"]
+    assert r["pending_after_independent"] and r["independent_waits"] == 0 and r["independent_host_tasks"] >= 1
+    assert r["dependent_saw_kernel"] and r["done_after_dependent"]
 
