@@ -10,7 +10,9 @@ topology change, long groups; test_scoped_graph_queue_cuda.py:333-341: the
 deferred queue). An external provider's kernel on the runtime's stream is ordered before
 the publication that follows it (test_scoped_domains_cuda.py:267-300), and
 host work waits only for the device work it conflicts with, checked against a
-kernel delayed by a bounded spin (test_scoped_host_completion_cuda.py). The
+kernel delayed by a bounded spin (test_scoped_host_completion_cuda.py), and
+sparse sections move exactly through real pitched copies
+(test_scoped_direct_copy_cuda.py). The
 client checks every value it reads back and prints the runtime's statistics
 as one JSON line per scenario.
 """
@@ -355,8 +357,165 @@ static int completion() {
     return 0;
 }
 
+// exact sparse transfers through real DMA: the halo of a 134 x 70 x 70 array moves as its six faces, stripes
+// one byte wide of a byte array move as twenty pitched copies, and mirrors that both hold the values survive
+// interleaved read-only use without transfers
+constexpr size_t EX = 134, EY = 70, EZ = 70, EN = EX * EY * EZ;
+__global__ void fill_index(double *p) {
+    const size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < EN) p[i] = 1000000.0 + i;
+}
+__global__ void fill_bytes(unsigned char *p, size_t n) {
+    const size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < n) p[i] = i % 251 + 1;
+}
+static bool in_halo(size_t x, size_t y, size_t z) { return x < 3 || x >= 131 || y < 3 || y >= 67 || z < 2 || z >= 68; }
+
+static int exact_faces() {
+    static double host[EN], got[EN];
+    for (size_t i = 0; i < EN; ++i) host[i] = -7.0;
+    fort_scope_t ctx = 0;
+    fort_buffer_t b = 0;
+    CHECK(fort_scope_create(0, &ctx));
+    size_t shape[3] = {EX, EY, EZ};
+    int64_t lower[3] = {-10, 2, -100};
+    fort_scope_layout layout{3, FORT_SCOPE_REAL64, 8, host, shape, lower, 1};
+    CHECK(fort_scope_register(ctx, 1, 1, &layout, 1, &b));
+    int previous = 0;
+    void *raw = nullptr;
+    CHECK(fort_scope_gpu_enter(ctx, &previous, &raw));
+    cudaStream_t stream = static_cast<cudaStream_t>(raw);
+    fort_scope_access write_all = whole(FORT_SCOPE_WRITE_ALL | FORT_SCOPE_OVERWRITE_ALL);
+    double *device = nullptr;
+    CHECK(fort_scope_device_begin(ctx, b, &write_all, reinterpret_cast<void **>(&device)));
+    fill_index<<<(EN + 255) / 256, 256, 0, stream>>>(device);
+    if (cudaGetLastError() != cudaSuccess) return 1;
+    CHECK(fort_scope_note_launch(ctx));
+    CHECK(fort_scope_device_end(ctx, b));
+    size_t lo[3] = {3, 3, 2}, hi[3] = {131, 67, 68};
+    fort_scope_section interior{lo, hi};
+    fort_scope_access overwrite{0, 0, nullptr, 1, &interior, 1, &interior};
+    CHECK(fort_scope_host_begin(ctx, b, &overwrite));
+    for (size_t z = 2; z < 68; ++z)
+        for (size_t y = 3; y < 67; ++y)
+            for (size_t x = 3; x < 131; ++x) host[x + EX * (y + EY * z)] = -42.0;
+    CHECK(fort_scope_host_end(ctx, b));
+    CHECK(observe(ctx, b));
+    fort_scope_stats first{}, mirrored{}, after{}, before{}, uploaded{};
+    CHECK(fort_scope_stats_get(ctx, &first));
+    const size_t face_bytes = (EN - size_t(128) * 64 * 66) * sizeof(double);
+    int bad = 0;
+    for (size_t z = 0; z < EZ; ++z)
+        for (size_t y = 0; y < EY; ++y)
+            for (size_t x = 0; x < EX; ++x) {
+                const size_t i = x + EX * (y + EY * z);
+                bad += host[i] != (in_halo(x, y, z) ? 1000000.0 + i : -42.0);
+            }
+    fort_scope_access read_all = whole(FORT_SCOPE_READ_ALL);
+    CHECK(fort_scope_device_begin(ctx, b, &read_all, reinterpret_cast<void **>(&device)));
+    CHECK(fort_scope_device_end(ctx, b));
+    CHECK(fort_scope_wait(ctx));
+    CHECK(fort_scope_stats_get(ctx, &mirrored));
+    for (int n = 0; n < 20; ++n) {
+        CHECK(fort_scope_host_begin(ctx, b, &read_all));
+        CHECK(fort_scope_host_end(ctx, b));
+        CHECK(fort_scope_device_begin(ctx, b, &read_all, reinterpret_cast<void **>(&device)));
+        CHECK(fort_scope_device_end(ctx, b));
+    }
+    CHECK(fort_scope_stats_get(ctx, &after));
+    size_t lows[6][3] = {{0, 0, 0}, {131, 0, 0}, {3, 0, 0}, {3, 67, 0}, {3, 3, 0}, {3, 3, 68}};
+    size_t highs[6][3] = {{3, EY, EZ}, {EX, EY, EZ}, {131, 3, EZ}, {131, EY, EZ}, {131, 67, 2}, {131, 67, EZ}};
+    fort_scope_section faces[6];
+    for (int n = 0; n < 6; ++n) faces[n] = {lows[n], highs[n]};
+    fort_scope_access halo_write{0, 0, nullptr, 6, faces, 6, faces};
+    CHECK(fort_scope_host_begin(ctx, b, &halo_write));
+    for (size_t z = 0; z < EZ; ++z)
+        for (size_t y = 0; y < EY; ++y)
+            for (size_t x = 0; x < EX; ++x)
+                if (in_halo(x, y, z)) host[x + EX * (y + EY * z)] = 2000000.0 + (x + EX * (y + EY * z));
+    CHECK(fort_scope_host_end(ctx, b));
+    CHECK(fort_scope_stats_get(ctx, &before));
+    CHECK(fort_scope_device_begin(ctx, b, &read_all, reinterpret_cast<void **>(&device)));
+    CHECK(fort_scope_device_end(ctx, b));
+    CHECK(fort_scope_wait(ctx));
+    CHECK(fort_scope_stats_get(ctx, &uploaded));
+    if (cudaMemcpy(got, device, sizeof got, cudaMemcpyDeviceToHost) != cudaSuccess) return 1;
+    for (size_t i = 0; i < EN; ++i) bad += got[i] != host[i];
+    CHECK(fort_scope_gpu_leave(ctx, previous));
+    CHECK(fort_scope_close(ctx));
+    std::printf("{\"scenario\": \"faces\", \"bad\": %d, \"downloads\": %llu, \"download_bytes\": %llu, "
+                "\"face_bytes\": %zu, \"interleaved_transfers\": %llu, \"uploads\": %llu, \"upload_bytes\": %llu}\n",
+                bad, (unsigned long long)first.downloads, (unsigned long long)first.download_bytes, face_bytes,
+                (unsigned long long)(after.uploads - mirrored.uploads + after.downloads - mirrored.downloads),
+                (unsigned long long)(uploaded.uploads - before.uploads),
+                (unsigned long long)(uploaded.upload_bytes - before.upload_bytes));
+    return 0;
+}
+
+static int byte_stripes() {
+    constexpr size_t a = 135, b = 71, d = 71, n = a * b * d;
+    static unsigned char host[n], got[n];
+    std::memset(host, 0, sizeof host);
+    fort_scope_t ctx = 0;
+    fort_buffer_t buffer = 0;
+    CHECK(fort_scope_create(0, &ctx));
+    size_t shape[3] = {a, b, d};
+    int64_t lower[3] = {-5, -9, 100};
+    fort_scope_layout layout{3, FORT_SCOPE_BYTES, 1, host, shape, lower, 1};
+    CHECK(fort_scope_register(ctx, 1, 1, &layout, 1, &buffer));
+    int previous = 0;
+    void *raw = nullptr;
+    CHECK(fort_scope_gpu_enter(ctx, &previous, &raw));
+    cudaStream_t stream = static_cast<cudaStream_t>(raw);
+    fort_scope_access overwrite_all = whole(FORT_SCOPE_WRITE_ALL | FORT_SCOPE_OVERWRITE_ALL);
+    unsigned char *device = nullptr;
+    CHECK(fort_scope_device_begin(ctx, buffer, &overwrite_all, reinterpret_cast<void **>(&device)));
+    fill_bytes<<<(n + 255) / 256, 256, 0, stream>>>(device, n);
+    if (cudaGetLastError() != cudaSuccess) return 1;
+    CHECK(fort_scope_note_launch(ctx));
+    CHECK(fort_scope_device_end(ctx, buffer));
+    size_t lo[20][3], hi[20][3];
+    fort_scope_section sections[20];
+    for (size_t k = 0; k < 20; ++k) {
+        lo[k][0] = k * 6 + 1;
+        lo[k][1] = lo[k][2] = 0;
+        hi[k][0] = k * 6 + 2;
+        hi[k][1] = b;
+        hi[k][2] = d;
+        sections[k] = {lo[k], hi[k]};
+    }
+    fort_scope_access reads{0, 20, sections, 0, nullptr, 0, nullptr};
+    CHECK(fort_scope_host_begin(ctx, buffer, &reads));
+    CHECK(fort_scope_host_end(ctx, buffer));
+    int bad = 0;
+    auto selected = [&](size_t i) { const size_t x = i % a; return x >= 1 && x <= 115 && (x - 1) % 6 == 0; };
+    for (size_t i = 0; i < n; ++i) bad += host[i] != (selected(i) ? i % 251 + 1 : 0);
+    fort_scope_stats first{}, last{};
+    CHECK(fort_scope_stats_get(ctx, &first));
+    fort_scope_access writes{0, 0, nullptr, 20, sections, 20, sections};
+    CHECK(fort_scope_host_begin(ctx, buffer, &writes));
+    for (size_t i = 0; i < n; ++i)
+        if (selected(i)) host[i] = 255 - i % 251;
+    CHECK(fort_scope_host_end(ctx, buffer));
+    CHECK(fort_scope_device_begin(ctx, buffer, &reads, reinterpret_cast<void **>(&device)));
+    CHECK(fort_scope_device_end(ctx, buffer));
+    CHECK(fort_scope_wait(ctx));
+    if (cudaMemcpy(got, device, n, cudaMemcpyDeviceToHost) != cudaSuccess) return 1;
+    for (size_t i = 0; i < n; ++i) bad += got[i] != (selected(i) ? 255 - i % 251 : i % 251 + 1);
+    CHECK(fort_scope_stats_get(ctx, &last));
+    CHECK(fort_scope_gpu_leave(ctx, previous));
+    CHECK(fort_scope_close(ctx));
+    std::printf("{\"scenario\": \"stripes\", \"bad\": %d, \"downloads\": %llu, \"download_bytes\": %llu, "
+                "\"uploads\": %llu, \"upload_bytes\": %llu, \"stripe_bytes\": %zu}\n",
+                bad, (unsigned long long)first.downloads, (unsigned long long)first.download_bytes,
+                (unsigned long long)last.uploads, (unsigned long long)last.upload_bytes, 20 * b * d);
+    return 0;
+}
+
 int main(int argc, char **argv) {
     const std::string mode = argc > 1 ? argv[1] : "";
+    if (mode == "faces") return exact_faces();
+    if (mode == "stripes") return byte_stripes();
     if (mode == "completion") return completion();
     if (mode == "external") return external();
     if (mode == "queue") return queue_replay();
@@ -382,8 +541,11 @@ def client(tmp_path_factory):
     return exe
 
 
-def _run(client: Path, mode: str):
-    run = subprocess.run([str(client), mode], capture_output=True, text=True, timeout=120)
+def _run(client: Path, mode: str, **env):
+    import os
+
+    run = subprocess.run([str(client), mode], capture_output=True, text=True, timeout=120,
+                         env={**os.environ, **env})
     assert run.returncode == 0, run.stdout + run.stderr
     return {r["scenario"]: r for r in map(json.loads, run.stdout.splitlines())}
 
@@ -430,4 +592,21 @@ def test_host_work_waits_only_for_the_device_work_it_conflicts_with(client):
     r = _run(client, "completion")["completion"]
     assert r["pending_after_independent"] and r["independent_waits"] == 0 and r["independent_host_tasks"] >= 1
     assert r["dependent_saw_kernel"] and r["done_after_dependent"]
+
+
+def test_sparse_sections_move_exactly_through_real_copies(client):
+    """The halo of a 134 x 70 x 70 array (lower bounds -10, 2, -100) comes home as its six faces and goes back as
+    six uploads of exactly those bytes; mirrors that both hold the values survive twenty interleaved read-only
+    uses without a transfer; twenty byte stripes one element wide move as twenty pitched copies each way.
+    Arrays are kept as device mirrors here (no in-place use of the host array), as the reference's direct
+    transport keeps them (reference: test_scoped_direct_copy_cuda.py:111-118)."""
+    faces = _run(client, "faces", FORT_SCOPE_HOST_IN_PLACE="0")["faces"]
+    assert faces["bad"] == 0
+    assert (faces["downloads"], faces["download_bytes"]) == (6, faces["face_bytes"])
+    assert faces["interleaved_transfers"] == 0
+    assert (faces["uploads"], faces["upload_bytes"]) == (6, faces["face_bytes"])
+    stripes = _run(client, "stripes", FORT_SCOPE_HOST_IN_PLACE="0")["stripes"]
+    assert stripes["bad"] == 0
+    assert (stripes["downloads"], stripes["download_bytes"]) == (20, stripes["stripe_bytes"])
+    assert (stripes["uploads"], stripes["upload_bytes"]) == (20, stripes["stripe_bytes"])
 
