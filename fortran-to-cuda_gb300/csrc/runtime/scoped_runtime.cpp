@@ -34,6 +34,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <deque>
+#include <initializer_list>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -1441,6 +1442,56 @@ void release_scratch(Context *c) {
     }
 }
 
+// The statistics of a context as it closes, one `FORT_SCOPED evidence` JSON
+// line per kind that saw any use (the reference's records, same keys):
+// graphs, host completions, the task queue, residency.
+void evidence(Context *c) {
+    if (!tracing()) return;
+    const bool complete = !c->poisoned && !c->domain->poisoned;
+    const std::string head = "FORT_SCOPED evidence {\"schema_version\":1,\"context\":" + std::to_string(c->handle) +
+                             ",\"domain_version\":1,\"domain\":" + std::to_string(c->domain->handle) +
+                             ",\"domain_role\":\"" + (c->private_domain ? "storage" : "execution") + "\"";
+    auto record = [&](const char *event, const std::string &extra,
+                      std::initializer_list<std::pair<const char *, uint64_t>> fields) {
+        std::string line = head + ",\"event\":\"" + event + "\",\"stats_version\":1,\"complete\":" +
+                           (complete ? "true" : "false") + extra;
+        for (const auto &f : fields) line += std::string(",\"") + f.first + "\":" + std::to_string(f.second);
+        line += "}\n";
+        std::fputs(line.c_str(), stderr);
+    };
+    const auto &g = c->graph_stats;
+    const auto &q = c->queue_stats;
+    const auto &k = c->completion;
+    const auto &r = c->domain->residency;
+    if (g.creations || q.direct_kernels)
+        record("graph_statistics", "",
+               {{"creations", g.creations}, {"instantiations", g.instantiations}, {"rebuilds", g.rebuilds},
+                {"submissions", g.submissions}, {"replays", g.replays}, {"parameter_updates", g.parameter_updates},
+                {"logical_kernels", g.logical_kernels}, {"live_graphs", g.live_graphs},
+                {"destructions", g.destructions}});
+    if (k.event_records || k.independent_host_tasks)
+        record("completion_statistics", "",
+               {{"event_records", k.event_records}, {"event_queries", k.event_queries}, {"event_waits", k.event_waits},
+                {"stream_waits", k.stream_waits}, {"created_events", k.created_events},
+                {"reused_events", k.reused_events}, {"independent_host_tasks", k.independent_host_tasks}});
+    if (q.accepted_tasks || q.submissions || q.direct_submissions || q.direct_kernels || !q.queue_enabled ||
+        !q.graphs_enabled)
+        record("command_queue_statistics",
+               ",\"queue_enabled\":" + std::to_string(q.queue_enabled) + ",\"graphs_enabled\":" +
+                   std::to_string(q.graphs_enabled),
+               {{"accepted_tasks", q.accepted_tasks}, {"submissions", q.submissions},
+                {"conflict_flushes", q.conflict_flushes}, {"explicit_flushes", q.explicit_flushes},
+                {"pending_tasks", q.pending_tasks}, {"peak_pending_tasks", q.peak_pending_tasks},
+                {"copied_argument_bytes", q.copied_argument_bytes}, {"direct_submissions", q.direct_submissions},
+                {"direct_kernels", q.direct_kernels}, {"graph_resource_fallbacks", q.graph_resource_fallbacks}});
+    if (r.evictions)
+        record("residency_statistics", ",\"device_budget\":" + std::to_string(c->domain->budget),
+               {{"reserve_batches", r.reserve_batches}, {"requested_resources", r.requested_resources},
+                {"reuse_hits", r.reuse_hits}, {"evictions", r.evictions}, {"evicted_bytes", r.evicted_bytes},
+                {"dirty_evictions", r.dirty_evictions}, {"dirty_download_bytes", r.dirty_download_bytes},
+                {"pressure_flushes", r.pressure_flushes}});
+}
+
 void detach(Context *c) {
     if (c->copies_ready) {
         Backend::sync(c->copy_in);
@@ -1453,10 +1504,16 @@ void detach(Context *c) {
         Backend::sync(c->stream);
         for (auto *cache : {&c->graphs, &c->group_graphs})
             for (auto &kv : *cache)
-                if (kv.second.graph) Backend::graph_destroy(kv.second.graph);
+                if (kv.second.graph) {
+                    Backend::graph_destroy(kv.second.graph);
+                    kv.second.graph = nullptr;
+                    c->graph_stats.destructions++;
+                    c->graph_stats.live_graphs--;
+                }
         release_events(c);
         Backend::destroy_stream(c->stream);
     }
+    evidence(c);
     if (c->domain->borrower == c) c->domain->borrower = nullptr;
     g_retired.insert(c->handle);
     g_contexts.erase(c->handle);

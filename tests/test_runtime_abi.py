@@ -14,6 +14,7 @@ restated: this runtime's CPU backend runs test kernels as host functions.
 """
 
 import ctypes as c
+import json
 import os
 import shutil
 import subprocess
@@ -2438,6 +2439,13 @@ def test_queued_launches_report_the_provenance_they_were_accepted_under(tmp_path
     (register,) = [row for event, row in rows if event == "register"]
     assert register["bytes"] == "64" and "buffer" in register and register["generation"] == "1"
     assert register["domain_role"] == "storage"
+    # closing reports the context's statistics as evidence records, with the reference's keys
+    records = {r["event"]: r for r in (json.loads(line.removeprefix("FORT_SCOPED evidence "))
+                                       for line in run.stderr.splitlines() if line.startswith("FORT_SCOPED evidence "))}
+    graphs, queue = records["graph_statistics"], records["command_queue_statistics"]
+    assert graphs["complete"] and graphs["live_graphs"] == 0 and graphs["creations"] == graphs["destructions"] == 1
+    assert (graphs["replays"], graphs["submissions"], graphs["schema_version"]) == (1, 3, 1)
+    assert (queue["accepted_tasks"], queue["direct_submissions"], queue["direct_kernels"]) == (9, 1, 3)
 
 
 # ------------------------------------------------------------------------------- slab pipelines
