@@ -610,3 +610,19 @@ def test_sparse_sections_move_exactly_through_real_copies(client):
     assert (stripes["downloads"], stripes["download_bytes"]) == (20, stripes["stripe_bytes"])
     assert (stripes["uploads"], stripes["upload_bytes"]) == (20, stripes["stripe_bytes"])
 
+
+def test_closing_reports_the_graphs_it_destroyed(client):
+    """With tracing on, closing the context reports its graph and queue statistics as evidence records: complete,
+    no graph left alive, every graph created also destroyed (reference: test_scoped_graph_replay_cuda.py:241-258)."""
+    import os
+
+    run = subprocess.run([str(client), "group"], capture_output=True, text=True, timeout=120,
+                         env={**os.environ, "FORT_RUNTIME_TRACE": "1"})
+    assert run.returncode == 0, run.stdout + run.stderr
+    records = [json.loads(line.removeprefix("FORT_SCOPED evidence ")) for line in run.stderr.splitlines()
+               if line.startswith("FORT_SCOPED evidence ")]
+    (graphs,) = [r for r in records if r["event"] == "graph_statistics"]
+    assert graphs["complete"] and graphs["live_graphs"] == 0
+    assert graphs["creations"] == graphs["destructions"] == 2
+    assert run.stderr.count("FORT_SCOPED graph_submit ") == graphs["instantiations"] + graphs["replays"]
+
