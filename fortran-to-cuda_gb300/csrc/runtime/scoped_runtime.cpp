@@ -753,6 +753,24 @@ void budget_warning(Context *c, const char *consequence) {
 // prepared and not used by queued tasks: clean ones (dropped without a
 // download) before dirty ones, each kind least recently used first, ties by
 // handle.
+void make_room(Context *c, size_t bytes, const std::set<uint64_t> &keep);
+
+// Refuse a footprint that cannot fit even after evicting everything evictable,
+// before anything changes and before the device is brought up.
+void require_fit(Context *c, size_t bytes, const std::set<uint64_t> &keep) {
+    Domain *d = c->domain;
+    if (!d->budget_set || claimed(d) + bytes <= d->budget) return;
+    size_t evictable = 0;
+    for (auto &kv : d->buffers) {
+        Buffer *b = kv.second.get();
+        if (b->device && !keep.count(b->handle) && b->prepared == Buffer::NONE) evictable += b->bytes;
+    }
+    if (claimed(d) - evictable + bytes > d->budget) {
+        budget_warning(c, "loop nests whose arrays do not fit together run on the host");
+        raise(FORT_SCOPE_RESOURCE, "device budget too small for the task footprint");
+    }
+}
+
 void make_room(Context *c, size_t bytes, const std::set<uint64_t> &keep) {
     Domain *d = c->domain;
     if (!d->budget_set) return;
@@ -809,8 +827,12 @@ bool in_place_allowed() {
 void reserve(Context *c, const std::vector<Buffer *> &list, bool allow_in_place) {
     std::set<uint64_t> keep;
     size_t need = 0;
+    for (Buffer *b : list) keep.insert(b->handle);
+    size_t missing = 0;  // arrays without a mirror; one that goes in place later only makes this smaller
+    for (Buffer *b : list)
+        if (!b->device && !(b->mapped && b->host_rounds >= 1)) missing += b->bytes;
+    require_fit(c, missing, keep);
     for (Buffer *b : list) {
-        keep.insert(b->handle);
         pin_for_device(c, b);
         b->in_place = allow_in_place && in_place_allowed() && b->mapped && b->prepared == Buffer::NONE &&
                       b->host_touched && b->host_rounds >= 1;

@@ -223,7 +223,7 @@ def test_arrays_the_host_rewrites_every_step_are_streamed(resident, nx, ny, nz, 
         assert stats.upload_bytes <= 2 * sum(a.nbytes for a in ins)
 
 
-@pytest.mark.parametrize("use, visible", [("host", None), ("host", ""), ("device", None)])
+@pytest.mark.parametrize("use, visible", [("host", None), ("host", ""), ("zero", None), ("device", None)])
 def test_the_product_runtime_brings_the_device_up_only_for_device_work(use, visible, tmp_path):
     """The CUDA build: host-only use of 2 MiB arrays creates no stream and pins nothing, also with every device
     hidden; a device access brings the device up once (reference: test_scoped_runtime_cuda.py:404-410)."""

@@ -882,7 +882,8 @@ def test_a_declared_budget_evicts_and_the_host_carries_on(both):
 
 
 def test_a_zero_budget_allocates_nothing(both):
-    """(reference: test_scoped_runtime.py:656-667)"""
+    """A device access that cannot fit a zero budget is refused before the device is brought up (reference:
+    test_scoped_runtime.py:659-668)."""
     scope = abi.Scope(both)
     _, address = _array(np.arange(8, dtype=np.float64))
     _, h = scope.register(address, [8])
@@ -1606,6 +1607,11 @@ arrays[0][:] += 1.0
 assert lib.fort_scope_host_end(scope.handle, handles[0]) == abi.OK
 assert lib.fort_scope_observe_v1(scope.handle, (abi.U64 * 2)(*handles), 2) == abi.OK
 assert lib.fort_scope_unregister(scope.handle, handles[1]) == abi.OK
+if sys.argv[2] == "zero":  # a device access that cannot fit a zero budget is refused first
+    assert lib.fort_scope_set_device_budget(scope.handle, 0) == abi.OK
+    out = c.c_void_p()
+    assert lib.fort_scope_device_begin(scope.handle, handles[0], c.byref(abi.access(flags=abi.READ_ALL)),
+                                       c.byref(out)) == abi.RESOURCE
 if sys.argv[2] == "device":
     out = c.c_void_p()
     assert lib.fort_scope_device_begin(scope.handle, handles[0], c.byref(abi.access(flags=abi.READ_ALL)),
@@ -1616,11 +1622,12 @@ assert arrays[0][5] == 6.0
 """
 
 
-@pytest.mark.parametrize("use", ["host", "device"])
+@pytest.mark.parametrize("use", ["host", "zero", "device"])
 def test_host_only_use_never_initializes_the_device(both, use, tmp_path):
     """Registration, host access, observation of host-current arrays, unregistration and close bring no device
-    up; the first device access does, once (reference: test_scoped_host_completion_cuda.py:205-210,
-    test_scoped_runtime_cuda.py:404-410, traced as ``FORT_SCOPED initialize``)."""
+    up, nor does a device access refused by a zero budget; the first device access does, once (reference:
+    test_scoped_host_completion_cuda.py:205-210, test_scoped_runtime_cuda.py:404-410,
+    test_scoped_runtime.py:659-668, traced as ``FORT_SCOPED initialize``)."""
     script = tmp_path / "host_only.py"
     script.write_text(HOST_ONLY)
     package = os.path.join(ROOT, "fortran-to-cuda_gb300")
