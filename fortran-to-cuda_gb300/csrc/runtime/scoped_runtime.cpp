@@ -1582,21 +1582,31 @@ void copy_field(char *dst, const char *src) {
     dst[n] = 0;
 }
 
+// A positive count of bytes in decimal digits, optionally followed by one of
+// K, M or G (either case, powers of 1024); anything else, zero or a count that
+// overflows is refused.
 size_t parse_bytes(const char *text, bool *ok) {
-    char *end = nullptr;
-    const unsigned long long v = std::strtoull(text, &end, 10);
-    *ok = end != text;
-    unsigned long long scale = 1;
-    if (end && *end) {
-        switch (*end) {
-        case 'K': case 'k': scale = 1ULL << 10; break;
-        case 'M': case 'm': scale = 1ULL << 20; break;
-        case 'G': case 'g': scale = 1ULL << 30; break;
-        default: *ok = false;
-        }
-        if (end[1]) *ok = false;
+    *ok = false;
+    unsigned long long v = 0;
+    const char *p = text;
+    for (; *p >= '0' && *p <= '9'; ++p) {
+        if (v > (~0ULL - 9) / 10) return 0;
+        v = v * 10 + (unsigned long long)(*p - '0');
     }
-    return (size_t)(v * scale);
+    if (p == text) return 0;
+    unsigned shift = 0;
+    if (*p) {
+        switch (*p) {
+        case 'K': case 'k': shift = 10; break;
+        case 'M': case 'm': shift = 20; break;
+        case 'G': case 'g': shift = 30; break;
+        default: return 0;
+        }
+        if (p[1]) return 0;
+    }
+    if (!v || v > (~0ULL >> shift)) return 0;
+    *ok = true;
+    return (size_t)(v << shift);
 }
 
 } // namespace
@@ -1835,7 +1845,7 @@ int fort_scope_device_budget_default_v1(int device, size_t *bytes) {
         if (const char *text = std::getenv("FORT_RESIDENT_DEVICE_BUDGET")) {
             bool ok = false;
             const size_t v = parse_bytes(text, &ok);
-            if (!ok) raise(FORT_SCOPE_ARGUMENT, "FORT_RESIDENT_DEVICE_BUDGET must be bytes or a count with K, M or G");
+            if (!ok) raise(FORT_SCOPE_ARGUMENT, "FORT_RESIDENT_DEVICE_BUDGET must be a positive count of bytes, optionally with K, M or G");
             *bytes = v;
             return FORT_SCOPE_OK;
         }

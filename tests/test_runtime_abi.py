@@ -2134,12 +2134,17 @@ def test_domain_outlives_borrowing_context(both):
 
 
 def test_budget_default_from_environment(both, monkeypatch):
-    monkeypatch.setenv("FORT_RESIDENT_DEVICE_BUDGET", "3M")
+    """FORT_RESIDENT_DEVICE_BUDGET replaces the derived budget: a positive count of bytes with an optional K, M or
+    G; anything else is refused with the reference's message (reference: test_resident_default_budget_cuda.py:91-99)."""
     out = c.c_size_t()
-    assert both.fort_scope_device_budget_default_v1(0, c.byref(out)) == abi.OK
-    assert out.value == 3 << 20
-    monkeypatch.setenv("FORT_RESIDENT_DEVICE_BUDGET", "12x")
-    assert both.fort_scope_device_budget_default_v1(0, c.byref(out)) != abi.OK
+    for value, expected in (("3M", 3 << 20), ("3145728", 3145728), ("64K", 65536), ("5m", 5 << 20), ("1G", 1 << 30)):
+        monkeypatch.setenv("FORT_RESIDENT_DEVICE_BUDGET", value)
+        assert both.fort_scope_device_budget_default_v1(0, c.byref(out)) == abi.OK
+        assert out.value == expected
+    for value in ("12x", "lots", "-5", "0", "12Q", "1.5G", "+5", " 5", "99999999999999999999G"):
+        monkeypatch.setenv("FORT_RESIDENT_DEVICE_BUDGET", value)
+        assert both.fort_scope_device_budget_default_v1(0, c.byref(out)) == abi.ARGUMENT, value
+        assert b"FORT_RESIDENT_DEVICE_BUDGET must be a positive count of bytes" in both.fort_scope_error()
 
 
 def test_execution_error_poisons(both):
