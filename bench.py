@@ -211,7 +211,7 @@ def run_e2e(fields, steps, warmup, dist, torch):
 
     for _ in range(max(3, warmup)):
         step()
-    n = max(1, min(steps, 10))
+    n = max(1, min(steps, 20))
     barrier(dist, torch)
     t0 = time.perf_counter()
     marks = [t0]
