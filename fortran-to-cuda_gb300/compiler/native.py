@@ -211,15 +211,17 @@ def make_grid(nx, ny, nz, halo, dx, dy, dz, sx=None, sy=None) -> Grid:
     return Grid(nx, ny, nz, halo, sx or nx + 2 * halo, sy or ny + 2 * halo, dx, dy, dz)
 
 
-FACES, DIRECT = 0, 1
+FACES, DIRECT, FAST = 0, 1, 2  # enum f2c_kernel_variant
 
 
 def advection(grid: Grid, u, v, w, ut=None, vt=None, wt=None, scalars=(), scalar_out=(), mode=TENDENCY,
               dt=0.0, stream=0, variant=FACES) -> None:
     """Enqueue the fused advection launch on device pointers (ints).
 
-    ``variant`` FACES is the face-sharing kernel (the product path); DIRECT is the
-    straightforward per-point kernel kept as a cross-check.
+    ``variant`` FACES is the face-sharing kernel (the strict, bit-exact product
+    path); DIRECT is the straightforward per-point kernel kept as a cross-check;
+    FAST is the fast-fp kernel (FMA-contracted, factored; within 1e-12 of each
+    field's maximum).
     """
     fields = Fields()
     fields.u, fields.v, fields.w = u, v, w

@@ -6,6 +6,7 @@
 // compiler/tests/fixtures/stencils/{cvd,cdw}.f90:105-125) and up to four
 // passive-scalar tendencies, replacing the reference's four grid-stride
 // launches per procedure (compiler/emission/cuda/kernels.py:37-69).
+#include "advection_fast.cuh"
 #include "advection_faces.cuh"
 #include "advection_kernels.cuh"
 #include "procedures.cuh"
@@ -70,6 +71,7 @@ static int fill_args(const f2c_grid_v1 *g, const f2c_fields_v1 *f, AdvArgs &a) {
     a.sx = g->sx;
     a.plane = g->sx * g->sy;
     a.c = make_coefficients(g->dx, g->dy, g->dz);
+    a.f = make_fast_coefficients(g->dx, g->dy, g->dz, a.mode, a.dt);
     return 0;
 }
 
@@ -108,21 +110,48 @@ static cudaError_t launch_faces_dispatch(const AdvArgs &a, cudaStream_t s) {
     }
 }
 
+// Factored (fast-fp) kernel instantiations, with the same masks.
+template <int NS>
+static cudaError_t fast_for_mask(const AdvArgs &a, int mask, cudaStream_t s) {
+    const int sms = current_sm_count();
+    switch (mask) {
+    case 7: return launch_fast<NS, 7, kFaceTY>(a, sms, s);
+    case 1: return launch_fast<NS, 1, kFaceTY>(a, sms, s);
+    case 2: return launch_fast<NS, 2, kFaceTY>(a, sms, s);
+    case 4: return launch_fast<NS, 4, kFaceTY>(a, sms, s);
+    case 0: return NS > 0 ? launch_fast<NS, 0, kFaceTY>(a, sms, s) : cudaSuccess;
+    default: return launch_fast<NS, 7, kFaceTY>(a, sms, s);
+    }
+}
+
+static cudaError_t launch_fast_dispatch(const AdvArgs &a, cudaStream_t s) {
+    const int mask = (a.out[0] ? 1 : 0) | (a.out[1] ? 2 : 0) | (a.out[2] ? 4 : 0);
+    switch (a.nscalar) {
+    case 0: return fast_for_mask<0>(a, mask, s);
+    case 1: return fast_for_mask<1>(a, mask, s);
+    case 2: return fast_for_mask<2>(a, mask, s);
+    case 3: return fast_for_mask<3>(a, mask, s);
+    default: return fast_for_mask<4>(a, mask, s);
+    }
+}
+
 } // namespace f2c
 
 extern "C" int f2c_advection_variant_v1(const f2c_grid_v1 *grid, const f2c_fields_v1 *fields, int variant,
                                         void *stream) {
     AdvArgs a;
     if (int s = fill_args(grid, fields, a)) return s;
-    if (variant != 0 && variant != 1) return fail(1, "unknown advection kernel variant");
+    if (variant < F2C_KERNEL_FACES || variant > F2C_KERNEL_FAST) return fail(1, "unknown advection kernel variant");
     const cudaStream_t st = static_cast<cudaStream_t>(stream);
-    const cudaError_t e = variant == 0 ? launch_faces_dispatch(a, st) : launch_advection(a, st);
+    const cudaError_t e = variant == F2C_KERNEL_FACES  ? launch_faces_dispatch(a, st)
+                          : variant == F2C_KERNEL_FAST ? launch_fast_dispatch(a, st)
+                                                       : launch_advection(a, st);
     if (e != cudaSuccess) return fail(6, std::string("advection launch: ") + cudaGetErrorString(e));
     return 0;
 }
 
 extern "C" int f2c_advection_v1(const f2c_grid_v1 *grid, const f2c_fields_v1 *fields, void *stream) {
-    return f2c_advection_variant_v1(grid, fields, 0, stream);
+    return f2c_advection_variant_v1(grid, fields, F2C_KERNEL_FACES, stream);
 }
 
 extern "C" int f2c_halo_fill_v1(const f2c_grid_v1 *grid, double *const *fields, const int32_t *kinds, int32_t count,

@@ -30,6 +30,7 @@
 #include <cstdint>
 
 #include "advection_kernels.cuh"
+#include "device.cuh"
 
 namespace f2c {
 
@@ -311,12 +312,7 @@ __global__ void __launch_bounds__(kFaceThreads, kFaceCtasPerSM) advection_faces_
 // CTAs per SM are available (down to two levels, where the per-chunk prologue
 // stays a small fraction of the work).
 inline int chunk_depth(int nx, int ny, int nz) {
-    static int sms = 0;
-    if (!sms) {
-        int device = 0;
-        cudaGetDevice(&device);
-        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess || sms < 1) sms = 152;
-    }
+    const int sms = current_sm_count();
     const long long tiles = (long long)((nx + kFaceTX - 1) / kFaceTX) * ((ny + kFaceTY - 1) / kFaceTY);
     const long long want = 4LL * sms;
     long long kz = (tiles * nz + want - 1) / want;
@@ -328,13 +324,10 @@ inline int chunk_depth(int nx, int ny, int nz) {
 template <int NS, int MASK>
 cudaError_t launch_faces(const AdvArgs &a, cudaStream_t stream) {
     using Smem = FaceSmem<NS, MASK>;
-    static bool configured = false;
-    if (!configured) {
-        const cudaError_t e = cudaFuncSetAttribute(advection_faces_kernel<NS, MASK>,
-                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Smem::bytes);
-        if (e != cudaSuccess) return e;
-        configured = true;
-    }
+    static std::atomic<unsigned long long> configured{0};
+    const cudaError_t e =
+        configure_shared_once(configured, (const void *)advection_faces_kernel<NS, MASK>, (int)Smem::bytes);
+    if (e != cudaSuccess) return e;
     AdvArgs b = a;
     if (b.kz <= 0) b.kz = chunk_depth(b.nx, b.ny, b.nz);
     const dim3 block(kFaceTX, kFaceTY + 1, 1);

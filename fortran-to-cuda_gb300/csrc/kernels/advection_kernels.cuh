@@ -23,6 +23,7 @@ struct AdvArgs {
     int kz;  // levels per z-chunk of the face-sharing kernel
     long long sx, plane;
     Coefficients c;
+    FastCoefficients f;  // the factored (fast-fp) kernel's coefficients, for this mode and dt
 };
 
 struct HaloArgs {

@@ -95,6 +95,28 @@ struct Coefficients {
         return -(((fe - fw) + (fn - fs)) + (ft - fb));                                                              \
     }())
 
+// Coefficients of the factored (fast-fp) form of the same tendencies
+// (advection_fast.cuh). With A = 0.25/d per direction, the reference's
+// skew-symmetric average -(1/2)(div + adv) of each momentum component regroups,
+// in exact arithmetic, into one product per direction: the direction along the
+// component ("diagonal") carries -A/2 and the two others ("cross") -A/4.
+// Scalars use 0.5/d. In ADVANCE mode every coefficient is multiplied by dt, so
+// that out = in + dt*tendency costs no extra operation.
+struct FastCoefficients {
+    double gx, gy, gz;    // diagonal: -0.125/d (times dt)
+    double cx, cy, cz;    // cross: -0.0625/d (times dt)
+    double sx, sy, sz;    // scalar: 0.5/d (times dt)
+};
+
+inline FastCoefficients make_fast_coefficients(double dx, double dy, double dz, int advance, double dt) {
+    const double t = advance ? dt : 1.0;
+    FastCoefficients f;
+    f.gx = -(0.125 / dx) * t; f.gy = -(0.125 / dy) * t; f.gz = -(0.125 / dz) * t;
+    f.cx = -(0.0625 / dx) * t; f.cy = -(0.0625 / dy) * t; f.cz = -(0.0625 / dz) * t;
+    f.sx = (0.5 / dx) * t; f.sy = (0.5 / dy) * t; f.sz = (0.5 / dz) * t;
+    return f;
+}
+
 inline Coefficients make_coefficients(double dx, double dy, double dz) {
     Coefficients c;
     c.Ax = 0.25 / dx; c.Ay = 0.25 / dy; c.Az = 0.25 / dz;

@@ -61,9 +61,19 @@ const char *f2c_last_error(void);
  * not written. */
 int f2c_advection_v1(const f2c_grid_v1 *grid, const f2c_fields_v1 *fields, void *stream);
 
-/* The same computation by a chosen kernel: 0 = the face-sharing kernel that
- * f2c_advection_v1 runs, 1 = a direct per-point kernel kept as a cross-check.
- * Both are bit-identical to the oracle. */
+/* The same computation by a chosen kernel:
+ *   F2C_KERNEL_FACES (0): the face-sharing kernel that f2c_advection_v1 runs;
+ *   F2C_KERNEL_DIRECT (1): a direct per-point kernel kept as a cross-check;
+ *   both are bit-identical to the oracle (the reference's strict contract,
+ *   compiler/emission/numerical_contract.py:13-15);
+ *   F2C_KERNEL_FAST (2): the fast-fp kernel, the counterpart of the
+ *   reference's --fast-fp build (compiler/resident/build.py:22): FMA
+ *   contraction and an algebraically regrouped form of the same tendencies
+ *   (about 80 FP64 operations per point for U, V, W and three scalars, against
+ *   126). Results differ from the oracle by rounding only: every field within
+ *   1e-12 of its maximum magnitude (measured ~1e-15). In F2C_ADVANCE mode the
+ *   time step is folded into the coefficients. */
+enum f2c_kernel_variant { F2C_KERNEL_FACES = 0, F2C_KERNEL_DIRECT = 1, F2C_KERNEL_FAST = 2 };
 int f2c_advection_variant_v1(const f2c_grid_v1 *grid, const f2c_fields_v1 *fields, int variant, void *stream);
 
 /* One reference procedure as one launch (the reference resident build's
