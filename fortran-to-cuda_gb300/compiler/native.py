@@ -40,10 +40,14 @@ def nvcc() -> str:
     return found
 
 
+PROBE_DIR = CSRC / "probes"
+PROBE_LIBRARY = BUILD_DIR / "libf2c_probe.so"
+
+
 def sources() -> list[Path]:
-    """Every translation unit of the library (kernels, runtime, generated entries)."""
+    """Every translation unit of the library (kernels, runtime, generated entries); measurement probes apart."""
     found = sorted(CSRC.rglob("*.cu")) + sorted(CSRC.rglob("*.cpp"))
-    return [p for p in found if "_build" not in p.parts]
+    return [p for p in found if "_build" not in p.parts and PROBE_DIR not in p.parents]
 
 
 def _headers() -> list[Path]:
@@ -103,6 +107,33 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     return LIBRARY
 
 
+def build_probe(force: bool = False) -> Path:
+    """The benchmark's measurement probes (the live FP64 rate), a library of their own beside the product."""
+    srcs = sorted(PROBE_DIR.glob("*.cu"))
+    stamp = BUILD_DIR / "probe.fingerprint"
+    fingerprint = _fingerprint(srcs)
+    if not force and PROBE_LIBRARY.exists() and stamp.exists() and stamp.read_text() == fingerprint:
+        return PROBE_LIBRARY
+    BUILD_DIR.mkdir(exist_ok=True)
+    tmp = PROBE_LIBRARY.with_suffix(f".{os.getpid()}.tmp")
+    cmd = [nvcc(), *NVCC_FLAGS, "-shared", "-Xcompiler", "-fPIC", *map(str, srcs), "-o", str(tmp), "-lcudart"]
+    result = subprocess.run(cmd, capture_output=True, text=True)
+    if result.returncode != 0:
+        raise RuntimeError(f"probe build failed:\n{result.stdout}\n{result.stderr}")
+    os.replace(tmp, PROBE_LIBRARY)
+    stamp.write_text(fingerprint)
+    return PROBE_LIBRARY
+
+
+@lru_cache(maxsize=1)
+def probe() -> ctypes.CDLL:
+    """The measurement probe library (not part of the product path)."""
+    lib = ctypes.CDLL(str(PROBE_LIBRARY if PROBE_LIBRARY.exists() else build_probe()))
+    lib.f2c_fp64_rate_v1.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_double)]
+    lib.f2c_fp64_rate_v1.restype = ctypes.c_int
+    return lib
+
+
 def runtime() -> ctypes.CDLL:
     """The product library with the fort_scope_* signatures declared."""
     from .runtime import abi
@@ -152,6 +183,9 @@ class Fields(ctypes.Structure):
 TENDENCY, ADVANCE = 0, 1
 
 
+BATCH_HALO_OK, BATCH_FAST_FP = 1, 2  # f2c_batch_plan_v1.reserved flags
+
+
 class BatchPlan(ctypes.Structure):
     _fields_ = [("workspace", ctypes.c_void_p), ("workspace_bytes", ctypes.c_size_t), ("count", ctypes.c_int32),
                 ("nscalar", ctypes.c_int32), ("mask", ctypes.c_int32), ("items", ctypes.c_int32),
@@ -173,8 +207,6 @@ def load() -> ctypes.CDLL:
     lib.f2c_halo_fill_v1.argtypes = [ctypes.POINTER(Grid), ctypes.POINTER(ctypes.c_void_p),
                                      ctypes.POINTER(ctypes.c_int32), ctypes.c_int32, ctypes.c_void_p]
     lib.f2c_halo_fill_v1.restype = ctypes.c_int
-    lib.f2c_fp64_rate_v1.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_double)]
-    lib.f2c_fp64_rate_v1.restype = ctypes.c_int
     lib.f2c_batch_workspace_bytes_v1.argtypes = [ctypes.POINTER(Grid), ctypes.POINTER(ctypes.c_int32), ctypes.c_int32]
     lib.f2c_batch_workspace_bytes_v1.restype = ctypes.c_size_t
     lib.f2c_batch_prepare_v1.argtypes = [ctypes.POINTER(Grid), ctypes.POINTER(Fields), ctypes.POINTER(ctypes.c_int32),
@@ -246,7 +278,9 @@ def halo_fill(grid: Grid, pointers, kinds, stream=0) -> None:
 def fp64_rate(op: int, scratch_ptr: int, scratch_elems: int) -> float:
     """FP64 instructions/s of the current GPU: op 0 = add.rn.f64, op 1 = fma.rn.f64 (synchronous)."""
     out = ctypes.c_double(0.0)
-    check(load().f2c_fp64_rate_v1(op, ctypes.c_void_p(scratch_ptr), scratch_elems, ctypes.byref(out)))
+    status = probe().f2c_fp64_rate_v1(op, ctypes.c_void_p(scratch_ptr), scratch_elems, ctypes.byref(out))
+    if status != 0:
+        raise NativeError(status, "FP64 rate probe failed")
     return out.value
 
 
@@ -285,6 +319,13 @@ class Batch:
         check(load().f2c_batch_prepare_async_v1(self.grids, self.fields, self.kz, self.count,
                                                 ctypes.c_void_p(workspace), nbytes, ctypes.c_void_p(staging),
                                                 ctypes.c_void_p(stream), ctypes.byref(self.plan)))
+
+    def set_fast_fp(self, fast: bool = True) -> None:
+        """Step with the fast-fp kernel (F2C_BATCH_FAST_FP); preparation clears the choice."""
+        if fast:
+            self.plan.reserved |= BATCH_FAST_FP
+        else:
+            self.plan.reserved &= ~BATCH_FAST_FP
 
     def step(self, stream: int = 0) -> None:
         check(load().f2c_batch_step_v1(ctypes.byref(self.plan), ctypes.c_void_p(stream)))

@@ -28,8 +28,9 @@ class ResidentError(RuntimeError):
 
 
 class ResidentDomain:
-    def __init__(self, lib):
+    def __init__(self, lib, fast_fp: bool = False):
         self.lib = lib
+        self.fast_fp = fast_fp  # the context runs the fast-fp kernels (a resident build prepared with --fast-fp)
         self.domain = 0
         self.context = 0
         self.generation = 0
@@ -53,6 +54,8 @@ class ResidentDomain:
             self.require(self.lib.fort_scope_domain_create_v1(device, c.byref(dom)))
             self.require(self.lib.fort_scope_create_in_domain_v1(dom.value, c.byref(ctx)))
             self.require(self.lib.fort_scope_set_device_budget(ctx.value, budget))
+            if self.fast_fp:
+                self.require(self.lib.fort_scope_numerics_set_v1(ctx.value, abi.NUMERICS_FAST))
             self.domain, self.context = dom.value, ctx.value
         self.generation += 1
         self.active = True

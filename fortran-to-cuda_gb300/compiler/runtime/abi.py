@@ -11,6 +11,16 @@ OK, ARGUMENT, STALE, ALIAS, RESOURCE, BOUNDARY, EXECUTION, UNINITIALIZED, STATE,
 BYTES, REAL32, REAL64, INTEGER32, LOGICAL = range(5)
 READ_ALL, WRITE_ALL, OVERWRITE_ALL = 1, 2, 4
 NATIVE, GPU = 0, 1
+NUMERICS_STRICT, NUMERICS_FAST = 0, 1
+
+
+class SlabTiming(c.Structure):
+    _fields_ = [("version", c.c_uint32), ("slabs", c.c_uint32), ("span_ms", c.c_double), ("upload_ms", c.c_double),
+                ("kernel_ms", c.c_double), ("publish_ms", c.c_double), ("longest_upload_ms", c.c_double),
+                ("longest_kernel_ms", c.c_double), ("longest_publish_ms", c.c_double)]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_ if name != "version"}
 
 
 class Section(c.Structure):
@@ -177,6 +187,10 @@ SIGNATURES = {
     "graph_submit_v1": ([U64, U64, P(Kernel), SIZE], c.c_int),
     "device_reserve_slabs_v1": ([U64, P(U64), SIZE, P(c.c_void_p), P(c.c_int)], c.c_int),
     "slab_enqueue_v1": ([U64, U64, P(Task), SIZE, P(SIZE)], c.c_int),
+    "numerics_set_v1": ([U64, c.c_int], c.c_int),
+    "slab_timing_set_v1": ([U64, c.c_int], c.c_int),
+    "slab_timing_get_v1": ([U64, P(SlabTiming)], c.c_int),
+    "numerics_get_v1": ([U64, P(c.c_int)], c.c_int),
     "domain_workspace_reserve_v1": ([U64, SIZE, P(U64)], c.c_int),
     "domain_workspace_resize_v1": ([U64, U64, SIZE], c.c_int),
     "domain_workspace_release_v1": ([U64, U64], c.c_int),

@@ -19,6 +19,7 @@
 #include <deque>
 #include <vector>
 
+#include "../kernels/advection_fast.cuh"
 #include "../kernels/advection_faces.cuh"
 #include "../kernels/advection_kernels.cuh"
 #include "../kernels/procedures.cuh"
@@ -131,35 +132,47 @@ std::vector<fort_scope_plan_binding> bindings_of(std::deque<Use> &uses) {
     return bindings;
 }
 
+// Launch shape of the strict face-sharing kernel (fast = false) or of the
+// fast-fp kernel (fast = true) for `a`; `a.kz` is set for the chosen kernel.
 template <int NS, int MASK>
-void faces_spec(const AdvArgs &a, fort_scope_kernel_v1 &k) {
-    using Smem = FaceSmem<NS, MASK>;
-    static bool configured = false;
-    if (!configured) {
-        cudaFuncSetAttribute(advection_faces_kernel<NS, MASK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)Smem::bytes);
-        configured = true;
+int faces_spec(AdvArgs &a, bool fast, fort_scope_kernel_v1 &k) {
+    if (fast) {
+        a.kz = fast_chunk_depth(a.nx, a.ny, a.nz, kFaceTY, current_sm_count());
+        k.function = (const void *)advection_fast_kernel<NS, MASK, kFaceTY>;
+        k.shared_bytes = 0;
+    } else {
+        using Smem = FaceSmem<NS, MASK>;
+        static std::atomic<unsigned long long> configured{0};
+        const cudaError_t e =
+            configure_shared_once(configured, (const void *)advection_faces_kernel<NS, MASK>, (int)Smem::bytes);
+        if (e != cudaSuccess) return fort_scope_report_error(FORT_SCOPE_RESOURCE, "cannot configure the face kernel");
+        a.kz = chunk_depth(a.nx, a.ny, a.nz);
+        k.function = (const void *)advection_faces_kernel<NS, MASK>;
+        k.shared_bytes = Smem::bytes;
     }
-    k.function = (const void *)advection_faces_kernel<NS, MASK>;
     k.grid[0] = (a.nx + kFaceTX - 1) / kFaceTX;
     k.grid[1] = (a.ny + kFaceTY - 1) / kFaceTY;
     k.grid[2] = (a.nz + a.kz - 1) / a.kz;
     k.block[0] = kFaceTX;
     k.block[1] = kFaceTY + 1;
     k.block[2] = 1;
-    k.shared_bytes = Smem::bytes;
+    return FORT_SCOPE_OK;
 }
 
 template <int MASK>
-void faces_spec_ns(int ns, const AdvArgs &a, fort_scope_kernel_v1 &k) {
+int faces_spec_ns(int ns, AdvArgs &a, bool fast, fort_scope_kernel_v1 &k) {
     switch (ns) {
-    case 0: faces_spec<0, MASK>(a, k); break;
-    case 1: faces_spec<1, MASK>(a, k); break;
-    case 2: faces_spec<2, MASK>(a, k); break;
-    case 3: faces_spec<3, MASK>(a, k); break;
-    default: faces_spec<4, MASK>(a, k); break;
+    case 0: return faces_spec<0, MASK>(a, fast, k);
+    case 1: return faces_spec<1, MASK>(a, fast, k);
+    case 2: return faces_spec<2, MASK>(a, fast, k);
+    case 3: return faces_spec<3, MASK>(a, fast, k);
+    default: return faces_spec<4, MASK>(a, fast, k);
     }
 }
+
+// Graph-cache keys of fast-fp launches differ from the strict ones, so a
+// context that changes its contract never replays a graph of the other kernel.
+constexpr uint64_t kFastKeyMask = 0x6a09e667f3bcc909ULL;
 
 // Levels per slab when a step is cut into slabs to overlap host transfers with
 // the kernels: about 2.5 M points a slab (measured on GB300 over plane sizes
@@ -202,7 +215,7 @@ std::vector<int> slab_bounds(int nz, int planes) {
 // [k0, k1) with every array pointer moved to plane k0 (the kernel addresses
 // planes relative to its interior start and reads one plane either side).
 int enqueue_step_slabs(const EntryCall &call, const Geometry &g, const std::deque<Use> &roles, const AdvArgs &whole,
-                       int ns) {
+                       int ns, bool fast) {
     const std::vector<int> bounds = slab_bounds((int)g.n[2], slab_planes(g.n[0], g.n[1]));
     const int count = (int)bounds.size() - 1;
     std::vector<AdvArgs> args(count);
@@ -225,7 +238,6 @@ int enqueue_step_slabs(const EntryCall &call, const Geometry &g, const std::dequ
             a.st[n] += shift;
         }
         a.nz = k1 - k0;
-        a.kz = chunk_depth(a.nx, a.ny, a.nz);
         Geometry slab = g;
         slab.n[2] = k1 - k0;
         slab.z0 = k0;
@@ -243,13 +255,14 @@ int enqueue_step_slabs(const EntryCall &call, const Geometry &g, const std::dequ
         argument_of[s] = &args[s];
         fort_scope_kernel_v1 &k = tasks[s].kernel;
         k.version = FORT_SCOPE_GRAPH_ABI_VERSION;
-        faces_spec_ns<7>(ns, a, k);
+        if (int st = faces_spec_ns<7>(ns, a, fast, k)) return st;
         k.arguments = &argument_of[s];
         k.argument_count = 1;
         tasks[s].bindings = bindings[s].data();
         tasks[s].binding_count = bindings[s].size();
     }
-    return fort_scope_slab_enqueue_v1(call.context, call.code_key, tasks.data(), tasks.size(), sizes.data());
+    return fort_scope_slab_enqueue_v1(call.context, fast ? call.code_key ^ kFastKeyMask : call.code_key, tasks.data(),
+                                      tasks.size(), sizes.data());
 }
 
 const void *procedure_function(Template t) {
@@ -342,6 +355,9 @@ int run(const EntryCall &call) {
     for (int n = 0; n < call.nints; ++n)
         if (!call.ints[n]) return fort_scope_report_error(FORT_SCOPE_ARGUMENT, "null shared scalar argument");
     if (call.mode == FORT_SCOPE_NATIVE) return declined();
+    int numerics = FORT_SCOPE_NUMERICS_STRICT;
+    if (int s = fort_scope_numerics_get_v1(call.context, &numerics)) return s;
+    const bool fast = numerics == FORT_SCOPE_NUMERICS_FAST;
 
     const Template t = call.kind;
     const int ns = call.nscalar;
@@ -522,10 +538,11 @@ int run(const EntryCall &call) {
         adv.nx = (int)g.n[0]; adv.ny = (int)g.n[1]; adv.nz = (int)g.n[2]; adv.h = (int)g.h;
         adv.sx = sx; adv.plane = plane;
         adv.c = make_coefficients(*call.reals[0], *call.reals[1], *call.reals[2]);
-        adv.kz = chunk_depth(adv.nx, adv.ny, adv.nz);
-        if (t == Template::Cdu) faces_spec_ns<1>(0, adv, kernel);
-        else if (t == Template::Cdv) faces_spec_ns<2>(0, adv, kernel);
-        else faces_spec_ns<4>(0, adv, kernel);
+        adv.f = make_fast_coefficients(*call.reals[0], *call.reals[1], *call.reals[2], 0, 0.0);
+        const int st = t == Template::Cdu   ? faces_spec_ns<1>(0, adv, fast, kernel)
+                       : t == Template::Cdv ? faces_spec_ns<2>(0, adv, fast, kernel)
+                                            : faces_spec_ns<4>(0, adv, fast, kernel);
+        if (st) return st;
         argument = &adv;
         argument_size = sizeof adv;
     } else if (procedure) {
@@ -557,9 +574,9 @@ int run(const EntryCall &call) {
         adv.nx = (int)g.n[0]; adv.ny = (int)g.n[1]; adv.nz = (int)g.n[2]; adv.h = (int)g.h;
         adv.sx = sx; adv.plane = plane;
         adv.c = make_coefficients(*call.reals[0], *call.reals[1], *call.reals[2]);
-        adv.kz = chunk_depth(adv.nx, adv.ny, adv.nz);
-        if (pipelined) return enqueue_step_slabs(call, g, uses, adv, ns);
-        faces_spec_ns<7>(ns, adv, kernel);
+        adv.f = make_fast_coefficients(*call.reals[0], *call.reals[1], *call.reals[2], adv.mode, adv.dt);
+        if (pipelined) return enqueue_step_slabs(call, g, uses, adv, ns, fast);
+        if (int st = faces_spec_ns<7>(ns, adv, fast, kernel)) return st;
         argument = &adv;
         argument_size = sizeof adv;
     } else if (t == Template::Diffusion) {
@@ -615,7 +632,10 @@ int run(const EntryCall &call) {
     task.bindings = bindings.data();
     task.binding_count = bindings.size();
     const size_t sizes[1] = {argument_size};
-    const int status = fort_scope_graph_enqueue_v1(call.context, call.code_key, &task, sizes);
+    // the fused procedures and steps ran their fast-fp kernel: keep their graphs apart from the strict ones
+    const bool fast_kernel = fast && (step || t == Template::Cdu || t == Template::Cdv || t == Template::Cdw);
+    const int status =
+        fort_scope_graph_enqueue_v1(call.context, fast_kernel ? call.code_key ^ kFastKeyMask : call.code_key, &task, sizes);
     if (status == FORT_SCOPE_OK) return FORT_SCOPE_OK;
     if (status == FORT_SCOPE_EXECUTION) return status;
     // nothing was accepted: only definitions were forgotten, which the original statements redefine

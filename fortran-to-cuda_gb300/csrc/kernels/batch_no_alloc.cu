@@ -185,6 +185,7 @@ extern "C" int f2c_batch_step_static_v1(const f2c_grid_v1 *grids, const f2c_fiel
         a.sx = g.sx;
         a.plane = g.sx * g.sy;
         a.c = make_coefficients(g.dx, g.dy, g.dz);
+        a.f = make_fast_coefficients(g.dx, g.dy, g.dz, a.mode, a.dt);
         const int c = kz && kz[n] > 0 ? kz[n] : kFaceKZ;
         const int tx = (int)((g.nx + kFaceTX - 1) / kFaceTX), ty = (int)((g.ny + kFaceTY - 1) / kFaceTY);
         for (int k0 = 0; k0 < g.nz; k0 += c)

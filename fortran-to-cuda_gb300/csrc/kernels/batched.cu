@@ -7,6 +7,7 @@
 #include <vector>
 
 #include "../../../include/f2c_batch.h"
+#include "advection_fast.cuh"
 #include "advection_faces.cuh"
 
 namespace f2c {
@@ -47,40 +48,57 @@ __global__ void __launch_bounds__(kFaceThreads, kFaceCtasPerSM)
     }
 }
 
+// The same persistent loop over the fast-fp tile (advection_fast.cuh).
+template <int NS, int MASK>
+__global__ void __launch_bounds__(kFaceThreads, kFaceCtasPerSM)
+    advection_batched_fast_kernel(const AdvArgs *__restrict__ instances, const BatchItem *__restrict__ items,
+                                  int nitems, unsigned *counter) {
+    __shared__ double smem[FastSmem<kFaceTY>::doubles];
+    __shared__ int slot;
+    for (;;) {
+        if (threadIdx.x == 0 && threadIdx.y == 0) slot = (int)atomicAdd(counter, 1u);
+        __syncthreads();
+        const int n = slot;
+        __syncthreads();  // every thread has read the slot (and left the previous tile) before the next one
+        if (n >= nitems) return;
+        const BatchItem it = items[n];
+        fast_tile<NS, MASK, kFaceTY>(instances[it.instance], it.tile_x, it.tile_y, it.k0, it.k1, smem);
+    }
+}
+
 struct Kernel {
     const void *fn;
     size_t smem;
+    cudaError_t status;
 };
 
 template <int NS, int MASK>
-Kernel kernel_of() {
-    static bool configured = false;
-    if (!configured) {
-        cudaFuncSetAttribute(advection_batched_kernel<NS, MASK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)FaceSmem<NS, MASK>::bytes);
-        configured = true;
-    }
-    return {(const void *)advection_batched_kernel<NS, MASK>, FaceSmem<NS, MASK>::bytes};
+Kernel kernel_of(bool fast) {
+    if (fast) return {(const void *)advection_batched_fast_kernel<NS, MASK>, 0, cudaSuccess};
+    static std::atomic<unsigned long long> configured{0};
+    const cudaError_t e = configure_shared_once(configured, (const void *)advection_batched_kernel<NS, MASK>,
+                                                (int)FaceSmem<NS, MASK>::bytes);
+    return {(const void *)advection_batched_kernel<NS, MASK>, FaceSmem<NS, MASK>::bytes, e};
 }
 
 template <int MASK>
-Kernel kernel_for_ns(int ns) {
+Kernel kernel_for_ns(int ns, bool fast) {
     switch (ns) {
-    case 0: return kernel_of<0, MASK>();
-    case 1: return kernel_of<1, MASK>();
-    case 2: return kernel_of<2, MASK>();
-    case 3: return kernel_of<3, MASK>();
-    default: return kernel_of<4, MASK>();
+    case 0: return kernel_of<0, MASK>(fast);
+    case 1: return kernel_of<1, MASK>(fast);
+    case 2: return kernel_of<2, MASK>(fast);
+    case 3: return kernel_of<3, MASK>(fast);
+    default: return kernel_of<4, MASK>(fast);
     }
 }
 
-Kernel kernel_for(int ns, int mask) {
+Kernel kernel_for(int ns, int mask, bool fast) {
     switch (mask) {
-    case 1: return kernel_for_ns<1>(ns);
-    case 2: return kernel_for_ns<2>(ns);
-    case 4: return kernel_for_ns<4>(ns);
-    case 0: return kernel_for_ns<0>(ns);
-    default: return kernel_for_ns<7>(ns);
+    case 1: return kernel_for_ns<1>(ns, fast);
+    case 2: return kernel_for_ns<2>(ns, fast);
+    case 4: return kernel_for_ns<4>(ns, fast);
+    case 0: return kernel_for_ns<0>(ns, fast);
+    default: return kernel_for_ns<7>(ns, fast);
     }
 }
 
@@ -152,6 +170,7 @@ int build(const f2c_grid_v1 *grids, const f2c_fields_v1 *fields, const int32_t *
         a.sx = g.sx;
         a.plane = g.sx * g.sy;
         a.c = make_coefficients(g.dx, g.dy, g.dz);
+        a.f = make_fast_coefficients(g.dx, g.dy, g.dz, a.mode, a.dt);
         if (g.nz < g.halo + 1 || g.nx < g.halo || g.ny < g.halo) out.halo_ok = false;
     }
     if (mask != 7 && mask != 1 && mask != 2 && mask != 4 && mask != 0) mask = 7;
@@ -188,12 +207,18 @@ size_t items_offset(int count) { return descs_offset() + align_up(sizeof(AdvArgs
 
 // The plan of a built batch whose descriptors and items are (being) copied into `workspace`.
 int finish(const Built &b, int32_t count, void *workspace, size_t workspace_bytes, f2c_batch_plan_v1 *plan) {
-    const Kernel k = kernel_for(b.ns, b.mask);
-    int device = 0, sms = 0, per_sm = 0;
-    cudaGetDevice(&device);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-    const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k.fn, kFaceThreads, k.smem);
-    if (e != cudaSuccess || per_sm < 1) return fail(6, "batch kernel does not fit on an SM");
+    // the persistent grid is sized for the larger of the two kernels' occupancies' minimum, so that either
+    // numerical contract can run the plan (F2C_BATCH_FAST_FP may be set after preparation)
+    const int sms = current_sm_count();
+    int per_sm = 1 << 30;
+    for (const bool fast : {false, true}) {
+        const Kernel k = kernel_for(b.ns, b.mask, fast);
+        if (k.status != cudaSuccess) return fail(6, std::string("batch kernel set-up: ") + cudaGetErrorString(k.status));
+        int n = 0;
+        const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k.fn, kFaceThreads, k.smem);
+        if (e != cudaSuccess || n < 1) return fail(6, "batch kernel does not fit on an SM");
+        per_sm = std::min(per_sm, n);
+    }
     plan->workspace = workspace;
     plan->workspace_bytes = workspace_bytes;
     plan->count = count;
@@ -201,7 +226,7 @@ int finish(const Built &b, int32_t count, void *workspace, size_t workspace_byte
     plan->mask = b.mask;
     plan->items = (int32_t)b.items.size();
     plan->ctas = (uint32_t)std::min<size_t>((size_t)sms * per_sm, b.items.size());
-    plan->reserved = b.halo_ok ? 1u : 0u;
+    plan->reserved = b.halo_ok ? F2C_BATCH_HALO_OK : 0u;
     return 0;
 }
 
@@ -290,11 +315,9 @@ extern "C" int f2c_batch_prepare_async_v1(const f2c_grid_v1 *grids, const f2c_fi
 extern "C" int f2c_batch_halo_v1(const f2c_batch_plan_v1 *plan, void *stream) {
     if (!plan || !plan->workspace || plan->count <= 0) return fail(1, "batch plan not prepared");
     if (plan->count > kBatchHaloMaxInstances) return fail(1, "batch halo fill takes at most 4096 instances");
-    if (!(plan->reserved & 1u)) return fail(1, "halo fill needs nz > halo, nx >= halo and ny >= halo in every instance");
+    if (!(plan->reserved & F2C_BATCH_HALO_OK)) return fail(1, "halo fill needs nz > halo, nx >= halo and ny >= halo in every instance");
     const AdvArgs *descs = reinterpret_cast<const AdvArgs *>(static_cast<char *>(plan->workspace) + descs_offset());
-    int device = 0, sms = 0;
-    cudaGetDevice(&device);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    const int sms = current_sm_count();
     const int count = plan->count, nfields = 3 + plan->nscalar;
     const size_t shared = sizeof(long long) * (size_t)(count + 1);
     batch_halo_kernel<<<(unsigned)(sms > 0 ? sms * 8 : 1216), kBatchHaloThreads, shared,
@@ -313,7 +336,8 @@ extern "C" int f2c_batch_step_v1(const f2c_batch_plan_v1 *plan, void *stream) {
     const BatchItem *items = reinterpret_cast<const BatchItem *>(base + items_offset(plan->count));
     cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(unsigned), s);
     if (e != cudaSuccess) return fail(6, std::string("batch counter reset: ") + cudaGetErrorString(e));
-    const Kernel k = kernel_for(plan->nscalar, plan->mask);
+    const Kernel k = kernel_for(plan->nscalar, plan->mask, (plan->reserved & F2C_BATCH_FAST_FP) != 0);
+    if (k.status != cudaSuccess) return fail(6, std::string("batch kernel set-up: ") + cudaGetErrorString(k.status));
     int nitems = plan->items;
     void *args[] = {(void *)&descs, (void *)&items, (void *)&nitems, (void *)&counter};
     e = cudaLaunchKernel(k.fn, dim3(plan->ctas), dim3(kFaceTX, kFaceTY + 1, 1), args, k.smem, s);

@@ -150,6 +150,15 @@ struct Backend {
     }
     static void destroy_event(Event) {}
     static bool record(Event, Stream) { return true; }
+    // Timing events: work here is synchronous, every interval reads as zero.
+    static bool make_timing_event(Event *e) {
+        *e = 1;
+        return true;
+    }
+    static bool elapsed(Event, Event, float *ms) {
+        *ms = 0.0f;
+        return true;
+    }
     static bool query(Event) { return false; }
     static bool wait_event(Event) { return !std::getenv("F2C_TEST_FAIL_WAIT"); }
     // Host arrays are never pinned here, unless a test asks for the mapped
@@ -272,6 +281,9 @@ struct Backend {
         if (e) cudaEventDestroy(e);
     }
     static bool record(Event e, Stream s) { return ok(cudaEventRecord(e, s)); }
+    static bool make_timing_event(Event *e) { return ok(cudaEventCreate(e)); }
+    // Milliseconds between two completed timing events (the later one is waited for).
+    static bool elapsed(Event a, Event b, float *ms) { return ok(cudaEventSynchronize(b)) && ok(cudaEventElapsedTime(ms, a, b)); }
     // Complete or not; a failure of the work shows at the wait. "Not ready" is an
     // answer, not an error: should it be left as the last error, it is cleared so
     // that no later launch check reads it.

@@ -178,6 +178,16 @@ struct Context {
     Stream copy_in = nullptr, copy_out = nullptr;
     bool copies_ready = false;
     bool queue_enabled = true, graphs_enabled = true;
+    int numerics = 0;  // FORT_SCOPE_NUMERICS_STRICT or FORT_SCOPE_NUMERICS_FAST, for the entries' kernels
+    // Timing of slab sequences (off unless asked for): per slab, events around its uploads (copy stream 1),
+    // its kernel (the context stream) and its publications (copy stream 2); those of the last sequence.
+    struct SlabMarks {
+        Backend::Event up0{}, up1{}, k0{}, k1{}, p0{}, p1{};
+        bool made = false, uploaded = false, published = false;
+    };
+    bool slab_timing = false;
+    std::vector<SlabMarks> slab_marks;
+    size_t slab_marks_used = 0;
     uint64_t queue_work_limit = uint64_t(1) << 18;
     std::vector<Task> pending;
     uint64_t pending_threads = 0;
@@ -1324,6 +1334,27 @@ void run_slabs(Context *c, std::vector<Task> &tasks, std::vector<std::vector<Bou
     join(c->copy_in, c->stream);
     join(c->copy_out, c->stream);
     std::map<Buffer *, Region> publishing, uploading;
+    // optional timing marks, one set per slab (events made once and reused)
+    Context::SlabMarks *marks = nullptr;
+    if (c->slab_timing) {
+        if (c->slab_marks.size() < tasks.size()) c->slab_marks.resize(tasks.size());
+        for (size_t n = 0; n < tasks.size(); ++n) {
+            auto &m = c->slab_marks[n];
+            if (!m.made) {
+                bool good = true;
+                for (Backend::Event *e : {&m.up0, &m.up1, &m.k0, &m.k1, &m.p0, &m.p1})
+                    good = Backend::make_timing_event(e) && good;
+                if (!good) raise(FORT_SCOPE_RESOURCE, "cannot create timing events: " + Backend::last_error());
+                m.made = true;
+            }
+            m.uploaded = m.published = false;
+        }
+        c->slab_marks_used = tasks.size();
+        marks = c->slab_marks.data();
+    }
+    auto mark = [&](Backend::Event e, Stream s) {
+        if (!Backend::record(e, s)) poison(c, std::string("timing event failed: ") + Backend::last_error());
+    };
     for (size_t n = 0; n < tasks.size(); ++n) {
         bool uploaded = false;
         for (auto &x : bound[n]) {
@@ -1331,6 +1362,10 @@ void run_slabs(Context *c, std::vector<Task> &tasks, std::vector<std::vector<Bou
             Region up = needed(b, x.effects);
             up.remove(b->device_valid);
             if (up.empty()) continue;
+            if (marks && !uploaded) {
+                mark(marks[n].up0, c->copy_in);
+                marks[n].uploaded = true;
+            }
             Region moved = up;
             if (!publish.count(b)) {
                 // the whole planes spanning the need, less what the device holds: one run (up to a host
@@ -1366,7 +1401,10 @@ void run_slabs(Context *c, std::vector<Task> &tasks, std::vector<std::vector<Bou
             settle(c, b, b->defined, b->host_valid, device);
             uploaded = true;
         }
-        if (uploaded) join(c->stream, c->copy_in);
+        if (uploaded) {
+            if (marks) mark(marks[n].up1, c->copy_in);
+            join(c->stream, c->copy_in);
+        }
         bool clash = false;
         for (auto &x : bound[n]) {
             auto it = publishing.find(x.buffer);
@@ -1374,8 +1412,10 @@ void run_slabs(Context *c, std::vector<Task> &tasks, std::vector<std::vector<Bou
         }
         if (clash) join(c->stream, c->copy_out);
         trace_line(c, "slab_launch", 0, n);
+        if (marks) mark(marks[n].k0, c->stream);
         if (!Backend::launch(tasks[n].spec, c->stream))
             poison(c, std::string("kernel launch failed: ") + Backend::last_error());
+        if (marks) mark(marks[n].k1, c->stream);
         for (auto &x : bound[n]) device_commit(c, x.buffer, x.effects.writes, x.effects.overwrites);
         bool ordered = false;
         for (auto &x : bound[n]) {
@@ -1387,6 +1427,10 @@ void run_slabs(Context *c, std::vector<Task> &tasks, std::vector<std::vector<Bou
             if (!ordered) {
                 join(c->copy_out, c->stream);
                 ordered = true;
+                if (marks) {
+                    mark(marks[n].p0, c->copy_out);
+                    marks[n].published = true;
+                }
             }
             copy_region(c, b, down, false, c->copy_out);
             publishing[b].add(down);
@@ -1394,6 +1438,7 @@ void run_slabs(Context *c, std::vector<Task> &tasks, std::vector<std::vector<Bou
             host.add(down);
             settle(c, b, b->defined, host, b->device_valid);
         }
+        if (marks && marks[n].published) mark(marks[n].p1, c->copy_out);
     }
     join(c->stream, c->copy_in);
     join(c->stream, c->copy_out);
@@ -1514,7 +1559,16 @@ void evidence(Context *c) {
                 {"pressure_flushes", r.pressure_flushes}});
 }
 
+void drop_slab_marks(Context *c) {
+    for (auto &m : c->slab_marks)
+        if (m.made)
+            for (Backend::Event e : {m.up0, m.up1, m.k0, m.k1, m.p0, m.p1}) Backend::destroy_event(e);
+    c->slab_marks.clear();
+    c->slab_marks_used = 0;
+}
+
 void detach(Context *c) {
+    drop_slab_marks(c);
     if (c->copies_ready) {
         Backend::sync(c->copy_in);
         Backend::sync(c->copy_out);
@@ -2491,6 +2545,72 @@ int fort_scope_device_reserve_slabs_v1(fort_scope_t context, const fort_buffer_t
             devices[n] = b->in_place ? b->mapped : b->device;
         }
         *pipelined = any ? 1 : 0;
+        return FORT_SCOPE_OK;
+    });
+}
+
+int fort_scope_slab_timing_set_v1(fort_scope_t context, int enabled) {
+    return guarded([&] {
+        Context *c = find_context(context);
+        c->slab_timing = enabled != 0;
+        if (!c->slab_timing) drop_slab_marks(c);
+        return FORT_SCOPE_OK;
+    });
+}
+
+int fort_scope_slab_timing_get_v1(fort_scope_t context, fort_scope_slab_timing_v1 *out) {
+    return guarded([&] {
+        if (!out) raise(FORT_SCOPE_ARGUMENT, "null slab timing output");
+        Context *c = find_context(context);
+        if (!c->slab_timing || c->slab_marks_used == 0) raise(FORT_SCOPE_STATE, "no timed slab sequence");
+        fort_scope_slab_timing_v1 r{};
+        r.version = 1;
+        r.slabs = (uint32_t)c->slab_marks_used;
+        auto span = [&](Backend::Event a, Backend::Event b) {
+            float ms = 0.0f;
+            if (!Backend::elapsed(a, b, &ms)) raise(FORT_SCOPE_EXECUTION, "timing events failed: " + Backend::last_error());
+            return (double)ms;
+        };
+        // the sequence starts at its first upload (or its first kernel when nothing was uploaded) and ends
+        // at the later of its last kernel and its last publication
+        const auto &first = c->slab_marks[0];
+        const Backend::Event origin = first.uploaded ? first.up0 : first.k0;
+        for (size_t n = 0; n < c->slab_marks_used; ++n) {
+            const auto &m = c->slab_marks[n];
+            const double k = span(m.k0, m.k1);
+            r.kernel_ms += k;
+            r.longest_kernel_ms = std::max(r.longest_kernel_ms, k);
+            r.span_ms = std::max(r.span_ms, span(origin, m.k1));
+            if (m.uploaded) {
+                const double u = span(m.up0, m.up1);
+                r.upload_ms += u;
+                r.longest_upload_ms = std::max(r.longest_upload_ms, u);
+            }
+            if (m.published) {
+                const double p = span(m.p0, m.p1);
+                r.publish_ms += p;
+                r.longest_publish_ms = std::max(r.longest_publish_ms, p);
+                r.span_ms = std::max(r.span_ms, span(origin, m.p1));
+            }
+        }
+        *out = r;
+        return FORT_SCOPE_OK;
+    });
+}
+
+int fort_scope_numerics_set_v1(fort_scope_t context, int numerics) {
+    return guarded([&] {
+        if (numerics != FORT_SCOPE_NUMERICS_STRICT && numerics != FORT_SCOPE_NUMERICS_FAST)
+            raise(FORT_SCOPE_ARGUMENT, "unknown numerical contract");
+        find_context(context)->numerics = numerics;
+        return FORT_SCOPE_OK;
+    });
+}
+
+int fort_scope_numerics_get_v1(fort_scope_t context, int *numerics) {
+    return guarded([&] {
+        if (!numerics) raise(FORT_SCOPE_ARGUMENT, "null numerical contract output");
+        *numerics = find_context(context)->numerics;
         return FORT_SCOPE_OK;
     });
 }

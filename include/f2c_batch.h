@@ -34,8 +34,16 @@ typedef struct f2c_batch_plan_v1 {
     size_t workspace_bytes;
     int32_t count, nscalar, mask, items;
     uint32_t ctas;             /* persistent grid size */
-    uint32_t reserved;         /* bit 0: every instance admits f2c_batch_halo_v1 */
+    uint32_t reserved;         /* flags: F2C_BATCH_HALO_OK (set by preparation), F2C_BATCH_FAST_FP (caller's) */
 } f2c_batch_plan_v1;
+
+/* Plan flags. F2C_BATCH_HALO_OK: every instance admits f2c_batch_halo_v1
+ * (set by preparation). F2C_BATCH_FAST_FP: f2c_batch_step_v1 runs the fast-fp
+ * kernel (F2C_KERNEL_FAST of f2c_advection.h: FMA contraction and regrouped
+ * sums, each field within 1e-12 of its maximum of the strict result) instead of
+ * the bit-exact one; the caller sets it after preparation, which clears it. */
+#define F2C_BATCH_HALO_OK 1u
+#define F2C_BATCH_FAST_FP 2u
 
 /* Bytes of workspace for `count` instances cut into z-chunks of kz[i] levels (kz NULL: 32). */
 size_t f2c_batch_workspace_bytes_v1(const f2c_grid_v1 *grids, const int32_t *kz, int32_t count);

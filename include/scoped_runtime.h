@@ -318,6 +318,40 @@ int fort_scope_device_reserve_slabs_v1(fort_scope_t context, const fort_buffer_t
 int fort_scope_slab_enqueue_v1(fort_scope_t context, uint64_t code_key, const fort_scope_graph_task_v1 *tasks,
                                size_t count, const size_t *argument_sizes);
 
+/* Timing of slab sequences (extension, off by default). While enabled, each
+ * sequence records device timing events around every slab's uploads, kernel and
+ * publications; fort_scope_slab_timing_get_v1 waits for the last sequence and
+ * reports its span (first upload to last kernel or publication) and the summed
+ * and longest durations of each kind. FORT_SCOPE_STATE when nothing was timed.
+ * Disabling drops the events. */
+typedef struct fort_scope_slab_timing_v1 {
+    uint32_t version;
+    uint32_t slabs;
+    double span_ms;
+    double upload_ms, kernel_ms, publish_ms;
+    double longest_upload_ms, longest_kernel_ms, longest_publish_ms;
+} fort_scope_slab_timing_v1;
+int fort_scope_slab_timing_set_v1(fort_scope_t context, int enabled);
+int fort_scope_slab_timing_get_v1(fort_scope_t context, fort_scope_slab_timing_v1 *out);
+
+/* ---- numerical contract of a context (extension; the reference fixes it at build time) ----
+ *
+ * The reference compiles its generated entries either with the strict options
+ * (compiler/emission/numerical_contract.py:13-15) or, under the resident
+ * build's --fast-fp, with FMA contraction (compiler/resident/build.py:22,66-67).
+ * This library's entries are prebuilt with both kernels; the contract is chosen
+ * per context instead. FORT_SCOPE_NUMERICS_STRICT (the default) runs kernels
+ * that round exactly like the strict native control; FORT_SCOPE_NUMERICS_FAST
+ * lets the entries that have a fast-fp kernel (the fused momentum procedures
+ * and the advection steps) use it: FMA contraction and regrouped sums, each
+ * field within 1e-12 of its maximum magnitude of the strict result. A resident
+ * build prepared with --fast-fp sets it when its domain opens an epoch. Tasks
+ * already queued keep the contract they were accepted under. */
+#define FORT_SCOPE_NUMERICS_STRICT 0
+#define FORT_SCOPE_NUMERICS_FAST 1
+int fort_scope_numerics_set_v1(fort_scope_t context, int numerics);
+int fort_scope_numerics_get_v1(fort_scope_t context, int *numerics);
+
 #ifdef __cplusplus
 }
 #endif

@@ -122,3 +122,37 @@ def test_batched_halo_refuses_instances_too_small_for_the_fill(cuda):
     batch.prepare(ws.data_ptr(), ws.numel())
     with pytest.raises(native.NativeError, match="halo fill needs"):
         batch.halo()
+
+
+def test_fast_batch_on_the_ensemble_shapes(cuda):
+    """The 64-instance ensemble (nx, ny from {64..256}, nz from {32, 64, 96}, seed 1; U, V, W + 1 scalar) stepped
+    by the fast-fp persistent kernel: every instance within the fast-fp tolerance of the oracle, and bit-identical
+    to the fast kernel launched on each instance alone (the same tile arithmetic)."""
+    import tolerance
+
+    shapes = wl.ensemble_shapes(64, seed=1)
+    inst = []
+    for n, (nx, ny, nz) in enumerate(shapes):
+        geo = wl.Geometry(nx, ny, nz, halo=2)
+        f = wl.advection_fields(geo, seed=1000 + n, nscalar=1)
+        ins = [cuda.from_numpy(a).cuda() for a in f.arrays()]
+        outs = [cuda.full_like(t, float("nan")) for t in ins]
+        grid = native.make_grid(nx, ny, nz, 2, geo.dx, geo.dy, geo.dz)
+        p, q = [t.data_ptr() for t in ins], [t.data_ptr() for t in outs]
+        inst.append((geo, f, ins, outs, grid, native.make_fields(*p[:3], *q[:3], scalars=p[3:], scalar_out=q[3:])))
+    batch = native.Batch([x[4] for x in inst], [x[5] for x in inst])
+    ws = cuda.empty(batch.workspace_bytes(), dtype=cuda.uint8, device="cuda")
+    batch.prepare(ws.data_ptr(), ws.numel())
+    batch.set_fast_fp()
+    batch.step()
+    cuda.cuda.synchronize()
+    for geo, f, ins, outs, grid, fields in inst:
+        alone = [cuda.full_like(t, float("nan")) for t in ins]
+        p, q = [t.data_ptr() for t in ins], [t.data_ptr() for t in alone]
+        native.advection(grid, *p[:3], *q[:3], scalars=p[3:], scalar_out=q[3:], variant=native.FAST)
+        ref = api.advection_step({"U": f.U, "V": f.V, "W": f.W}, geo.dx, geo.dy, geo.dz, geo.halo, f.scalars)
+        inner = geo.interior()
+        for got, one, name in zip(outs, alone, ["U", "V", "W", "S0"]):
+            g = got.cpu().numpy()[inner]
+            assert np.array_equal(_bits(g), _bits(one.cpu().numpy()[inner])), name
+            tolerance.check(g, ref[name][inner], name)

@@ -12,27 +12,13 @@ maximum).
 
 import numpy as np
 import pytest
+import tolerance
 
 from compiler import native
 from compiler import workloads as wl
 from oracle import api
 
 pytestmark = pytest.mark.gpu
-
-NORMWISE = 1e-12
-POINTWISE = 1e-9  # where |oracle| >= 1e-3 * max |oracle|
-
-
-def errors(got, ref):
-    """(normwise, pointwise) relative errors of one field's interior."""
-    d = np.abs(got - ref)
-    scale = np.abs(ref).max()
-    if scale == 0:  # an exactly vanishing tendency (e.g. one periodic cell): the residue itself is the error
-        return float(d.max()), 0.0
-    normwise = d.max() / scale
-    big = np.abs(ref) >= 1e-3 * scale
-    pointwise = (d[big] / np.maximum(np.abs(ref[big]), 1e-300)).max()
-    return float(normwise), float(pointwise)
 
 
 def _run(torch, fields, mode=native.TENDENCY, dt=0.0, which=("U", "V", "W"), scalars=True, pitch=None):
@@ -70,11 +56,7 @@ def _oracle(fields, mode=native.TENDENCY, dt=0.0):
 def _check(got, ref, geo, names):
     inner = geo.interior()
     for name, g, r in zip(names, got, ref):
-        gi, ri = g[inner], r[inner]
-        assert np.isfinite(gi).all(), f"{name}: a point was not written"
-        normwise, pointwise = errors(gi, ri)
-        assert normwise <= NORMWISE, f"{name}: normwise relative error {normwise:.3e}"
-        assert pointwise <= POINTWISE, f"{name}: pointwise relative error {pointwise:.3e}"
+        tolerance.check(g[inner], r[inner], name)
 
 
 @pytest.mark.parametrize("shape,halo,nscalar", [((3, 5, 2), 1, 0), ((1, 1, 1), 1, 1), ((12, 10, 6), 2, 3),

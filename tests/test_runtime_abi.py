@@ -3246,3 +3246,57 @@ def test_slab_pipeline_keeps_coherence_compact(monkeypatch):
     assert np.array_equal(y, want.ravel())
     assert scope.stats().reconciliations == 0
     assert lib.fort_scope_close(scope.handle) == abi.OK
+
+
+# ------------------------------------------------------------------------------- numerical contract
+
+
+def test_numerics_contract_per_context(ours):
+    """The strict contract is every context's default; a context can switch to fast-fp and back, unknown
+    contracts and null outputs are argument errors, and a closed context is stale (extension: the reference
+    fixes the contract when its entries are compiled, compiler/resident/build.py:22,66-67)."""
+    a, b = abi.Scope(ours), abi.Scope(ours)
+    got = c.c_int(-1)
+    assert ours.fort_scope_numerics_get_v1(a.handle, c.byref(got)) == abi.OK
+    assert got.value == abi.NUMERICS_STRICT
+    assert ours.fort_scope_numerics_set_v1(a.handle, abi.NUMERICS_FAST) == abi.OK
+    assert ours.fort_scope_numerics_get_v1(a.handle, c.byref(got)) == abi.OK and got.value == abi.NUMERICS_FAST
+    # the other context keeps its own contract
+    assert ours.fort_scope_numerics_get_v1(b.handle, c.byref(got)) == abi.OK and got.value == abi.NUMERICS_STRICT
+    assert ours.fort_scope_numerics_set_v1(a.handle, 2) == abi.ARGUMENT
+    assert ours.fort_scope_numerics_set_v1(a.handle, -1) == abi.ARGUMENT
+    assert ours.fort_scope_numerics_get_v1(a.handle, None) == abi.ARGUMENT
+    assert ours.fort_scope_numerics_get_v1(a.handle, c.byref(got)) == abi.OK and got.value == abi.NUMERICS_FAST
+    assert ours.fort_scope_numerics_set_v1(a.handle, abi.NUMERICS_STRICT) == abi.OK
+    assert ours.fort_scope_close(b.handle) == abi.OK
+    assert ours.fort_scope_numerics_set_v1(b.handle, abi.NUMERICS_FAST) == abi.STALE
+    assert ours.fort_scope_numerics_get_v1(12345, c.byref(got)) == abi.ARGUMENT
+
+
+def test_slab_timing_reports_the_last_sequence(monkeypatch):
+    """Timing of slab sequences is off by default (nothing to report: FORT_SCOPE_STATE); once enabled, the last
+    sequence's slab count is reported with its intervals (zero on the synchronous CPU backend); disabling drops it."""
+    monkeypatch.setenv("F2C_TEST_MAPPED", "1")
+    lib = _ours()
+    scope = abi.Scope(lib)
+    x, xa = _array(np.arange(NX_S * NY_S * NZ_S, dtype=np.float64))
+    y, ya = _array(np.zeros(NX_S * NY_S * NZ_S))
+    _, hx = scope.register(xa, [NX_S, NY_S, NZ_S])
+    _, hy = scope.register(ya, [NX_S, NY_S, NZ_S])
+    fn = _plane_sum_kernel([])
+    timing = abi.SlabTiming()
+    assert lib.fort_scope_slab_timing_get_v1(scope.handle, c.byref(timing)) == abi.STATE
+    assert lib.fort_scope_slab_timing_get_v1(scope.handle, None) == abi.ARGUMENT
+    assert lib.fort_scope_slab_timing_set_v1(scope.handle, 1) == abi.OK
+    for bounds in ([(1, 4), (4, 7), (7, 9)], [(1, 5), (5, 9)]):
+        status, devices, _ = _reserve_slabs(lib, scope, [hx, hy])
+        assert status == abi.OK
+        tasks, sizes, keep = _slab_tasks(fn, devices, hx, hy, bounds)
+        assert lib.fort_scope_slab_enqueue_v1(scope.handle, 11, tasks, len(bounds), sizes) == abi.OK
+        assert lib.fort_scope_slab_timing_get_v1(scope.handle, c.byref(timing)) == abi.OK
+        assert (timing.version, timing.slabs) == (1, len(bounds))
+        assert timing.span_ms >= 0.0 and timing.kernel_ms >= 0.0
+    assert lib.fort_scope_slab_timing_set_v1(scope.handle, 0) == abi.OK
+    assert lib.fort_scope_slab_timing_get_v1(scope.handle, c.byref(timing)) == abi.STATE
+    assert lib.fort_scope_close(scope.handle) == abi.OK
+    assert lib.fort_scope_slab_timing_set_v1(scope.handle, 1) == abi.STALE
