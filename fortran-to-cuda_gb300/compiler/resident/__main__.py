@@ -7,8 +7,10 @@ reference's (compiler/resident/__main__.py:18-65): the same arguments are
 accepted with the same meaning where they apply to this library. ``--cxx`` and
 ``--nvcc`` are not needed (the entries are prebuilt in libf2c_gb300.so) and are
 only checked to exist when given; ``--architecture`` must name the one this
-library is built for (103a); ``--fast-fp`` is refused, because the entries are
-built with the strict numerical contract only; ``--input`` trees belong to
+library is built for (103a); ``--fast-fp`` builds both trees without the strict
+host option and opens the resident build's contexts under the fast-fp
+numerical contract (the library's fast-fp kernels: FMA contraction and
+regrouped sums, within 1e-12 of the strict result); ``--input`` trees belong to
 applications outside the advection path and are refused. Errors print
 ``error: ...`` and exit with status 1.
 """
@@ -40,7 +42,8 @@ def main(argv=None) -> int:
     parser.add_argument("--architecture")
     parser.add_argument("--cmake", default="cmake")
     parser.add_argument("--jobs", type=int, default=8)
-    parser.add_argument("--fast-fp", action="store_true")
+    parser.add_argument("--fast-fp", action="store_true",
+                        help="FMA contraction and regrouped sums instead of the strict numerical contract")
     args = parser.parse_args(argv)
     try:
         if args.jobs < 1:
@@ -49,8 +52,6 @@ def main(argv=None) -> int:
             raise ValueError("choose preparation or building prepared sources")
         if args.input:
             raise ValueError("--input trees describe applications outside the advection path")
-        if args.fast_fp:
-            raise ValueError("the entries of this library are built with the strict numerical contract only")
         if args.architecture and args.architecture.lower() not in ARCHITECTURES:
             raise ValueError(f"this library is built for sm_103a, not {args.architecture}")
         for tool in (args.cxx, args.nvcc):
@@ -62,7 +63,7 @@ def main(argv=None) -> int:
             name = report["application"]
         else:
             app = application.load(args.description, args.variant)
-            application.prepare(app, output)
+            application.prepare(app, output, fast_fp=args.fast_fp)
             report, name = app.report, app.name
         outcome = "prepared" if args.prepare_only else build.configure_and_build(output, args.fortran, args.cmake,
                                                                                   args.jobs)

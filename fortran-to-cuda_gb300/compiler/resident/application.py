@@ -216,15 +216,19 @@ def apply_edit(text: str, edit: Edit) -> str:
     return text[:start] + edit.text.replace("{original}", text[start:end]) + text[end:]
 
 
-def prepare(app: Application, output) -> Application:
-    """Write the resident sources, the native copies and the build into ``output``."""
+def prepare(app: Application, output, fast_fp: bool = False) -> Application:
+    """Write the resident sources, the native copies and the build into ``output``.
+
+    ``fast_fp`` is the reference's --fast-fp (compiler/resident/build.py:22,66-67): both builds drop the strict
+    host option, and the resident one opens its contexts under the fast-fp numerical contract."""
     output = Path(output)
     resident_dir = output / "resident"
     native_dir = output / "native"
     resident_dir.mkdir(parents=True, exist_ok=True)
     native_dir.mkdir(parents=True, exist_ok=True)
     patterns = [p for s in app.selections for p in s.procedures]
-    report = {"application": app.name, "variant": app.variant, "entries": [], "directives": []}
+    report = {"application": app.name, "variant": app.variant, "entries": [], "directives": [],
+              "numerics": "fast" if fast_fp else "strict"}
     nests = {s.label: 0 for s in app.selections}
     texts, spliced_units, entry_arrays = {}, set(), {}
     for src in app.sources:
@@ -262,5 +266,5 @@ def prepare(app: Application, output) -> Application:
     app.report = report
     from . import build
 
-    build.write_cmake(app, output)
+    build.write_cmake(app, output, fast_fp=fast_fp)
     return app

@@ -5,7 +5,11 @@ Two object libraries, as the reference's build (compiler/resident/build.py:53-11
 prepared ones plus this library's Fortran modules (fort_scoped_memory,
 fort_resident_domain, fort_resident_application and the entry interfaces),
 linked against libf2c_gb300.so. Every language gets the strict numerical
-options (-ffp-contract=off). One executable per [[executable]].
+options (-ffp-contract=off), except under --fast-fp, where, as in the
+reference's build (compiler/resident/build.py:22,57-66), both builds drop them
+and the resident objects are preprocessed with F2C_FAST_FP, so that the
+residency domain opens its contexts under the fast-fp contract (the entries
+then run the library's fast-fp kernels). One executable per [[executable]].
 """
 
 from __future__ import annotations
@@ -26,10 +30,10 @@ def _cmake_list(items) -> str:
     return " ".join(f'"{i}"' for i in items)
 
 
-def write_cmake(app, output) -> Path:
+def write_cmake(app, output, fast_fp: bool = False) -> Path:
     output = Path(output)
     modules_dir = native.PACKAGE_ROOT / "fortran"
-    options = list(app.build.get("fortran_options", [])) + list(STRICT) + ["-cpp"]
+    options = list(app.build.get("fortran_options", [])) + ([] if fast_fp else list(STRICT)) + ["-cpp"]
     defines = [f"-D{d}" for d in app.defines]
     link = [x for x in app.build.get("link", []) if x != "OpenMP::OpenMP_Fortran"]
     libraries = list(app.build.get("libraries", []))
@@ -49,6 +53,7 @@ def write_cmake(app, output) -> Path:
         '"${CMAKE_BINARY_DIR}/resident-modules")',
         "target_compile_options(native_objects PRIVATE ${F2C_FORTRAN_OPTIONS})",
         "target_compile_options(resident_objects PRIVATE ${F2C_FORTRAN_OPTIONS})",
+        *(["target_compile_definitions(resident_objects PRIVATE F2C_FAST_FP)"] if fast_fp else []),
         "target_link_libraries(native_objects PUBLIC OpenMP::OpenMP_Fortran " + " ".join(link) + ")",
         "target_link_libraries(resident_objects PUBLIC OpenMP::OpenMP_Fortran " + " ".join(link) + ")",
     ]

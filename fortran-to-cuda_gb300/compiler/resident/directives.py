@@ -176,7 +176,7 @@ def generate(name: str, items: list, clauses: dict, indent: str, domain: Domain,
     if name == "active":
         return _block(indent, domain, [f"{items[0]} = {r}%active"])
     if name == "release":
-        return _block(indent, domain, [f"if ({r}%active) then", *(f"  call {r}%release({a})" for a in items),
+        return _block(indent, domain, [f"if ({r}%active) then", *(f"  call {r}%release_real({a})" for a in items),
                                        "endif"])
     if name == "observe":
         return _observe(items, active, indent, domain, origin)

@@ -604,7 +604,7 @@ def _precise(an: Analysis, u: Unit, ind: str, modes: dict, dom: Domain, released
     if reads:
         head += _handles(an, u, f"{p}_seen", reads, ind + "    ", r) + [f"{ind}    call {r}%observe({p}_seen)"]
     for name in releases:
-        head += _guard(an.attrs_of(u, name), name, f"call {r}%release({name})", ind + "    ")
+        head += _guard(an.attrs_of(u, name), name, f"call {r}%release_real({name})", ind + "    ")
     if writes:
         head += _handles(an, u, f"{p}_held", writes, ind + "    ", r) + [f"{ind}    call {r}%host_modify({p}_held)"]
     head.append(f"{ind}  endif")

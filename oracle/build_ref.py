@@ -17,7 +17,8 @@ import shutil
 import subprocess
 from pathlib import Path
 
-REFERENCE = Path("/root/reference")
+# The reference checkout: F2C_REFERENCE_ROOT, else where the development machine keeps it.
+REFERENCE = Path(os.environ.get("F2C_REFERENCE_ROOT", "/root/reference"))
 SOURCE = REFERENCE / "compiler" / "runtime" / "scoped_runtime.cu"
 OUT_DIR = Path(__file__).resolve().parent / "_ref"
 LIBRARY = OUT_DIR / "libscoped_ref.so"

@@ -157,7 +157,7 @@ def test_reads_writes_and_releases_get_their_blocks(wrapped):
     assert records[("main.f90", line("deallocate(U2)"))] == {
         "file": "main.f90", "line": line("deallocate(U2)"), "block": "release", "arrays": ["u", "u2", "v", "w"]}
     tail = main[main.index("deallocate(U2)") - 600:]
-    assert "if (allocated(u2)) call resident%release(u2)" in tail
+    assert "if (allocated(u2)) call resident%release_real(u2)" in tail
 
 
 def test_entry_calls_and_unbound_statements_are_left_alone(wrapped):

@@ -19,7 +19,9 @@ from compiler import emission
 from compiler.resident import __main__ as cli
 from compiler.resident import application, directives, fortran, splice
 
-CDU_TOML = Path("/root/reference/benchmarks/cdu/cdu.toml")
+from oracle.build_ref import REFERENCE  # noqa: E402  (the reference checkout, when this machine has one)
+
+CDU_TOML = REFERENCE / "benchmarks" / "cdu" / "cdu.toml"
 
 SYNTHETIC = """\
 ! kernels
@@ -96,7 +98,7 @@ def test_procedure_finder_locates_executable_parts():
     ("!$fort close", "call resident%close()"),
     ("!$fort publish if(step == n)", "if (resident%active .and. (step == n)) call resident%publish()"),
     ("!$fort active(on_device)", "on_device = resident%active"),
-    ("!$fort release(tmp, work%buf)", "call resident%release(work%buf)"),
+    ("!$fort release(tmp, work%buf)", "call resident%release_real(work%buf)"),
 ])
 def test_directives_expand_to_residency_calls(line, call):
     text, records = directives.expand("program p\n    " + line + "\nend program p\n", origin="p")
@@ -200,7 +202,7 @@ def test_observe_brings_one_field_of_an_array_of_derived_type_back():
 
 def test_release_retires_temporaries_without_bringing_them_back():
     block, _ = _expand("!$fort release(tmp, work)")
-    assert "if (flow%active) then\n    call flow%release(tmp)\n    call flow%release(work)\n  endif" in block
+    assert "if (flow%active) then\n    call flow%release_real(tmp)\n    call flow%release_real(work)\n  endif" in block
 
 
 @pytest.mark.parametrize("line, message", [
@@ -354,7 +356,7 @@ def test_cli_takes_the_reference_command_line(tmp_path, capsys):
     # building what was prepared: no Fortran compiler here, so it stops after the preparation it finds
     assert cli.main([app, "--output", out, "--build-prepared"]) == 0
     assert json.loads(capsys.readouterr().out)["application"] == "Synthetic"
-    for extra, message in ((["--architecture", "86"], "built for sm_103a"), (["--fast-fp"], "strict"),
+    for extra, message in ((["--architecture", "86"], "built for sm_103a"),
                            (["--input", "elmm=/tmp"], "outside the advection path"),
                            (["--prepare-only", "--build-prepared"], "choose preparation")):
         assert cli.main([app, "--output", out, *extra]) == 1
@@ -439,3 +441,23 @@ def test_edits_locate_by_anchor_call_span_procedure_and_module_end():
 def test_edits_are_checked_where_the_description_is_read(tmp_path, edit, message):
     with pytest.raises(application.DescriptionError, match=message):
         application.load(_write_app(tmp_path, extra=edit))
+
+
+def test_cli_fast_fp_drops_the_strict_option_and_sets_the_contract(tmp_path, capsys):
+    """--fast-fp (the reference's option, compiler/resident/__main__.py:34-35): both builds drop
+    -ffp-contract=off (compiler/resident/build.py:57-66) and the resident objects are preprocessed with
+    F2C_FAST_FP, under which the residency domain opens its contexts in the fast-fp numerical contract."""
+    app = str(_write_app(tmp_path))
+    strict, fast = tmp_path / "strict", tmp_path / "fast"
+    assert cli.main([app, "--output", str(strict), "--prepare-only"]) == 0
+    assert cli.main([app, "--output", str(fast), "--prepare-only", "--fast-fp"]) == 0
+    capsys.readouterr()
+    strict_cmake, fast_cmake = (strict / "CMakeLists.txt").read_text(), (fast / "CMakeLists.txt").read_text()
+    assert "-ffp-contract=off" in strict_cmake and "-ffp-contract=off" not in fast_cmake
+    assert "F2C_FAST_FP" not in strict_cmake
+    assert "target_compile_definitions(resident_objects PRIVATE F2C_FAST_FP)" in fast_cmake
+    assert json.loads((fast / "resident_build.json").read_text())["numerics"] == "fast"
+    assert json.loads((strict / "resident_build.json").read_text())["numerics"] == "strict"
+    domain = (Path(emission.PACKAGE_ROOT) / "fortran" / "fort_resident_domain.f90").read_text()
+    block = domain[domain.index("#ifdef F2C_FAST_FP"):domain.index("#endif")]
+    assert "fort_scope_numerics_set_v1(self%context, FORT_SCOPE_NUMERICS_FAST)" in block
