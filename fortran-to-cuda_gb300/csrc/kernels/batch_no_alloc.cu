@@ -56,7 +56,8 @@ AdvArgs g_descriptors[F2C_BATCH_NO_ALLOC_MAX_INSTANCES];
 NoAllocItem g_items[F2C_BATCH_NO_ALLOC_MAX_ITEMS];
 
 template <int NS, int MASK>
-__global__ void __launch_bounds__(kFaceThreads, 1) no_alloc_batched_kernel(unsigned char *scratch, int nitems) {
+__global__ void __launch_bounds__(kFaceThreads, kFaceCtasPerSM) no_alloc_batched_kernel(unsigned char *scratch,
+                                                                                 int nitems) {
     extern __shared__ double smem[];
     __shared__ int slot;
     unsigned *counter = reinterpret_cast<unsigned *>(scratch);
@@ -76,17 +77,16 @@ __global__ void __launch_bounds__(kFaceThreads, 1) no_alloc_batched_kernel(unsig
 struct NoAllocKernel {
     const void *fn;
     size_t smem;
+    cudaError_t status;  // of the shared-memory limit set on the current device
 };
 
+// The kernel's dynamic shared-memory limit is a property of each device: set once per device ordinal.
 template <int NS, int MASK>
 NoAllocKernel no_alloc_kernel() {
-    static bool configured = false;
-    if (!configured) {
-        cudaFuncSetAttribute(no_alloc_batched_kernel<NS, MASK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)FaceSmem<NS, MASK>::bytes);
-        configured = true;
-    }
-    return {(const void *)no_alloc_batched_kernel<NS, MASK>, FaceSmem<NS, MASK>::bytes};
+    static std::atomic<unsigned long long> configured{0};
+    const cudaError_t e = configure_shared_once(configured, (const void *)no_alloc_batched_kernel<NS, MASK>,
+                                                (int)FaceSmem<NS, MASK>::bytes);
+    return {(const void *)no_alloc_batched_kernel<NS, MASK>, FaceSmem<NS, MASK>::bytes, e};
 }
 
 template <int MASK>
@@ -219,9 +219,10 @@ extern "C" int f2c_batch_step_static_v1(const f2c_grid_v1 *grids, const f2c_fiel
     if (e == cudaSuccess) e = cudaMemsetAsync(base, 0, sizeof(unsigned), st);
     if (e != cudaSuccess) return fail(6, std::string("no-allocation batch staging: ") + cudaGetErrorString(e));
     const NoAllocKernel k = no_alloc_kernel_for(ns, mask);
-    int device = 0, sms = 0, per_sm = 0;
-    cudaGetDevice(&device);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    if (k.status != cudaSuccess)
+        return fail(6, std::string("no-allocation batch kernel set-up: ") + cudaGetErrorString(k.status));
+    const int sms = current_sm_count();
+    int per_sm = 0;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k.fn, kFaceThreads, k.smem);
     if (e != cudaSuccess || per_sm < 1) return fail(6, "no-allocation batch kernel does not fit on an SM");
     const unsigned ctas = (unsigned)std::min<size_t>((size_t)sms * per_sm, at);

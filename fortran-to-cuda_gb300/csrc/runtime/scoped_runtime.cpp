@@ -1896,7 +1896,9 @@ int fort_scope_device_budget_default_v1(int device, size_t *bytes) {
     return guarded([&] {
         if (!bytes) raise(FORT_SCOPE_ARGUMENT, "null budget output");
         if (device < 0) raise(FORT_SCOPE_ARGUMENT, "negative device ordinal");
-        if (const char *text = std::getenv("FORT_RESIDENT_DEVICE_BUDGET")) {
+        // an empty value reads as unset: the budget is then derived from the device
+        const char *text = std::getenv("FORT_RESIDENT_DEVICE_BUDGET");
+        if (text && text[0]) {
             bool ok = false;
             const size_t v = parse_bytes(text, &ok);
             if (!ok) raise(FORT_SCOPE_ARGUMENT, "FORT_RESIDENT_DEVICE_BUDGET must be a positive count of bytes, optionally with K, M or G");
@@ -1909,9 +1911,12 @@ int fort_scope_device_budget_default_v1(int device, size_t *bytes) {
         const bool ok = Backend::memory_info(&free_bytes, &total);
         Backend::select(previous);
         if (!ok) raise(FORT_SCOPE_RESOURCE, "cannot query device memory: " + Backend::last_error());
+        // the driver, graphs and library plans allocate outside the budget: a sixteenth of the device, at least
+        // 512 MiB, stays free
         size_t reserve = total / 16;
         if (reserve < (size_t(512) << 20)) reserve = size_t(512) << 20;
-        *bytes = free_bytes > reserve ? free_bytes - reserve : 0;
+        if (free_bytes <= reserve) raise(FORT_SCOPE_RESOURCE, "the device has no free memory for a residency domain");
+        *bytes = free_bytes - reserve;
         return FORT_SCOPE_OK;
     });
 }

@@ -2145,6 +2145,26 @@ def test_budget_default_from_environment(both, monkeypatch):
         monkeypatch.setenv("FORT_RESIDENT_DEVICE_BUDGET", value)
         assert both.fort_scope_device_budget_default_v1(0, c.byref(out)) == abi.ARGUMENT, value
         assert b"FORT_RESIDENT_DEVICE_BUDGET must be a positive count of bytes" in both.fort_scope_error()
+    # an empty value reads as unset: the budget is derived (the reference's `stated && stated[0]`)
+    monkeypatch.setenv("FORT_RESIDENT_DEVICE_BUDGET", "")
+    assert both.fort_scope_device_budget_default_v1(0, c.byref(out)) == abi.OK
+    assert out.value > 0
+
+
+def test_budget_default_needs_free_memory_beyond_the_reserve(ours, monkeypatch):
+    """The derived budget is the free memory less a sixteenth of the device (at least 512 MiB); a device with no
+    more free than that is refused in the reference's words (scoped_runtime.cu:1766-1769), not given a zero
+    budget. The CPU backend's device has 16 GiB; its free bytes come from F2C_TEST_FREE_BYTES."""
+    monkeypatch.delenv("FORT_RESIDENT_DEVICE_BUDGET", raising=False)
+    out = c.c_size_t()
+    assert ours.fort_scope_device_budget_default_v1(0, c.byref(out)) == abi.OK
+    assert out.value == (12 << 30) - (1 << 30)
+    monkeypatch.setenv("F2C_TEST_FREE_BYTES", str((1 << 30) + 4096))
+    assert ours.fort_scope_device_budget_default_v1(0, c.byref(out)) == abi.OK and out.value == 4096
+    for free in (1 << 30, 100 << 20, 0):
+        monkeypatch.setenv("F2C_TEST_FREE_BYTES", str(free))
+        assert ours.fort_scope_device_budget_default_v1(0, c.byref(out)) == abi.RESOURCE
+        assert b"the device has no free memory for a residency domain" in ours.fort_scope_error()
 
 
 def test_execution_error_poisons(both):
