@@ -456,6 +456,8 @@ def run_gb300(args):
         del oracle_out
     if rank == 0 and world == 1 and not args.no_batched:
         result["batched"] = batched_summary(args, torch)
+    if rank == 0 and world == 1 and not args.no_serving:
+        result["serving"] = serving_summary(args, torch)
     if rank == 0:
         print(json.dumps(result), flush=True)
     if dist is not None:
@@ -535,6 +537,20 @@ def _graph_time(torch, stream, fn, steps, warmup):
     return start.elapsed_time(stop) / steps
 
 
+def _stream_time(torch, stream, fn, steps, warmup):
+    """ms per call of ``fn(stream)`` (which launches its own graph), CUDA events on the stream."""
+    for _ in range(warmup):
+        fn(stream.cuda_stream)
+    torch.cuda.synchronize()
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    start.record(stream)
+    for _ in range(steps):
+        fn(stream.cuda_stream)
+    stop.record(stream)
+    torch.cuda.synchronize()
+    return start.elapsed_time(stop) / steps
+
+
 def ensemble_measure(torch, count, steps, warmup, tune=False, numerics=("fast", "strict")):
     """The ensemble configuration: ``count`` uneven instances (nx, ny from {64..256}, nz from {32, 64, 96}, seed 1),
     U, V, W + 1 scalar. Per numerical contract: one persistent launch per step (autotuned z-chunks) against the
@@ -556,21 +572,26 @@ def ensemble_measure(torch, count, steps, warmup, tune=False, numerics=("fast", 
     stream = torch.cuda.Stream()
     gpu = torch.cuda.get_device_name(0)
 
-    def batch_time(kz, fast, n_steps=5, n_warmup=3):
-        batch = native.Batch([x[3] for x in inst], [x[4] for x in inst], kz=kz)
+    def batch_time(kz, fast, rows=8, n_steps=5, n_warmup=3):
+        # one step = one replay of the batch's own CUDA graph (counter reset + persistent launch)
+        batch = native.Batch([x[3] for x in inst], [x[4] for x in inst], kz=kz, tile_rows=rows)
         ws = torch.empty(batch.workspace_bytes(), dtype=torch.uint8, device="cuda")
         batch.prepare(ws.data_ptr(), ws.numel(), stream.cuda_stream)
         batch.set_fast_fp(fast)
-        return _graph_time(torch, stream, lambda s: batch.step(s), n_steps, n_warmup) * 1e-3
+        return _stream_time(torch, stream, lambda s: batch.graph_step(s), n_steps, n_warmup) * 1e-3
 
-    tuned = scheduling.tune(shapes, gpu, nscalar, lambda kz: batch_time(kz, True)) if tune else None
-    kz = scheduling.kz_for(shapes, gpu, nscalar)
-    out = {"instances": len(shapes), "points": points, "steps": steps, "warmup": warmup,
-           "kz": {scheduling.bucket(nz): k for (_, _, nz), k in zip(shapes, kz)}, "tuned": tuned}
+    tuned = {}
+    if tune:
+        for name in numerics:
+            tuned[name] = scheduling.tune(shapes, gpu, nscalar, lambda kz, rows: batch_time(kz, name == "fast", rows),
+                                          numerics=name)
+    out = {"instances": len(shapes), "points": points, "steps": steps, "warmup": warmup, "tuned": tuned or None}
     with ClockSampler(0) as sampler:
         for name in numerics:
             fast = name == "fast"
-            batched_s = batch_time(kz, fast, n_steps=steps, n_warmup=warmup)
+            kz = scheduling.kz_for(shapes, gpu, nscalar, numerics=name)
+            rows = scheduling.rows_for(gpu, nscalar, numerics=name)
+            batched_s = batch_time(kz, fast, rows, n_steps=steps, n_warmup=warmup)
             variant = native.FAST if fast else native.FACES
 
             def one_at_a_time(s):
@@ -582,6 +603,8 @@ def ensemble_measure(torch, count, steps, warmup, tune=False, numerics=("fast", 
             plain_ms = _graph_time(torch, stream, one_at_a_time, steps, warmup)
             value, plain = points / batched_s / 1e9, points / (plain_ms * 1e-3) / 1e9
             out[name] = {"value": value, "ms_per_step": batched_s * 1e3,
+                         "shapes": {"tile": f"32x{rows}",
+                                    "kz": {scheduling.bucket(nz): k for (_, _, nz), k in zip(shapes, kz)}},
                          "plain_resident": {"value": plain, "ms_per_step": plain_ms,
                                             "how": f"{len(shapes)} single-instance launches per step, one graph"},
                          "batched_over_plain": value / plain}
@@ -596,6 +619,29 @@ def batched_summary(args, torch):
     del inst
     torch.cuda.empty_cache()
     return out
+
+
+def serving_summary(args, torch):
+    """The compact serving object of the default bench line: two arrival rates, 500 jobs each."""
+    from compiler import serving
+
+    count = max(20, args.jobs)
+    serving.warm_up(torch, args.numerics)
+    rates = []
+    with ClockSampler(0) as sampler:
+        for rate in (200.0, 2000.0):
+            r = serving.measure_rate(torch, rate, count, args.numerics)
+            cb, serial, model = r["continuous_batching"], r["serial_plain"], r["serial_device_model"]
+            rates.append({"rate_jobs_per_s": rate, "jobs": count,
+                          "continuous_batching": {k: cb[k] for k in ("gpts_per_s", "jobs_per_s", "p50_ms", "p99_ms",
+                                                                     "wall_s", "ticks")},
+                          "server": {k: cb["server"][k] for k in ("graph_builds", "graph_replays", "plan_builds",
+                                                                  "bursts", "peak_active", "peak_job_bytes",
+                                                                  "refused_admissions")},
+                          "serial_plain": {k: serial[k] for k in ("gpts_per_s", "p50_ms", "p99_ms", "wall_s")},
+                          "serial_device_model": {k: model[k] for k in ("gpts_per_s", "p50_ms", "p99_ms")},
+                          "throughput_ratio": r["throughput_ratio"], "over_device_model": r["over_device_model"]})
+    return {"numerics": args.numerics, "config": serving.config(), "rates": rates, "clocks": sampler.summary()}
 
 
 def run_batched(args):
@@ -635,7 +681,7 @@ def run_batched(args):
         "ms_per_step": head["ms_per_step"], "higher_is_better": True, "dtype": "f64", "data": "synthetic (seeded)",
         "numerics": args.numerics,
         "config": {"workload": f"{out['instances']} instances, nx,ny in {{64..256}}, nz in {{32,64,96}}, seed 1",
-                   "points": points, "kz": out["kz"]},
+                   "points": points, "shapes": head["shapes"]},
         "plain_resident": head["plain_resident"], "batched_over_plain": head["batched_over_plain"],
         "per_numerics": {k: out[k] for k in ("fast", "strict")},
         "reference_style_resident": {"value": procedure_rate, "ms_per_step": procedure_ms,
@@ -745,6 +791,7 @@ def main():
     parser.add_argument("--impl", choices=("gb300", "reference"), default="gb300")
     parser.add_argument("--no-cpu-baseline", action="store_true")
     parser.add_argument("--no-batched", action="store_true", help="leave the ensemble object out of the line")
+    parser.add_argument("--no-serving", action="store_true", help="leave the serving object out of the line")
     parser.add_argument("--numerics", choices=("fast", "strict"), default="fast",
                         help="the headline kernel: fast-fp (default; within 1e-12 of the oracle) or strict "
                              "(bit-identical); the other is timed beside it")
@@ -754,7 +801,7 @@ def main():
                         default="advection", help="the headline step (default) or another configuration")
     parser.add_argument("--tune", action="store_true", help="batched: run the z-chunk autotuner first")
     parser.add_argument("--instances", type=int, default=64, help="batched: the first N instances of the ensemble")
-    parser.add_argument("--jobs", type=int, default=50, help="serving: jobs per arrival rate")
+    parser.add_argument("--jobs", type=int, default=500, help="serving: jobs per arrival rate")
     args = parser.parse_args()
     args.warmup = max(3, args.warmup)
     if args.size:

@@ -192,6 +192,40 @@ class BatchPlan(ctypes.Structure):
                 ("ctas", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
 
 
+class ServeOptions(ctypes.Structure):
+    _fields_ = [("version", ctypes.c_uint32), ("flags", ctypes.c_uint32), ("max_active", ctypes.c_uint32),
+                ("depth", ctypes.c_uint32), ("budget_bytes", ctypes.c_uint64), ("reserve_bytes", ctypes.c_uint64),
+                ("tick_points", ctypes.c_uint64), ("burst_points", ctypes.c_uint64)]
+
+
+class ServeJob(ctypes.Structure):
+    _fields_ = [("nx", ctypes.c_int64), ("ny", ctypes.c_int64), ("nz", ctypes.c_int64), ("halo", ctypes.c_int64),
+                ("dx", ctypes.c_double), ("dy", ctypes.c_double), ("dz", ctypes.c_double), ("dt", ctypes.c_double),
+                ("nscalar", ctypes.c_int32), ("steps", ctypes.c_int32), ("seed", ctypes.c_uint64),
+                ("arrival", ctypes.c_double), ("flags", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+
+
+class ServeDone(ctypes.Structure):
+    _fields_ = [("id", ctypes.c_uint64), ("arrival", ctypes.c_double), ("admitted", ctypes.c_double),
+                ("finished", ctypes.c_double), ("status", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
+class ServeStats(ctypes.Structure):
+    _fields_ = [("version", ctypes.c_uint32), ("reserved", ctypes.c_uint32),
+                *[(n, ctypes.c_uint64) for n in ("admitted", "finished", "ticks", "bursts", "graph_builds",
+                                                  "graph_replays", "direct_launches", "plan_builds",
+                                                  "refused_admissions", "peak_active", "peak_job_bytes")],
+                ("idle_s", ctypes.c_double)]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_ if name not in ("version", "reserved")}
+
+
+SERVE_ABI_VERSION = 1
+SERVE_DIRECT = 1        # f2c_serve_options_v1.flags
+SERVE_KEEP_RESULT = 1   # f2c_serve_job_v1.flags
+
+
 @lru_cache(maxsize=1)
 def load() -> ctypes.CDLL:
     """Load the native library (building it first if needed). Raises if it cannot be had."""
@@ -220,11 +254,44 @@ def load() -> ctypes.CDLL:
                                                ctypes.c_size_t, ctypes.c_void_p, ctypes.c_void_p,
                                                ctypes.POINTER(BatchPlan)]
     lib.f2c_batch_prepare_async_v1.restype = ctypes.c_int
+    lib.f2c_batch_workspace_bytes_rows_v1.argtypes = [ctypes.POINTER(Grid), ctypes.POINTER(ctypes.c_int32),
+                                                      ctypes.c_int32, ctypes.c_int32]
+    lib.f2c_batch_workspace_bytes_rows_v1.restype = ctypes.c_size_t
+    lib.f2c_batch_prepare_rows_v1.argtypes = [ctypes.POINTER(Grid), ctypes.POINTER(Fields),
+                                              ctypes.POINTER(ctypes.c_int32), ctypes.c_int32, ctypes.c_int32,
+                                              ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_void_p,
+                                              ctypes.POINTER(BatchPlan)]
+    lib.f2c_batch_prepare_rows_v1.restype = ctypes.c_int
+    lib.f2c_batch_graph_create_v1.argtypes = [ctypes.POINTER(BatchPlan), ctypes.POINTER(ctypes.c_void_p)]
+    lib.f2c_batch_graph_create_v1.restype = ctypes.c_int
+    lib.f2c_batch_graph_launch_v1.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+    lib.f2c_batch_graph_launch_v1.restype = ctypes.c_int
+    lib.f2c_batch_graph_destroy_v1.argtypes = [ctypes.c_void_p]
+    lib.f2c_batch_graph_destroy_v1.restype = ctypes.c_int
     lib.f2c_batch_halo_v1.argtypes = [ctypes.POINTER(BatchPlan), ctypes.c_void_p]
     lib.f2c_batch_halo_v1.restype = ctypes.c_int
     lib.f2c_procedure_v1.argtypes = [ctypes.c_int, ctypes.POINTER(Grid), ctypes.c_void_p, ctypes.c_void_p,
                                      ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double, ctypes.c_void_p]
     lib.f2c_procedure_v1.restype = ctypes.c_int
+    lib.f2c_seed_fields_v1.argtypes = [ctypes.POINTER(Grid), ctypes.c_uint64, ctypes.c_int32,
+                                       ctypes.POINTER(ctypes.c_void_p), ctypes.c_void_p]
+    lib.f2c_seed_fields_v1.restype = ctypes.c_int
+    u64 = ctypes.c_uint64
+    for name, args in (("create", [u64, ctypes.POINTER(ServeOptions), ctypes.POINTER(u64)]),
+                       ("submit", [u64, ctypes.POINTER(ServeJob), ctypes.POINTER(u64)]),
+                       ("poll", [u64, ctypes.POINTER(ServeDone), ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]),
+                       ("drain", [u64, ctypes.c_double]),
+                       ("result", [u64, u64, ctypes.c_int32, ctypes.POINTER(ctypes.POINTER(ctypes.c_double))]),
+                       ("release", [u64, u64]),
+                       ("stats_get", [u64, ctypes.POINTER(ServeStats)]),
+                       ("destroy", [u64])):
+        fn = getattr(lib, f"f2c_serve_{name}_v1")
+        fn.argtypes = args
+        fn.restype = ctypes.c_int
+    lib.f2c_serve_clock_v1.argtypes = [u64]
+    lib.f2c_serve_clock_v1.restype = ctypes.c_double
+    lib.f2c_serve_error_v1.argtypes = [u64]
+    lib.f2c_serve_error_v1.restype = ctypes.c_char_p
     return lib
 
 
@@ -298,30 +365,40 @@ def make_fields(u, v, w, ut=None, vt=None, wt=None, scalars=(), scalar_out=(), m
 
 
 class Batch:
-    """A prepared batch: instances' grids and fields, a device workspace (caller-owned pointer) and the plan."""
+    """A prepared batch: instances' grids and fields, a device workspace (caller-owned pointer) and the plan.
 
-    def __init__(self, grids, fields, kz=None):
+    ``tile_rows`` is the tile height (4, 8 or 16; 4 and 16 run the fast-fp kernel only). ``graph_step`` replays
+    the step as a CUDA graph the batch captures on its first call and keeps until it is re-prepared or freed.
+    """
+
+    def __init__(self, grids, fields, kz=None, tile_rows: int = 8):
         self.count = len(grids)
         self.grids = (Grid * self.count)(*grids)
         self.fields = (Fields * self.count)(*fields)
         self.kz = (ctypes.c_int32 * self.count)(*kz) if kz else None
+        self.tile_rows = tile_rows
         self.plan = BatchPlan()
+        self._graph = None
 
     def workspace_bytes(self) -> int:
-        return load().f2c_batch_workspace_bytes_v1(self.grids, self.kz, self.count)
+        return load().f2c_batch_workspace_bytes_rows_v1(self.grids, self.kz, self.count, self.tile_rows)
 
     def prepare(self, workspace: int, nbytes: int, stream: int = 0) -> None:
-        check(load().f2c_batch_prepare_v1(self.grids, self.fields, self.kz, self.count, ctypes.c_void_p(workspace),
-                                          nbytes, ctypes.c_void_p(stream), ctypes.byref(self.plan)))
+        self._drop_graph()
+        check(load().f2c_batch_prepare_rows_v1(self.grids, self.fields, self.kz, self.count, self.tile_rows,
+                                               ctypes.c_void_p(workspace), nbytes, None, ctypes.c_void_p(stream),
+                                               ctypes.byref(self.plan)))
 
     def prepare_async(self, workspace: int, nbytes: int, staging: int, stream: int = 0) -> None:
         """Plan through host ``staging`` memory without waiting (see f2c_batch_prepare_async_v1)."""
-        check(load().f2c_batch_prepare_async_v1(self.grids, self.fields, self.kz, self.count,
-                                                ctypes.c_void_p(workspace), nbytes, ctypes.c_void_p(staging),
-                                                ctypes.c_void_p(stream), ctypes.byref(self.plan)))
+        self._drop_graph()
+        check(load().f2c_batch_prepare_rows_v1(self.grids, self.fields, self.kz, self.count, self.tile_rows,
+                                               ctypes.c_void_p(workspace), nbytes, ctypes.c_void_p(staging),
+                                               ctypes.c_void_p(stream), ctypes.byref(self.plan)))
 
     def set_fast_fp(self, fast: bool = True) -> None:
-        """Step with the fast-fp kernel (F2C_BATCH_FAST_FP); preparation clears the choice."""
+        """Step with the fast-fp kernel (F2C_BATCH_FAST_FP); preparation clears the choice for 8-row tiles."""
+        self._drop_graph()
         if fast:
             self.plan.reserved |= BATCH_FAST_FP
         else:
@@ -330,9 +407,35 @@ class Batch:
     def step(self, stream: int = 0) -> None:
         check(load().f2c_batch_step_v1(ctypes.byref(self.plan), ctypes.c_void_p(stream)))
 
+    def graph_step(self, stream: int = 0) -> None:
+        """The step as a replay of the batch's own CUDA graph (captured on the first call)."""
+        if self._graph is None:
+            out = ctypes.c_void_p()
+            check(load().f2c_batch_graph_create_v1(ctypes.byref(self.plan), ctypes.byref(out)))
+            self._graph = out.value
+        check(load().f2c_batch_graph_launch_v1(ctypes.c_void_p(self._graph), ctypes.c_void_p(stream)))
+
     def halo(self, stream: int = 0) -> None:
         """Boundary fill of every instance's outputs, one launch."""
         check(load().f2c_batch_halo_v1(ctypes.byref(self.plan), ctypes.c_void_p(stream)))
+
+    def _drop_graph(self) -> None:
+        if self._graph is not None:
+            load().f2c_batch_graph_destroy_v1(ctypes.c_void_p(self._graph))
+            self._graph = None
+
+    def __del__(self):
+        try:
+            self._drop_graph()
+        except Exception:
+            pass
+
+
+def seed_fields(grid: Grid, seed: int, pointers, stream=0) -> None:
+    """Seeded sine-mode fields (U, V, W, then scalars) written on the device, ghosts filled (f2c_seed_fields_v1)."""
+    n = len(pointers)
+    ptrs = (ctypes.c_void_p * n)(*pointers)
+    check(load().f2c_seed_fields_v1(ctypes.byref(grid), seed, n - 3, ptrs, ctypes.c_void_p(stream)))
 
 
 SET, MULTIPLY, CDU_DIV, CDU_ADV, CDV_DIV, CDV_ADV, CDW_DIV, CDW_ADV = range(8)

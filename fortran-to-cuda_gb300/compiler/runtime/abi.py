@@ -188,6 +188,7 @@ SIGNATURES = {
     "device_reserve_slabs_v1": ([U64, P(U64), SIZE, P(c.c_void_p), P(c.c_int)], c.c_int),
     "slab_enqueue_v1": ([U64, U64, P(Task), SIZE, P(SIZE)], c.c_int),
     "numerics_set_v1": ([U64, c.c_int], c.c_int),
+    "host_pinning_set_v1": ([U64, c.c_int], c.c_int),
     "slab_timing_set_v1": ([U64, c.c_int], c.c_int),
     "slab_timing_get_v1": ([U64, P(SlabTiming)], c.c_int),
     "numerics_get_v1": ([U64, P(c.c_int)], c.c_int),

@@ -2,16 +2,17 @@
 
 A job asks for ``steps`` forward-Euler steps (dt = 0.1, with the boundary fill
 after each) of an advection instance: seeded sine-mode U, V, W and 0-3
-scalars on an nx x ny x nz grid. The server keeps every admitted job's fields
-resident on the device (two buffer sets, ping-pong) until its last step. Each
-tick advances the jobs with the least remaining work, up to about 4 M grid
-points, by one step: per scalar count one persistent batched launch over the
-union of their tiles (``f2c_batch_*``) and one batched boundary fill. Jobs are
-admitted as they arrive while slots and memory allow (a device-memory budget,
-150 GB by default); their fields are generated on a side stream and they join
-the ticks once ready, so their steps overlap on the device with the running
-jobs' steps. Every job's arithmetic is the single-instance kernel's, so a job's
-result is the same alone and in any mix, bit for bit.
+scalars on an nx x ny x nz grid. ``Server`` drives the native server of
+``include/f2c_serve.h``: a worker thread in the library admits jobs as they
+arrive while free device memory covers them, keeps each job's two field sets
+in the residency runtime's device mirrors from admission to retirement (its
+first set seeded on the device, nothing moved to the host between steps), and
+advances the jobs with the least remaining work, up to about 4 M grid points a
+tick, as one persistent batched launch per scalar count plus one batched
+boundary fill, two ticks of a selection captured once as a CUDA graph and
+replayed while the selection holds. Every job's arithmetic is the
+single-instance kernel's, so a job's result is the same alone and in any mix,
+bit for bit.
 
 The open-loop arrival stream and the job sizes follow the serving
 configuration: Poisson arrivals at a given rate; nx and ny drawn independently
@@ -23,6 +24,7 @@ the same per-job work; ``serial_timeline`` models it from device times alone.
 
 from __future__ import annotations
 
+import ctypes
 import math
 import time
 from dataclasses import dataclass, field
@@ -35,12 +37,9 @@ from . import workloads as wl
 DT = 0.1
 BUDGET_BYTES = 150 * 10**9
 MAX_ACTIVE = 256
-# grid points advanced per tick before further jobs wait for the next tick: about 1 ms of work. Measured on
-# GB300 (50 jobs per rate): ticks of 4M points keep throughput equal to serving one job at a time and halve the
-# median latency at low rates; larger ticks trade median latency for a few percent of throughput, and 2M-point
-# ticks leave the GPU waiting for the host
+# grid points advanced per tick before further jobs wait for the next tick: about 1 ms of work
 TICK_POINTS = 4_000_000
-BURST = 8  # ticks issued at once while the selection holds
+NUMERICS = {"fast": native.FAST, "strict": native.FACES}
 
 
 @dataclass
@@ -54,13 +53,8 @@ class Job:
     steps: int
     seed: int
     halo: int = 2
-    # server state
-    ready: object = None        # event: the fields generated at admission are complete
     admitted: float = -1.0
     finished: float = -1.0
-    done: int = 0
-    buffers: list = field(default_factory=list)   # [set A tensors, set B tensors]
-    grid: object = None
     result: list = field(default_factory=list)
 
     @property
@@ -74,13 +68,6 @@ class Job:
     def device_bytes(self) -> int:
         g = self.geometry
         return 2 * (3 + self.nscalar) * int(np.prod(g.shape)) * 8
-
-
-def tick_chunk_depth(shapes, sms: int) -> int:
-    """One z-chunk depth for a tick's batch: deep chunks (up to 32 levels) while the tick has work for four
-    CTAs per SM, shallower (down to 2) for small ticks, so that their tiles still spread over every SM."""
-    columns = sum(((nx + 31) // 32) * ((ny + 7) // 8) * nz for (nx, ny, nz) in shapes)
-    return int(min(32, max(2, -(-columns // (4 * sms)))))
 
 
 def log_uniform_int(rng, lo, hi):
@@ -102,230 +89,131 @@ def poisson_jobs(count: int, rate: float, seed: int = 0) -> list[Job]:
     return jobs
 
 
+class ServeError(RuntimeError):
+    pass
+
+
 class Server:
-    """Continuous-batching server on one GPU (``torch`` provides device memory and the stream).
+    """Continuous batching through the native server, on a residency domain of its own.
 
-    A tick advances the selected jobs by one step: per scalar count, one
-    batched step over all their tiles and one batched boundary fill. A plan
-    depends only on which jobs step and which of their two buffer sets is
-    current, so it repeats every other tick while the selection holds: plans
-    are cached (each with its own device workspace, built once without
-    stalling the stream through ``prepare_async``), ticks are ordered by
-    events, and the host runs at most ``depth`` ticks ahead of the device. A
-    job whose last step is issued is retired once that tick's event has
-    completed.
-
-    Which jobs step in a tick: those with the least remaining work (steps left
-    x points) first, until the tick holds ``tick_points`` grid points; the rest
-    stay resident and wait (shortest remaining work first, so short jobs leave
-    early while every tick still fills the GPU). ``tick_points=None`` steps every
-    active job every tick.
+    ``numerics`` is the domain's numerical contract ("fast": the fast-fp kernels, "strict": bit-identical to the
+    oracle). ``tick_points=None`` steps every resident job every tick. ``graphs=False`` launches ticks directly.
+    ``keep_results`` publishes every job's final fields into ``Job.result`` (numpy arrays, padded layout).
     """
 
-    def __init__(self, torch, budget_bytes: int = BUDGET_BYTES, max_active: int = MAX_ACTIVE, keep_results=False,
-                 depth: int = 4, tick_points: int | None = TICK_POINTS):
-        self.torch = torch
-        self.tick_points = tick_points
+    def __init__(self, torch=None, numerics: str = "fast", budget_bytes: int = BUDGET_BYTES,
+                 max_active: int = MAX_ACTIVE, keep_results: bool = False, depth: int = 4,
+                 tick_points: int | None = TICK_POINTS, graphs: bool = True, device: int = 0):
+        self.numerics = numerics
         self.budget = budget_bytes
         self.max_active = max_active
         self.keep_results = keep_results
         self.depth = depth
-        self.stream = torch.cuda.Stream()
-        self.admit_stream = torch.cuda.Stream()  # admissions run beside the ticks, not between them
-        self.active: list[Job] = []
-        self.claimed = 0
-        self.ticks = 0
-        self.launches = 0
-        self.sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
-        self.plans = {}        # (scalars, ((job, parity), ...)) -> (Batch, workspace, staging), most recent last
-        self.plan_builds = 0
-        self.inflight = []     # (event, plans used, jobs finishing at this tick)
+        self.tick_points = tick_points
+        self.graphs = graphs
+        self.device = device
+        self.stats = {}
 
-    # -- job lifetime ---------------------------------------------------------------------------
-    def _admit(self, job: Job, now: float) -> None:
-        torch = self.torch
-        geo = job.geometry
-        with torch.cuda.stream(self.admit_stream):
-            first = wl.advection_fields_device(geo, job.seed, job.nscalar, torch)
-            second = [torch.empty_like(t) for t in first]
-        for t in first + second:
-            t.record_stream(self.stream)
-        job.grid = native.make_grid(geo.nx, geo.ny, geo.nz, geo.halo, geo.dx, geo.dy, geo.dz)
-        kinds = [0, 0, 1] + [0] * job.nscalar
-        native.halo_fill(job.grid, [t.data_ptr() for t in first], kinds, stream=self.admit_stream.cuda_stream)
-        job.ready = torch.cuda.Event()
-        job.ready.record(self.admit_stream)
-        self.launches += 1
-        job.buffers = [first, second]
-        job.admitted = now
-        self.claimed += job.device_bytes()
-        self.active.append(job)
-
-    def _retire(self, job: Job, now: float) -> None:
-        current = job.buffers[job.done % 2]
-        if self.keep_results:
-            job.result = [t.cpu().numpy() for t in current]
-        else:
-            current[0].view(-1)[:1].cpu()  # the job's answer is read back (one value; fields stay for inspection)
-        job.finished = now
-        job.buffers = []
-        self.claimed -= job.device_bytes()
-
-    def fits(self, job: Job) -> bool:
-        return len(self.active) < self.max_active and self.claimed + job.device_bytes() <= self.budget
-
-    def _plan(self, nscalar: int, jobs: list[Job]):
-        """The cached plan of one group's step (built on first use; the 16 most recent are kept)."""
-        key = (nscalar, tuple((job.ident, job.done % 2) for job in jobs))
-        plan = self.plans.pop(key, None)
-        if plan is None:
-            torch = self.torch
-            grids, fields = [], []
-            for job in jobs:
-                src, dst = job.buffers[job.done % 2], job.buffers[1 - job.done % 2]
-                p, q = [t.data_ptr() for t in src], [t.data_ptr() for t in dst]
-                grids.append(job.grid)
-                fields.append(native.make_fields(*p[:3], *q[:3], scalars=p[3:], scalar_out=q[3:],
-                                                 mode=native.ADVANCE, dt=DT))
-            kz = tick_chunk_depth([(j.nx, j.ny, j.nz) for j in jobs], self.sms)
-            batch = native.Batch(grids, fields, kz=[kz] * len(jobs))
-            need = batch.workspace_bytes()
-            workspace = torch.empty(need, dtype=torch.uint8, device="cuda")
-            staging = torch.empty(need, dtype=torch.uint8, pin_memory=True)
-            batch.prepare_async(workspace.data_ptr(), need, staging.data_ptr(), self.stream.cuda_stream)
-            plan = (batch, workspace, staging)
-            self.plan_builds += 1
-        self.plans[key] = plan
-        while len(self.plans) > 16:  # ticks still in flight hold their own references
-            self.plans.pop(next(iter(self.plans)))
-        return plan
-
-    # -- one tick: every active job advances one step --------------------------------------------
-    def _ready(self) -> list[Job]:
-        """Active jobs whose admission has completed."""
-        out = []
-        for job in self.active:
-            if job.ready is not None and job.ready.query():
-                job.ready = None
-            if job.ready is None:
-                out.append(job)
-        return out
-
-    def select(self) -> list[Job]:
-        """The jobs that step in the next tick (among those whose fields are ready)."""
-        ready = self._ready()
-        if self.tick_points is None:
-            return ready
-        chosen, total = [], 0
-        for job in sorted(ready, key=lambda j: ((j.steps - j.done) * j.points, j.ident)):
-            if chosen and total >= self.tick_points:
-                break
-            chosen.append(job)
-            total += job.points
-        return chosen
-
-    def tick(self):
-        """Issue ticks of the selected jobs; returns (the plans used, the jobs whose last step was issued).
-
-        The selection cannot change before one of its jobs finishes (only selected jobs make progress, and
-        arrivals are admitted between calls), so while it holds, up to ``BURST`` ticks of at most
-        4 x ``tick_points`` points in all are issued at once: each is two launches of cached plans."""
-        stepping = self.select()
-        if not stepping:
-            return [], []
-        groups = {}
-        for job in stepping:
-            groups.setdefault(job.nscalar, []).append(job)
-        points = sum(job.points for job in stepping)
-        budget = 4 * (self.tick_points or points)
-        burst = max(1, min(BURST, min(job.steps - job.done for job in stepping), budget // max(points, 1)))
-        s = self.stream.cuda_stream
-        used = []
-        for _ in range(burst):
-            for nscalar, jobs in sorted(groups.items()):
-                plan = self._plan(nscalar, jobs)
-                plan[0].step(s)
-                plan[0].halo(s)
-                used.append(plan)
-                self.launches += 2
-            for job in stepping:
-                job.done += 1
-            self.ticks += 1
-        finishing = [job for job in stepping if job.done >= job.steps]
-        return used, finishing
-
-    # -- the open-loop run ------------------------------------------------------------------------
     def run(self, jobs: list[Job]) -> dict:
-        torch = self.torch
-        pending = sorted(jobs, key=lambda j: j.arrival)
-        waiting: list[Job] = []
-        start = time.perf_counter()
-        i = 0
+        from .resident.domain import ResidentDomain
+
+        lib = native.runtime()
+        dom = ResidentDomain(lib, fast_fp=self.numerics == "fast")
+        dom.begin_epoch(device=self.device)
+        # the jobs' arrays never move between host and device while in use: no pinning
+        dom.require(lib.fort_scope_host_pinning_set_v1(dom.context, 0))
+        opts = native.ServeOptions(version=native.SERVE_ABI_VERSION, flags=0 if self.graphs else native.SERVE_DIRECT,
+                                   max_active=self.max_active, depth=self.depth, budget_bytes=self.budget,
+                                   reserve_bytes=0, tick_points=self.tick_points or (1 << 62), burst_points=0)
+        handle = ctypes.c_uint64()
+        self._check(lib.f2c_serve_create_v1(dom.context, ctypes.byref(opts), ctypes.byref(handle)), 0)
+        server = handle.value
+        try:
+            return self._serve(lib, server, jobs)
+        finally:
+            lib.f2c_serve_destroy_v1(server)
+            dom.close()
+
+    def _check(self, status: int, server: int) -> None:
+        if status != 0:
+            lib = native.load()
+            text = lib.f2c_serve_error_v1(server) if server else native.runtime().fort_scope_error()
+            raise ServeError(f"server status {status}: {text.decode(errors='replace')}")
+
+    def _serve(self, lib, server: int, jobs: list[Job]) -> dict:
+        ordered = sorted(jobs, key=lambda j: j.arrival)
+        start = lib.f2c_serve_clock_v1(server) + 0.01  # the stream starts once every job is queued
+        by_id = {}
+        for job in ordered:
+            g = job.geometry
+            spec = native.ServeJob(nx=g.nx, ny=g.ny, nz=g.nz, halo=g.halo, dx=g.dx, dy=g.dy, dz=g.dz, dt=DT,
+                                   nscalar=job.nscalar, steps=job.steps, seed=job.seed,
+                                   arrival=start + job.arrival,
+                                   flags=native.SERVE_KEEP_RESULT if self.keep_results else 0, reserved=0)
+            ident = ctypes.c_uint64()
+            self._check(lib.f2c_serve_submit_v1(server, ctypes.byref(spec), ctypes.byref(ident)), server)
+            by_id[ident.value] = job
+        self._check(lib.f2c_serve_drain_v1(server, -1.0), server)
+        records = (native.ServeDone * max(1, len(ordered)))()
+        count = ctypes.c_size_t()
+        self._check(lib.f2c_serve_poll_v1(server, records, len(ordered), ctypes.byref(count)), server)
         finished = []
-
-        def drain(block: bool) -> None:
-            # retire the jobs of completed ticks, oldest first; `block` waits for the oldest one
-            while self.inflight:
-                event, _, done = self.inflight[0]
-                if block:
-                    event.synchronize()
-                    block = False
-                elif not event.query():
-                    return
-                now = time.perf_counter() - start
-                for job in done:
-                    self._retire(job, now)
-                    finished.append(job)
-                self.inflight.pop(0)
-
-        while i < len(pending) or waiting or self.active or self.inflight:
-            now = time.perf_counter() - start
-            while i < len(pending) and pending[i].arrival <= now:
-                waiting.append(pending[i])
-                i += 1
-            while waiting and self.fits(waiting[0]):
-                self._admit(waiting.pop(0), now)
-            if not self.active:
-                if self.inflight:
-                    drain(True)
-                    continue
-                if i < len(pending):  # idle until the next arrival
-                    delay = pending[i].arrival - (time.perf_counter() - start)
-                    if delay > 0:
-                        time.sleep(delay)
-                    continue
-                if waiting:
-                    raise RuntimeError("a job does not fit the device budget on its own")
-                break
-            if len(self.inflight) >= self.depth:
-                drain(True)
-            if not any(job.ready is None or job.ready.query() for job in self.active):
-                # every active job is still being admitted: wait for the first of them
-                next(job for job in self.active).ready.synchronize()
-                continue
-            used, done = self.tick()
-            event = torch.cuda.Event()
-            event.record(self.stream)
-            self.inflight.append((event, used, done))
-            if done:
-                self.active = [j for j in self.active if j.done < j.steps]
-            drain(False)
-        wall = time.perf_counter() - start
-        out = summarise(finished, wall, self.ticks, self.launches)
-        out["plan_builds"] = self.plan_builds
+        for r in records[:count.value]:
+            job = by_id[r.id]
+            if r.status != 0:
+                raise ServeError(f"job {job.ident} failed with status {r.status}")
+            job.admitted, job.finished = r.admitted - start, r.finished - start
+            finished.append(job)
+            if self.keep_results:
+                shape = job.geometry.shape
+                out = []
+                for f in range(3 + job.nscalar):
+                    ptr = ctypes.POINTER(ctypes.c_double)()
+                    self._check(lib.f2c_serve_result_v1(server, r.id, f, ctypes.byref(ptr)), server)
+                    out.append(np.ctypeslib.as_array(ptr, shape=shape).copy())
+                job.result = out
+                self._check(lib.f2c_serve_release_v1(server, r.id), server)
+        stats = native.ServeStats()
+        self._check(lib.f2c_serve_stats_get_v1(server, ctypes.byref(stats)), server)
+        self.stats = stats.as_dict()
+        wall = max((j.finished for j in finished), default=0.0)
+        out = summarise(finished, wall, stats.ticks, stats.graph_replays + stats.direct_launches)
+        out["server"] = self.stats
         return out
+
+
+def _device_job(torch, job: Job, stream):
+    """A job's two field sets as torch tensors, the first seeded on the device (as the server seeds it)."""
+    geo = job.geometry
+    with torch.cuda.stream(stream):
+        a = [torch.empty(geo.shape, dtype=torch.float64, device="cuda") for _ in range(3 + job.nscalar)]
+        b = [torch.empty_like(t) for t in a]
+    grid = native.make_grid(geo.nx, geo.ny, geo.nz, geo.halo, geo.dx, geo.dy, geo.dz)
+    native.seed_fields(grid, job.seed, [t.data_ptr() for t in a], stream=stream.cuda_stream)
+    return grid, [a, b]
+
+
+def _plain_steps(grid, bufs, job: Job, variant: int, stream: int) -> None:
+    kinds = [0, 0, 1] + [0] * job.nscalar
+    for n in range(job.steps):
+        src, dst = bufs[n % 2], bufs[1 - n % 2]
+        p, q = [t.data_ptr() for t in src], [t.data_ptr() for t in dst]
+        native.advection(grid, *p[:3], *q[:3], scalars=p[3:], scalar_out=q[3:], mode=native.ADVANCE, dt=DT,
+                         stream=stream, variant=variant)
+        native.halo_fill(grid, q, kinds, stream=stream)
 
 
 class SerialServer:
     """The same open-loop stream served one job at a time through the single-instance path.
 
-    A job is admitted when the previous one has finished (and it has arrived): its fields are generated on the
-    device as the continuous server does, each step is one advection launch and one boundary fill, and the job
-    is retired (one value read back) when its last step completes. Wall-clock, like ``Server.run``.
+    A job is admitted when the previous one has finished (and it has arrived): its fields are seeded on the
+    device as the continuous server seeds them, each step is one advection launch and one boundary fill, and the
+    job is retired (one value read back) when its last step completes. Wall-clock, like ``Server.run``.
     """
 
-    def __init__(self, torch):
+    def __init__(self, torch, numerics: str = "fast"):
         self.torch = torch
+        self.variant = NUMERICS[numerics]
         self.stream = torch.cuda.Stream()
         self.launches = 0
 
@@ -337,23 +225,10 @@ class SerialServer:
             delay = job.arrival - (time.perf_counter() - start)
             if delay > 0:
                 time.sleep(delay)
-            geo = job.geometry
-            with torch.cuda.stream(self.stream):
-                a = wl.advection_fields_device(geo, job.seed, job.nscalar, torch)
-                b = [torch.empty_like(t) for t in a]
-            grid = native.make_grid(geo.nx, geo.ny, geo.nz, geo.halo, geo.dx, geo.dy, geo.dz)
-            kinds = [0, 0, 1] + [0] * job.nscalar
-            s = self.stream.cuda_stream
-            native.halo_fill(grid, [t.data_ptr() for t in a], kinds, stream=s)
             job.admitted = time.perf_counter() - start
-            bufs = [a, b]
-            for n in range(job.steps):
-                src, dst = bufs[n % 2], bufs[1 - n % 2]
-                p, q = [t.data_ptr() for t in src], [t.data_ptr() for t in dst]
-                native.advection(grid, *p[:3], *q[:3], scalars=p[3:], scalar_out=q[3:], mode=native.ADVANCE,
-                                 dt=DT, stream=s)
-                native.halo_fill(grid, q, kinds, stream=s)
-            self.launches += 1 + 2 * job.steps
+            grid, bufs = _device_job(torch, job, self.stream)
+            _plain_steps(grid, bufs, job, self.variant, self.stream.cuda_stream)
+            self.launches += 2 + 2 * job.steps
             with torch.cuda.stream(self.stream):
                 bufs[job.steps % 2][0].view(-1)[:1].cpu()
             job.finished = time.perf_counter() - start
@@ -372,26 +247,14 @@ def summarise(jobs: list[Job], wall: float, ticks: int = 0, launches: int = 0) -
             "ticks": ticks, "launches": launches}
 
 
-def solo_seconds(torch, job: Job) -> float:
+def solo_seconds(torch, job: Job, numerics: str = "fast") -> float:
     """Device time of one job run alone through the single-instance path (direct launches, one stream)."""
-    geo = job.geometry
     stream = torch.cuda.Stream()
-    with torch.cuda.stream(stream):
-        a = wl.advection_fields_device(geo, job.seed, job.nscalar, torch)
-        b = [torch.empty_like(t) for t in a]
-    grid = native.make_grid(geo.nx, geo.ny, geo.nz, geo.halo, geo.dx, geo.dy, geo.dz)
-    kinds = [0, 0, 1] + [0] * job.nscalar
-    native.halo_fill(grid, [t.data_ptr() for t in a], kinds, stream=stream.cuda_stream)
+    grid, bufs = _device_job(torch, job, stream)
     start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     stream.synchronize()
     start.record(stream)
-    bufs = [a, b]
-    for n in range(job.steps):
-        src, dst = bufs[n % 2], bufs[1 - n % 2]
-        p, q = [t.data_ptr() for t in src], [t.data_ptr() for t in dst]
-        native.advection(grid, *p[:3], *q[:3], scalars=p[3:], scalar_out=q[3:], mode=native.ADVANCE, dt=DT,
-                         stream=stream.cuda_stream)
-        native.halo_fill(grid, q, kinds, stream=stream.cuda_stream)
+    _plain_steps(grid, bufs, job, NUMERICS[numerics], stream.cuda_stream)
     stop.record(stream)
     stream.synchronize()
     return start.elapsed_time(stop) * 1e-3
@@ -409,47 +272,55 @@ def serial_timeline(jobs: list[Job], solo: dict) -> dict:
     return summarise(out, t)
 
 
-def bench_main(args) -> None:
-    """``bench.py --workload serving``: rates swept over {50, ..., 2000} jobs/s; continuous batching vs serial.
+def measure_rate(torch, rate: float, count: int, numerics: str = "fast", every_tick: bool = False) -> dict:
+    """One rate: continuous batching, the serial server and the device-time model of serial service."""
+    served = Server(torch, numerics=numerics).run(poisson_jobs(count, rate, seed=int(rate)))
+    torch.cuda.synchronize()
+    out = {"rate_jobs_per_s": rate, "jobs": count, "continuous_batching": served}
+    if every_tick:
+        out["every_job_every_tick"] = Server(torch, numerics=numerics, tick_points=None).run(
+            poisson_jobs(count, rate, seed=int(rate)))
+    serial = SerialServer(torch, numerics).run(poisson_jobs(count, rate, seed=int(rate)))
+    torch.cuda.synchronize()
+    jobs = poisson_jobs(count, rate, seed=int(rate))
+    model = serial_timeline(jobs, {j.ident: solo_seconds(torch, j, numerics) for j in jobs})
+    torch.cuda.empty_cache()
+    out.update({"serial_plain": serial, "serial_device_model": model,
+                "throughput_ratio": served["gpts_per_s"] / serial["gpts_per_s"] if serial["gpts_per_s"] else None,
+                "over_device_model": served["gpts_per_s"] / model["gpts_per_s"] if model["gpts_per_s"] else None,
+                "p99_ratio": served["p99_ms"] / serial["p99_ms"] if serial["p99_ms"] else None})
+    return out
 
-    Both servers run the same open-loop stream in wall-clock time with the same per-job work (fields generated
-    on the device at admission, one value read back at retirement); ``serial_device_model`` adds the
-    device-time-only FIFO model of the serial server (no host work at all) for reference.
-    """
+
+def warm_up(torch, numerics: str = "fast") -> None:
+    """Untimed first use of both servers (module loading, first allocations)."""
+    Server(torch, numerics=numerics).run(poisson_jobs(8, 2000.0, seed=1))
+    SerialServer(torch, numerics).run(poisson_jobs(8, 2000.0, seed=1))
+    torch.cuda.synchronize()
+
+
+def bench_main(args) -> None:
+    """``bench.py --workload serving``: rates swept over {50, ..., 2000} jobs/s; continuous batching vs serial."""
     import json
 
     import torch
 
     rates = (50, 100, 200, 500, 1000, 2000)
-    count = max(20, getattr(args, "jobs", 50))
-    # untimed warm-up of both servers (module loading, first allocations, plan building)
-    Server(torch).run(poisson_jobs(8, 2000.0, seed=1))
-    SerialServer(torch).run(poisson_jobs(8, 2000.0, seed=1))
-    torch.cuda.synchronize()
-    results = []
-    for rate in rates:
-        served = Server(torch).run(poisson_jobs(count, rate, seed=int(rate)))
-        torch.cuda.synchronize()
-        every = Server(torch, tick_points=None).run(poisson_jobs(count, rate, seed=int(rate)))
-        torch.cuda.synchronize()
-        serial = SerialServer(torch).run(poisson_jobs(count, rate, seed=int(rate)))
-        torch.cuda.synchronize()
-        jobs = poisson_jobs(count, rate, seed=int(rate))
-        model = serial_timeline(jobs, {j.ident: solo_seconds(torch, j) for j in jobs})
-        results.append({"rate_jobs_per_s": rate, "continuous_batching": served, "every_job_every_tick": every,
-                        "serial_plain": serial,
-                         "serial_device_model": model,
-                         "throughput_ratio": served["gpts_per_s"] / serial["gpts_per_s"] if serial["gpts_per_s"]
-                         else None,
-                         "p99_ratio": served["p99_ms"] / serial["p99_ms"] if serial["p99_ms"] else None})
-        torch.cuda.empty_cache()
+    count = max(20, getattr(args, "jobs", 500))
+    numerics = getattr(args, "numerics", "fast")
+    warm_up(torch, numerics)
+    results = [measure_rate(torch, rate, count, numerics, every_tick=True) for rate in rates]
     print(json.dumps({"metric": "serving: jobs/s, Gpts/s and p50/p99 job latency (continuous batching vs serial)",
-                      "unit": "Gpts/s", "jobs_per_rate": count, "dtype": "f64",
-                      "config": {"workload": "Poisson arrivals; nx,ny log-uniform [48,320] (independent draws), "
-                                             "nz log-uniform [24,128], 0-3 scalars, 1-100 Euler steps",
-                                 "budget_bytes": BUDGET_BYTES,
-                                 "policy": f"shortest remaining work first, {TICK_POINTS} points per tick"},
-                      "results": results}), flush=True)
+                      "unit": "Gpts/s", "jobs_per_rate": count, "dtype": "f64", "numerics": numerics,
+                      "config": config(), "results": results}), flush=True)
 
 
-__all__ = ["Job", "Server", "SerialServer", "poisson_jobs", "serial_timeline", "solo_seconds", "bench_main", "summarise"]
+def config() -> dict:
+    return {"workload": "Poisson arrivals; nx,ny log-uniform [48,320] (independent draws), nz log-uniform [24,128], "
+                        "0-3 scalars, 1-100 Euler steps, fields seeded on the device",
+            "budget_bytes": BUDGET_BYTES,
+            "policy": f"shortest remaining work first, {TICK_POINTS} points per tick, two-tick graphs"}
+
+
+__all__ = ["Job", "Server", "SerialServer", "poisson_jobs", "serial_timeline", "solo_seconds", "bench_main",
+           "summarise", "measure_rate", "warm_up", "config"]

@@ -205,3 +205,88 @@ def advection_fields_device(geo: Geometry, seed: int, nscalar: int, torch, devic
             s.copy_(torch.as_tensor(blob(geo, centre=(0.5, 0.5, 0.25 + 0.25 * (n - 2))), device=device))
         out.append(s)
     return out
+
+
+# --- host statement of the device job generator (f2c_seed_fields_v1) -------------------------------
+
+_MASK = (1 << 64) - 1
+_GOLDEN = 0x9E3779B97F4A7C15
+
+
+def _mix64_int(z: int) -> int:
+    z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & _MASK
+    z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & _MASK
+    return z ^ (z >> 31)
+
+
+def _mix64(z: np.ndarray) -> np.ndarray:
+    z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+    z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+    return z ^ (z >> np.uint64(31))
+
+
+def _uniform(key: int, n: np.ndarray) -> np.ndarray:
+    z = np.uint64(key) + np.uint64(_GOLDEN) * (n + np.uint64(1))
+    return (_mix64(z) >> np.uint64(11)).astype(np.float64) * 2.0 ** -53
+
+
+def seeded_fields_reference(geo: Geometry, seed: int, nscalar: int = 0) -> list:
+    """The fields ``f2c_seed_fields_v1`` writes on the device, computed on the host with numpy.
+
+    Per velocity four sine modes (wavenumbers 1..4 per axis and a phase, drawn on the host from a splitmix64
+    stream of the seed) at the staggered position, plus N(0, 0.05) noise from counter-based draws of the point's
+    interior index (Box-Muller); scalar 0 uniform in [280, 300], scalar 1 in [0, 0.02], further scalars Gaussian
+    blobs; ghosts filled by the boundary rule. Agrees with the device to the rounding of sin/cos/log/exp.
+    """
+    with np.errstate(over="ignore"):
+        state = _mix64_int(seed ^ 0x5EEDF1E1D5)
+
+        def draw() -> int:
+            nonlocal state
+            state = (state + _GOLDEN) & _MASK
+            return _mix64_int(state)
+
+        lengths = (geo.nx * geo.dx, geo.ny * geo.dy, geo.nz * geo.dz)
+        modes = []
+        for _ in range(3):
+            per = []
+            for _ in range(4):
+                k = [1.0 + float(draw() % 4) for _ in range(3)]
+                phi = 2.0 * math.pi * (float(draw() >> 11) * 2.0 ** -53)
+                per.append([2.0 * math.pi * k[a] / lengths[a] for a in range(3)] + [phi])
+            modes.append(per)
+        keys = [draw() for _ in range(7)]
+        k, j, i = np.meshgrid(np.arange(geo.nz), np.arange(geo.ny), np.arange(geo.nx), indexing="ij")
+        n = (i + geo.nx * (j + geo.ny * k)).astype(np.uint64)
+        out = []
+        for c in range(3):
+            x = (i + (1.0 if c == 0 else 0.5)) * geo.dx
+            y = (j + (1.0 if c == 1 else 0.5)) * geo.dy
+            z = (k + (1.0 if c == 2 else 0.5)) * geo.dz
+            v = np.zeros(n.shape)
+            for ax, ay, az, phi in modes[c]:
+                v += np.sin(az * z + ay * y + (ax * x + phi))
+            u1 = 1.0 - _uniform(keys[c], np.uint64(2) * n)
+            u2 = _uniform(keys[c], np.uint64(2) * n + np.uint64(1))
+            v += 0.05 * (np.sqrt(-2.0 * np.log(u1)) * np.cos(2.0 * math.pi * u2))
+            out.append(v)
+        lx, ly, lz = lengths
+        sigma = 0.125 * min(lx, ly, lz)
+        for s in range(nscalar):
+            if s == 0:
+                v = 280.0 + 20.0 * _uniform(keys[3], n)
+            elif s == 1:
+                v = 0.02 * _uniform(keys[4], n)
+            else:
+                x = (i + 0.5) * geo.dx - 0.5 * lx
+                y = (j + 0.5) * geo.dy - 0.5 * ly
+                z = (k + 0.5) * geo.dz - (0.25 + 0.25 * (s - 2)) * lz
+                v = np.exp(-(x * x + y * y + z * z) / (2.0 * sigma * sigma))
+            out.append(v)
+    fields = []
+    for c, v in enumerate(out):
+        f = np.zeros(geo.shape)
+        f[geo.interior()] = v
+        fields.append(fill_halo(f, 1 if c == 2 else 0, geo.halo))
+    return fields
+

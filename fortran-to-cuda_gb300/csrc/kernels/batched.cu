@@ -48,12 +48,16 @@ __global__ void __launch_bounds__(kFaceThreads, kFaceCtasPerSM)
     }
 }
 
-// The same persistent loop over the fast-fp tile (advection_fast.cuh).
-template <int NS, int MASK>
-__global__ void __launch_bounds__(kFaceThreads, kFaceCtasPerSM)
+// The same persistent loop over the fast-fp tile (advection_fast.cuh), tiles of 32 x TY points: TY + 1
+// warps per CTA; small tiles run more CTAs per SM (the register budget at 96 per thread).
+template <int TY>
+constexpr int fast_ctas_per_sm() { return TY <= 4 ? 4 : (TY <= 8 ? 2 : 1); }
+
+template <int NS, int MASK, int TY>
+__global__ void __launch_bounds__(fast_threads<TY>(), fast_ctas_per_sm<TY>())
     advection_batched_fast_kernel(const AdvArgs *__restrict__ instances, const BatchItem *__restrict__ items,
                                   int nitems, unsigned *counter) {
-    __shared__ double smem[FastSmem<kFaceTY>::doubles];
+    __shared__ double smem[FastSmem<TY>::doubles];
     __shared__ int slot;
     for (;;) {
         if (threadIdx.x == 0 && threadIdx.y == 0) slot = (int)atomicAdd(counter, 1u);
@@ -62,7 +66,7 @@ __global__ void __launch_bounds__(kFaceThreads, kFaceCtasPerSM)
         __syncthreads();  // every thread has read the slot (and left the previous tile) before the next one
         if (n >= nitems) return;
         const BatchItem it = items[n];
-        fast_tile<NS, MASK, kFaceTY>(instances[it.instance], it.tile_x, it.tile_y, it.k0, it.k1, smem);
+        fast_tile<NS, MASK, TY>(instances[it.instance], it.tile_x, it.tile_y, it.k0, it.k1, smem);
     }
 }
 
@@ -73,8 +77,14 @@ struct Kernel {
 };
 
 template <int NS, int MASK>
-Kernel kernel_of(bool fast) {
-    if (fast) return {(const void *)advection_batched_fast_kernel<NS, MASK>, 0, cudaSuccess};
+Kernel kernel_of(bool fast, int rows) {
+    if (fast) {
+        switch (rows) {
+        case 4: return {(const void *)advection_batched_fast_kernel<NS, MASK, 4>, 0, cudaSuccess};
+        case 16: return {(const void *)advection_batched_fast_kernel<NS, MASK, 16>, 0, cudaSuccess};
+        default: return {(const void *)advection_batched_fast_kernel<NS, MASK, 8>, 0, cudaSuccess};
+        }
+    }
     static std::atomic<unsigned long long> configured{0};
     const cudaError_t e = configure_shared_once(configured, (const void *)advection_batched_kernel<NS, MASK>,
                                                 (int)FaceSmem<NS, MASK>::bytes);
@@ -82,47 +92,60 @@ Kernel kernel_of(bool fast) {
 }
 
 template <int MASK>
-Kernel kernel_for_ns(int ns, bool fast) {
+Kernel kernel_for_ns(int ns, bool fast, int rows) {
     switch (ns) {
-    case 0: return kernel_of<0, MASK>(fast);
-    case 1: return kernel_of<1, MASK>(fast);
-    case 2: return kernel_of<2, MASK>(fast);
-    case 3: return kernel_of<3, MASK>(fast);
-    default: return kernel_of<4, MASK>(fast);
+    case 0: return kernel_of<0, MASK>(fast, rows);
+    case 1: return kernel_of<1, MASK>(fast, rows);
+    case 2: return kernel_of<2, MASK>(fast, rows);
+    case 3: return kernel_of<3, MASK>(fast, rows);
+    default: return kernel_of<4, MASK>(fast, rows);
     }
 }
 
-Kernel kernel_for(int ns, int mask, bool fast) {
+Kernel kernel_for(int ns, int mask, bool fast, int rows) {
     switch (mask) {
-    case 1: return kernel_for_ns<1>(ns, fast);
-    case 2: return kernel_for_ns<2>(ns, fast);
-    case 4: return kernel_for_ns<4>(ns, fast);
-    case 0: return kernel_for_ns<0>(ns, fast);
-    default: return kernel_for_ns<7>(ns, fast);
+    case 1: return kernel_for_ns<1>(ns, fast, rows);
+    case 2: return kernel_for_ns<2>(ns, fast, rows);
+    case 4: return kernel_for_ns<4>(ns, fast, rows);
+    case 0: return kernel_for_ns<0>(ns, fast, rows);
+    default: return kernel_for_ns<7>(ns, fast, rows);
     }
+}
+
+// Tile rows of a plan (the fast-fp kernel's tile height; 8 for plans of the strict kernel).
+int plan_rows(const f2c_batch_plan_v1 *plan) {
+    const int r = (int)((plan->reserved >> 8) & 0xffu);
+    return r ? r : kFaceTY;
 }
 
 int chunk(const int32_t *kz, int n) { return kz && kz[n] > 0 ? kz[n] : kFaceKZ; }
 
-size_t item_count(const f2c_grid_v1 *grids, const int32_t *kz, int count) {
+size_t item_count(const f2c_grid_v1 *grids, const int32_t *kz, int count, int rows) {
     size_t items = 0;
     for (int n = 0; n < count; ++n) {
         const f2c_grid_v1 &g = grids[n];
         const int c = chunk(kz, n);
-        items += (size_t)((g.nx + kFaceTX - 1) / kFaceTX) * ((g.ny + kFaceTY - 1) / kFaceTY) * ((g.nz + c - 1) / c);
+        items += (size_t)((g.nx + kFaceTX - 1) / kFaceTX) * ((g.ny + rows - 1) / rows) * ((g.nz + c - 1) / c);
     }
     return items;
 }
+
+bool rows_ok(int rows) { return rows == 4 || rows == 8 || rows == 16; }
 
 }  // namespace
 }  // namespace f2c
 
 using namespace f2c;
 
-extern "C" size_t f2c_batch_workspace_bytes_v1(const f2c_grid_v1 *grids, const int32_t *kz, int32_t count) {
-    if (!grids || count <= 0) return 0;
+extern "C" size_t f2c_batch_workspace_bytes_rows_v1(const f2c_grid_v1 *grids, const int32_t *kz, int32_t count,
+                                                    int32_t tile_rows) {
+    if (!grids || count <= 0 || !rows_ok(tile_rows)) return 0;
     return align_up(sizeof(BatchHeader)) + align_up(sizeof(AdvArgs) * (size_t)count) +
-           align_up(sizeof(BatchItem) * item_count(grids, kz, count));
+           align_up(sizeof(BatchItem) * item_count(grids, kz, count, tile_rows));
+}
+
+extern "C" size_t f2c_batch_workspace_bytes_v1(const f2c_grid_v1 *grids, const int32_t *kz, int32_t count) {
+    return f2c_batch_workspace_bytes_rows_v1(grids, kz, count, kFaceTY);
 }
 
 namespace f2c {
@@ -131,12 +154,15 @@ namespace {
 struct Built {
     std::vector<AdvArgs> descs;
     std::vector<BatchItem> items;
-    int ns = -1, mask = -1;
+    int ns = -1, mask = -1, rows = kFaceTY;
     bool halo_ok = true; // every instance admits the boundary fill (nz > halo, nx and ny >= halo)
 };
 
-int build(const f2c_grid_v1 *grids, const f2c_fields_v1 *fields, const int32_t *kz, int32_t count, Built &out) {
+int build(const f2c_grid_v1 *grids, const f2c_fields_v1 *fields, const int32_t *kz, int32_t count, int rows,
+          Built &out) {
     if (!grids || !fields || count <= 0) return fail(1, "empty batch");
+    if (!rows_ok(rows)) return fail(1, "tile rows must be 4, 8 or 16");
+    out.rows = rows;
     std::vector<AdvArgs> &descs = out.descs;
     descs.assign((size_t)count, AdvArgs{});
     int ns = -1, mask = -1;
@@ -178,11 +204,11 @@ int build(const f2c_grid_v1 *grids, const f2c_fields_v1 *fields, const int32_t *
     // the flattened queue: full-depth items first (largest first), then the partial ones
     std::vector<BatchItem> &items = out.items;
     items.clear();
-    items.reserve(item_count(grids, kz, count));
+    items.reserve(item_count(grids, kz, count, rows));
     for (int n = 0; n < count; ++n) {
         const f2c_grid_v1 &g = grids[n];
         const int c = chunk(kz, n);
-        const int tx = (int)((g.nx + kFaceTX - 1) / kFaceTX), ty = (int)((g.ny + kFaceTY - 1) / kFaceTY);
+        const int tx = (int)((g.nx + kFaceTX - 1) / kFaceTX), ty = (int)((g.ny + rows - 1) / rows);
         if (tx > 32767 || ty > 32767) return fail(1, "instance too wide for the tile queue");
         for (int k0 = 0; k0 < g.nz; k0 += c)
             for (int y = 0; y < ty; ++y)
@@ -192,7 +218,7 @@ int build(const f2c_grid_v1 *grids, const f2c_fields_v1 *fields, const int32_t *
     auto cost = [&](const BatchItem &it) {
         const f2c_grid_v1 &g = grids[it.instance];
         const long long w = std::min<long long>(kFaceTX, g.nx - (long long)it.tile_x * kFaceTX);
-        const long long h = std::min<long long>(kFaceTY, g.ny - (long long)it.tile_y * kFaceTY);
+        const long long h = std::min<long long>(rows, g.ny - (long long)it.tile_y * rows);
         return w * h * (it.k1 - it.k0);
     };
     std::stable_sort(items.begin(), items.end(),
@@ -207,15 +233,18 @@ size_t items_offset(int count) { return descs_offset() + align_up(sizeof(AdvArgs
 
 // The plan of a built batch whose descriptors and items are (being) copied into `workspace`.
 int finish(const Built &b, int32_t count, void *workspace, size_t workspace_bytes, f2c_batch_plan_v1 *plan) {
-    // the persistent grid is sized for the larger of the two kernels' occupancies' minimum, so that either
-    // numerical contract can run the plan (F2C_BATCH_FAST_FP may be set after preparation)
+    // the persistent grid is sized for the smaller occupancy of the kernels that can run the plan (either
+    // numerical contract for 8-row tiles, since F2C_BATCH_FAST_FP may be set after preparation; the fast-fp
+    // kernel alone for 4- and 16-row tiles)
     const int sms = current_sm_count();
     int per_sm = 1 << 30;
     for (const bool fast : {false, true}) {
-        const Kernel k = kernel_for(b.ns, b.mask, fast);
+        if (!fast && b.rows != kFaceTY) continue;
+        const Kernel k = kernel_for(b.ns, b.mask, fast, b.rows);
         if (k.status != cudaSuccess) return fail(6, std::string("batch kernel set-up: ") + cudaGetErrorString(k.status));
         int n = 0;
-        const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k.fn, kFaceThreads, k.smem);
+        const int threads = kFaceTX * (b.rows + 1);
+        const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k.fn, threads, k.smem);
         if (e != cudaSuccess || n < 1) return fail(6, "batch kernel does not fit on an SM");
         per_sm = std::min(per_sm, n);
     }
@@ -226,7 +255,8 @@ int finish(const Built &b, int32_t count, void *workspace, size_t workspace_byte
     plan->mask = b.mask;
     plan->items = (int32_t)b.items.size();
     plan->ctas = (uint32_t)std::min<size_t>((size_t)sms * per_sm, b.items.size());
-    plan->reserved = b.halo_ok ? F2C_BATCH_HALO_OK : 0u;
+    plan->reserved = (b.halo_ok ? F2C_BATCH_HALO_OK : 0u) | (b.rows != kFaceTY ? F2C_BATCH_FAST_FP : 0u) |
+                     ((uint32_t)b.rows << 8);
     return 0;
 }
 
@@ -273,24 +303,44 @@ __global__ void __launch_bounds__(kBatchHaloThreads) batch_halo_kernel(const Adv
 }  // namespace
 }  // namespace f2c
 
+extern "C" int f2c_batch_prepare_rows_v1(const f2c_grid_v1 *grids, const f2c_fields_v1 *fields, const int32_t *kz,
+                                         int32_t count, int32_t tile_rows, void *workspace, size_t workspace_bytes,
+                                         void *staging, void *stream, f2c_batch_plan_v1 *plan) {
+    if (!grids || !fields || count <= 0 || !plan) return fail(1, "empty batch");
+    if (!workspace) return fail(1, "null batch workspace");
+    if (!rows_ok(tile_rows)) return fail(1, "tile rows must be 4, 8 or 16");
+    if (workspace_bytes < f2c_batch_workspace_bytes_rows_v1(grids, kz, count, tile_rows))
+        return fail(4, "batch workspace too small");
+    Built b;
+    if (int s = build(grids, fields, kz, count, tile_rows, b)) return s;
+    char *base = static_cast<char *>(workspace);
+    const cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const size_t descs = descs_offset(), items = items_offset(count);
+    cudaError_t e;
+    if (staging) {  // through the caller's host staging, without waiting
+        char *host = static_cast<char *>(staging);
+        std::memcpy(host + descs, b.descs.data(), sizeof(AdvArgs) * b.descs.size());
+        std::memcpy(host + items, b.items.data(), sizeof(BatchItem) * b.items.size());
+        const size_t bytes = items + sizeof(BatchItem) * b.items.size() - descs;
+        e = cudaMemcpyAsync(base + descs, host + descs, bytes, cudaMemcpyHostToDevice, s);
+    } else {
+        e = cudaMemcpyAsync(base + descs, b.descs.data(), sizeof(AdvArgs) * b.descs.size(), cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(base + items, b.items.data(), sizeof(BatchItem) * b.items.size(),
+                                cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    }
+    if (e != cudaSuccess) return fail(6, std::string("batch prepare: ") + cudaGetErrorString(e));
+    return finish(b, count, workspace, workspace_bytes, plan);
+}
+
 extern "C" int f2c_batch_prepare_v1(const f2c_grid_v1 *grids, const f2c_fields_v1 *fields, const int32_t *kz,
                                     int32_t count, void *workspace, size_t workspace_bytes, void *stream,
                                     f2c_batch_plan_v1 *plan) {
     if (!grids || !fields || count <= 0 || !plan) return fail(1, "empty batch");
     if (!workspace) return fail(1, "null batch workspace");
-    if (workspace_bytes < f2c_batch_workspace_bytes_v1(grids, kz, count)) return fail(4, "batch workspace too small");
-    Built b;
-    if (int s = build(grids, fields, kz, count, b)) return s;
-    char *base = static_cast<char *>(workspace);
-    const cudaStream_t s = static_cast<cudaStream_t>(stream);
-    cudaError_t e = cudaMemcpyAsync(base + descs_offset(), b.descs.data(), sizeof(AdvArgs) * b.descs.size(),
-                                    cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync(base + items_offset(count), b.items.data(), sizeof(BatchItem) * b.items.size(),
-                            cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess) return fail(6, std::string("batch prepare: ") + cudaGetErrorString(e));
-    return finish(b, count, workspace, workspace_bytes, plan);
+    return f2c_batch_prepare_rows_v1(grids, fields, kz, count, kFaceTY, workspace, workspace_bytes, nullptr, stream,
+                                     plan);
 }
 
 extern "C" int f2c_batch_prepare_async_v1(const f2c_grid_v1 *grids, const f2c_fields_v1 *fields, const int32_t *kz,
@@ -298,18 +348,8 @@ extern "C" int f2c_batch_prepare_async_v1(const f2c_grid_v1 *grids, const f2c_fi
                                           void *stream, f2c_batch_plan_v1 *plan) {
     if (!grids || !fields || count <= 0 || !plan) return fail(1, "empty batch");
     if (!workspace || !staging) return fail(1, "null batch workspace or staging");
-    if (workspace_bytes < f2c_batch_workspace_bytes_v1(grids, kz, count)) return fail(4, "batch workspace too small");
-    Built b;
-    if (int s = build(grids, fields, kz, count, b)) return s;
-    char *host = static_cast<char *>(staging);
-    const size_t descs = descs_offset(), items = items_offset(count);
-    std::memcpy(host + descs, b.descs.data(), sizeof(AdvArgs) * b.descs.size());
-    std::memcpy(host + items, b.items.data(), sizeof(BatchItem) * b.items.size());
-    const size_t bytes = items + sizeof(BatchItem) * b.items.size() - descs;
-    const cudaError_t e = cudaMemcpyAsync(static_cast<char *>(workspace) + descs, host + descs, bytes,
-                                          cudaMemcpyHostToDevice, static_cast<cudaStream_t>(stream));
-    if (e != cudaSuccess) return fail(6, std::string("batch prepare: ") + cudaGetErrorString(e));
-    return finish(b, count, workspace, workspace_bytes, plan);
+    return f2c_batch_prepare_rows_v1(grids, fields, kz, count, kFaceTY, workspace, workspace_bytes, staging, stream,
+                                     plan);
 }
 
 extern "C" int f2c_batch_halo_v1(const f2c_batch_plan_v1 *plan, void *stream) {
@@ -329,6 +369,10 @@ extern "C" int f2c_batch_halo_v1(const f2c_batch_plan_v1 *plan, void *stream) {
 
 extern "C" int f2c_batch_step_v1(const f2c_batch_plan_v1 *plan, void *stream) {
     if (!plan || !plan->workspace || plan->items <= 0) return fail(1, "batch plan not prepared");
+    const int rows = plan_rows(plan);
+    const bool fast = (plan->reserved & F2C_BATCH_FAST_FP) != 0;
+    if (!rows_ok(rows)) return fail(1, "batch plan with unknown tile rows");
+    if (!fast && rows != kFaceTY) return fail(1, "tiles of 4 or 16 rows run only the fast-fp kernel");
     const cudaStream_t s = static_cast<cudaStream_t>(stream);
     char *base = static_cast<char *>(plan->workspace);
     unsigned *counter = reinterpret_cast<unsigned *>(base);
@@ -336,11 +380,46 @@ extern "C" int f2c_batch_step_v1(const f2c_batch_plan_v1 *plan, void *stream) {
     const BatchItem *items = reinterpret_cast<const BatchItem *>(base + items_offset(plan->count));
     cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(unsigned), s);
     if (e != cudaSuccess) return fail(6, std::string("batch counter reset: ") + cudaGetErrorString(e));
-    const Kernel k = kernel_for(plan->nscalar, plan->mask, (plan->reserved & F2C_BATCH_FAST_FP) != 0);
+    const Kernel k = kernel_for(plan->nscalar, plan->mask, fast, rows);
     if (k.status != cudaSuccess) return fail(6, std::string("batch kernel set-up: ") + cudaGetErrorString(k.status));
     int nitems = plan->items;
     void *args[] = {(void *)&descs, (void *)&items, (void *)&nitems, (void *)&counter};
-    e = cudaLaunchKernel(k.fn, dim3(plan->ctas), dim3(kFaceTX, kFaceTY + 1, 1), args, k.smem, s);
+    e = cudaLaunchKernel(k.fn, dim3(plan->ctas), dim3(kFaceTX, rows + 1, 1), args, k.smem, s);
     if (e != cudaSuccess) return fail(6, std::string("batch launch: ") + cudaGetErrorString(e));
+    return 0;
+}
+
+extern "C" int f2c_batch_graph_create_v1(const f2c_batch_plan_v1 *plan, void **graph) {
+    if (!plan || !graph) return fail(1, "null plan or graph output");
+    *graph = nullptr;
+    cudaStream_t capture = nullptr;
+    cudaError_t e = cudaStreamCreateWithFlags(&capture, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return fail(6, std::string("batch graph stream: ") + cudaGetErrorString(e));
+    e = cudaStreamBeginCapture(capture, cudaStreamCaptureModeThreadLocal);
+    int status = e == cudaSuccess ? f2c_batch_step_v1(plan, capture) : 6;
+    cudaGraph_t g = nullptr;
+    const cudaError_t end = e == cudaSuccess ? cudaStreamEndCapture(capture, &g) : e;
+    cudaGraphExec_t exec = nullptr;
+    if (status == 0 && end == cudaSuccess) {
+        e = cudaGraphInstantiate(&exec, g, 0);
+        if (e != cudaSuccess) status = fail(6, std::string("batch graph instantiation: ") + cudaGetErrorString(e));
+    } else if (status == 0) {
+        status = fail(6, std::string("batch graph capture: ") + cudaGetErrorString(end));
+    }
+    if (g) cudaGraphDestroy(g);
+    cudaStreamDestroy(capture);
+    if (status == 0) *graph = exec;
+    return status;
+}
+
+extern "C" int f2c_batch_graph_launch_v1(void *graph, void *stream) {
+    if (!graph) return fail(1, "null batch graph");
+    const cudaError_t e = cudaGraphLaunch(static_cast<cudaGraphExec_t>(graph), static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return fail(6, std::string("batch graph launch: ") + cudaGetErrorString(e));
+    return 0;
+}
+
+extern "C" int f2c_batch_graph_destroy_v1(void *graph) {
+    if (graph) cudaGraphExecDestroy(static_cast<cudaGraphExec_t>(graph));
     return 0;
 }

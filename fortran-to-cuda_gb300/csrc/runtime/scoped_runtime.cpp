@@ -179,6 +179,7 @@ struct Context {
     bool copies_ready = false;
     bool queue_enabled = true, graphs_enabled = true;
     int numerics = 0;  // FORT_SCOPE_NUMERICS_STRICT or FORT_SCOPE_NUMERICS_FAST, for the entries' kernels
+    int pin_host = -1;  // pinning of this context's host arrays at first device use: -1 FORT_SCOPE_PIN_HOST, 0 off, 1 on
     // Timing of slab sequences (off unless asked for): per slab, events around its uploads (copy stream 1),
     // its kernel (the context stream) and its publications (copy stream 2); those of the last sequence.
     struct SlabMarks {
@@ -323,8 +324,8 @@ void ensure_stream(Context *c) {
 void pin_for_device(Context *c, Buffer *b) {
     if (b->pin_tried) return;
     b->pin_tried = true;
-    if (b->bytes < (Backend::cpu ? size_t(0) : size_t(1) << 20) || !b->bytes || !env_flag("FORT_SCOPE_PIN_HOST", true))
-        return;
+    const bool pinning = c->pin_host < 0 ? env_flag("FORT_SCOPE_PIN_HOST", true) : c->pin_host != 0;
+    if (b->bytes < (Backend::cpu ? size_t(0) : size_t(1) << 20) || !b->bytes || !pinning) return;
     ensure_stream(c);
     b->pinned_host = Backend::pin(b->host, b->bytes, &b->mapped);
 }
@@ -2608,6 +2609,14 @@ int fort_scope_numerics_set_v1(fort_scope_t context, int numerics) {
         if (numerics != FORT_SCOPE_NUMERICS_STRICT && numerics != FORT_SCOPE_NUMERICS_FAST)
             raise(FORT_SCOPE_ARGUMENT, "unknown numerical contract");
         find_context(context)->numerics = numerics;
+        return FORT_SCOPE_OK;
+    });
+}
+
+int fort_scope_host_pinning_set_v1(fort_scope_t context, int enabled) {
+    return guarded([&] {
+        if (enabled < -1 || enabled > 1) raise(FORT_SCOPE_ARGUMENT, "pinning is -1 (environment), 0 or 1");
+        find_context(context)->pin_host = enabled;
         return FORT_SCOPE_OK;
     });
 }

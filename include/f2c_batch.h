@@ -41,9 +41,12 @@ typedef struct f2c_batch_plan_v1 {
  * (set by preparation). F2C_BATCH_FAST_FP: f2c_batch_step_v1 runs the fast-fp
  * kernel (F2C_KERNEL_FAST of f2c_advection.h: FMA contraction and regrouped
  * sums, each field within 1e-12 of its maximum of the strict result) instead of
- * the bit-exact one; the caller sets it after preparation, which clears it. */
+ * the bit-exact one; the caller sets it after preparation, which clears it
+ * (and sets it for tiles of 4 or 16 rows, which only the fast-fp kernel runs).
+ * Bits 8-15 hold the plan's tile rows (0 reads as 8). */
 #define F2C_BATCH_HALO_OK 1u
 #define F2C_BATCH_FAST_FP 2u
+#define F2C_BATCH_TILE_ROWS(reserved) ((((reserved) >> 8) & 0xffu) ? (((reserved) >> 8) & 0xffu) : 8u)
 
 /* Bytes of workspace for `count` instances cut into z-chunks of kz[i] levels (kz NULL: 32). */
 size_t f2c_batch_workspace_bytes_v1(const f2c_grid_v1 *grids, const int32_t *kz, int32_t count);
@@ -63,6 +66,28 @@ int f2c_batch_step_v1(const f2c_batch_plan_v1 *plan, void *stream);
 int f2c_batch_prepare_async_v1(const f2c_grid_v1 *grids, const f2c_fields_v1 *fields, const int32_t *kz,
                                int32_t count, void *workspace, size_t workspace_bytes, void *staging, void *stream,
                                f2c_batch_plan_v1 *plan);
+
+/* Tile shapes. The plans above cut every instance into tiles of 32 x 8
+ * columns. These entries take the tile height: 4, 8 or 16 rows (one warp per
+ * row plus an edge warp; 4-row tiles run four CTAs per SM, 8-row two, 16-row
+ * one). Tiles of 4 or 16 rows run the fast-fp kernel only; results do not
+ * depend on the tile shape or the z-chunk depths, bit for bit. `staging` NULL
+ * prepares synchronously on `stream` (as f2c_batch_prepare_v1), otherwise as
+ * f2c_batch_prepare_async_v1 does. */
+size_t f2c_batch_workspace_bytes_rows_v1(const f2c_grid_v1 *grids, const int32_t *kz, int32_t count,
+                                         int32_t tile_rows);
+int f2c_batch_prepare_rows_v1(const f2c_grid_v1 *grids, const f2c_fields_v1 *fields, const int32_t *kz,
+                              int32_t count, int32_t tile_rows, void *workspace, size_t workspace_bytes,
+                              void *staging, void *stream, f2c_batch_plan_v1 *plan);
+
+/* A plan's step (counter reset + persistent launch) captured once as an
+ * executable CUDA graph (`*graph` receives a cudaGraphExec_t), launched on any
+ * stream and destroyed by the caller. The graph reads the plan's workspace at
+ * each launch; it stays valid while the workspace and the instances' arrays
+ * do. The plan's flags are fixed at capture. */
+int f2c_batch_graph_create_v1(const f2c_batch_plan_v1 *plan, void **graph);
+int f2c_batch_graph_launch_v1(void *graph, void *stream);
+int f2c_batch_graph_destroy_v1(void *graph);
 
 /* Boundary fill of every instance's outputs in one launch on `stream` (the
  * per-instance rule of f2c_halo_fill_v1: U, V and scalars periodic in x and y

@@ -352,6 +352,16 @@ int fort_scope_slab_timing_get_v1(fort_scope_t context, fort_scope_slab_timing_v
 int fort_scope_numerics_set_v1(fort_scope_t context, int numerics);
 int fort_scope_numerics_get_v1(fort_scope_t context, int *numerics);
 
+/* ---- host pinning of a context (extension; the reference has no counterpart) ----
+ *
+ * Host arrays of 1 MiB or more are pinned in place the first time the device
+ * is about to use them, so that their copies run as DMA. A caller whose arrays
+ * never move between host and device while in use (a server that defines its
+ * jobs' fields on the device and reads back only some results) turns this off
+ * for its context: 0 never pins, 1 always pins, -1 (the default) follows
+ * FORT_SCOPE_PIN_HOST. Arrays already pinned stay pinned. */
+int fort_scope_host_pinning_set_v1(fort_scope_t context, int enabled);
+
 #ifdef __cplusplus
 }
 #endif

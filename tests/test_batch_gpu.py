@@ -156,3 +156,46 @@ def test_fast_batch_on_the_ensemble_shapes(cuda):
             g = got.cpu().numpy()[inner]
             assert np.array_equal(_bits(g), _bits(one.cpu().numpy()[inner])), name
             tolerance.check(g, ref[name][inner], name)
+
+
+@pytest.mark.parametrize("rows", [4, 8, 16])
+@pytest.mark.parametrize("kz", [None, [3, 7, 32, 16, 2]])
+def test_fast_batch_tile_shapes_equal_single_launches(cuda, rows, kz):
+    """Every tile height and chunk depth gives the single-instance fast-fp kernel's values bit for bit, and the
+    oracle's within the fast-fp tolerance; the batch's own graph replays the same step."""
+    from tolerance import check
+
+    inst = _setup(cuda, 2)
+    batch = native.Batch([x[4] for x in inst], [x[5] for x in inst], kz=kz, tile_rows=rows)
+    ws = cuda.empty(batch.workspace_bytes(), dtype=cuda.uint8, device="cuda")
+    batch.prepare(ws.data_ptr(), ws.numel())
+    if rows != 8:
+        assert batch.plan.reserved & native.BATCH_FAST_FP  # set by preparation: only the fast-fp kernel has them
+    else:
+        batch.set_fast_fp(True)
+    assert (batch.plan.reserved >> 8) & 0xFF == rows
+    for _ in range(2):
+        batch.graph_step()
+    cuda.cuda.synchronize()
+    for geo, f, ins, outs, grid, fields in inst:
+        single = [cuda.full_like(t, float("nan")) for t in ins]
+        p, q = [t.data_ptr() for t in ins], [t.data_ptr() for t in single]
+        native.advection(grid, *p[:3], *q[:3], scalars=p[3:], scalar_out=q[3:], variant=native.FAST)
+        cuda.cuda.synchronize()
+        ref = api.advection_step({"U": f.U, "V": f.V, "W": f.W}, geo.dx, geo.dy, geo.dz, geo.halo, f.scalars)
+        for got, one, name in zip(outs, single, ["U", "V", "W", "S0", "S1"]):
+            g = got.cpu().numpy()[geo.interior()]
+            assert np.array_equal(_bits(g), _bits(one.cpu().numpy()[geo.interior()])), name
+            check(g, ref[name][geo.interior()], name)
+
+
+def test_strict_step_refuses_short_and_tall_tiles(cuda):
+    inst = _setup(cuda, 0)
+    batch = native.Batch([x[4] for x in inst], [x[5] for x in inst], tile_rows=16)
+    ws = cuda.empty(batch.workspace_bytes(), dtype=cuda.uint8, device="cuda")
+    batch.prepare(ws.data_ptr(), ws.numel())
+    batch.set_fast_fp(False)
+    with pytest.raises(native.NativeError, match="fast-fp"):
+        batch.step()
+    with pytest.raises(native.NativeError, match="tile rows"):
+        native.Batch([x[4] for x in inst], [x[5] for x in inst], tile_rows=12).prepare(ws.data_ptr(), ws.numel())
