@@ -7,7 +7,7 @@ scalars on an nx x ny x nz grid. ``Server`` drives the native server of
 arrive while free device memory covers them, keeps each job's two field sets
 in the residency runtime's device mirrors from admission to retirement (its
 first set seeded on the device, nothing moved to the host between steps), and
-advances the jobs with the least remaining work, up to about 4 M grid points a
+advances the jobs with the least remaining work, up to about 8 M grid points a
 tick, as one persistent batched launch per scalar count plus one batched
 boundary fill, two ticks of a selection captured once as a CUDA graph and
 replayed while the selection holds. Every job's arithmetic is the
@@ -37,8 +37,10 @@ from . import workloads as wl
 DT = 0.1
 BUDGET_BYTES = 150 * 10**9
 MAX_ACTIVE = 256
-# grid points advanced per tick before further jobs wait for the next tick: about 1 ms of work
-TICK_POINTS = 4_000_000
+# grid points advanced per tick before further jobs wait for the next tick: about 1.3 ms of fast-fp work. Measured
+# on GB300 (500 jobs at 200 and 2000 jobs/s): 4 M-point ticks gave 1.04-1.06x the device-time model of serial
+# service with a median latency of 86 ms at 200 jobs/s, 8 M 1.07-1.09x and 135 ms, 16 M 1.09-1.11x and 231 ms
+TICK_POINTS = 8_000_000
 NUMERICS = {"fast": native.FAST, "strict": native.FACES}
 
 

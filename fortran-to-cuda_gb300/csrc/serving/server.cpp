@@ -17,9 +17,10 @@
 //  * A selection (jobs with the least remaining work, up to tick_points points)
 //    is planned once: per scalar count one persistent batched plan for each of
 //    two consecutive ticks, in fixed device workspace slots staged through
-//    pinned host slots. The two ticks are captured as one CUDA graph and
-//    replayed while the selection holds; a one-tick graph serves an odd
-//    remainder. The eight most recent selections stay cached.
+//    pinned host slots. The two ticks are captured as one CUDA graph, each
+//    scalar group's chain on a branch of its own so that the groups' launches
+//    overlap, and replayed while the selection holds; a one-tick graph serves
+//    an odd remainder. The eight most recent selections stay cached.
 //  * One worker thread issues bursts of ticks and keeps at most `depth` of them
 //    in flight; completion is seen through one event per burst.
 #include <cuda_runtime.h>
@@ -110,6 +111,7 @@ struct Server {
     // worker state
     f2c_serve_stats_v1 counts{};
     cudaStream_t ctx_stream = nullptr, stream = nullptr, capture = nullptr;
+    cudaStream_t branch[F2C_MAX_SCALARS] = {};  // capture branches of the scalar groups after the first
     char *slot_device = nullptr, *slot_host = nullptr;
     std::vector<uint64_t> slot_busy_until;  // burst sequence after which a free slot may be rewritten
     std::vector<bool> slot_used;
@@ -489,18 +491,43 @@ void launch_tick(const Selection &sel, int t, cudaStream_t stream) {
     }
 }
 
+// The selection's ticks as one graph. Each scalar group's ticks form a chain of its own (a job depends on
+// nothing but itself), captured on a stream of its own: the groups' persistent launches run side by side,
+// so that one group's tail overlaps another's work.
 cudaGraphExec_t capture(Server *s, const Selection &sel, int ticks) {
+    const size_t groups = sel.ticks[0].size();
+    std::vector<cudaEvent_t> marks;
+    auto mark = [&](cudaStream_t st) {
+        cudaEvent_t e;
+        cuda(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "capture event");
+        marks.push_back(e);
+        cuda(cudaEventRecord(e, st), "capture fork/join");
+        return e;
+    };
     cuda(cudaStreamBeginCapture(s->capture, cudaStreamCaptureModeThreadLocal), "capture begin");
     try {
-        for (int t = 0; t < ticks; ++t) launch_tick(sel, t, s->capture);
+        const cudaEvent_t fork = mark(s->capture);
+        for (size_t g = 1; g < groups; ++g) cuda(cudaStreamWaitEvent(s->branch[g - 1], fork, 0), "capture fork");
+        for (size_t g = 0; g < groups; ++g) {
+            const cudaStream_t st = g ? s->branch[g - 1] : s->capture;
+            for (int t = 0; t < ticks; ++t) {
+                const Plan &p = sel.ticks[t][g];
+                kernel(f2c_batch_step_v1(&p.plan, st), "tick step");
+                kernel(f2c_batch_halo_v1(&p.plan, st), "tick boundary fill");
+            }
+        }
+        for (size_t g = 1; g < groups; ++g) cuda(cudaStreamWaitEvent(s->capture, mark(s->branch[g - 1]), 0), "capture join");
     } catch (...) {
         cudaGraph_t g = nullptr;
         cudaStreamEndCapture(s->capture, &g);
         if (g) cudaGraphDestroy(g);
+        for (cudaEvent_t e : marks) cudaEventDestroy(e);
         throw;
     }
     cudaGraph_t graph = nullptr;
-    cuda(cudaStreamEndCapture(s->capture, &graph), "capture end");
+    const cudaError_t end = cudaStreamEndCapture(s->capture, &graph);
+    for (cudaEvent_t e : marks) cudaEventDestroy(e);
+    cuda(end, "capture end");
     cudaGraphExec_t exec = nullptr;
     const cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
     cudaGraphDestroy(graph);
@@ -618,6 +645,7 @@ void worker_main(Server *s) {
         cuda(cudaDeviceGetAttribute(&s->sms, cudaDevAttrMultiProcessorCount, device), "SM count");
         cuda(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking), "stream");
         cuda(cudaStreamCreateWithFlags(&s->capture, cudaStreamNonBlocking), "capture stream");
+        for (cudaStream_t &b : s->branch) cuda(cudaStreamCreateWithFlags(&b, cudaStreamNonBlocking), "capture stream");
         runtime(fort_scope_domain_workspace_reserve_v1(s->domain, kSlotBytes * kSlots, &s->workspace_lease),
                 "plan workspace");
         cuda(cudaMalloc(&s->slot_device, kSlotBytes * kSlots), "plan workspace");
@@ -698,6 +726,8 @@ void worker_main(Server *s) {
     if (s->slot_host) cudaFreeHost(s->slot_host);
     if (s->workspace_lease) (void)fort_scope_domain_workspace_release_v1(s->domain, s->workspace_lease);
     if (s->capture) cudaStreamDestroy(s->capture);
+    for (cudaStream_t b : s->branch)
+        if (b) cudaStreamDestroy(b);
     if (s->stream) cudaStreamDestroy(s->stream);
     if (ctx_stream) (void)fort_scope_gpu_leave(s->context, previous);
     std::lock_guard<std::mutex> g(s->lock);
@@ -720,7 +750,7 @@ extern "C" int f2c_serve_create_v1(fort_scope_t context, const f2c_serve_options
     if (opt.flags & ~F2C_SERVE_DIRECT) return fail(FORT_SCOPE_ARGUMENT, "unknown server flags");
     if (!opt.max_active) opt.max_active = 256;
     if (!opt.depth) opt.depth = 4;
-    if (!opt.tick_points) opt.tick_points = 4000000;
+    if (!opt.tick_points) opt.tick_points = 8000000;
     if (!opt.burst_points) opt.burst_points = 32000000;
     fort_scope_domain_t domain = 0;
     if (int st = fort_scope_domain_get_v1(context, &domain)) return fail(st, fort_scope_error());

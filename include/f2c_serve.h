@@ -16,7 +16,8 @@
  * remaining work (steps left x points), up to `tick_points` grid points, step
  * once, as one persistent batched launch per scalar count (f2c_batch.h) and
  * one batched boundary fill. Two consecutive ticks of the same selection are
- * captured once as a CUDA graph and replayed while the selection holds; the
+ * captured once as a CUDA graph (the scalar groups on parallel branches, so
+ * that their launches overlap) and replayed while the selection holds; the
  * last few selections stay cached. Every job's arithmetic is the
  * single-instance kernel's, so a job's result is the same alone and in any mix,
  * bit for bit. The numerical contract is the context's
@@ -64,7 +65,7 @@ typedef struct f2c_serve_options_v1 {
     uint32_t depth;          /* bursts of ticks in flight on the device (0: 4) */
     uint64_t budget_bytes;   /* device bytes all resident jobs may hold (0: no limit beyond the domain's) */
     uint64_t reserve_bytes;  /* device memory left free at every admission (0: max(total/16, 512 MiB)) */
-    uint64_t tick_points;    /* grid points stepped per tick (0: 4,000,000) */
+    uint64_t tick_points;    /* grid points stepped per tick (0: 8,000,000) */
     uint64_t burst_points;   /* grid points issued per scheduling decision (0: 32,000,000) */
 } f2c_serve_options_v1;
 
