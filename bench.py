@@ -169,6 +169,18 @@ def whole_job_value(points_per_rank: int, world: int, steps: int, slowest_ms: fl
     return points_per_rank * world * steps / (slowest_ms * 1e-3) / 1e9
 
 
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu), for the CPU baseline's record."""
+    try:
+        text = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+    except (OSError, subprocess.SubprocessError):
+        return "unknown"
+    for line in text.splitlines():
+        if line.startswith("Model name:"):
+            return line.split(":", 1)[1].strip()
+    return "unknown"
+
+
 def cpu_oracle_sample(fields, budget_s: float = 12.0):
     """Time the C oracle (all host threads) on the full workload; returns (Gpts/s, threads, sample text)."""
     from oracle import api
@@ -200,6 +212,7 @@ def parity_report(device_outputs, oracle_out, geo, names):
         report[name] = {
             "normwise_rel": float(d.max() / scale) if scale else float(d.max()),
             "pointwise_rel": float((d[big] / np.maximum(np.abs(ref[big]), 1e-300)).max()) if big.any() else 0.0,
+            "bit_identical": int(np.count_nonzero(got.view(np.int64) == ref.view(np.int64))),
             "bit_identical_frac": float(np.count_nonzero(got.view(np.int64) == ref.view(np.int64)) / got.size),
         }
     return report
@@ -444,7 +457,8 @@ def run_gb300(args):
                              "kernel": kernel_names["fast"], "headline": True}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         v, cores, sample, oracle_out = cpu_oracle_sample(fields)
-        result["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
+        result["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample,
+                                  "cpu": cpu_model(), "nproc": os.cpu_count()}
         names = ["U", "V", "W", *[f"S{n}" for n in range(NSCALAR)]]
         parity = {}
         for name in KERNELS:
@@ -510,6 +524,7 @@ def run_reference(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded sine modes + noise)",
         "config": config_object(1),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample,
+                         "cpu": cpu_model(), "nproc": os.cpu_count(),
                          "note": "C restatement of cdu.f90/cvd.f90/cdw.f90 (-O3 -fopenmp -ffp-contract=off); "
                                  "the reference's Fortran control needs gfortran, absent on both machines"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
