@@ -101,12 +101,15 @@ class Server:
     ``numerics`` is the domain's numerical contract ("fast": the fast-fp kernels, "strict": bit-identical to the
     oracle). ``tick_points=None`` steps every resident job every tick. ``graphs=False`` launches ticks directly.
     ``keep_results`` publishes every job's final fields into ``Job.result`` (numpy arrays, padded layout).
+    ``reserve_bytes`` is the device memory every admission leaves free (0: max(total/16, 512 MiB)).
     """
 
     def __init__(self, torch=None, numerics: str = "fast", budget_bytes: int = BUDGET_BYTES,
                  max_active: int = MAX_ACTIVE, keep_results: bool = False, depth: int = 4,
-                 tick_points: int | None = TICK_POINTS, graphs: bool = True, device: int = 0):
+                 tick_points: int | None = TICK_POINTS, graphs: bool = True, device: int = 0,
+                 reserve_bytes: int = 0):
         self.numerics = numerics
+        self.reserve = reserve_bytes
         self.budget = budget_bytes
         self.max_active = max_active
         self.keep_results = keep_results
@@ -126,7 +129,8 @@ class Server:
         dom.require(lib.fort_scope_host_pinning_set_v1(dom.context, 0))
         opts = native.ServeOptions(version=native.SERVE_ABI_VERSION, flags=0 if self.graphs else native.SERVE_DIRECT,
                                    max_active=self.max_active, depth=self.depth, budget_bytes=self.budget,
-                                   reserve_bytes=0, tick_points=self.tick_points or (1 << 62), burst_points=0)
+                                   reserve_bytes=self.reserve, tick_points=self.tick_points or (1 << 62),
+                                   burst_points=0)
         handle = ctypes.c_uint64()
         self._check(lib.f2c_serve_create_v1(dom.context, ctypes.byref(opts), ctypes.byref(handle)), 0)
         server = handle.value

@@ -146,3 +146,28 @@ def test_seeded_fields_follow_the_recipe(cuda):
         assert np.array_equal(g, api.halo(g.copy(), 1 if n == 2 else 0, job.geometry.halo))
     # the noise is N(0, 0.05) and the first scalar uniform in [280, 300]
     assert 280.0 <= got[3][inner].min() and got[3][inner].max() <= 300.0
+
+
+@pytest.mark.gpu
+def test_admission_follows_free_device_memory(cuda):
+    """With the reserve set so that the device's free memory covers two jobs, at most two are resident."""
+    jobs = [serving.Job(n, 0.0, 128, 120, 64, 2, 4, seed=700 + n) for n in range(5)]
+    per_job = jobs[0].device_bytes()
+    cuda.cuda.synchronize()
+    free, _ = cuda.cuda.mem_get_info()
+    # the server's own plan slots (64 MiB) come out of free memory too
+    server = serving.Server(cuda, keep_results=True, reserve_bytes=free - (64 << 20) - int(2.5 * per_job))
+    summary = server.run(jobs)
+    assert summary["jobs"] == 5
+    assert server.stats["peak_active"] <= 2 and server.stats["refused_admissions"] > 0
+    alone = serving.Job(4, 0.0, 128, 120, 64, 2, 4, seed=704)
+    serving.Server(cuda, keep_results=True).run([alone])
+    assert _same(jobs[4].result, alone.result)
+
+
+@pytest.mark.gpu
+def test_no_free_memory_refuses_the_job(cuda):
+    job = serving.Job(0, 0.0, 48, 48, 24, 0, 1, seed=3)
+    free, total = cuda.cuda.mem_get_info()
+    with pytest.raises(serving.ServeError, match="status 4"):
+        serving.Server(cuda, reserve_bytes=total).run([job])
