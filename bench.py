@@ -719,19 +719,24 @@ def run_small(args):
     b = [torch.zeros_like(x) for x in a]
     grid = native.make_grid(geo.nx, geo.ny, geo.nz, geo.halo, geo.dx, geo.dy, geo.dz)
 
-    def ten_steps(s):
-        src, dst = a, b
-        for _ in range(10):
-            native.advection(grid, *[t.data_ptr() for t in src], *[t.data_ptr() for t in dst], mode=native.ADVANCE,
-                             dt=0.1, stream=s)
-            native.halo_fill(grid, [t.data_ptr() for t in dst], [0, 0, 1], stream=s)
-            src, dst = dst, src
+    def ten_steps(variant):
+        def launch(s):
+            src, dst = a, b
+            for _ in range(10):
+                native.advection(grid, *[t.data_ptr() for t in src], *[t.data_ptr() for t in dst],
+                                 mode=native.ADVANCE, dt=0.1, stream=s, variant=variant)
+                native.halo_fill(grid, [t.data_ptr() for t in dst], [0, 0, 1], stream=s)
+                src, dst = dst, src
+        return launch
 
     stream = torch.cuda.Stream()
-    ms = _graph_time(torch, stream, ten_steps, args.steps, args.warmup)
+    us = {name: _graph_time(torch, stream, ten_steps(KERNELS[name]), args.steps, args.warmup) * 1e3 / 10
+          for name in (args.numerics, "strict" if args.numerics == "fast" else "fast")}
+    head = us[args.numerics]
     print(json.dumps({
         "metric": "64x64x32 advance step latency (U,V,W Euler dt=0.1 + boundary fill; 10 steps per graph)",
-        "value": ms * 1e3 / 10, "unit": "us/step", "higher_is_better": False, "gpts_per_s": geo.points * 10 / ms / 1e6,
+        "value": head, "unit": "us/step", "higher_is_better": False, "gpts_per_s": geo.points / head / 1e3,
+        "numerics": args.numerics, "us_per_step": us,
         "steps": args.steps * 10, "warmup": args.warmup, "dtype": "f64", "data": "synthetic (seeded sine modes)",
         "config": {"workload": "64x64x32 halo 2, 2 launches per step", "l2": "resident in L2: latency, not roofline"},
         "gpu_launches": args.steps * 20}), flush=True)
@@ -817,6 +822,7 @@ def main():
     parser.add_argument("--tune", action="store_true", help="batched: run the z-chunk autotuner first")
     parser.add_argument("--instances", type=int, default=64, help="batched: the first N instances of the ensemble")
     parser.add_argument("--jobs", type=int, default=500, help="serving: jobs per arrival rate")
+    parser.add_argument("--rates", type=float, nargs="+", help="serving: arrival rates (jobs/s) of --workload serving")
     args = parser.parse_args()
     args.warmup = max(3, args.warmup)
     if args.size:

@@ -311,7 +311,7 @@ def bench_main(args) -> None:
 
     import torch
 
-    rates = (50, 100, 200, 500, 1000, 2000)
+    rates = tuple(getattr(args, "rates", None) or (50, 100, 200, 500, 1000, 2000))
     count = max(20, getattr(args, "jobs", 500))
     numerics = getattr(args, "numerics", "fast")
     warm_up(torch, numerics)

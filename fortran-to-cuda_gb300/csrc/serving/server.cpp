@@ -32,6 +32,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <deque>
+#include <exception>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -697,6 +698,13 @@ void worker_main(Server *s) {
         if (!s->failure) {
             s->failure = f.status;
             s->error = f.message;
+        }
+        s->finished_cv.notify_all();
+    } catch (const std::exception &e) {  // host memory exhausted and the like: the server stops, it does not abort
+        std::lock_guard<std::mutex> g(s->lock);
+        if (!s->failure) {
+            s->failure = FORT_SCOPE_RESOURCE;
+            s->error = std::string("server worker: ") + e.what();
         }
         s->finished_cv.notify_all();
     }

@@ -120,7 +120,7 @@ int f2c_serve_stats_get_v1(f2c_server_t server, f2c_serve_stats_v1 *stats);
 /* Last failure text of the server (never NULL). */
 const char *f2c_serve_error_v1(f2c_server_t server);
 /* Stop the worker (jobs not finished are dropped: their arrays are released)
- * and free the server. */
+ * and free the server. No other call on the same server may overlap it. */
 int f2c_serve_destroy_v1(f2c_server_t server);
 
 #ifdef __cplusplus
