@@ -195,7 +195,7 @@ class BatchPlan(ctypes.Structure):
 class ServeOptions(ctypes.Structure):
     _fields_ = [("version", ctypes.c_uint32), ("flags", ctypes.c_uint32), ("max_active", ctypes.c_uint32),
                 ("depth", ctypes.c_uint32), ("budget_bytes", ctypes.c_uint64), ("reserve_bytes", ctypes.c_uint64),
-                ("tick_points", ctypes.c_uint64), ("burst_points", ctypes.c_uint64)]
+                ("tick_points", ctypes.c_uint64), ("burst_points", ctypes.c_uint64), ("starve_s", ctypes.c_double)]
 
 
 class ServeJob(ctypes.Structure):

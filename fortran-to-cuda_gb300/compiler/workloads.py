@@ -230,14 +230,22 @@ def _uniform(key: int, n: np.ndarray) -> np.ndarray:
     return (_mix64(z) >> np.uint64(11)).astype(np.float64) * 2.0 ** -53
 
 
+def _uniform24(key: int, n: np.ndarray) -> np.ndarray:
+    z = np.uint64(key) + np.uint64(_GOLDEN) * (n + np.uint64(1))
+    return (_mix64(z) >> np.uint64(40)).astype(np.float32) * np.float32(2.0 ** -24)
+
+
 def seeded_fields_reference(geo: Geometry, seed: int, nscalar: int = 0) -> list:
     """The fields ``f2c_seed_fields_v1`` writes on the device, computed on the host with numpy.
 
     Per velocity four sine modes (wavenumbers 1..4 per axis and a phase, drawn on the host from a splitmix64
     stream of the seed) at the staggered position, plus N(0, 0.05) noise from counter-based draws of the point's
-    interior index (Box-Muller); scalar 0 uniform in [280, 300], scalar 1 in [0, 0.02], further scalars Gaussian
-    blobs; ghosts filled by the boundary rule. Agrees with the device to the rounding of sin/cos/log/exp.
+    interior index (Box-Muller), evaluated in single precision in the device's order of operations; scalar 0
+    uniform in [280, 300] and scalar 1 in [0, 0.02] (53-bit draws), further scalars Gaussian blobs (single
+    precision); ghosts filled by the boundary rule. Agrees with the device to the rounding of the single-precision
+    sin, cos, log and exp (a few units in the last place of a float).
     """
+    f32 = np.float32
     with np.errstate(over="ignore"):
         state = _mix64_int(seed ^ 0x5EEDF1E1D5)
 
@@ -253,35 +261,37 @@ def seeded_fields_reference(geo: Geometry, seed: int, nscalar: int = 0) -> list:
             for _ in range(4):
                 k = [1.0 + float(draw() % 4) for _ in range(3)]
                 phi = 2.0 * math.pi * (float(draw() >> 11) * 2.0 ** -53)
-                per.append([2.0 * math.pi * k[a] / lengths[a] for a in range(3)] + [phi])
+                per.append([f32(2.0 * math.pi * k[a] / lengths[a]) for a in range(3)] + [f32(phi)])
             modes.append(per)
         keys = [draw() for _ in range(7)]
         k, j, i = np.meshgrid(np.arange(geo.nz), np.arange(geo.ny), np.arange(geo.nx), indexing="ij")
         n = (i + geo.nx * (j + geo.ny * k)).astype(np.uint64)
+        fi, fj, fk = i.astype(f32), j.astype(f32), k.astype(f32)
+        dx, dy, dz = f32(geo.dx), f32(geo.dy), f32(geo.dz)
         out = []
         for c in range(3):
-            x = (i + (1.0 if c == 0 else 0.5)) * geo.dx
-            y = (j + (1.0 if c == 1 else 0.5)) * geo.dy
-            z = (k + (1.0 if c == 2 else 0.5)) * geo.dz
-            v = np.zeros(n.shape)
+            x = (fi + f32(1.0 if c == 0 else 0.5)) * dx
+            y = (fj + f32(1.0 if c == 1 else 0.5)) * dy
+            z = (fk + f32(1.0 if c == 2 else 0.5)) * dz
+            v = np.zeros(n.shape, dtype=f32)
             for ax, ay, az, phi in modes[c]:
-                v += np.sin(az * z + ay * y + (ax * x + phi))
-            u1 = 1.0 - _uniform(keys[c], np.uint64(2) * n)
-            u2 = _uniform(keys[c], np.uint64(2) * n + np.uint64(1))
-            v += 0.05 * (np.sqrt(-2.0 * np.log(u1)) * np.cos(2.0 * math.pi * u2))
-            out.append(v)
-        lx, ly, lz = lengths
-        sigma = 0.125 * min(lx, ly, lz)
+                v = v + np.sin(az * z + ay * y + (ax * x + phi))
+            u1 = f32(1.0) - _uniform24(keys[c], np.uint64(2) * n)
+            u2 = _uniform24(keys[c], np.uint64(2) * n + np.uint64(1))
+            v = v + f32(0.05) * (np.sqrt(f32(-2.0) * np.log(u1)) * np.cos(f32(6.28318530717958648) * u2))
+            out.append(v.astype(np.float64))
+        lx, ly, lz = (f32(geo.nx) * dx, f32(geo.ny) * dy, f32(geo.nz) * dz)
+        sigma = f32(0.125) * min(lx, ly, lz)
         for s in range(nscalar):
             if s == 0:
                 v = 280.0 + 20.0 * _uniform(keys[3], n)
             elif s == 1:
                 v = 0.02 * _uniform(keys[4], n)
             else:
-                x = (i + 0.5) * geo.dx - 0.5 * lx
-                y = (j + 0.5) * geo.dy - 0.5 * ly
-                z = (k + 0.5) * geo.dz - (0.25 + 0.25 * (s - 2)) * lz
-                v = np.exp(-(x * x + y * y + z * z) / (2.0 * sigma * sigma))
+                x = (fi + f32(0.5)) * dx - f32(0.5) * lx
+                y = (fj + f32(0.5)) * dy - f32(0.5) * ly
+                z = (fk + f32(0.5)) * dz - f32(0.25 + 0.25 * (s - 2)) * lz
+                v = np.exp(-(x * x + y * y + z * z) / (f32(2.0) * sigma * sigma)).astype(np.float64)
             out.append(v)
     fields = []
     for c, v in enumerate(out):
@@ -289,4 +299,3 @@ def seeded_fields_reference(geo: Geometry, seed: int, nscalar: int = 0) -> list:
         f[geo.interior()] = v
         fields.append(fill_halo(f, 1 if c == 2 else 0, geo.halo))
     return fields
-

@@ -542,7 +542,12 @@ std::vector<Job *> select_jobs(Server *s) {
     std::vector<Job *> ready;
     for (auto &j : s->active)
         if (j->done < j->spec.steps) ready.push_back(j.get());
-    std::sort(ready.begin(), ready.end(), [](const Job *a, const Job *b) {
+    // jobs waiting longer than starve_s go first, oldest first; the others by least remaining work
+    const double starving_before = s->opt.starve_s > 0 ? s->now() - s->opt.starve_s : -1e300;
+    std::sort(ready.begin(), ready.end(), [&](const Job *a, const Job *b) {
+        const bool sa = a->spec.arrival < starving_before, sb = b->spec.arrival < starving_before;
+        if (sa != sb) return sa;
+        if (sa && a->spec.arrival != b->spec.arrival) return a->spec.arrival < b->spec.arrival;
         return a->remaining() != b->remaining() ? a->remaining() < b->remaining() : a->id < b->id;
     });
     std::vector<Job *> chosen;
@@ -756,6 +761,7 @@ extern "C" int f2c_serve_create_v1(fort_scope_t context, const f2c_serve_options
         opt = *options;
     }
     if (opt.flags & ~F2C_SERVE_DIRECT) return fail(FORT_SCOPE_ARGUMENT, "unknown server flags");
+    if (!(opt.starve_s >= 0.0)) return fail(FORT_SCOPE_ARGUMENT, "starve_s must be zero or positive");
     if (!opt.max_active) opt.max_active = 256;
     if (!opt.depth) opt.depth = 4;
     if (!opt.tick_points) opt.tick_points = 8000000;

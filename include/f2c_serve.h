@@ -13,8 +13,8 @@
  * own budget must each cover the job.
  *
  * A worker thread advances the resident jobs in ticks: the jobs with the least
- * remaining work (steps left x points), up to `tick_points` grid points, step
- * once, as one persistent batched launch per scalar count (f2c_batch.h) and
+ * remaining work (steps left x points; jobs older than `starve_s` first), up
+ * to `tick_points` grid points, step once, as one persistent batched launch per scalar count (f2c_batch.h) and
  * one batched boundary fill. Two consecutive ticks of the same selection are
  * captured once as a CUDA graph (the scalar groups on parallel branches, so
  * that their launches overlap) and replayed while the selection holds; the
@@ -47,8 +47,11 @@ extern "C" {
  * N(0, 0.05) noise on the interior; scalar 0 is uniform in [280, 300], scalar 1
  * uniform in [0, 0.02], scalars 2 and 3 Gaussian blobs; ghost layers are then
  * filled as f2c_halo_fill_v1 does. The values depend only on the seed and the
- * geometry (a counter-based generator), never on the launch. `fields` holds
- * 3 + nscalar device pointers. Asynchronous on `stream`. */
+ * geometry (a counter-based generator), never on the launch. The modes, the
+ * noise and the blobs are evaluated in single precision and stored as FP64
+ * (synthetic inputs: FP64 transcendentals would cost several steps of the job);
+ * the uniform scalars carry 53 random bits. `fields` holds 3 + nscalar device
+ * pointers. Asynchronous on `stream`. */
 int f2c_seed_fields_v1(const f2c_grid_v1 *grid, uint64_t seed, int32_t nscalar, double *const *fields,
                        void *stream);
 
@@ -67,6 +70,8 @@ typedef struct f2c_serve_options_v1 {
     uint64_t reserve_bytes;  /* device memory left free at every admission (0: max(total/16, 512 MiB)) */
     uint64_t tick_points;    /* grid points stepped per tick (0: 8,000,000) */
     uint64_t burst_points;   /* grid points issued per scheduling decision (0: 32,000,000) */
+    double starve_s;         /* a job waiting longer than this since its arrival goes first, oldest first
+                                (0: least remaining work always decides) */
 } f2c_serve_options_v1;
 
 /* Job flags. F2C_SERVE_KEEP_RESULT: publish the final fields to host memory

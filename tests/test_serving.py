@@ -136,8 +136,11 @@ def test_seeded_fields_follow_the_recipe(cuda):
     got = _seeded(cuda, job)
     want = wl.seeded_fields_reference(job.geometry, job.seed, job.nscalar)
     inner = job.geometry.interior()
-    for g, w in zip(got, want):
-        assert np.allclose(g[inner], w[inner], rtol=0, atol=1e-13)
+    for n, (g, w) in enumerate(zip(got, want)):
+        if n in (3, 4):  # the uniform scalars: 53-bit draws, exact
+            assert np.array_equal(g[inner], w[inner])
+        else:  # single-precision sin, cos, log and exp may differ by a few units in a float's last place
+            assert np.allclose(g[inner], w[inner], rtol=0, atol=2e-5)
     # deterministic, ghosts filled as the boundary rule says
     assert _same(got, _seeded(cuda, job))
     from oracle import api
