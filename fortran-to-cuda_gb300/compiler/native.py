@@ -180,7 +180,7 @@ class Fields(ctypes.Structure):
                 ("s", ctypes.c_void_p * MAX_SCALARS), ("st", ctypes.c_void_p * MAX_SCALARS)]
 
 
-TENDENCY, ADVANCE = 0, 1
+TENDENCY, ADVANCE, ADVANCE_FILLED = 0, 1, 2
 
 
 BATCH_HALO_OK, BATCH_FAST_FP = 1, 2  # f2c_batch_plan_v1.reserved flags

@@ -8,9 +8,9 @@ arrive while free device memory covers them, keeps each job's two field sets
 in the residency runtime's device mirrors from admission to retirement (its
 first set seeded on the device, nothing moved to the host between steps), and
 advances the jobs with the least remaining work, up to about 8 M grid points a
-tick, as one persistent batched launch per scalar count plus one batched
-boundary fill, two ticks of a selection captured once as a CUDA graph and
-replayed while the selection holds. Every job's arithmetic is the
+tick, as one persistent batched launch per scalar count that also fills the
+new fields' ghost layers, two ticks of a selection captured once as a CUDA
+graph and replayed while the selection holds. Every job's arithmetic is the
 single-instance kernel's, so a job's result is the same alone and in any mix,
 bit for bit.
 
@@ -207,21 +207,20 @@ def _device_job(torch, job: Job, stream):
 
 
 def _plain_steps(grid, bufs, job: Job, variant: int, stream: int) -> None:
-    kinds = [0, 0, 1] + [0] * job.nscalar
+    """The job's steps through the single-instance path: one launch per step (advance and boundary fill)."""
     for n in range(job.steps):
         src, dst = bufs[n % 2], bufs[1 - n % 2]
         p, q = [t.data_ptr() for t in src], [t.data_ptr() for t in dst]
-        native.advection(grid, *p[:3], *q[:3], scalars=p[3:], scalar_out=q[3:], mode=native.ADVANCE, dt=DT,
+        native.advection(grid, *p[:3], *q[:3], scalars=p[3:], scalar_out=q[3:], mode=native.ADVANCE_FILLED, dt=DT,
                          stream=stream, variant=variant)
-        native.halo_fill(grid, q, kinds, stream=stream)
 
 
 class SerialServer:
     """The same open-loop stream served one job at a time through the single-instance path.
 
     A job is admitted when the previous one has finished (and it has arrived): its fields are seeded on the
-    device as the continuous server seeds them, each step is one advection launch and one boundary fill, and the
-    job is retired (one value read back) when its last step completes. Wall-clock, like ``Server.run``.
+    device as the continuous server seeds them, each step is one advection launch that also fills the boundary,
+    and the job is retired (one value read back) when its last step completes. Wall-clock, like ``Server.run``.
     """
 
     def __init__(self, torch, numerics: str = "fast"):
@@ -241,7 +240,7 @@ class SerialServer:
             job.admitted = time.perf_counter() - start
             grid, bufs = _device_job(torch, job, self.stream)
             _plain_steps(grid, bufs, job, self.variant, self.stream.cuda_stream)
-            self.launches += 2 + 2 * job.steps
+            self.launches += 2 + job.steps
             with torch.cuda.stream(self.stream):
                 bufs[job.steps % 2][0].view(-1)[:1].cpu()
             job.finished = time.perf_counter() - start

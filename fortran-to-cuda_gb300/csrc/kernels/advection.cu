@@ -28,6 +28,14 @@ int fail(int status, const std::string &message) {
     return status;
 }
 
+// The output mode is known, and a filled advance has room for the boundary fill's images.
+int check_mode(const f2c_grid_v1 *g, int mode) {
+    if (mode != F2C_TENDENCY && mode != F2C_ADVANCE && mode != F2C_ADVANCE_FILLED) return fail(1, "unknown output mode");
+    if (mode == F2C_ADVANCE_FILLED && (g->nz < g->halo + 1 || g->nx < g->halo || g->ny < g->halo))
+        return fail(1, "a filled advance needs nz > halo, nx >= halo and ny >= halo");
+    return 0;
+}
+
 static bool aligned8(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 7u) == 0; }
 
 int check_grid(const f2c_grid_v1 *g) {
@@ -47,7 +55,9 @@ static int fill_args(const f2c_grid_v1 *g, const f2c_fields_v1 *f, AdvArgs &a) {
     if (!f) return fail(1, "null field record");
     if (!f->u || !f->v || !f->w) return fail(1, "U, V and W are required");
     if (f->nscalar < 0 || f->nscalar > F2C_MAX_SCALARS) return fail(1, "scalar count out of range");
-    if (f->mode != F2C_TENDENCY && f->mode != F2C_ADVANCE) return fail(1, "unknown output mode");
+    if (int s = check_mode(g, f->mode)) return s;
+    if (f->mode == F2C_ADVANCE_FILLED && (!f->ut || !f->vt || !f->wt))
+        return fail(1, "a filled advance needs the U, V and W outputs");
     std::memset(&a, 0, sizeof a);
     a.u = f->u; a.v = f->v; a.w = f->w;
     a.out[0] = f->ut; a.out[1] = f->vt; a.out[2] = f->wt;
@@ -100,6 +110,15 @@ static cudaError_t faces_for_mask(const AdvArgs &a, int mask, cudaStream_t s) {
 }
 
 static cudaError_t launch_faces_dispatch(const AdvArgs &a, cudaStream_t s) {
+    if (a.mode == F2C_ADVANCE_FILLED) {
+        switch (a.nscalar) {
+        case 0: return launch_faces<0, 7 | kFillMask>(a, s);
+        case 1: return launch_faces<1, 7 | kFillMask>(a, s);
+        case 2: return launch_faces<2, 7 | kFillMask>(a, s);
+        case 3: return launch_faces<3, 7 | kFillMask>(a, s);
+        default: return launch_faces<4, 7 | kFillMask>(a, s);
+        }
+    }
     const int mask = (a.out[0] ? 1 : 0) | (a.out[1] ? 2 : 0) | (a.out[2] ? 4 : 0);
     switch (a.nscalar) {
     case 0: return faces_for_mask<0>(a, mask, s);
@@ -125,6 +144,16 @@ static cudaError_t fast_for_mask(const AdvArgs &a, int mask, cudaStream_t s) {
 }
 
 static cudaError_t launch_fast_dispatch(const AdvArgs &a, cudaStream_t s) {
+    if (a.mode == F2C_ADVANCE_FILLED) {
+        const int sms = current_sm_count();
+        switch (a.nscalar) {
+        case 0: return launch_fast<0, 7 | kFillMask, kFaceTY>(a, sms, s);
+        case 1: return launch_fast<1, 7 | kFillMask, kFaceTY>(a, sms, s);
+        case 2: return launch_fast<2, 7 | kFillMask, kFaceTY>(a, sms, s);
+        case 3: return launch_fast<3, 7 | kFillMask, kFaceTY>(a, sms, s);
+        default: return launch_fast<4, 7 | kFillMask, kFaceTY>(a, sms, s);
+        }
+    }
     const int mask = (a.out[0] ? 1 : 0) | (a.out[1] ? 2 : 0) | (a.out[2] ? 4 : 0);
     switch (a.nscalar) {
     case 0: return fast_for_mask<0>(a, mask, s);

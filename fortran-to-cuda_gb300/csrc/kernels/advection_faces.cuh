@@ -85,7 +85,7 @@ struct FaceSmem {
 // FaceSmem<NS, MASK>::bytes. Starts and ends with the shared face buffers free.
 template <int NS, int MASK>
 __device__ __forceinline__ void faces_tile(const AdvArgs &a, int tile_x, int tile_y, int k0, int k1, double *smem) {
-    constexpr bool DO_U = MASK & 1, DO_V = MASK & 2, DO_W = MASK & 4;
+    constexpr bool DO_U = MASK & 1, DO_V = MASK & 2, DO_W = MASK & 4, FILL = (MASK & kFillMask) != 0;
     using Smem = FaceSmem<NS, MASK>;
     constexpr int NF = Smem::NF;
     double *xface = smem;                         // [2][NF][XF]
@@ -269,7 +269,7 @@ __device__ __forceinline__ void faces_tile(const AdvArgs &a, int tile_x, int til
                 const double Vadv = (sVx + Vs) + LD(V, p, 1, -1, 0);
                 const double Wadv = (sWx + Wm) + LD(W, p, 1, 0, -1);
                 const double adv = ((c.Bux * (Ue - Uw)) * U0 + (c.Buy * (Un - Us)) * Vadv) + (c.Buz * (Up - Um)) * Wadv;
-                if (a.out[0]) store_result(a.out[0], U, p, exact_half(r - adv), a.mode, a.dt);
+                if (a.out[0]) store_point_t<FILL>(a.out[0], U, p, exact_half(r - adv), a, 0, i, j, k);
                 FUzb = FUz;
             }
             if (DO_V) {
@@ -277,7 +277,7 @@ __device__ __forceinline__ void faces_tile(const AdvArgs &a, int tile_x, int til
                 const double Uadv = (sUy + Uw) + LD(U, p, -1, 1, 0);
                 const double Wadv = (sWy + Wm) + LD(W, p, 0, 1, -1);
                 const double adv = ((c.Bvx * (Ve - Vw)) * Uadv + (c.Bvy * (Vn - Vs)) * V0) + (c.Bvz * (Vp - Vm)) * Wadv;
-                if (a.out[1]) store_result(a.out[1], V, p, exact_half(r - adv), a.mode, a.dt);
+                if (a.out[1]) store_point_t<FILL>(a.out[1], V, p, exact_half(r - adv), a, 0, i, j, k);
                 FVzb = FVz;
             }
             if (DO_W) {
@@ -285,14 +285,14 @@ __device__ __forceinline__ void faces_tile(const AdvArgs &a, int tile_x, int til
                 const double Uadv = (sUz + Uw) + LD(U, p, -1, 0, 1);
                 const double Vadv = (sVz + Vs) + LD(V, p, 0, -1, 1);
                 const double adv = ((c.Bwx * (We - Ww)) * Uadv + (c.Bwy * (Wn - Ws)) * Vadv) + (c.Bwz * (Wp - Wm)) * W0;
-                if (a.out[2]) store_result(a.out[2], W, p, exact_half(r - adv), a.mode, a.dt);
+                if (a.out[2]) store_point_t<FILL>(a.out[2], W, p, exact_half(r - adv), a, 1, i, j, k);
                 FWzb = FWz;
             }
 #pragma unroll
             for (int n = 0; n < NS; ++n) {
                 const double st = opaque_negate(((fe[n] - xf[(3 + n) * Smem::XF + xw]) + (fn[n] - yf[(3 + n) * Smem::YF + ys])) +
                                     (ft[n] - ftb[n]));
-                if (a.st[n]) store_result(a.st[n], a.s[n], p, st, a.mode, a.dt);
+                if (a.st[n]) store_point_t<FILL>(a.st[n], a.s[n], p, st, a, 0, i, j, k);
                 ftb[n] = ft[n];
             }
         }

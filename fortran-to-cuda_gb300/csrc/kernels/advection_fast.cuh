@@ -86,6 +86,7 @@ __device__ __forceinline__ double along_term(double f1, double f0, double c) {
 template <int NS, int MASK, int TY>
 __device__ __forceinline__ void fast_tile(const AdvArgs &a, int tile_x, int tile_y, int k0, int k1, double *smem) {
     constexpr bool DU = MASK & 1, DV = (MASK >> 1) & 1, DW = (MASK >> 2) & 1, DS = NS > 0;
+    constexpr bool filled = (MASK & kFillMask) != 0;  // F2C_ADVANCE_FILLED: outputs with their ghost images
     // face sums each point computes (at its north/east/top faces)
     constexpr bool F_UY = DU || DV, F_VX = DU || DV, F_UZ = DU || DW, F_WX = DU || DW, F_VZ = DV || DW,
                    F_WY = DV || DW;
@@ -103,7 +104,7 @@ __device__ __forceinline__ void fast_tile(const AdvArgs &a, int tile_x, int tile
     const double *__restrict__ V = a.v;
     const double *__restrict__ W = a.w;
     const FastCoefficients c = a.f;
-    const bool advance = a.mode == 1;
+    const bool advance = a.mode != 0;
     const int cj = edge ? j0 - 1 : j;
     long long p = (long long)(i + a.h) + sx * (long long)(cj + a.h) + plane * (long long)(k0 + a.h);
     long long pw = (long long)(i0 - 1 + a.h) + sx * (long long)(j0 + lane + a.h) + plane * (long long)(k0 + a.h);
@@ -229,7 +230,7 @@ __device__ __forceinline__ void fast_tile(const AdvArgs &a, int tile_x, int tile
                 double t = __fma_rn(c.cz, Z, advance ? U0 : 0.0);
                 t = __fma_rn(c.cy, Y, t);
                 t = __fma_rn(c.gx, X, t);
-                if (a.out[0]) a.out[0][p] = t;
+                if (a.out[0]) { if (filled) store_filled(a.out[0], 0, a, i, j, k, t); else a.out[0][p] = t; }
             }
             if (DV) {
                 const double X = cross_term(sVx, wVx, sUy, wUy);
@@ -238,7 +239,7 @@ __device__ __forceinline__ void fast_tile(const AdvArgs &a, int tile_x, int tile
                 double t = __fma_rn(c.cz, Z, advance ? V0 : 0.0);
                 t = __fma_rn(c.gy, Y, t);
                 t = __fma_rn(c.cx, X, t);
-                if (a.out[1]) a.out[1][p] = t;
+                if (a.out[1]) { if (filled) store_filled(a.out[1], 0, a, i, j, k, t); else a.out[1][p] = t; }
             }
             if (DW) {
                 const double X = cross_term(sWx, wWx, sUz, wUz);
@@ -247,7 +248,7 @@ __device__ __forceinline__ void fast_tile(const AdvArgs &a, int tile_x, int tile
                 double t = __fma_rn(c.gz, Z, advance ? W0 : 0.0);
                 t = __fma_rn(c.cy, Y, t);
                 t = __fma_rn(c.cx, X, t);
-                if (a.out[2]) a.out[2][p] = t;
+                if (a.out[2]) { if (filled) store_filled(a.out[2], 1, a, i, j, k, t); else a.out[2][p] = t; }
             }
             if (DS) {
                 const double scV = south[4 * SLOT + at];
@@ -263,7 +264,7 @@ __device__ __forceinline__ void fast_tile(const AdvArgs &a, int tile_x, int tile
                     t = __fma_rn(scV, LD(S, p, 0, -1, 0), t);
                     t = __fma_rn(-cW, LD(S, p, 0, 0, 1), t);
                     t = __fma_rn(bcW, LD(S, p, 0, 0, -1), t);
-                    if (a.st[n]) a.st[n][p] = t;
+                    if (a.st[n]) { if (filled) store_filled(a.st[n], 0, a, i, j, k, t); else a.st[n][p] = t; }
                 }
             }
             // carry up the march

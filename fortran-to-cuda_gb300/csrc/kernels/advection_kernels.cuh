@@ -34,12 +34,77 @@ struct HaloArgs {
     long long sx, plane;
 };
 
+// Bit 8 of a fused kernel's MASK template argument: the outputs are stored with their ghost images
+// (F2C_ADVANCE_FILLED); used with all three velocity outputs (MASK 7 | kFillMask).
+constexpr int kFillMask = 8;
+
 __device__ __forceinline__ void store_result(double *out, const double *in, long long p, double t, int mode,
                                              double dt) {
     if (mode == 0) {
         out[p] = t;
     } else {
         out[p] = __ldg(in + p) + dt * t;
+    }
+}
+
+// Output mode F2C_ADVANCE_FILLED: the new value v of interior point (i, j, k)
+// is stored with every ghost the boundary fill (halo_row) would copy from it,
+// so that the step needs no fill launch: periodic images in x and y, and in z
+// the mirror (kind 0) or, for W (kind 1), the zero wall faces at levels h-1
+// and h+nz-1 (written by the points of interior levels 0 and nz-1) and the
+// sign-flipped mirrors beyond. Every ghost has exactly one source point, and
+// the values are those the fill copies, so the result equals an advance step
+// followed by f2c_halo_fill_v1 bit for bit. Needs nx >= h, ny >= h, nz > h.
+__device__ __forceinline__ void store_filled(double *f, int kind, const AdvArgs &a, int i, int j, int k, double v) {
+    const int h = a.h, nx = a.nx, ny = a.ny, nz = a.nz;
+    // x and y targets: the point's own column and row and their periodic images (-1: none)
+    const int x0 = i + h, x1 = i < h ? i + h + nx : -1, x2 = i >= nx - h ? i + h - nx : -1;
+    const int y0 = j + h, y1 = j < h ? j + h + ny : -1, y2 = j >= ny - h ? j + h - ny : -1;
+    const long long sx = a.sx, plane = a.plane;
+    auto level = [&](int z, double val) {
+        double *base = f + plane * z;
+        auto row = [&](int y) {
+            if (y < 0) return;
+            double *r = base + sx * y;
+            r[x0] = val;
+            if (x1 >= 0) r[x1] = val;
+            if (x2 >= 0) r[x2] = val;
+        };
+        row(y0);
+        row(y1);
+        row(y2);
+    };
+    if (kind == 0) {
+        level(k + h, v);
+        if (k < h) level(h - 1 - k, v);
+        if (k >= nz - h) level(h + 2 * nz - 1 - k, v);
+    } else {
+        level(k + h, k == nz - 1 ? 0.0 : v);
+        if (k == 0) level(h - 1, 0.0);
+        if (k <= h - 2) level(h - 2 - k, -v);
+        if (k >= nz - 1 - h && k <= nz - 2) level(h + 2 * nz - 2 - k, -v);
+    }
+}
+
+// store_result, or for F2C_ADVANCE_FILLED the advanced value with its ghost images.
+__device__ __forceinline__ void store_point(double *out, const double *in, long long p, double t, const AdvArgs &a,
+                                            int kind, int i, int j, int k) {
+    if (a.mode == 2) {
+        store_filled(out, kind, a, i, j, k, __ldg(in + p) + a.dt * t);
+    } else {
+        store_result(out, in, p, t, a.mode, a.dt);
+    }
+}
+
+// The same with the fill chosen at compile time (the face-sharing kernels' MASK bit 8, kFillMask): kernels
+// without it keep their register budget.
+template <bool FILL>
+__device__ __forceinline__ void store_point_t(double *out, const double *in, long long p, double t, const AdvArgs &a,
+                                              int kind, int i, int j, int k) {
+    if (FILL) {
+        store_filled(out, kind, a, i, j, k, __ldg(in + p) + a.dt * t);
+    } else {
+        store_result(out, in, p, t, a.mode, a.dt);
     }
 }
 
@@ -60,14 +125,14 @@ __global__ void __launch_bounds__(BX *BY) advection_direct_kernel(const AdvArgs 
     long long p = (long long)(i + a.h) + sx * (long long)(j + a.h) + plane * (long long)(k0 + a.h);
 #define F2C_AT(A, di, dj, dk) __ldg((A) + p + (di) + (dj)*sx + (dk)*plane)
     for (int k = k0; k < k1; ++k, p += plane) {
-        if (a.out[0]) store_result(a.out[0], U, p, F2C_CDU_POINT(F2C_AT, a.c), a.mode, a.dt);
-        if (a.out[1]) store_result(a.out[1], V, p, F2C_CDV_POINT(F2C_AT, a.c), a.mode, a.dt);
-        if (a.out[2]) store_result(a.out[2], W, p, F2C_CDW_POINT(F2C_AT, a.c), a.mode, a.dt);
+        if (a.out[0]) store_point(a.out[0], U, p, F2C_CDU_POINT(F2C_AT, a.c), a, 0, i, j, k);
+        if (a.out[1]) store_point(a.out[1], V, p, F2C_CDV_POINT(F2C_AT, a.c), a, 0, i, j, k);
+        if (a.out[2]) store_point(a.out[2], W, p, F2C_CDW_POINT(F2C_AT, a.c), a, 1, i, j, k);
 #pragma unroll
         for (int n = 0; n < kMaxScalars; ++n) {
             if (n < a.nscalar && a.st[n]) {
                 const double *__restrict__ S = a.s[n];
-                store_result(a.st[n], S, p, F2C_SCALAR_POINT(F2C_AT, S, a.c), a.mode, a.dt);
+                store_point(a.st[n], S, p, F2C_SCALAR_POINT(F2C_AT, S, a.c), a, 0, i, j, k);
             }
         }
     }

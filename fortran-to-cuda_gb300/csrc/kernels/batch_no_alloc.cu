@@ -26,6 +26,7 @@
 namespace f2c {
 int fail(int status, const std::string &message);
 int check_grid(const f2c_grid_v1 *g);
+int check_mode(const f2c_grid_v1 *g, int mode);
 
 namespace {
 
@@ -152,6 +153,8 @@ extern "C" int f2c_batch_step_static_v1(const f2c_grid_v1 *grids, const f2c_fiel
             return fail(1, "batch instances differ in scalars, outputs or mode");
         }
         if (kz && kz[n] < 0) return fail(1, "negative z-chunk depth");
+        if (int s = check_mode(&grids[n], f.mode)) return s;
+        if (f.mode == F2C_ADVANCE_FILLED) return fail(1, "the no-allocation step takes the tendency or advance mode");
         const int c = kz && kz[n] > 0 ? kz[n] : kFaceKZ;
         const f2c_grid_v1 &g = grids[n];
         const long long tx = (g.nx + kFaceTX - 1) / kFaceTX, ty = (g.ny + kFaceTY - 1) / kFaceTY;

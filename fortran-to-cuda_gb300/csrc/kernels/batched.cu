@@ -13,6 +13,7 @@
 namespace f2c {
 int fail(int status, const std::string &message);
 int check_grid(const f2c_grid_v1 *g);
+int check_mode(const f2c_grid_v1 *g, int mode);
 
 struct BatchItem {
     int instance;
@@ -104,6 +105,7 @@ Kernel kernel_for_ns(int ns, bool fast, int rows) {
 
 Kernel kernel_for(int ns, int mask, bool fast, int rows) {
     switch (mask) {
+    case 7 | kFillMask: return kernel_for_ns<7 | kFillMask>(ns, fast, rows);
     case 1: return kernel_for_ns<1>(ns, fast, rows);
     case 2: return kernel_for_ns<2>(ns, fast, rows);
     case 4: return kernel_for_ns<4>(ns, fast, rows);
@@ -179,6 +181,7 @@ int build(const f2c_grid_v1 *grids, const f2c_fields_v1 *fields, const int32_t *
             return fail(1, "batch instances differ in scalars, outputs or mode");
         }
         if (kz && kz[n] < 0) return fail(1, "negative z-chunk depth");
+        if (int s = check_mode(&grids[n], f.mode)) return s;
         AdvArgs &a = descs[(size_t)n];
         std::memset(&a, 0, sizeof a);
         a.u = f.u; a.v = f.v; a.w = f.w;
@@ -201,6 +204,10 @@ int build(const f2c_grid_v1 *grids, const f2c_fields_v1 *fields, const int32_t *
     }
     if (mask != 7 && mask != 1 && mask != 2 && mask != 4 && mask != 0) mask = 7;
     if (mask == 0 && ns == 0) return fail(1, "batch computes nothing");
+    if (fields[0].mode == F2C_ADVANCE_FILLED) {
+        if (mask != 7) return fail(1, "a filled advance needs the U, V and W outputs");
+        mask = 7 | kFillMask;
+    }
     // the flattened queue: full-depth items first (largest first), then the partial ones
     std::vector<BatchItem> &items = out.items;
     items.clear();

@@ -15,8 +15,9 @@
 //    (where mirrors are allocated and seeded) by events. The runtime's calls
 //    that wait for the context stream therefore never wait for ticks.
 //  * A selection (jobs with the least remaining work, up to tick_points points)
-//    is planned once: per scalar count one persistent batched plan for each of
-//    two consecutive ticks, in fixed device workspace slots staged through
+//    is planned once: per scalar count one persistent batched plan (a filled
+//    advance: the step and its boundary fill in one launch) for each of two
+//    consecutive ticks, in fixed device workspace slots staged through
 //    pinned host slots. The two ticks are captured as one CUDA graph, each
 //    scalar group's chain on a branch of its own so that the groups' launches
 //    overlap, and replayed while the selection holds; a one-tick graph serves
@@ -461,7 +462,7 @@ void plan_tick(Server *s, Selection &sel, int t) {
             f.u = j->dev[src][0]; f.v = j->dev[src][1]; f.w = j->dev[src][2];
             f.ut = j->dev[dst][0]; f.vt = j->dev[dst][1]; f.wt = j->dev[dst][2];
             f.nscalar = j->spec.nscalar;
-            f.mode = F2C_ADVANCE;
+            f.mode = F2C_ADVANCE_FILLED;  // the step and its boundary fill in one launch
             f.dt = j->spec.dt;
             for (int n = 0; n < j->spec.nscalar; ++n) {
                 f.s[n] = j->dev[src][3 + n];
@@ -486,10 +487,7 @@ void plan_tick(Server *s, Selection &sel, int t) {
 }
 
 void launch_tick(const Selection &sel, int t, cudaStream_t stream) {
-    for (const Plan &p : sel.ticks[t]) {
-        kernel(f2c_batch_step_v1(&p.plan, stream), "tick step");
-        kernel(f2c_batch_halo_v1(&p.plan, stream), "tick boundary fill");
-    }
+    for (const Plan &p : sel.ticks[t]) kernel(f2c_batch_step_v1(&p.plan, stream), "tick step");
 }
 
 // The selection's ticks as one graph. Each scalar group's ticks form a chain of its own (a job depends on
@@ -512,9 +510,7 @@ cudaGraphExec_t capture(Server *s, const Selection &sel, int ticks) {
         for (size_t g = 0; g < groups; ++g) {
             const cudaStream_t st = g ? s->branch[g - 1] : s->capture;
             for (int t = 0; t < ticks; ++t) {
-                const Plan &p = sel.ticks[t][g];
-                kernel(f2c_batch_step_v1(&p.plan, st), "tick step");
-                kernel(f2c_batch_halo_v1(&p.plan, st), "tick boundary fill");
+                kernel(f2c_batch_step_v1(&sel.ticks[t][g].plan, st), "tick step");
             }
         }
         for (size_t g = 1; g < groups; ++g) cuda(cudaStreamWaitEvent(s->capture, mark(s->branch[g - 1]), 0), "capture join");
@@ -602,7 +598,7 @@ void issue(Server *s) {
                 launch_tick(*sel, 0, s->stream);
                 launch_tick(*sel, 1, s->stream);
             }
-            s->counts.direct_launches += (uint64_t)pairs * 2 * 2 * sel->ticks[0].size();
+            s->counts.direct_launches += (uint64_t)pairs * 2 * sel->ticks[0].size();
         } else {
             if (!sel->two) sel->two = capture(s, *sel, 2);
             for (int r = 0; r < pairs; ++r) cuda(cudaGraphLaunch(sel->two, s->stream), "graph launch");
@@ -612,7 +608,7 @@ void issue(Server *s) {
     } else {
         if (direct) {
             launch_tick(*sel, 0, s->stream);
-            s->counts.direct_launches += 2 * sel->ticks[0].size();
+            s->counts.direct_launches += sel->ticks[0].size();
         } else {
             if (!sel->one) sel->one = capture(s, *sel, 1);
             cuda(cudaGraphLaunch(sel->one, s->stream), "graph launch");

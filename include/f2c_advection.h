@@ -38,8 +38,12 @@ typedef struct f2c_grid_v1 {
 
 /* Output modes. TENDENCY writes the tendency (the reference's U2, V2, W2).
  * ADVANCE writes out = in + dt*tendency (forward Euler, double-buffered: the
- * outputs must not alias any input). */
-enum f2c_output_mode { F2C_TENDENCY = 0, F2C_ADVANCE = 1 };
+ * outputs must not alias any input). ADVANCE_FILLED is ADVANCE with the
+ * outputs' ghost layers filled in the same launch, bit for bit as
+ * f2c_halo_fill_v1 fills them afterwards (U, V and scalars periodic in x and y
+ * and mirrored in z, W with zero wall faces): a complete step in one launch;
+ * it needs nz > halo, nx >= halo and ny >= halo. */
+enum f2c_output_mode { F2C_TENDENCY = 0, F2C_ADVANCE = 1, F2C_ADVANCE_FILLED = 2 };
 
 typedef struct f2c_fields_v1 {
     const double *u, *v, *w;      /* velocities, required */
@@ -58,7 +62,7 @@ const char *f2c_last_error(void);
 /* Tendencies (or Euler-advanced fields) of U, V, W and the scalars on the
  * interior, in one fused z-marching launch. Bit-identical to the oracle's
  * per-point expressions (built with --fmad=false). Ghost layers of outputs are
- * not written. */
+ * not written, except in F2C_ADVANCE_FILLED mode. */
 int f2c_advection_v1(const f2c_grid_v1 *grid, const f2c_fields_v1 *fields, void *stream);
 
 /* The same computation by a chosen kernel:

@@ -14,8 +14,8 @@
  *
  * A worker thread advances the resident jobs in ticks: the jobs with the least
  * remaining work (steps left x points; jobs older than `starve_s` first), up
- * to `tick_points` grid points, step once, as one persistent batched launch per scalar count (f2c_batch.h) and
- * one batched boundary fill. Two consecutive ticks of the same selection are
+ * to `tick_points` grid points, step once, as one persistent batched launch per scalar count (f2c_batch.h) that
+ * also fills the new fields' ghost layers (F2C_ADVANCE_FILLED). Two consecutive ticks of the same selection are
  * captured once as a CUDA graph (the scalar groups on parallel branches, so
  * that their launches overlap) and replayed while the selection holds; the
  * last few selections stay cached. Every job's arithmetic is the
