@@ -163,10 +163,10 @@ struct Backend {
     static bool wait_event(Event) { return !std::getenv("F2C_TEST_FAIL_WAIT"); }
     // Host arrays are never pinned here, unless a test asks for the mapped
     // case (F2C_TEST_MAPPED): then the "device-usable" address is the array.
-    static bool pin(void *p, size_t, void **mapped) {
-        if (!std::getenv("F2C_TEST_MAPPED")) return false;
+    static int pin(void *p, size_t, void **mapped) {
+        if (!std::getenv("F2C_TEST_MAPPED")) return 0;
         *mapped = p;
-        return true;
+        return 1;
     }
     static void unpin(void *) {}
     // Work is synchronous: every stream is already joined.
@@ -303,20 +303,37 @@ struct Backend {
         cudaEventDestroy(e);
         return good;
     }
-    // Pin a host array in place and map it into the device address space;
-    // `mapped` receives the address a kernel uses to reach it over NVLink-C2C.
-    static bool pin(void *p, size_t bytes, void **mapped) {
-        cudaError_t e = cudaHostRegister(p, bytes, cudaHostRegisterMapped | cudaHostRegisterPortable);
-        if (e != cudaSuccess) {
+    // Whether the host byte at `p` is page-locked memory that CUDA knows (the
+    // caller's cudaHostAlloc or cudaHostRegister).
+    static bool page_locked(const void *p) {
+        cudaPointerAttributes attr{};
+        if (cudaPointerGetAttributes(&attr, p) != cudaSuccess) {
             cudaGetLastError();
             return false;
         }
-        e = cudaHostGetDevicePointer(mapped, p, 0);
-        if (e != cudaSuccess) {
+        return attr.type == cudaMemoryTypeHost;
+    }
+    // Pin a host array in place and map it into the device address space;
+    // `mapped` receives the address a kernel uses to reach it over NVLink-C2C.
+    // Returns 1 when this call pinned it (unpin it later), 2 when the caller's
+    // memory was page-locked already (its first and last bytes; leave it
+    // pinned), 0 when it could not be pinned.
+    static int pin(void *p, size_t bytes, void **mapped) {
+        int how = 1;
+        if (page_locked(p) && page_locked(static_cast<const char *>(p) + bytes - 1)) {
+            how = 2;
+        } else {
+            const cudaError_t r = cudaHostRegister(p, bytes, cudaHostRegisterMapped | cudaHostRegisterPortable);
+            if (r != cudaSuccess) {
+                cudaGetLastError();
+                return 0;
+            }
+        }
+        if (cudaHostGetDevicePointer(mapped, p, 0) != cudaSuccess) {
             cudaGetLastError();
             *mapped = nullptr;
         }
-        return true;
+        return how;
     }
     static void unpin(void *p) {
         if (cudaHostUnregister(p) != cudaSuccess) cudaGetLastError();

@@ -18,7 +18,8 @@
 //    cudaGraphExecKernelNodeSetParams for the nodes whose arguments changed
 //    (the reference's policy, compiler/runtime/scoped_graphs.hpp:140-235).
 //  * Host arrays of 1 MiB or more are pinned in place at registration
-//    (FORT_SCOPE_PIN_HOST=0 disables it) so uploads and downloads run as DMA
+//    (FORT_SCOPE_PIN_HOST=0 disables it; arrays already page-locked by the
+//    caller are used as they are) so uploads and downloads run as DMA
 //    over NVLink-C2C without staging, and are mapped into the device address
 //    space. An array the host writes or reads back between every device use
 //    (two uses in a row) is then accessed IN PLACE: its tasks get the mapped
@@ -92,7 +93,8 @@ struct Buffer {
     size_t extents[kMaxRank] = {};
     int64_t lower[kMaxRank] = {};
     void *device = nullptr;
-    bool pinned_host = false;
+    bool pinned_host = false;  // page-locked (and mapped) for DMA
+    bool pinned_here = false;  // ... by this runtime, which unpins it
     bool pin_tried = false;      // pinning is tried once, at the array's first device use
     void *mapped = nullptr;      // device-usable address of the pinned host array
     bool host_touched = true;    // the host wrote or read it since its last device use
@@ -327,7 +329,9 @@ void pin_for_device(Context *c, Buffer *b) {
     const bool pinning = c->pin_host < 0 ? env_flag("FORT_SCOPE_PIN_HOST", true) : c->pin_host != 0;
     if (b->bytes < (Backend::cpu ? size_t(0) : size_t(1) << 20) || !b->bytes || !pinning) return;
     ensure_stream(c);
-    b->pinned_host = Backend::pin(b->host, b->bytes, &b->mapped);
+    const int how = Backend::pin(b->host, b->bytes, &b->mapped);
+    b->pinned_host = how != 0;
+    b->pinned_here = how == 1;
 }
 
 void ensure_copy_streams(Context *c) {
@@ -1495,7 +1499,7 @@ Domain *make_domain(int device) {
 
 void destroy_buffer(Context *c, Buffer *b) {
     release_mirror(c, b);
-    if (b->pinned_host) Backend::unpin(b->host);
+    if (b->pinned_here) Backend::unpin(b->host);
     c->domain->by_identity.erase(b->identity);
     g_retired.insert(b->handle);
     c->domain->buffers.erase(b->handle);
