@@ -266,7 +266,7 @@ def run_e2e(fields, steps, warmup, dist, torch, fast_fp=False):
             dom.require(lib.fort_scope_slab_timing_set_v1(dom.context, 1))
     phases.clear()
     device.clear()
-    n = max(1, min(steps, 20))
+    n = max(1, min(steps, 40))
     gc_was = gc.isenabled()
     gc.disable()  # the timed steps allocate little; a collection inside one would be the interpreter's, not ours
     barrier(dist, torch)

@@ -223,6 +223,42 @@ def test_arrays_the_host_rewrites_every_step_are_streamed(resident, nx, ny, nz, 
         assert stats.upload_bytes <= 2 * sum(a.nbytes for a in ins)
 
 
+@pytest.mark.parametrize("nx, ny, nz", [(96, 64, 16), (512, 512, 24)])
+def test_arrays_the_caller_page_locked_are_used_as_they_are(resident, cuda, nx, ny, nz):
+    """Host arrays in memory the caller already page-locked (cudaHostAlloc, here through torch) are taken as
+    pinned without a second registration, streamed like the runtime's own pinned arrays, and stay usable (and
+    page-locked) after the domain closes."""
+    dom, fns = resident
+    geo = wl.Geometry(nx, ny, nz, halo=2)
+    f = wl.advection_fields(geo, seed=9, nscalar=1)
+    keep = [cuda.empty(a.shape, dtype=cuda.float64).pin_memory() for a in f.arrays() * 2]
+    ins, outs = [t.numpy() for t in keep[:4]], [t.numpy() for t in keep[4:]]
+    for a, src in zip(ins, f.arrays()):
+        a[...] = src
+    for a in outs:
+        a[...] = 0.0
+    dom.begin_epoch()
+    h_in = [dom.bind_real64(a) for a in ins]
+    h_out = [dom.bind_real64(a) for a in outs]
+    arrays = [*h_out[:3], *h_in[:3], h_in[3], h_out[3]]
+    for step in range(4):
+        dom.host_modify(h_in)
+        for a, src in zip(ins, f.arrays()):
+            a[...] = src * (1.0 + 0.5 * step)
+        assert _call(fns, dom, "advection::step1", arrays, [geo.dx, geo.dy, geo.dz],
+                     [geo.nx, geo.ny, geo.nz, geo.halo]) == abi.OK
+        dom.observe(h_out)
+        ref = api.advection_step({"U": ins[0], "V": ins[1], "W": ins[2]}, geo.dx, geo.dy, geo.dz, geo.halo, ins[3:])
+        for got, name in zip(outs, ["U", "V", "W", "S0"]):
+            assert _same(got[geo.interior()], ref[name][geo.interior()])
+    dom.end_epoch()
+    dom.close()
+    assert all(t.is_pinned() for t in keep)
+    dev = keep[0].cuda(non_blocking=True)  # still page-locked: an asynchronous copy from it works
+    cuda.cuda.synchronize()
+    assert _same(dev.cpu().numpy(), ins[0])
+
+
 @pytest.mark.parametrize("use, visible", [("host", None), ("host", ""), ("zero", None), ("device", None)])
 def test_the_product_runtime_brings_the_device_up_only_for_device_work(use, visible, tmp_path):
     """The CUDA build: host-only use of 2 MiB arrays creates no stream and pins nothing, also with every device
