@@ -174,3 +174,23 @@ def test_no_free_memory_refuses_the_job(cuda):
     free, total = cuda.cuda.mem_get_info()
     with pytest.raises(serving.ServeError, match="status 4"):
         serving.Server(cuda, reserve_bytes=total).run([job])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("numerics", ["fast", "strict"])
+def test_a_poisson_mix_equals_one_job_at_a_time(cuda, numerics):
+    """24 jobs of the serving distribution through continuous batching, each bit-identical to the same job run
+    alone through the single-instance path (seeded alike, one filled-advance launch per step)."""
+    jobs = serving.poisson_jobs(24, rate=3000.0, seed=77)
+    for job in jobs:  # keep the test short: at most 12 steps per job
+        job.steps = 1 + job.steps % 12
+    served = serving.Server(cuda, numerics=numerics, keep_results=True, tick_points=3_000_000)
+    served.run(jobs)
+    assert served.stats["graph_replays"] > 0
+    stream = cuda.cuda.Stream()
+    for job in jobs:
+        grid, bufs = serving._device_job(cuda, job, stream)
+        serving._plain_steps(grid, bufs, job, serving.NUMERICS[numerics], stream.cuda_stream)
+        stream.synchronize()
+        alone = [t.cpu().numpy() for t in bufs[job.steps % 2]]
+        assert _same(job.result, alone), job.ident
