@@ -108,7 +108,15 @@ class ClockSampler:
         self.file.flush()
         return False
 
+    summary_cache = None
+
     def summary(self):
+        if self.summary_cache is not None:
+            return self.summary_cache
+        self.summary_cache = self._summary()
+        return self.summary_cache
+
+    def _summary(self):
         try:
             text = Path(self.file.name).read_text()
             os.unlink(self.file.name)
@@ -414,6 +422,9 @@ def run_gb300(args):
                 traffic = float(line.split("=")[1])
     fp64_peak = max(fp64_add, fp64_fma)
 
+    clock_mhz = sampler.summary().get("sm_mhz") or 2070.0
+    nominal_fp64 = 2.0 * torch.cuda.get_device_properties(local).multi_processor_count * clock_mhz * 1e6
+
     def fp64_roofline(name, ms):
         ops = fp64_ops_per_point(NSCALAR, name)
         rate = ops * points / (ms * 1e-3)
@@ -434,7 +445,10 @@ def run_gb300(args):
                      "frac": achieved / peak, "traffic": traffic, "peak_source": f"{peak_kind} hbm_gbs",
                      "algorithmic_bytes_per_launch": alg, "kernel": kernel_names[primary]},
         "fp64_roofline": {**fp64_roofline(primary, ms_per_step), "peak_add_rn": fp64_add, "peak_fma_rn": fp64_fma,
-                          "peak_source": "measured live", "kernel": kernel_names[primary]},
+                          "peak_source": "measured live", "kernel": kernel_names[primary],
+                          # the instruction rate ncu states for the FP64 pipe: 2 lanes per clock per SM
+                          "nominal_ops_per_s": nominal_fp64,
+                          "frac_of_nominal": fp64_roofline(primary, ms_per_step)["achieved_ops_per_s"] / nominal_fp64},
         secondary if secondary == "strict" else "fast_fp": {
             "value": whole_job_value(points, world, 1, other_ms), "ms_per_step": other_ms, "steps": other_steps,
             "kernel": kernel_names[secondary], "fp64_roofline": fp64_roofline(secondary, other_ms)},
