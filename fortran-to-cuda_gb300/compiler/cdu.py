@@ -1,6 +1,6 @@
 """The cdu benchmark driver, run as the resident build runs it.
 
-``python -m compiler.cdu [--nx 64 --ny 64 --nz 64 --iterations 100 --warmup 5 --seed 20261123]``
+``python -m compiler.cdu [--nx 64 --ny 64 --nz 64 --iterations 100 --warmup 5 --seed 20261123] [--fast-fp]``
 
 Restates ``benchmarks/cdu/src/main.f90`` (allocation :47-51, dx = 1/N :54-56,
 warm-up and timed loop :67-79, report :86-92) with the residency directives
@@ -14,7 +14,9 @@ interior of U2 in array-element order, as ``sum(real(U2(2:NX+1, ...), 8))``.
 
 The fields are uniform [0, 1) from numpy's generator (gfortran's
 ``random_number`` cannot be reproduced here), one ghost layer, every value
-drawn as ``random_number`` fills whole arrays.
+drawn as ``random_number`` fills whole arrays. ``--fast-fp`` runs the driver
+as a resident build prepared with the reference's ``--fast-fp`` runs it: the
+domain's context under the fast-fp numerical contract.
 """
 
 from __future__ import annotations
@@ -37,14 +39,14 @@ def sequential_sum(values: np.ndarray) -> float:
     return float(np.cumsum(flat)[-1]) if flat.size else 0.0
 
 
-def run(nx: int, ny: int, nz: int, iterations: int, warmup: int, seed: int) -> dict:
+def run(nx: int, ny: int, nz: int, iterations: int, warmup: int, seed: int, fast_fp: bool = False) -> dict:
     fields = wl.reference_driver_fields(nx, ny, nz, seed)
     geo = fields.geometry
     u, v, w = fields.U, fields.V, fields.W
     u2 = np.zeros_like(u)
     lib = native.runtime()
     entries = emission.bind(lib)
-    dom = ResidentDomain(lib)
+    dom = ResidentDomain(lib, fast_fp=fast_fp)
     reals, ints = [geo.dx, geo.dy, geo.dz], [nx, ny, nz]
 
     def cdu(handles):
@@ -95,8 +97,9 @@ def main(argv=None) -> int:
     parser.add_argument("--iterations", type=int, default=100)
     parser.add_argument("--warmup", type=int, default=5)
     parser.add_argument("--seed", type=int, default=20261123)
+    parser.add_argument("--fast-fp", action="store_true", help="the fast-fp numerical contract (FMA contraction)")
     args = parser.parse_args(argv)
-    print(report(run(args.nx, args.ny, args.nz, args.iterations, args.warmup, args.seed)))
+    print(report(run(args.nx, args.ny, args.nz, args.iterations, args.warmup, args.seed, args.fast_fp)))
     return 0
 
 

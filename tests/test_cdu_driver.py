@@ -40,3 +40,17 @@ def test_driver_checksum_equals_the_oracle(cuda):
     interior = (slice(1, nz + 1), slice(1, ny + 1), slice(1, nx + 1))
     assert np.array_equal(r["u2"][interior].view(np.int64), ref[interior].view(np.int64))
     assert r["checksum"] == cdu.sequential_sum(ref[interior])
+
+
+@pytest.mark.gpu
+def test_driver_fast_fp_is_within_the_tolerance(cuda):
+    from oracle import api
+    from tolerance import check
+
+    nx, ny, nz = 40, 24, 16
+    r = cdu.run(nx, ny, nz, iterations=2, warmup=1, seed=7, fast_fp=True)
+    f = wl.reference_driver_fields(nx, ny, nz, 7)
+    ref = api.momentum("cdu", np.zeros_like(f.U), f.U, f.V, f.W, f.geometry.dx, f.geometry.dy, f.geometry.dz, 1)
+    interior = (slice(1, nz + 1), slice(1, ny + 1), slice(1, nx + 1))
+    check(r["u2"][interior], ref[interior], "U2")
+    assert not np.array_equal(r["u2"][interior].view(np.int64), ref[interior].view(np.int64))  # the fast kernel ran
