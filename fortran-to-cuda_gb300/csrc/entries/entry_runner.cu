@@ -196,7 +196,11 @@ int slab_planes(long long nx, long long ny) {
 // uploads run, and its drain, when only publications run); at most 62 slabs.
 std::vector<int> slab_bounds(int nz, int planes) {
     planes = std::max(planes, (nz + 59) / 60);
-    const int edge = std::max(1, planes / 2);
+    static const int fixed_edge = [] {
+        const char *v = std::getenv("F2C_SLAB_EDGE");  // levels of the first and last slab (read once per process)
+        return v ? std::atoi(v) : 0;
+    }();
+    const int edge = fixed_edge > 0 ? std::min(fixed_edge, planes) : std::max(1, planes / 2);
     std::vector<int> b{0};
     if (nz < 2 * edge + planes) {
         const int count = std::max(1, nz / std::max(1, planes));
