@@ -199,3 +199,14 @@ def test_strict_step_refuses_short_and_tall_tiles(cuda):
         batch.step()
     with pytest.raises(native.NativeError, match="tile rows"):
         native.Batch([x[4] for x in inst], [x[5] for x in inst], tile_rows=12).prepare(ws.data_ptr(), ws.numel())
+
+
+def test_batch_rejects_an_instance_too_wide_for_the_tile_queue(cuda):
+    """Item tile indices are 16-bit: an instance wider than 32767 tiles is refused before any device work (the
+    field pointers below are never dereferenced)."""
+    wide = native.make_grid(32767 * 32 + 1, 8, 4, 2, 1.0, 1.0, 1.0)
+    fake = 256
+    fields = native.make_fields(fake, fake, fake, fake, fake, fake)
+    batch = native.Batch([wide], [fields])
+    with pytest.raises(native.NativeError, match="too wide"):
+        batch.prepare(fake, 1 << 30)
