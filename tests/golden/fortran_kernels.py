@@ -3,11 +3,15 @@
 No Fortran compiler exists on the machines this project runs on, so the golden
 vectors of the advection procedures are produced by executing the reference's
 own source text with this interpreter of the free-form Fortran subset those
-kernels are written in: modules and subroutines, type declarations with
-intent, parameter and explicit or assumed lower bounds, DO loops, CALL, scalar
-and array-element assignment, and expressions of numeric literals (kind
-suffixes and d exponents), names, array elements, unary and binary + - * /
-and parentheses. OpenMP directives are comments.
+kernels and their test programs are written in: modules, programs, subroutines
+and functions, type declarations with intent, parameter, allocatable and
+explicit or assumed lower bounds, ALLOCATE and DEALLOCATE, DO loops, CALL,
+scalar, element, section and whole-array assignment, WRITE of values (kept, not
+formatted), the intrinsics sin, cos, exp, log, sqrt, abs, real, dble, min and
+max, and expressions of numeric literals (kind suffixes and d exponents),
+names, array elements, unary and binary + - * / ** and parentheses. The C
+preprocessor's #define, #ifdef, #ifndef, #else and #endif are applied first,
+with the caller's definitions. OpenMP directives are comments.
 
 Arithmetic is IEEE binary64 with round-to-nearest, evaluated in the order the
 Fortran expression tree gives (left to right within one precedence level,
@@ -25,6 +29,7 @@ Arrays are numpy arrays in C order with the Fortran index order reversed
 
 from __future__ import annotations
 
+import math
 import re
 from dataclasses import dataclass, field
 
@@ -33,7 +38,8 @@ import numpy as np
 # ---- lexing -----------------------------------------------------------------------------------------
 
 _TOKEN = re.compile(r"""
-    (?P<num>(\d+\.\d*|\.\d+|\d+)([ed][+-]?\d+)?(_[a-z_]\w*)?)
+    (?P<str>'[^']*'|"[^"]*")
+  | (?P<num>(\d+\.\d*|\.\d+|\d+)([ed][+-]?\d+)?(_[a-z_]\w*)?)
   | (?P<name>[a-z_]\w*)
   | (?P<op>\*\*|::|[-+*/(),=:%])
   | (?P<space>\s+)
@@ -47,16 +53,60 @@ def _tokens(text: str) -> list[str]:
         if not m:
             raise SyntaxError(f"cannot read Fortran text at: {text[pos:pos + 30]!r}")
         pos = m.end()
-        if m.lastgroup != "space":
+        if m.lastgroup == "str":
+            out.append(m.group(0))
+        elif m.lastgroup != "space":
             out.append(m.group(0).lower())
     return out
+
+
+def _preprocess(source: str, defines: dict) -> str:
+    """#define / #ifdef / #ifndef / #else / #endif, then the macros substituted as whole words."""
+    macros = {k.lower(): str(v) for k, v in defines.items()}
+    out, active = [], [True]
+    for raw in source.splitlines():
+        text = raw.strip()
+        if text.startswith("#"):
+            words = text[1:].split()
+            if not words:
+                continue
+            word = words[0]
+            if word in ("ifdef", "ifndef"):
+                present = words[1].lower() in macros
+                active.append(active[-1] and (present if word == "ifdef" else not present))
+            elif word == "else":
+                active[-1] = active[-2] and not active[-1]
+            elif word == "endif":
+                active.pop()
+            elif word == "define" and active[-1]:
+                macros[words[1].lower()] = " ".join(words[2:])
+            continue
+        if not active[-1]:
+            continue
+        for name, value in macros.items():
+            raw = re.sub(rf"\b{re.escape(name)}\b", value, raw, flags=re.I)
+        out.append(raw)
+    return "\n".join(out)
+
+
+def _strip_comment(line: str) -> str:
+    quote = None
+    for n, ch in enumerate(line):
+        if quote:
+            if ch == quote:
+                quote = None
+        elif ch in "'\"":
+            quote = ch
+        elif ch == "!":
+            return line[:n]
+    return line
 
 
 def _statements(source: str) -> list[str]:
     """Free-form lines joined across '&' continuations, comments (and OpenMP sentinels) removed."""
     lines, pending = [], ""
     for raw in source.splitlines():
-        line = raw.split("!", 1)[0].rstrip()
+        line = _strip_comment(raw).rstrip()
         if not line.strip() or line.lstrip().startswith("#"):  # blank, comment or preprocessor line
             continue
         text = line.strip()
@@ -125,6 +175,16 @@ class Do:
 class Call:
     name: str
     args: list
+
+
+@dataclass
+class Allocate:
+    items: list  # (name, [subscripts]) pairs
+
+
+@dataclass
+class Write:
+    values: list
 
 
 @dataclass
@@ -242,12 +302,15 @@ def _split_top(toks, sep=","):
 class Source:
     """The subroutines of one or more Fortran source files."""
 
-    def __init__(self, *texts: str):
+    def __init__(self, *texts: str, defines: dict | None = None):
         self.subroutines: dict[str, Subroutine] = {}
+        self.programs: dict[str, Subroutine] = {}
         self.parameters: dict[str, object] = {}
         self.globals: dict[str, object] = {}  # module variables (the caller sets them before a call)
+        self.output: list = []                # the values WRITE statements produced, in order
+        self.program_arrays: dict = {}        # the arrays of the last program run (DEALLOCATE keeps them here)
         for text in texts:
-            self._read(_statements(text))
+            self._read(_statements(_preprocess(text, defines or {})))
 
     def _read(self, lines):
         stack: list[list] = []
@@ -267,9 +330,30 @@ class Source:
                 if what in ("subroutine", "function"):
                     self.subroutines[current.name] = current
                     current = None
+                elif what == "program":
+                    self.programs[current.name] = current
+                    current = None
                 continue
             if head == "enddo":
                 stack.pop()
+                continue
+            if head == "program":
+                current = Subroutine(toks[1], [])
+                stack = [current.body]
+                continue
+            if head == "allocate":
+                items = []
+                for item in _split_top(toks[2:-1]):
+                    ref = _parse_expr(item)
+                    items.append((ref.name, ref.args))
+                stack[-1].append(Allocate(items))
+                continue
+            if head == "deallocate":
+                continue
+            if head == "write":
+                close = next(n for n in range(1, len(toks)) if toks[n] == ")" and
+                             toks[:n + 1].count("(") == toks[:n + 1].count(")"))
+                stack[-1].append(Write([_parse_expr(a) for a in _split_top(toks[close + 1:]) if a]))
                 continue
             if head == "subroutine":
                 name = toks[1]
@@ -315,9 +399,11 @@ class Source:
                 decl.intent = a[2]
             if a and a[0] == "parameter":
                 decl.parameter = True
+            if a and a[0] == "allocatable":
+                decl.array = True
         for entity in _split_top(toks[cut + 1:]):
             name = entity[0]
-            d = Decl(decl.intent, False, (), None)
+            d = Decl(decl.intent, decl.array, (), None)
             if len(entity) > 1 and entity[1] == "(":
                 dims = _split_top(entity[2:entity.index(")") if ")" in entity else len(entity)])
                 d.array = True
@@ -345,6 +431,9 @@ class Source:
         if len(args) != len(sub.args):
             raise TypeError(f"{name} takes {len(sub.args)} arguments")
         env = {}
+        for name, d in sub.decls.items():  # the unit's own named constants
+            if d.parameter is not None and d.parameter is not True and name not in sub.args:
+                env[name] = self._eval(d.parameter, env)
         for formal, actual in zip(sub.args, args):
             d = sub.decls.get(formal, Decl())
             if d.array:
@@ -354,6 +443,18 @@ class Source:
                 env[formal] = actual
         self._run(sub.body, env)
         return env.get(sub.result) if sub.result else None
+
+    def run_program(self, name: str) -> list:
+        """Run a main program; returns (and keeps in ``output``) the values its WRITE statements produced."""
+        self.output = []
+        prog = self.programs[name.lower()]
+        env = {}
+        for nm, d in prog.decls.items():
+            if d.parameter is not None and d.parameter is not True:
+                env[nm] = self._eval(d.parameter, env)
+        self._run(prog.body, env)
+        self.program_arrays = {k: v[1] for k, v in env.items() if isinstance(v, tuple)}
+        return self.output
 
     def _run(self, body, env):
         for st in body:
@@ -365,6 +466,20 @@ class Source:
                     for v in range(lo, hi + 1):
                         env[st.var] = v
                         self._run(st.body, env)
+            elif isinstance(st, Allocate):
+                for name, dims in st.items:
+                    lows, extents = [], []
+                    for d in dims:
+                        if isinstance(d, Section):
+                            lo, hi = int(self._eval(d.lower, env)), int(self._eval(d.upper, env))
+                        else:
+                            lo, hi = 1, int(self._eval(d, env))
+                        lows.append(lo)
+                        extents.append(hi - lo + 1)
+                    env[name] = ("array", np.full(tuple(reversed(extents)), np.nan), tuple(lows))
+            elif isinstance(st, Write):
+                for v in st.values:
+                    self.output.append(float(self._eval(v, env)))
             elif isinstance(st, Call):
                 actual = []
                 for a in st.args:
@@ -387,7 +502,11 @@ class Source:
 
     def _assign(self, target, value, env):
         if isinstance(target, Name):
-            env[target.name] = value
+            entry = env.get(target.name)
+            if isinstance(entry, tuple):  # the whole array
+                entry[1][...] = value
+            else:
+                env[target.name] = value
             return
         kind, arr, lows = env[target.name]
         arr[self._index(target.args, lows, env)] = value
@@ -409,6 +528,8 @@ class Source:
                 actual = [env[a.name][1] if isinstance(a, Name) and isinstance(env.get(a.name), tuple)
                           else self._eval(a, env) for a in node.args]
                 return self.call(node.name, *actual)
+            if not isinstance(entry, tuple) and node.name in _INTRINSICS:
+                return _INTRINSICS[node.name](self, node.args, env)
             if not isinstance(entry, tuple):
                 raise NameError(f"{node.name} is not an array here")
             _, arr, lows = entry
@@ -502,3 +623,41 @@ def _real(v):
     if isinstance(v, np.ndarray) and v.dtype.kind in "iu":
         return v.astype(np.float64)
     return v
+
+
+def _elementwise(fn):
+    """A libm function applied value by value (the C library's results, as a compiled Fortran program gets)."""
+    def apply(v):
+        if isinstance(v, np.ndarray):
+            return np.vectorize(fn, otypes=[np.float64])(v.astype(np.float64))
+        return fn(float(v))
+    return apply
+
+
+def _intrinsic(fn):
+    return lambda src, args, env: fn(src._eval(args[0], env))
+
+
+def _real_intrinsic(src, args, env):  # real(x [, kind]) / dble(x): the kind is double precision here
+    v = src._eval(args[0], env)
+    return v.astype(np.float64) if isinstance(v, np.ndarray) else float(v)
+
+
+def _fold(op):
+    def apply(src, args, env):
+        vals = [src._eval(a, env) for a in args]
+        out = vals[0]
+        for v in vals[1:]:
+            out = op(out, v)
+        return out
+    return apply
+
+
+_INTRINSICS = {
+    "sin": _intrinsic(_elementwise(math.sin)), "cos": _intrinsic(_elementwise(math.cos)),
+    "exp": _intrinsic(_elementwise(math.exp)), "log": _intrinsic(_elementwise(math.log)),
+    "sqrt": _intrinsic(_elementwise(math.sqrt)), "abs": _intrinsic(np.abs),
+    "real": _real_intrinsic, "dble": _real_intrinsic,
+    "max": _fold(np.maximum), "min": _fold(np.minimum),
+    "kind": lambda src, args, env: 8,  # kinds only name the precision; every real here is binary64
+}

@@ -13,7 +13,13 @@ generated from) by the Fortran-subset interpreter ``fortran_kernels.py``
 * ``compiler/tests/apps/box/stepper.f90`` ``diffuse`` with its ``params``
   module (two ghost layers, lower bound -1 as declared there);
 * the Jacobi sweep of ``compiler/tests/apps/relax/relax.f90`` (its DO nest,
-  taken verbatim from the program and run on arrays of lower bound 0).
+  taken verbatim from the program and run on arrays of lower bound 0);
+* the reference's own correctness-test programs for the three procedures,
+  ``compiler/tests/fixtures/stencils/{cdu,cvd,cdw}_main.f90`` (deterministic
+  sin/cos inputs, one call, the interior of the result written one value per
+  line), at their default 16 x 16 x 16 and at 12 x 10 x 8 through their
+  VAR_NX/VAR_NY/VAR_NZ macros: the written values and the inputs the programs
+  built (sin and cos from this machine's C library) are stored.
 
 Inputs are uniform in [0, 1) (velocities shifted to [-1, 1)), stored with the
 outputs, so nothing of the platform's libm enters the check. Run from the
@@ -77,6 +83,30 @@ def jacobi_source() -> Source:
                   f"{nest}\nend subroutine sweep\nend module relax_nest\n")
 
 
+MAIN_PROGRAMS = (("cdu", "cdu.f90", "cdu_main.f90", "cdu_test"), ("cdv", "cvd.f90", "cvd_main.f90", "cdv_test"),
+                 ("cdw", "cdw.f90", "cdw_main.f90", "cdw_test"))
+MAIN_SIZES = ((16, 16, 16), (12, 10, 8))
+
+
+def main_program_cases() -> dict:
+    """Each test program run as written; the inputs it built and the values it wrote."""
+    stencils = REFERENCE / "compiler/tests/fixtures/stencils"
+    out = {}
+    for n, (nx, ny, nz) in enumerate(MAIN_SIZES):
+        defines = {} if (nx, ny, nz) == (16, 16, 16) else {"VAR_NX": nx, "VAR_NY": ny, "VAR_NZ": nz}
+        out[f"main{n}_size"] = np.array([nx, ny, nz], dtype=np.float64)
+        for which, module, program, unit in MAIN_PROGRAMS:
+            src = Source((stencils / module).read_text(), (stencils / program).read_text(), defines=defines)
+            out[f"main{n}_{which}"] = np.array(src.run_program(unit))
+            arrays = src.program_arrays
+            for k in "uvw":
+                key = f"main{n}_{k.upper()}"
+                if key in out:
+                    assert np.array_equal(out[key], arrays[k])  # the three programs build the same inputs
+                out[key] = arrays[k]
+    return out
+
+
 def advection_case(src: Source, nx, ny, nz, ghosts, dx, dy, dz, seed) -> dict:
     rng = np.random.default_rng(seed)
     shape = (nz + 2 * ghosts, ny + 2 * ghosts, nx + 2 * ghosts)
@@ -135,6 +165,7 @@ def generate() -> dict:
     jacobi_source().call("sweep", u, v, n)
     out["jac_case"] = np.array(JACOBI_CASE, dtype=np.float64)
     out["jac_u"], out["jac_v"] = u, v[1:-1, 1:-1].copy()
+    out.update(main_program_cases())
     return out
 
 

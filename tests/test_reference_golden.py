@@ -1,7 +1,8 @@
 """The oracle pinned to the reference's own source: golden vectors computed by executing the reference's Fortran.
 
 ``tests/golden/reference_kernels.npz`` holds outputs of the reference procedures (cdu.f90, cvd.f90, cdw.f90, the
-box app's stepper.f90 diffuse, relax.f90's Jacobi sweep) run from their source text by the Fortran-subset
+box app's stepper.f90 diffuse, relax.f90's Jacobi sweep) and of the reference's correctness-test programs of the
+three procedures (cdu_main.f90, cvd_main.f90, cdw_main.f90) run from their source text by the Fortran-subset
 interpreter ``tests/golden/fortran_kernels.py`` (``tests/golden/make_reference_golden.py`` made them). The C oracle
 must reproduce them bit for bit; where the reference checkout is present, the fixtures are regenerated from it
 and must not have changed.
@@ -42,6 +43,20 @@ def test_oracle_equals_the_reference_procedures(n):
     tend = api.advection_step(fields, dx, dy, dz, g)
     for c, k in zip("uvw", "UVW"):
         assert np.array_equal(_bits(tend[k][inner]), _bits(FIXTURE[f"adv{n}_cd{c}"])), (n, k)
+
+
+@pytest.mark.parametrize("n", [0, 1])
+def test_oracle_reproduces_the_reference_test_programs(n):
+    """cdu_main.f90, cvd_main.f90 and cdw_main.f90 (the reference's correctness tests of the three procedures)
+    wrote these values; the oracle computes them from the same inputs, bit for bit, in the programs' order."""
+    nx, ny, nz = (int(v) for v in FIXTURE[f"main{n}_size"])
+    fields = {k: FIXTURE[f"main{n}_{k}"].copy() for k in "UVW"}
+    tend = api.advection_step(fields, 1.0 / nx, 1.0 / ny, 1.0 / nz, 1)
+    inner = (slice(1, nz + 1), slice(1, ny + 1), slice(1, nx + 1))
+    for which, key in (("cdu", "U"), ("cdv", "V"), ("cdw", "W")):
+        written = FIXTURE[f"main{n}_{which}"]
+        assert written.size == nx * ny * nz
+        assert np.array_equal(_bits(tend[key][inner].ravel()), _bits(written)), which
 
 
 def test_oracle_stencils_equal_the_reference():
@@ -131,3 +146,34 @@ def test_fixtures_regenerate_from_the_reference_source():
     for key, value in fresh.items():
         assert np.array_equal(_bits(value), _bits(FIXTURE[key]), equal_nan=False) if value.dtype == np.float64 \
             else np.array_equal(value, FIXTURE[key]), key
+
+
+def test_interpreter_runs_programs_with_the_preprocessor():
+    src = fk.Source("""
+! a program in the shape of the reference's test drivers
+#ifndef NSIZE
+#  define NSIZE 3
+#endif
+program probe
+    implicit none
+    integer, parameter :: rp = kind(1.0d0)
+    integer, parameter :: N = NSIZE
+    real(rp), allocatable :: a(:), b(:)
+    integer :: i
+    allocate(a(N), b(0:N))
+    b = 0.5_rp
+    do i = 1, N
+        a(i) = sin(real(i, rp) * 0.3_rp) + max(b(i), 0.25_rp)
+    end do
+    do i = 1, N
+        write(*, '(g0.17)') a(i)
+    end do
+    deallocate(a, b)
+end program probe
+""", defines={"NSIZE": 4})
+    out = src.run_program("probe")
+    import math
+
+    assert out == [math.sin(float(i) * 0.3) + 0.5 for i in range(1, 5)]
+    assert src.program_arrays["b"].shape == (5,)
+    assert fk.Source("#ifdef X\\nmodule bad\\n#else\\nmodule good\\n#endif\\nend module\\n").subroutines == {}

@@ -43,6 +43,27 @@ def test_fused_step_equals_the_reference(cuda, n, variant):
             assert np.array_equal(_bits(got), _bits(want)), c_
 
 
+@pytest.mark.parametrize("n", [0, 1])
+@pytest.mark.parametrize("variant", [native.FACES, native.FAST])
+def test_kernels_reproduce_the_reference_test_programs(cuda, n, variant):
+    """The values the reference's cdu_main.f90, cvd_main.f90 and cdw_main.f90 write, from the fused launch."""
+    from tolerance import check
+
+    nx, ny, nz = (int(v) for v in FIXTURE[f"main{n}_size"])
+    grid = native.make_grid(nx, ny, nz, 1, 1.0 / nx, 1.0 / ny, 1.0 / nz)
+    dev = [cuda.from_numpy(FIXTURE[f"main{n}_{k}"].copy()).cuda() for k in "UVW"]
+    out = [cuda.full_like(t, float("nan")) for t in dev]
+    native.advection(grid, *[t.data_ptr() for t in dev], *[t.data_ptr() for t in out], variant=variant)
+    cuda.cuda.synchronize()
+    inner = (slice(1, nz + 1), slice(1, ny + 1), slice(1, nx + 1))
+    for t, which in zip(out, ("cdu", "cdv", "cdw")):
+        got, written = t.cpu().numpy()[inner].ravel(), FIXTURE[f"main{n}_{which}"]
+        if variant == native.FAST:
+            check(got, written, which)
+        else:
+            assert np.array_equal(_bits(got), _bits(written)), which
+
+
 def test_procedure_launches_equal_the_reference(cuda):
     """Each procedure as one launch (the reference's structure) on case 0's inputs, bit for bit."""
     grid, d, inner = _case(0, cuda)
