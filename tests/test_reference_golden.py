@@ -8,7 +8,6 @@ must reproduce them bit for bit; where the reference checkout is present, the fi
 and must not have changed.
 """
 
-import os
 import sys
 from pathlib import Path
 
@@ -134,13 +133,11 @@ end module probe
     assert list(a) == list(np.cumsum(np.arange(1.0, 7.0)))
 
 
-REFERENCE = Path(os.environ.get("F2C_REFERENCE_ROOT", "/root/reference"))
+import make_reference_golden as mk  # noqa: E402  (the generator names where the reference checkout lies)
 
 
-@pytest.mark.skipif(not (REFERENCE / "benchmarks/cdu/src/cdu.f90").exists(), reason="reference checkout absent")
+@pytest.mark.skipif(not (mk.REFERENCE / "benchmarks/cdu/src/cdu.f90").exists(), reason="reference checkout absent")
 def test_fixtures_regenerate_from_the_reference_source():
-    import make_reference_golden as mk
-
     fresh = mk.generate()
     assert sorted(fresh) == sorted(FIXTURE.files)
     for key, value in fresh.items():
