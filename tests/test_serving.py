@@ -194,3 +194,18 @@ def test_a_poisson_mix_equals_one_job_at_a_time(cuda, numerics):
         stream.synchronize()
         alone = [t.cpu().numpy() for t in bufs[job.steps % 2]]
         assert _same(job.result, alone), job.ident
+
+
+@pytest.mark.gpu
+def test_edge_sized_jobs_and_four_scalars(cuda):
+    """Jobs at the smallest grids the boundary rule allows (nx = ny = halo, nz = halo + 1), with four scalars,
+    mixed with ordinary ones: each equals the same job alone."""
+    shapes = [(2, 2, 3, 4, 3), (2, 5, 3, 0, 2), (33, 2, 4, 4, 5), (70, 41, 29, 4, 4), (64, 64, 24, 1, 6)]
+    jobs = [serving.Job(n, 0.001 * n, a, b, c, s, t, seed=900 + n) for n, (a, b, c, s, t) in enumerate(shapes)]
+    serving.Server(cuda, keep_results=True).run(jobs)
+    stream = cuda.cuda.Stream()
+    for job in jobs:
+        grid, bufs = serving._device_job(cuda, job, stream)
+        serving._plain_steps(grid, bufs, job, serving.NUMERICS["fast"], stream.cuda_stream)
+        stream.synchronize()
+        assert _same(job.result, [t.cpu().numpy() for t in bufs[job.steps % 2]]), job.ident
