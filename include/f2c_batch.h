@@ -113,9 +113,8 @@ int f2c_batch_halo_v1(const f2c_batch_plan_v1 *plan, void *stream);
  * Limits: at most F2C_BATCH_NO_ALLOC_MAX_INSTANCES instances and
  * F2C_BATCH_NO_ALLOC_MAX_ITEMS work items (32 x 8 column tiles times z-chunks);
  * larger batches are rejected with FORT_SCOPE_ARGUMENT and a message naming the
- * limit. The first call on a device looks up the array's device address (with
- * that device current), so that first call must come before any stream capture
- * on that device. Each call copies its descriptors and tile queue into the
+ * limit. The first call on a device looks up the array's device address with
+ * that device current. Each call copies its descriptors and tile queue into the
  * array from host arrays that the library rewrites on the next call, and
  * clears the counter. Every call shares and overwrites the array, so calls that
  * overlap on the GPU, or that come from several host threads at once, race.
