@@ -609,6 +609,42 @@ def ensemble_measure(torch, count, steps, warmup, tune=False, numerics=("fast", 
         batch.set_fast_fp(fast)
         return _stream_time(torch, stream, lambda s: batch.graph_step(s), n_steps, n_warmup) * 1e-3
 
+    def resident_entries_time(fast, n_steps, n_warmup):
+        # each instance alone, one after another, through the residency runtime: its steps are calls of the
+        # generated entry advection::step<N> inside one epoch, with its fields already resident on the device
+        from compiler import emission
+        from compiler.resident.domain import ResidentDomain
+        from compiler.runtime import abi
+
+        lib = native.runtime()
+        functions = emission.bind(lib)
+        dom = ResidentDomain(lib, fast_fp=fast)
+        dom.begin_epoch()
+        calls = []
+        try:
+            for geo, ins, outs, grid, fields in inst:
+                h_in = [dom.bind_real64(t.cpu().numpy()) for t in ins]
+                h_out = [dom.bind_real64(np.zeros(tuple(t.shape))) for t in outs]
+                calls.append((f"advection::step{len(ins) - 3}", [*h_out[:3], *h_in[:3], *h_in[3:], *h_out[3:]],
+                              [geo.dx, geo.dy, geo.dz], [geo.nx, geo.ny, geo.nz, geo.halo]))
+
+            def run(count):
+                for entry, arrays, reals, ints in calls:
+                    for _ in range(count):
+                        status = emission.call(functions, entry, dom.context, abi.GPU, arrays, reals, ints)
+                        if status != abi.OK:
+                            raise RuntimeError(f"{entry} returned {status}: {lib.fort_scope_error().decode()}")
+
+            run(max(1, n_warmup))
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            run(n_steps)
+            torch.cuda.synchronize()
+            return (time.perf_counter() - t0) / n_steps
+        finally:
+            dom.end_epoch()
+            dom.close()
+
     tuned = {}
     if tune:
         for name in numerics:
@@ -630,13 +666,20 @@ def ensemble_measure(torch, count, steps, warmup, tune=False, numerics=("fast", 
                                      variant=variant)
 
             plain_ms = _graph_time(torch, stream, one_at_a_time, steps, warmup)
+            entries_s = resident_entries_time(fast, steps, warmup)
             value, plain = points / batched_s / 1e9, points / (plain_ms * 1e-3) / 1e9
+            entries = points / entries_s / 1e9
             out[name] = {"value": value, "ms_per_step": batched_s * 1e3,
                          "shapes": {"tile": f"32x{rows}",
                                     "kz": {scheduling.bucket(nz): k for (_, _, nz), k in zip(shapes, kz)}},
                          "plain_resident": {"value": plain, "ms_per_step": plain_ms,
                                             "how": f"{len(shapes)} single-instance launches per step, one graph"},
-                         "batched_over_plain": value / plain}
+                         "batched_over_plain": value / plain,
+                         "resident_entries": {"value": entries, "ms_per_step": entries_s * 1e3,
+                                              "how": "each instance alone, one after another, its steps through the "
+                                                     "generated entry advection::step1 in a residency epoch, fields "
+                                                     "resident; wall clock with a device synchronisation either side"},
+                         "batched_over_resident_entries": value / entries}
     out["clocks"] = sampler.summary()
     return out, inst, stream
 
@@ -712,6 +755,8 @@ def run_batched(args):
         "config": {"workload": f"{out['instances']} instances, nx,ny in {{64..256}}, nz in {{32,64,96}}, seed 1",
                    "points": points, "shapes": head["shapes"]},
         "plain_resident": head["plain_resident"], "batched_over_plain": head["batched_over_plain"],
+        "resident_entries": head["resident_entries"],
+        "batched_over_resident_entries": head["batched_over_resident_entries"],
         "per_numerics": {k: out[k] for k in ("fast", "strict")},
         "reference_style_resident": {"value": procedure_rate, "ms_per_step": procedure_ms,
                                      "how": "per instance: set, div, adv, multiply for U, V, W + 1 scalar launch "
