@@ -20,7 +20,8 @@
 //    rounded subnormal case handled in integer arithmetic as well).
 //
 // Every other operation follows the reference grouping (advection_point.cuh),
-// so results are bit-identical to the oracle. Operation count per point:
+// so results are bit-identical to the oracle. The products are computed on the
+// integer pipes (pmul below), which round exactly as DMUL does. Operation count per point:
 // U, V, W: 9 face sums + 18 flux products + 15 flux differences + 48
 // advective-form operations = 90; scalars: 3 shared coefficient products +
 // 11 per scalar.
@@ -31,8 +32,17 @@
 
 #include "advection_kernels.cuh"
 #include "device.cuh"
+#include "soft_fp64.cuh"
 
 namespace f2c {
+
+// Products on the integer pipes (soft_fp64.cuh): bit-identical to DMUL, they
+// take the multiplications off the FP64 pipe that bounds these kernels
+// (measured at 512 x 512 x 128 with three scalars: this strict kernel 8.74 ->
+// 8.15 ms, the fast-fp one 4.98 -> 4.28 ms, outputs unchanged bit for bit).
+// Additions stay on the FP64 pipe: the integer addition needs about as many
+// issue slots of the ALU pipe as it saves on the FP64 one (measured slower).
+__device__ __forceinline__ double pmul(double a, double b) { return mul_rn_int(a, b); }
 
 constexpr int kFaceTX = 32;       // points per tile along x (one warp)
 constexpr int kFaceTY = 8;        // compute warps per tile (points along y)
@@ -163,29 +173,29 @@ __device__ __forceinline__ void faces_tile(const AdvArgs &a, int tile_x, int til
             if (DO_V || DO_W) sVz = Vp + V0;
             if (DO_W) sWz = Wp + W0;
             if (DO_U) {
-                FUx = (c.Ax * sUx) * sUx;
-                FUy = (c.Ay * sUy) * sVx;
-                FUz = (c.Az * sUz) * sWx;
+                FUx = pmul(pmul(c.Ax, sUx), sUx);
+                FUy = pmul(pmul(c.Ay, sUy), sVx);
+                FUz = pmul(pmul(c.Az, sUz), sWx);
             }
             if (DO_V) {
-                FVx = (c.Ax * sVx) * sUy;
-                FVy = (c.Ay * sVy) * sVy;
-                FVz = (c.Az * sVz) * sWy;
+                FVx = pmul(pmul(c.Ax, sVx), sUy);
+                FVy = pmul(pmul(c.Ay, sVy), sVy);
+                FVz = pmul(pmul(c.Az, sVz), sWy);
             }
             if (DO_W) {
-                FWx = (c.Ax * sWx) * sUz;
-                FWy = (c.Ay * sWy) * sVz;
-                FWz = (c.Az * sWz) * sWz;
+                FWx = pmul(pmul(c.Ax, sWx), sUz);
+                FWy = pmul(pmul(c.Ay, sWy), sVz);
+                FWz = pmul(pmul(c.Az, sWz), sWz);
             }
             if (NS > 0) {
-                const double SxU = c.Sx * U0, SyV = c.Sy * V0, SzW = c.Sz * W0;
+                const double SxU = pmul(c.Sx, U0), SyV = pmul(c.Sy, V0), SzW = pmul(c.Sz, W0);
 #pragma unroll
                 for (int n = 0; n < NS; ++n) {
                     const double *__restrict__ S = a.s[n];
                     S0[n] = LD(S, p, 0, 0, 0);
-                    fe[n] = SxU * (LD(S, p, 1, 0, 0) + S0[n]);
-                    fn[n] = SyV * (LD(S, p, 0, 1, 0) + S0[n]);
-                    ft[n] = SzW * (LD(S, p, 0, 0, 1) + S0[n]);
+                    fe[n] = pmul(SxU, LD(S, p, 1, 0, 0) + S0[n]);
+                    fn[n] = pmul(SyV, LD(S, p, 0, 1, 0) + S0[n]);
+                    ft[n] = pmul(SzW, LD(S, p, 0, 0, 1) + S0[n]);
                 }
             }
             const int xo = warp * (kFaceTX + 1) + lane + 1;
@@ -268,7 +278,7 @@ __device__ __forceinline__ void faces_tile(const AdvArgs &a, int tile_x, int til
                 const double r = opaque_negate(((FUx - xf[0 * Smem::XF + xw]) + (FUy - yf[0 * Smem::YF + ys])) + (FUz - FUzb));
                 const double Vadv = (sVx + Vs) + LD(V, p, 1, -1, 0);
                 const double Wadv = (sWx + Wm) + LD(W, p, 1, 0, -1);
-                const double adv = ((c.Bux * (Ue - Uw)) * U0 + (c.Buy * (Un - Us)) * Vadv) + (c.Buz * (Up - Um)) * Wadv;
+                const double adv = (pmul(pmul(c.Bux, Ue - Uw), U0) + pmul(pmul(c.Buy, Un - Us), Vadv)) + pmul(pmul(c.Buz, Up - Um), Wadv);
                 if (a.out[0]) store_point_t<FILL>(a.out[0], U, p, exact_half(r - adv), a, 0, i, j, k);
                 FUzb = FUz;
             }
@@ -276,7 +286,7 @@ __device__ __forceinline__ void faces_tile(const AdvArgs &a, int tile_x, int til
                 const double r = opaque_negate(((FVy - yf[1 * Smem::YF + ys]) + (FVx - xf[1 * Smem::XF + xw])) + (FVz - FVzb));
                 const double Uadv = (sUy + Uw) + LD(U, p, -1, 1, 0);
                 const double Wadv = (sWy + Wm) + LD(W, p, 0, 1, -1);
-                const double adv = ((c.Bvx * (Ve - Vw)) * Uadv + (c.Bvy * (Vn - Vs)) * V0) + (c.Bvz * (Vp - Vm)) * Wadv;
+                const double adv = (pmul(pmul(c.Bvx, Ve - Vw), Uadv) + pmul(pmul(c.Bvy, Vn - Vs), V0)) + pmul(pmul(c.Bvz, Vp - Vm), Wadv);
                 if (a.out[1]) store_point_t<FILL>(a.out[1], V, p, exact_half(r - adv), a, 0, i, j, k);
                 FVzb = FVz;
             }
@@ -284,7 +294,7 @@ __device__ __forceinline__ void faces_tile(const AdvArgs &a, int tile_x, int til
                 const double r = opaque_negate(((FWz - FWzb) + (FWy - yf[2 * Smem::YF + ys])) + (FWx - xf[2 * Smem::XF + xw]));
                 const double Uadv = (sUz + Uw) + LD(U, p, -1, 0, 1);
                 const double Vadv = (sVz + Vs) + LD(V, p, 0, -1, 1);
-                const double adv = ((c.Bwx * (We - Ww)) * Uadv + (c.Bwy * (Wn - Ws)) * Vadv) + (c.Bwz * (Wp - Wm)) * W0;
+                const double adv = (pmul(pmul(c.Bwx, We - Ww), Uadv) + pmul(pmul(c.Bwy, Wn - Ws), Vadv)) + pmul(pmul(c.Bwz, Wp - Wm), W0);
                 if (a.out[2]) store_point_t<FILL>(a.out[2], W, p, exact_half(r - adv), a, 1, i, j, k);
                 FWzb = FWz;
             }

@@ -4,11 +4,14 @@
 // the strict contract for FMA contraction. This kernel goes further in the same
 // direction: it evaluates the same tendencies as the strict face-sharing kernel
 // (advection_faces.cuh) through an algebraically regrouped form that spends
-// about 80 FP64 instructions per grid point (U, V, W and three scalars) where
-// the reference grouping needs 126. GB300 issues FP64 at about two lane
-// operations per clock per SM, so the instruction count is what bounds the
-// step; everything else here (loads, shuffles, shared memory, integer work)
-// runs on otherwise idle pipes.
+// about 80 floating-point operations per grid point (U, V, W and three
+// scalars) where the reference grouping needs 126. GB300 issues FP64 at about
+// two lane operations per clock per SM, so the FP64 instruction count is what
+// bounds the step; everything else here (loads, shuffles, shared memory,
+// integer work) runs on otherwise idle pipes. That includes the twelve plain
+// products, which are computed on the integer pipes (pmul, soft_fp64.cuh; the
+// same correctly rounded values), leaving 68 instructions per point on the
+// FP64 pipe.
 //
 // Regrouping (exact in real arithmetic; A = 0.25/d per direction). For the U
 // component of benchmarks/cdu/src/cdu.f90:66-71,96-101 with the final
@@ -71,13 +74,13 @@ constexpr int fast_threads() { return kFastTX * (TY + 1); }
 __device__ __forceinline__ double cross_term(double p, double pn, double q, double qn) {
     const double a = __fma_rn(3.0, q, qn);
     const double b = __fma_rn(3.0, qn, q);
-    return __fma_rn(p, a, -(pn * b));
+    return __fma_rn(p, a, -pmul(pn, b));
 }
 
 // (f1 - f0)(f1 + f0 + 4 c): the direction along a momentum component, from its
 // values one point either side (f1, f0) and at the point (c).
 __device__ __forceinline__ double along_term(double f1, double f0, double c) {
-    return (f1 - f0) * __fma_rn(4.0, c, f1 + f0);
+    return pmul(f1 - f0, __fma_rn(4.0, c, f1 + f0));
 }
 
 // One tile: columns [tile_x*32, +32) x [tile_y*TY, +TY) of the interior, levels
@@ -145,9 +148,9 @@ __device__ __forceinline__ void fast_tile(const AdvArgs &a, int tile_x, int tile
             if (F_VZ) sVz = Vp + V0;
             if (F_WY) sWy = LD(W, p, 0, 1, 0) + W0;
             if (DS) {
-                cU = c.sx * U0;
-                cV = c.sy * V0;
-                cW = c.sz * W0;
+                cU = pmul(c.sx, U0);
+                cV = pmul(c.sy, V0);
+                cW = pmul(c.sz, W0);
             }
             const int at = (warp + 1) * ROW + lane;
             if (DU) {
