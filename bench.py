@@ -52,18 +52,30 @@ def algorithmic_bytes_per_point(nscalar: int, mode: str = "tendency") -> int:
     return 2 * (24 + 8 * nscalar)
 
 
-def fp64_ops_per_point(nscalar: int, numerics: str = "strict") -> int:
-    """FP64 operations per point of each kernel's expression DAG (every face value computed once).
+def fp64_ops_per_point(nscalar: int, numerics: str = "strict", mode: str = "tendency") -> int:
+    """FP64-pipe instructions per point of each kernel's expression DAG (every face value computed once).
 
-    strict (the reference grouping): U, V, W: 9 face sums + 18 flux products + 15 flux differences + 51
-    advective-form operations (3 of them the exact halving, counted conservatively although it runs on the
-    integer pipe); scalars: 3 shared coefficient products + 11 per scalar.
-    fast (factored FMA form): U, V, W: 6 face sums + 15 per component (one product per direction, accumulated
-    by FMA); scalars: 3 scaled velocities + 5 for the shared divergence term + 7 per scalar.
+    The products that are not part of an FMA run on the integer pipes (``mul_rn_int``, rounded exactly as DMUL)
+    and the exact halving is an exponent decrement; neither is counted here (``int_pipe_ops_per_point``).
+    strict (the reference grouping): U, V, W: 9 face sums, 15 flux differences, 30 advective-form sums and
+    differences; scalars: 8 sums and differences each.
+    fast (factored FMA form): U, V, W: 6 face sums + 12 per component (3 for the direction along it, 3 for each
+    across, 3 to accumulate, of which a tendency's first is a plain product); scalars: 5 for the shared divergence
+    term + 7 FMAs per scalar (6 in a tendency).
     """
+    tendency = mode == "tendency"
     if numerics == "fast":
-        return 51 + (8 + 7 * nscalar if nscalar else 0)
-    return 93 + (3 + 11 * nscalar if nscalar else 0)
+        return 6 + 3 * (12 - tendency) + (5 + (7 - tendency) * nscalar if nscalar else 0)
+    return 54 + 8 * nscalar
+
+
+def int_pipe_ops_per_point(nscalar: int, numerics: str = "strict", mode: str = "tendency") -> int:
+    """Floating-point operations per point that run on the integer pipes: plain products, and the strict
+    kernel's exact halving of U, V, W."""
+    tendency = mode == "tendency"
+    if numerics == "fast":
+        return 9 + 3 * tendency + (3 + tendency * nscalar if nscalar else 0)
+    return 36 + 3 + (3 + 3 * nscalar if nscalar else 0)
 
 
 def hbm_peak():
@@ -429,7 +441,7 @@ def run_gb300(args):
         ops = fp64_ops_per_point(NSCALAR, name)
         rate = ops * points / (ms * 1e-3)
         return {"achieved_ops_per_s": rate, "peak_ops_per_s": fp64_peak, "frac": rate / fp64_peak,
-                "ops_per_point": ops}
+                "ops_per_point": ops, "int_pipe_ops_per_point": int_pipe_ops_per_point(NSCALAR, name)}
 
     kernel_ms = {primary: ms_per_step, secondary: other_ms}
     kernel_names = {"fast": "advection_fast_kernel<3,7,8>", "strict": "advection_faces_kernel<3,7>"}

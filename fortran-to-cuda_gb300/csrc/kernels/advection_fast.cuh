@@ -84,10 +84,12 @@ __device__ __forceinline__ double along_term(double f1, double f0, double c) {
 }
 
 // One tile: columns [tile_x*32, +32) x [tile_y*TY, +TY) of the interior, levels
-// [k0, k1). Called by every thread of a (32, TY+1) block; `smem` holds
+// [k0, k1), for one output mode (ADVANCE: forward Euler, else the tendency).
+// Called by every thread of a (32, TY+1) block; `smem` holds
 // FastSmem<TY>::doubles. Starts and ends with the exchange buffers free.
-template <int NS, int MASK, int TY>
-__device__ __forceinline__ void fast_tile(const AdvArgs &a, int tile_x, int tile_y, int k0, int k1, double *smem) {
+template <int NS, int MASK, int TY, bool ADVANCE>
+__device__ __forceinline__ void fast_tile_mode(const AdvArgs &a, int tile_x, int tile_y, int k0, int k1,
+                                               double *smem) {
     constexpr bool DU = MASK & 1, DV = (MASK >> 1) & 1, DW = (MASK >> 2) & 1, DS = NS > 0;
     constexpr bool filled = (MASK & kFillMask) != 0;  // F2C_ADVANCE_FILLED: outputs with their ghost images
     // face sums each point computes (at its north/east/top faces)
@@ -107,7 +109,6 @@ __device__ __forceinline__ void fast_tile(const AdvArgs &a, int tile_x, int tile
     const double *__restrict__ V = a.v;
     const double *__restrict__ W = a.w;
     const FastCoefficients c = a.f;
-    const bool advance = a.mode != 0;
     const int cj = edge ? j0 - 1 : j;
     long long p = (long long)(i + a.h) + sx * (long long)(cj + a.h) + plane * (long long)(k0 + a.h);
     long long pw = (long long)(i0 - 1 + a.h) + sx * (long long)(j0 + lane + a.h) + plane * (long long)(k0 + a.h);
@@ -230,7 +231,7 @@ __device__ __forceinline__ void fast_tile(const AdvArgs &a, int tile_x, int tile
                 const double X = along_term(LD(U, p, 1, 0, 0), LD(U, p, -1, 0, 0), U0);
                 const double Y = cross_term(sUy, south[0 * SLOT + at], sVx, south[1 * SLOT + at]);
                 const double Z = cross_term(sUz, bUz, sWx, bWx);
-                double t = __fma_rn(c.cz, Z, advance ? U0 : 0.0);
+                double t = ADVANCE ? __fma_rn(c.cz, Z, U0) : pmul(c.cz, Z);
                 t = __fma_rn(c.cy, Y, t);
                 t = __fma_rn(c.gx, X, t);
                 if (a.out[0]) { if (filled) store_filled(a.out[0], 0, a, i, j, k, t); else a.out[0][p] = t; }
@@ -239,7 +240,7 @@ __device__ __forceinline__ void fast_tile(const AdvArgs &a, int tile_x, int tile
                 const double X = cross_term(sVx, wVx, sUy, wUy);
                 const double Y = along_term(LD(V, p, 0, 1, 0), LD(V, p, 0, -1, 0), V0);
                 const double Z = cross_term(sVz, bVz, sWy, bWy);
-                double t = __fma_rn(c.cz, Z, advance ? V0 : 0.0);
+                double t = ADVANCE ? __fma_rn(c.cz, Z, V0) : pmul(c.cz, Z);
                 t = __fma_rn(c.gy, Y, t);
                 t = __fma_rn(c.cx, X, t);
                 if (a.out[1]) { if (filled) store_filled(a.out[1], 0, a, i, j, k, t); else a.out[1][p] = t; }
@@ -248,7 +249,7 @@ __device__ __forceinline__ void fast_tile(const AdvArgs &a, int tile_x, int tile
                 const double X = cross_term(sWx, wWx, sUz, wUz);
                 const double Y = cross_term(sWy, south[2 * SLOT + at], sVz, south[3 * SLOT + at]);
                 const double Z = along_term(Wp, Wm, W0);
-                double t = __fma_rn(c.gz, Z, advance ? W0 : 0.0);
+                double t = ADVANCE ? __fma_rn(c.gz, Z, W0) : pmul(c.gz, Z);
                 t = __fma_rn(c.cy, Y, t);
                 t = __fma_rn(c.cx, X, t);
                 if (a.out[2]) { if (filled) store_filled(a.out[2], 1, a, i, j, k, t); else a.out[2][p] = t; }
@@ -260,7 +261,7 @@ __device__ __forceinline__ void fast_tile(const AdvArgs &a, int tile_x, int tile
                 for (int n = 0; n < NS; ++n) {
                     const double *__restrict__ S = a.s[n];
                     const double S0 = LD(S, p, 0, 0, 0);
-                    double t = __fma_rn(S0, D, advance ? S0 : 0.0);
+                    double t = ADVANCE ? __fma_rn(S0, D, S0) : pmul(S0, D);
                     t = __fma_rn(-cU, LD(S, p, 1, 0, 0), t);
                     t = __fma_rn(wcU, LD(S, p, -1, 0, 0), t);
                     t = __fma_rn(-cV, LD(S, p, 0, 1, 0), t);
@@ -277,6 +278,21 @@ __device__ __forceinline__ void fast_tile(const AdvArgs &a, int tile_x, int tile
         }
     }
 #undef LD
+}
+
+// The tile in the instance's output mode. The mode is a template argument of
+// the tile so that a tendency's first term of each sum is a plain product
+// (pmul, off the FP64 pipe) rather than an FMA with a zero addend, which a
+// runtime choice would leave on the FP64 pipe; a filled advance is an advance.
+template <int NS, int MASK, int TY>
+__device__ __forceinline__ void fast_tile(const AdvArgs &a, int tile_x, int tile_y, int k0, int k1, double *smem) {
+    if constexpr ((MASK & kFillMask) != 0) {
+        fast_tile_mode<NS, MASK, TY, true>(a, tile_x, tile_y, k0, k1, smem);
+    } else if (a.mode != 0) {
+        fast_tile_mode<NS, MASK, TY, true>(a, tile_x, tile_y, k0, k1, smem);
+    } else {
+        fast_tile_mode<NS, MASK, TY, false>(a, tile_x, tile_y, k0, k1, smem);
+    }
 }
 
 template <int NS, int MASK, int TY>
