@@ -847,7 +847,8 @@ def run_stencils(args):
 
     ms = _graph_time(torch, stream, diffuse, args.steps, args.warmup) / 2
     results["diffusion7_384^3"] = {"ms_per_step": ms, "gpts_per_s": n ** 3 / ms / 1e6,
-                                   "hbm_frac": 16 * n ** 3 / (ms * 1e-3) / 1e9 / peak, "fp64_ops_per_point": 9}
+                                   "hbm_frac": 16 * n ** 3 / (ms * 1e-3) / 1e9 / peak, "fp64_ops_per_point": 7,
+                                   "int_pipe_ops_per_point": 2}
     del a, b
     n = 8192
     u, v = field((n + 2, n + 2)), torch.zeros((n + 2, n + 2), dtype=torch.float64, device="cuda")
@@ -858,7 +859,8 @@ def run_stencils(args):
 
     ms = _graph_time(torch, stream, sweep, args.steps, args.warmup) / 2
     results["jacobi5_8192^2"] = {"ms_per_step": ms, "gpts_per_s": n * n / ms / 1e6,
-                                 "hbm_frac": 16 * n * n / (ms * 1e-3) / 1e9 / peak, "fp64_ops_per_point": 3}
+                                 "hbm_frac": 16 * n * n / (ms * 1e-3) / 1e9 / peak, "fp64_ops_per_point": 3,
+                                 "int_pipe_ops_per_point": 1}
     del u, v
     n = 4096
     ez, hx, hy = (field((n + 2, n + 2)) for _ in range(3))
@@ -868,7 +870,8 @@ def run_stencils(args):
 
     ms = _graph_time(torch, stream, leap, args.steps, args.warmup)
     results["yee2d_4096^2"] = {"ms_per_step": ms, "gpts_per_s": n * n / ms / 1e6,
-                               "hbm_frac": 48 * n * n / (ms * 1e-3) / 1e9 / peak, "fp64_ops_per_point": 11}
+                               "hbm_frac": 48 * n * n / (ms * 1e-3) / 1e9 / peak, "fp64_ops_per_point": 8,
+                               "int_pipe_ops_per_point": 3}
     print(json.dumps({"metric": "generality stencils Gpts/s (100-step graphs)", "unit": UNIT, "dtype": "f64",
                       "steps": args.steps, "warmup": args.warmup, "results": results,
                       "peak_hbm_gbs": peak}), flush=True)

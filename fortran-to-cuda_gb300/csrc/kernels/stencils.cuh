@@ -13,6 +13,11 @@
 
 #include <cstdint>
 
+#include "soft_fp64.cuh"
+
+// The products below run on the integer pipes (mul_rn_int: the correctly
+// rounded product, the same bits as DMUL), leaving the FP64 pipe, which bounds
+// these stencils, to the additions.
 namespace f2c {
 
 // x * 2^e for an exact power-of-two factor, on the integer pipe when the
@@ -57,9 +62,9 @@ static __global__ void __launch_bounds__(kDiffBX *kDiffBY) diffusion7_kernel(con
     for (int k = k0; k < k1; ++k, q += plane) {
         const double above = __ldg(A + q + plane);
         const double sum = __ldg(A + q - 1) + __ldg(A + q + 1) + __ldg(A + q - sx) + __ldg(A + q + sx) + below + above;
-        const double num = sum - 6.0 * centre;
+        const double num = sum - mul_rn_int(6.0, centre);
         const double lap = p.dx2_pow2 ? scale_pow2(num, -p.dx2_exp, 1.0 / p.dx2) : num / p.dx2;
-        p.b[q] = centre + p.dtnu * lap;
+        p.b[q] = centre + mul_rn_int(p.dtnu, lap);
         below = centre;
         centre = above;
     }
@@ -108,8 +113,8 @@ static __global__ void __launch_bounds__(kYeeBX *kYeeBY) yee_h_kernel(const YeeA
     if (i >= p.nx || j >= p.ny) return;
     const long long q = (long long)(i + p.h) + p.sx * (long long)(j + p.h);
     const double e = __ldg(p.ez + q);
-    p.hx[q] = p.hx[q] - p.ch * (__ldg(p.ez + q + p.sx) - e);
-    p.hy[q] = p.hy[q] + p.ch * (__ldg(p.ez + q + 1) - e);
+    p.hx[q] = p.hx[q] - mul_rn_int(p.ch, __ldg(p.ez + q + p.sx) - e);
+    p.hy[q] = p.hy[q] + mul_rn_int(p.ch, __ldg(p.ez + q + 1) - e);
 }
 
 static __global__ void __launch_bounds__(kYeeBX *kYeeBY) yee_e_kernel(const YeeArgs p) {
@@ -117,7 +122,7 @@ static __global__ void __launch_bounds__(kYeeBX *kYeeBY) yee_e_kernel(const YeeA
     const int j = blockIdx.y * kYeeBY + threadIdx.y;
     if (i >= p.nx || j >= p.ny) return;
     const long long q = (long long)(i + p.h) + p.sx * (long long)(j + p.h);
-    p.ez[q] = p.ez[q] + p.ce * ((__ldg(p.hy + q) - __ldg(p.hy + q - 1)) - (__ldg(p.hx + q) - __ldg(p.hx + q - p.sx)));
+    p.ez[q] = p.ez[q] + mul_rn_int(p.ce, (__ldg(p.hy + q) - __ldg(p.hy + q - 1)) - (__ldg(p.hx + q) - __ldg(p.hx + q - p.sx)));
 }
 
 inline dim3 diffusion_grid(const DiffusionArgs &p) {
