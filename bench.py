@@ -55,10 +55,12 @@ def algorithmic_bytes_per_point(nscalar: int, mode: str = "tendency") -> int:
 def fp64_ops_per_point(nscalar: int, numerics: str = "strict", mode: str = "tendency") -> int:
     """FP64-pipe instructions per point of each kernel's expression DAG (every face value computed once).
 
-    The products that are not part of an FMA run on the integer pipes (``mul_rn_int``, rounded exactly as DMUL)
-    and the exact halving is an exponent decrement; neither is counted here (``int_pipe_ops_per_point``).
+    Products on the integer pipes (``mul_rn_int``, rounded exactly as DMUL) and the exact halving (an exponent
+    decrement) are not counted here (``int_pipe_ops_per_point``).
     strict (the reference grouping): U, V, W: 9 face sums, 15 flux differences, 30 advective-form sums and
-    differences; scalars: 8 sums and differences each.
+    differences, and the first product of each of the 9 face fluxes (the second product of each flux and the 18
+    advective-form products run on the integer pipes); scalars: 3 shared coefficient products, and per scalar 8
+    sums and differences and 3 face-flux products.
     fast (factored FMA form): U, V, W: 6 face sums + 12 per component (3 for the direction along it, 3 for each
     across, 3 to accumulate, of which a tendency's first is a plain product); scalars: 5 for the shared divergence
     term + 7 FMAs per scalar (6 in a tendency).
@@ -66,16 +68,16 @@ def fp64_ops_per_point(nscalar: int, numerics: str = "strict", mode: str = "tend
     tendency = mode == "tendency"
     if numerics == "fast":
         return 6 + 3 * (12 - tendency) + (5 + (7 - tendency) * nscalar if nscalar else 0)
-    return 54 + 8 * nscalar
+    return 63 + (3 + 11 * nscalar if nscalar else 0)
 
 
 def int_pipe_ops_per_point(nscalar: int, numerics: str = "strict", mode: str = "tendency") -> int:
-    """Floating-point operations per point that run on the integer pipes: plain products, and the strict
-    kernel's exact halving of U, V, W."""
+    """Floating-point operations per point that run on the integer pipes: products, and the strict kernel's exact
+    halving of U, V, W."""
     tendency = mode == "tendency"
     if numerics == "fast":
         return 9 + 3 * tendency + (3 + tendency * nscalar if nscalar else 0)
-    return 36 + 3 + (3 + 3 * nscalar if nscalar else 0)
+    return 27 + 3
 
 
 def hbm_peak():

@@ -20,8 +20,14 @@
 //    rounded subnormal case handled in integer arithmetic as well).
 //
 // Every other operation follows the reference grouping (advection_point.cuh),
-// so results are bit-identical to the oracle. The products are computed on the
-// integer pipes (pmul below), which round exactly as DMUL does. Operation count per point:
+// so results are bit-identical to the oracle. The advective-form products and
+// the second product of each face flux are computed on the integer pipes (pmul
+// below, rounded exactly as DMUL): 27 of the 48 products per point with three
+// scalars. That split balances the pipes; measured at 512 x 512 x 128 with
+// three scalars: 8.74 ms with every product a DMUL, 8.17 ms with all 48 on the
+// integer pipes (the FP64 pipe then waits on the longer integer chains, 62 %
+// busy), 7.33 ms with these 27 (7.69 with the advective ones alone, 7.46 with
+// both flux products as well). Operation count per point:
 // U, V, W: 9 face sums + 18 flux products + 15 flux differences + 48
 // advective-form operations = 90; scalars: 3 shared coefficient products +
 // 11 per scalar.
@@ -37,11 +43,9 @@
 namespace f2c {
 
 // Products on the integer pipes (soft_fp64.cuh): bit-identical to DMUL, they
-// take the multiplications off the FP64 pipe that bounds these kernels
-// (measured at 512 x 512 x 128 with three scalars: this strict kernel 8.74 ->
-// 8.15 ms, the fast-fp one 4.98 -> 4.28 ms, outputs unchanged bit for bit).
-// Additions stay on the FP64 pipe: the integer addition needs about as many
-// issue slots of the ALU pipe as it saves on the FP64 one (measured slower).
+// take multiplications off the FP64 pipe that bounds these kernels. Additions
+// stay on the FP64 pipe: an integer addition costs about as much time on the
+// ALU pipe as it saves on the FP64 one (measured slower).
 __device__ __forceinline__ double pmul(double a, double b) { return mul_rn_int(a, b); }
 
 constexpr int kFaceTX = 32;       // points per tile along x (one warp)
@@ -173,29 +177,29 @@ __device__ __forceinline__ void faces_tile(const AdvArgs &a, int tile_x, int til
             if (DO_V || DO_W) sVz = Vp + V0;
             if (DO_W) sWz = Wp + W0;
             if (DO_U) {
-                FUx = pmul(pmul(c.Ax, sUx), sUx);
-                FUy = pmul(pmul(c.Ay, sUy), sVx);
-                FUz = pmul(pmul(c.Az, sUz), sWx);
+                FUx = pmul(c.Ax * sUx, sUx);
+                FUy = pmul(c.Ay * sUy, sVx);
+                FUz = pmul(c.Az * sUz, sWx);
             }
             if (DO_V) {
-                FVx = pmul(pmul(c.Ax, sVx), sUy);
-                FVy = pmul(pmul(c.Ay, sVy), sVy);
-                FVz = pmul(pmul(c.Az, sVz), sWy);
+                FVx = pmul(c.Ax * sVx, sUy);
+                FVy = pmul(c.Ay * sVy, sVy);
+                FVz = pmul(c.Az * sVz, sWy);
             }
             if (DO_W) {
-                FWx = pmul(pmul(c.Ax, sWx), sUz);
-                FWy = pmul(pmul(c.Ay, sWy), sVz);
-                FWz = pmul(pmul(c.Az, sWz), sWz);
+                FWx = pmul(c.Ax * sWx, sUz);
+                FWy = pmul(c.Ay * sWy, sVz);
+                FWz = pmul(c.Az * sWz, sWz);
             }
             if (NS > 0) {
-                const double SxU = pmul(c.Sx, U0), SyV = pmul(c.Sy, V0), SzW = pmul(c.Sz, W0);
+                const double SxU = c.Sx * U0, SyV = c.Sy * V0, SzW = c.Sz * W0;
 #pragma unroll
                 for (int n = 0; n < NS; ++n) {
                     const double *__restrict__ S = a.s[n];
                     S0[n] = LD(S, p, 0, 0, 0);
-                    fe[n] = pmul(SxU, LD(S, p, 1, 0, 0) + S0[n]);
-                    fn[n] = pmul(SyV, LD(S, p, 0, 1, 0) + S0[n]);
-                    ft[n] = pmul(SzW, LD(S, p, 0, 0, 1) + S0[n]);
+                    fe[n] = SxU * (LD(S, p, 1, 0, 0) + S0[n]);
+                    fn[n] = SyV * (LD(S, p, 0, 1, 0) + S0[n]);
+                    ft[n] = SzW * (LD(S, p, 0, 0, 1) + S0[n]);
                 }
             }
             const int xo = warp * (kFaceTX + 1) + lane + 1;
