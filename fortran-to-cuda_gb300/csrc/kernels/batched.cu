@@ -32,20 +32,34 @@ namespace {
 constexpr size_t kAlign = 256;
 size_t align_up(size_t v) { return (v + kAlign - 1) / kAlign * kAlign; }
 
+// The tile's instance arguments, copied into shared memory by the whole CTA
+// (as 8-byte words) so that the tile reads its coefficients and pointers
+// from shared memory rather than through global loads of the instance table.
+static_assert(sizeof(AdvArgs) % 8 == 0 && alignof(AdvArgs) == 8, "instance arguments copied as 8-byte words");
+__device__ __forceinline__ void stage_args(AdvArgs *dst, const AdvArgs *src) {
+    const unsigned long long *from = reinterpret_cast<const unsigned long long *>(src);
+    unsigned long long *to = reinterpret_cast<unsigned long long *>(dst);
+    const int threads = blockDim.x * blockDim.y;
+    for (int w = threadIdx.y * blockDim.x + threadIdx.x; w < (int)(sizeof(AdvArgs) / 8); w += threads) to[w] = from[w];
+}
+
 template <int NS, int MASK>
 __global__ void __launch_bounds__(kFaceThreads, kFaceCtasPerSM)
     advection_batched_kernel(const AdvArgs *__restrict__ instances, const BatchItem *__restrict__ items, int nitems,
                              unsigned *counter) {
     extern __shared__ double smem[];
     __shared__ int slot;
+    __shared__ AdvArgs args;
     for (;;) {
         if (threadIdx.x == 0 && threadIdx.y == 0) slot = (int)atomicAdd(counter, 1u);
         __syncthreads();
         const int n = slot;
-        __syncthreads();  // every thread has read the slot before thread 0 takes the next one
+        __syncthreads();  // every thread has read the slot (and left the previous tile) before the next one
         if (n >= nitems) return;
         const BatchItem it = items[n];
-        faces_tile<NS, MASK>(instances[it.instance], it.tile_x, it.tile_y, it.k0, it.k1, smem);
+        stage_args(&args, instances + it.instance);
+        __syncthreads();
+        faces_tile<NS, MASK>(args, it.tile_x, it.tile_y, it.k0, it.k1, smem);
     }
 }
 
@@ -60,6 +74,7 @@ __global__ void __launch_bounds__(fast_threads<TY>(), fast_ctas_per_sm<TY>())
                                   int nitems, unsigned *counter) {
     __shared__ double smem[FastSmem<TY>::doubles];
     __shared__ int slot;
+    __shared__ AdvArgs args;
     for (;;) {
         if (threadIdx.x == 0 && threadIdx.y == 0) slot = (int)atomicAdd(counter, 1u);
         __syncthreads();
@@ -67,7 +82,9 @@ __global__ void __launch_bounds__(fast_threads<TY>(), fast_ctas_per_sm<TY>())
         __syncthreads();  // every thread has read the slot (and left the previous tile) before the next one
         if (n >= nitems) return;
         const BatchItem it = items[n];
-        fast_tile<NS, MASK, TY>(instances[it.instance], it.tile_x, it.tile_y, it.k0, it.k1, smem);
+        stage_args(&args, instances + it.instance);
+        __syncthreads();
+        fast_tile<NS, MASK, TY>(args, it.tile_x, it.tile_y, it.k0, it.k1, smem);
     }
 }
 
