@@ -136,9 +136,11 @@ std::vector<fort_scope_plan_binding> bindings_of(std::deque<Use> &uses) {
 // fast-fp kernel (fast = true) for `a`; `a.kz` is set for the chosen kernel.
 template <int NS, int MASK>
 int faces_spec(AdvArgs &a, bool fast, fort_scope_kernel_v1 &k) {
+    int ty = kFaceTY;  // rows of a tile
     if (fast) {
-        a.kz = fast_chunk_depth(a.nx, a.ny, a.nz, kFaceTY, current_sm_count());
-        k.function = (const void *)advection_fast_kernel<NS, MASK, kFaceTY>;
+        ty = kFastTY;
+        a.kz = fast_chunk_depth(a.nx, a.ny, a.nz, kFastTY, current_sm_count());
+        k.function = (const void *)advection_fast_kernel<NS, MASK, kFastTY>;
         k.shared_bytes = 0;
     } else {
         using Smem = FaceSmem<NS, MASK>;
@@ -151,10 +153,10 @@ int faces_spec(AdvArgs &a, bool fast, fort_scope_kernel_v1 &k) {
         k.shared_bytes = Smem::bytes;
     }
     k.grid[0] = (a.nx + kFaceTX - 1) / kFaceTX;
-    k.grid[1] = (a.ny + kFaceTY - 1) / kFaceTY;
+    k.grid[1] = (a.ny + ty - 1) / ty;
     k.grid[2] = (a.nz + a.kz - 1) / a.kz;
     k.block[0] = kFaceTX;
-    k.block[1] = kFaceTY + 1;
+    k.block[1] = ty + 1;
     k.block[2] = 1;
     return FORT_SCOPE_OK;
 }

@@ -134,12 +134,12 @@ template <int NS>
 static cudaError_t fast_for_mask(const AdvArgs &a, int mask, cudaStream_t s) {
     const int sms = current_sm_count();
     switch (mask) {
-    case 7: return launch_fast<NS, 7, kFaceTY>(a, sms, s);
-    case 1: return launch_fast<NS, 1, kFaceTY>(a, sms, s);
-    case 2: return launch_fast<NS, 2, kFaceTY>(a, sms, s);
-    case 4: return launch_fast<NS, 4, kFaceTY>(a, sms, s);
-    case 0: return NS > 0 ? launch_fast<NS, 0, kFaceTY>(a, sms, s) : cudaSuccess;
-    default: return launch_fast<NS, 7, kFaceTY>(a, sms, s);
+    case 7: return launch_fast<NS, 7, kFastTY>(a, sms, s);
+    case 1: return launch_fast<NS, 1, kFastTY>(a, sms, s);
+    case 2: return launch_fast<NS, 2, kFastTY>(a, sms, s);
+    case 4: return launch_fast<NS, 4, kFastTY>(a, sms, s);
+    case 0: return NS > 0 ? launch_fast<NS, 0, kFastTY>(a, sms, s) : cudaSuccess;
+    default: return launch_fast<NS, 7, kFastTY>(a, sms, s);
     }
 }
 
@@ -147,11 +147,11 @@ static cudaError_t launch_fast_dispatch(const AdvArgs &a, cudaStream_t s) {
     if (a.mode == F2C_ADVANCE_FILLED) {
         const int sms = current_sm_count();
         switch (a.nscalar) {
-        case 0: return launch_fast<0, 7 | kFillMask, kFaceTY>(a, sms, s);
-        case 1: return launch_fast<1, 7 | kFillMask, kFaceTY>(a, sms, s);
-        case 2: return launch_fast<2, 7 | kFillMask, kFaceTY>(a, sms, s);
-        case 3: return launch_fast<3, 7 | kFillMask, kFaceTY>(a, sms, s);
-        default: return launch_fast<4, 7 | kFillMask, kFaceTY>(a, sms, s);
+        case 0: return launch_fast<0, 7 | kFillMask, kFastTY>(a, sms, s);
+        case 1: return launch_fast<1, 7 | kFillMask, kFastTY>(a, sms, s);
+        case 2: return launch_fast<2, 7 | kFillMask, kFastTY>(a, sms, s);
+        case 3: return launch_fast<3, 7 | kFillMask, kFastTY>(a, sms, s);
+        default: return launch_fast<4, 7 | kFillMask, kFastTY>(a, sms, s);
         }
     }
     const int mask = (a.out[0] ? 1 : 0) | (a.out[1] ? 2 : 0) | (a.out[2] ? 4 : 0);

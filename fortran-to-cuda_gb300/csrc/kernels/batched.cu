@@ -65,8 +65,6 @@ __global__ void __launch_bounds__(kFaceThreads, kFaceCtasPerSM)
 
 // The same persistent loop over the fast-fp tile (advection_fast.cuh), tiles of 32 x TY points: TY + 1
 // warps per CTA; small tiles run more CTAs per SM (the register budget at 96 per thread).
-template <int TY>
-constexpr int fast_ctas_per_sm() { return TY <= 4 ? 4 : (TY <= 8 ? 2 : 1); }
 
 template <int NS, int MASK, int TY>
 __global__ void __launch_bounds__(fast_threads<TY>(), fast_ctas_per_sm<TY>())
