@@ -68,15 +68,17 @@ struct FastSmem {
 template <int TY>
 constexpr int fast_threads() { return kFastTX * (TY + 1); }
 
-// CTAs per SM a tile height is compiled for (96 registers a thread at four
-// 5-warp or two 9-warp CTAs, 96+ at one 17-warp CTA).
+// CTAs per SM a tile height is compiled for: the register budget follows
+// (96 registers a thread at four 5-warp CTAs, 72 at three 9-warp CTAs, 96+
+// at one 17-warp CTA; no spills at any of them). With the products on the
+// integer pipes more warps hide more of the FP64 and integer latencies:
+// measured at 512 x 512 x 128 with three scalars, 8-row tiles took 4.10 ms at
+// two CTAs per SM, 3.94 at three and 3.95 at four; 4-row tiles 4.06, 4.03 and
+// 4.03 at four, six and eight; 16-row tiles 4.31 at one and 4.09 at two.
 template <int TY>
-constexpr int fast_ctas_per_sm() { return TY <= 4 ? 4 : (TY <= 8 ? 2 : 1); }
+constexpr int fast_ctas_per_sm() { return TY <= 4 ? 4 : (TY <= 8 ? 3 : 1); }
 
-// Tile height of the single-instance launches: 8 rows at two CTAs per SM.
-// Measured at 512 x 512 x 128 with three scalars: 4.10 ms, against 4.06 for 4
-// rows at four CTAs and 4.31 for 16 rows at one; but 4 rows made the 64
-// uneven instances of the ensemble, launched one at a time, 4 % slower.
+// Tile height of the single-instance launches (8 rows: see above).
 constexpr int kFastTY = 8;
 
 // p(3q + qn) - pn(3qn + q): one direction of a momentum component across its
