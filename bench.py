@@ -446,7 +446,7 @@ def run_gb300(args):
                 "ops_per_point": ops, "int_pipe_ops_per_point": int_pipe_ops_per_point(NSCALAR, name)}
 
     kernel_ms = {primary: ms_per_step, secondary: other_ms}
-    kernel_names = {"fast": "advection_fast_kernel<3,7,8>", "strict": "advection_faces_kernel<3,7>"}
+    kernel_names = {"fast": "advection_fast_kernel<3,7,8,3>", "strict": "advection_faces_kernel<3,7>"}
     result = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",

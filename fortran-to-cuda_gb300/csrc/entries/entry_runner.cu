@@ -138,9 +138,15 @@ template <int NS, int MASK>
 int faces_spec(AdvArgs &a, bool fast, fort_scope_kernel_v1 &k) {
     int ty = kFaceTY;  // rows of a tile
     if (fast) {
+        const int sms = current_sm_count();
         ty = kFastTY;
-        a.kz = fast_chunk_depth(a.nx, a.ny, a.nz, kFastTY, current_sm_count());
-        k.function = (const void *)advection_fast_kernel<NS, MASK, kFastTY>;
+        a.kz = fast_chunk_depth(a.nx, a.ny, a.nz, kFastTY, sms);
+        // the build for three CTAs per SM when the launch has enough CTAs (as launch_fast chooses)
+        const long long ctas = (long long)((a.nx + kFastTX - 1) / kFastTX) * ((a.ny + kFastTY - 1) / kFastTY) *
+                               ((a.nz + a.kz - 1) / a.kz);
+        k.function = ctas >= (long long)kFastDeepCtas * (sms > 0 ? sms : 152)
+                         ? (const void *)advection_fast_kernel<NS, MASK, kFastTY, kFastDeepCtasPerSM>
+                         : (const void *)advection_fast_kernel<NS, MASK, kFastTY>;
         k.shared_bytes = 0;
     } else {
         using Smem = FaceSmem<NS, MASK>;

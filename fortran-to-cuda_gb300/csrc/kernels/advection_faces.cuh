@@ -56,8 +56,8 @@ constexpr int kFaceThreads = kFaceTX * (kFaceTY + 1);
 // integer and shared-memory latencies better than one CTA of 168 registers
 // (measured at 512 x 512 x 128: about 3 % faster with every product a DMUL,
 // 8.17 against 11.8 ms with every product on the integer pipes), and better
-// than three or four CTAs (72 or 56 registers, no spills): 7.33 ms with the
-// products split as below, against 8.04 and 8.06.
+// than three or four CTAs (72 or 56 registers, with more spills): 7.33 ms with
+// the products split as below, against 8.04 and 8.06.
 constexpr int kFaceCtasPerSM = 2;
 
 // Exact x * 0.5 without the FP64 pipe: for normal x the exponent field drops by

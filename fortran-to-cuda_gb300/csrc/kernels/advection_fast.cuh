@@ -68,18 +68,25 @@ struct FastSmem {
 template <int TY>
 constexpr int fast_threads() { return kFastTX * (TY + 1); }
 
-// CTAs per SM a tile height is compiled for: the register budget follows
-// (96 registers a thread at four 5-warp CTAs, 72 at three 9-warp CTAs, 96+
-// at one 17-warp CTA; no spills at any of them). With the products on the
-// integer pipes more warps hide more of the FP64 and integer latencies:
-// measured at 512 x 512 x 128 with three scalars, 8-row tiles took 4.10 ms at
-// two CTAs per SM, 3.94 at three and 3.95 at four; 4-row tiles 4.06, 4.03 and
-// 4.03 at four, six and eight; 16-row tiles 4.31 at one and 4.09 at two.
+// CTAs per SM a tile height is compiled for by default: the register budget
+// follows (96 registers a thread at four 5-warp or two 9-warp CTAs, more at
+// one 17-warp CTA).
 template <int TY>
-constexpr int fast_ctas_per_sm() { return TY <= 4 ? 4 : (TY <= 8 ? 3 : 1); }
+constexpr int fast_ctas_per_sm() { return TY <= 4 ? 4 : (TY <= 8 ? 2 : 1); }
 
-// Tile height of the single-instance launches (8 rows: see above).
+// Tile height of the single-instance launches, and the CTAs per SM their
+// kernel is compiled for when the launch has at least kFastDeepCtas CTAs per
+// SM of work (72 registers; the three-scalar step then spills about 240 bytes
+// a thread, served by L1). More warps hide more of the FP64 and integer
+// latencies of large grids; measured at 512 x 512 x 128 with three
+// scalars, 8-row tiles took 4.10 ms at two CTAs per SM, 3.94 at three and 3.95
+// at four (4-row tiles 4.06, 4.03 and 4.03 at four, six and eight; 16-row
+// tiles 4.31 at one and 4.09 at two). Smaller launches keep two CTAs: at three
+// the 64 uneven instances of the ensemble, launched one at a time, ran 6 %
+// slower, and so did the serving ticks' batched steps.
 constexpr int kFastTY = 8;
+constexpr int kFastDeepCtasPerSM = 3;
+constexpr int kFastDeepCtas = 8;
 
 // p(3q + qn) - pn(3qn + q): one direction of a momentum component across its
 // own axis, with p, pn the component's own face sums at the near and far face
@@ -308,8 +315,8 @@ __device__ __forceinline__ void fast_tile(const AdvArgs &a, int tile_x, int tile
     }
 }
 
-template <int NS, int MASK, int TY>
-__global__ void __launch_bounds__(fast_threads<TY>(), fast_ctas_per_sm<TY>()) advection_fast_kernel(const AdvArgs a) {
+template <int NS, int MASK, int TY, int CTAS = fast_ctas_per_sm<TY>()>
+__global__ void __launch_bounds__(fast_threads<TY>(), CTAS) advection_fast_kernel(const AdvArgs a) {
     __shared__ double smem[FastSmem<TY>::doubles];
     const int k0 = blockIdx.z * a.kz;
     fast_tile<NS, MASK, TY>(a, blockIdx.x, blockIdx.y, k0, min(k0 + a.kz, a.nz), smem);
@@ -332,7 +339,11 @@ cudaError_t launch_fast(const AdvArgs &a, int sms, cudaStream_t stream) {
     if (b.kz <= 0) b.kz = fast_chunk_depth(b.nx, b.ny, b.nz, TY, sms);
     const dim3 block(kFastTX, TY + 1, 1);
     const dim3 grid((b.nx + kFastTX - 1) / kFastTX, (b.ny + TY - 1) / TY, (b.nz + b.kz - 1) / b.kz);
-    advection_fast_kernel<NS, MASK, TY><<<grid, block, 0, stream>>>(b);
+    const long long ctas = (long long)grid.x * grid.y * grid.z;
+    if (TY == kFastTY && ctas >= (long long)kFastDeepCtas * (sms > 0 ? sms : 152))
+        advection_fast_kernel<NS, MASK, TY, kFastDeepCtasPerSM><<<grid, block, 0, stream>>>(b);
+    else
+        advection_fast_kernel<NS, MASK, TY><<<grid, block, 0, stream>>>(b);
     return cudaGetLastError();
 }
 
