@@ -24,7 +24,7 @@
 // the second product of each face flux are computed on the integer pipes (pmul
 // below, rounded exactly as DMUL): 27 of the 48 products per point with three
 // scalars. That split balances the pipes; measured at 512 x 512 x 128 with
-// three scalars: 8.74 ms with every product a DMUL, 8.17 ms with all 48 on the
+// three scalars (two CTAs per SM): 8.74 ms with every product a DMUL, 8.17 ms with all 48 on the
 // integer pipes (the FP64 pipe then waits on the longer integer chains, 62 %
 // busy), 7.33 ms with these 27 (7.69 with the advective ones alone, 7.46 with
 // both flux products as well). Operation count per point:
@@ -52,13 +52,14 @@ constexpr int kFaceTX = 32;       // points per tile along x (one warp)
 constexpr int kFaceTY = 8;        // compute warps per tile (points along y)
 constexpr int kFaceKZ = 32;       // levels per z-chunk
 constexpr int kFaceThreads = kFaceTX * (kFaceTY + 1);
-// Two CTAs per SM (96 registers a thread, a few spills): 18 warps hide the FP64,
-// integer and shared-memory latencies better than one CTA of 168 registers
-// (measured at 512 x 512 x 128: about 3 % faster with every product a DMUL,
-// 8.17 against 11.8 ms with every product on the integer pipes), and better
-// than three or four CTAs (72 or 56 registers, with more spills): 7.33 ms with
-// the products split as below, against 8.04 and 8.06.
-constexpr int kFaceCtasPerSM = 2;
+// Three CTAs per SM (72 registers a thread, a few spills served by L1): 27
+// warps hide the FP64, integer and shared-memory latencies. What made room for
+// the third CTA is phase B reading the point's own fluxes back from the shared
+// rows and its values again from L1 (ldg_again) instead of holding them in
+// registers across the barrier. Measured at 512 x 512 x 128 with three
+// scalars: 7.33 ms at two CTAs before that change (8.04 at three, with twice
+// the spills), 7.26 ms at two and 7.11 at three after it.
+constexpr int kFaceCtasPerSM = 3;
 
 // Exact x * 0.5 without the FP64 pipe: for normal x the exponent field drops by
 // one; for the smallest normals and subnormals the significand shifts right
@@ -85,6 +86,15 @@ __device__ __forceinline__ double opaque_negate(double x) {
     unsigned long long r;
     asm("xor.b64 %0, %1, 0x8000000000000000;" : "=l"(r) : "l"((unsigned long long)__double_as_longlong(x)));
     return __longlong_as_double((long long)r);
+}
+
+// A read-only global load the compiler must issue where it stands (not merged
+// with an earlier load of the same address), so that a value loaded before the
+// tile's barrier need not stay in a register across it.
+__device__ __forceinline__ double ldg_again(const double *q) {
+    double v;
+    asm volatile("ld.global.nc.f64 %0, [%1];" : "=d"(v) : "l"(q));
+    return v;
 }
 
 template <int NS, int MASK>
@@ -278,40 +288,46 @@ __device__ __forceinline__ void faces_tile(const AdvArgs &a, int tile_x, int til
         if (active) {
             const int xw = warp * (kFaceTX + 1) + lane;
             const int ys = warp * kFaceTX + lane;
+            // this point's own east / north fluxes are read back from the shared rows and its values again
+            // from memory (L1), rather than held in registers across the barrier
+            const int xo = xw + 1, yo = ys + kFaceTX;
+#define LDA(A, di, dj, dk) ldg_again((A) + p + (di) + (dj)*sx + (dk)*plane)
+            const double U0 = LDA(U, 0, 0, 0), V0 = LDA(V, 0, 0, 0), W0 = LDA(W, 0, 0, 0);
             const double Uw = LD(U, p, -1, 0, 0), Us = LD(U, p, 0, -1, 0), Um = LD(U, p, 0, 0, -1);
             const double Vw = LD(V, p, -1, 0, 0), Vs = LD(V, p, 0, -1, 0), Vm = LD(V, p, 0, 0, -1);
             const double Ww = LD(W, p, -1, 0, 0), Ws = LD(W, p, 0, -1, 0), Wm = LD(W, p, 0, 0, -1);
             if (DO_U) {
-                const double r = opaque_negate(((FUx - xf[0 * Smem::XF + xw]) + (FUy - yf[0 * Smem::YF + ys])) + (FUz - FUzb));
+                const double r = opaque_negate(((xf[0 * Smem::XF + xo] - xf[0 * Smem::XF + xw]) + (yf[0 * Smem::YF + yo] - yf[0 * Smem::YF + ys])) + (FUz - FUzb));
                 const double Vadv = (sVx + Vs) + LD(V, p, 1, -1, 0);
                 const double Wadv = (sWx + Wm) + LD(W, p, 1, 0, -1);
-                const double adv = (pmul(pmul(c.Bux, Ue - Uw), U0) + pmul(pmul(c.Buy, Un - Us), Vadv)) + pmul(pmul(c.Buz, Up - Um), Wadv);
+                const double adv = (pmul(pmul(c.Bux, LDA(U, 1, 0, 0) - Uw), U0) + pmul(pmul(c.Buy, LDA(U, 0, 1, 0) - Us), Vadv)) + pmul(pmul(c.Buz, LDA(U, 0, 0, 1) - Um), Wadv);
                 if (a.out[0]) store_point_t<FILL>(a.out[0], U, p, exact_half(r - adv), a, 0, i, j, k);
                 FUzb = FUz;
             }
             if (DO_V) {
-                const double r = opaque_negate(((FVy - yf[1 * Smem::YF + ys]) + (FVx - xf[1 * Smem::XF + xw])) + (FVz - FVzb));
+                const double r = opaque_negate(((yf[1 * Smem::YF + yo] - yf[1 * Smem::YF + ys]) + (xf[1 * Smem::XF + xo] - xf[1 * Smem::XF + xw])) + (FVz - FVzb));
                 const double Uadv = (sUy + Uw) + LD(U, p, -1, 1, 0);
                 const double Wadv = (sWy + Wm) + LD(W, p, 0, 1, -1);
-                const double adv = (pmul(pmul(c.Bvx, Ve - Vw), Uadv) + pmul(pmul(c.Bvy, Vn - Vs), V0)) + pmul(pmul(c.Bvz, Vp - Vm), Wadv);
+                const double adv = (pmul(pmul(c.Bvx, LDA(V, 1, 0, 0) - Vw), Uadv) + pmul(pmul(c.Bvy, LDA(V, 0, 1, 0) - Vs), V0)) + pmul(pmul(c.Bvz, LDA(V, 0, 0, 1) - Vm), Wadv);
                 if (a.out[1]) store_point_t<FILL>(a.out[1], V, p, exact_half(r - adv), a, 0, i, j, k);
                 FVzb = FVz;
             }
             if (DO_W) {
-                const double r = opaque_negate(((FWz - FWzb) + (FWy - yf[2 * Smem::YF + ys])) + (FWx - xf[2 * Smem::XF + xw]));
+                const double r = opaque_negate(((FWz - FWzb) + (yf[2 * Smem::YF + yo] - yf[2 * Smem::YF + ys])) + (xf[2 * Smem::XF + xo] - xf[2 * Smem::XF + xw]));
                 const double Uadv = (sUz + Uw) + LD(U, p, -1, 0, 1);
                 const double Vadv = (sVz + Vs) + LD(V, p, 0, -1, 1);
-                const double adv = (pmul(pmul(c.Bwx, We - Ww), Uadv) + pmul(pmul(c.Bwy, Wn - Ws), Vadv)) + pmul(pmul(c.Bwz, Wp - Wm), W0);
+                const double adv = (pmul(pmul(c.Bwx, LDA(W, 1, 0, 0) - Ww), Uadv) + pmul(pmul(c.Bwy, LDA(W, 0, 1, 0) - Ws), Vadv)) + pmul(pmul(c.Bwz, LDA(W, 0, 0, 1) - Wm), W0);
                 if (a.out[2]) store_point_t<FILL>(a.out[2], W, p, exact_half(r - adv), a, 1, i, j, k);
                 FWzb = FWz;
             }
 #pragma unroll
             for (int n = 0; n < NS; ++n) {
-                const double st = opaque_negate(((fe[n] - xf[(3 + n) * Smem::XF + xw]) + (fn[n] - yf[(3 + n) * Smem::YF + ys])) +
+                const double st = opaque_negate(((xf[(3 + n) * Smem::XF + xo] - xf[(3 + n) * Smem::XF + xw]) + (yf[(3 + n) * Smem::YF + yo] - yf[(3 + n) * Smem::YF + ys])) +
                                     (ft[n] - ftb[n]));
                 if (a.st[n]) store_point_t<FILL>(a.st[n], a.s[n], p, st, a, 0, i, j, k);
                 ftb[n] = ft[n];
             }
+#undef LDA
         }
     }
 #undef LD
