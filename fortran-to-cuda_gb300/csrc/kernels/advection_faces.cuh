@@ -292,7 +292,7 @@ __device__ __forceinline__ void faces_tile(const AdvArgs &a, int tile_x, int til
             // from memory (L1), rather than held in registers across the barrier
             const int xo = xw + 1, yo = ys + kFaceTX;
 #define LDA(A, di, dj, dk) ldg_again((A) + p + (di) + (dj)*sx + (dk)*plane)
-            const double U0 = LDA(U, 0, 0, 0), V0 = LDA(V, 0, 0, 0), W0 = LDA(W, 0, 0, 0);
+            const double Uc = LDA(U, 0, 0, 0), Vc = LDA(V, 0, 0, 0), Wc = LDA(W, 0, 0, 0);  // the point's own values
             const double Uw = LD(U, p, -1, 0, 0), Us = LD(U, p, 0, -1, 0), Um = LD(U, p, 0, 0, -1);
             const double Vw = LD(V, p, -1, 0, 0), Vs = LD(V, p, 0, -1, 0), Vm = LD(V, p, 0, 0, -1);
             const double Ww = LD(W, p, -1, 0, 0), Ws = LD(W, p, 0, -1, 0), Wm = LD(W, p, 0, 0, -1);
@@ -300,7 +300,7 @@ __device__ __forceinline__ void faces_tile(const AdvArgs &a, int tile_x, int til
                 const double r = opaque_negate(((xf[0 * Smem::XF + xo] - xf[0 * Smem::XF + xw]) + (yf[0 * Smem::YF + yo] - yf[0 * Smem::YF + ys])) + (FUz - FUzb));
                 const double Vadv = (sVx + Vs) + LD(V, p, 1, -1, 0);
                 const double Wadv = (sWx + Wm) + LD(W, p, 1, 0, -1);
-                const double adv = (pmul(pmul(c.Bux, LDA(U, 1, 0, 0) - Uw), U0) + pmul(pmul(c.Buy, LDA(U, 0, 1, 0) - Us), Vadv)) + pmul(pmul(c.Buz, LDA(U, 0, 0, 1) - Um), Wadv);
+                const double adv = (pmul(pmul(c.Bux, LDA(U, 1, 0, 0) - Uw), Uc) + pmul(pmul(c.Buy, LDA(U, 0, 1, 0) - Us), Vadv)) + pmul(pmul(c.Buz, LDA(U, 0, 0, 1) - Um), Wadv);
                 if (a.out[0]) store_point_t<FILL>(a.out[0], U, p, exact_half(r - adv), a, 0, i, j, k);
                 FUzb = FUz;
             }
@@ -308,7 +308,7 @@ __device__ __forceinline__ void faces_tile(const AdvArgs &a, int tile_x, int til
                 const double r = opaque_negate(((yf[1 * Smem::YF + yo] - yf[1 * Smem::YF + ys]) + (xf[1 * Smem::XF + xo] - xf[1 * Smem::XF + xw])) + (FVz - FVzb));
                 const double Uadv = (sUy + Uw) + LD(U, p, -1, 1, 0);
                 const double Wadv = (sWy + Wm) + LD(W, p, 0, 1, -1);
-                const double adv = (pmul(pmul(c.Bvx, LDA(V, 1, 0, 0) - Vw), Uadv) + pmul(pmul(c.Bvy, LDA(V, 0, 1, 0) - Vs), V0)) + pmul(pmul(c.Bvz, LDA(V, 0, 0, 1) - Vm), Wadv);
+                const double adv = (pmul(pmul(c.Bvx, LDA(V, 1, 0, 0) - Vw), Uadv) + pmul(pmul(c.Bvy, LDA(V, 0, 1, 0) - Vs), Vc)) + pmul(pmul(c.Bvz, LDA(V, 0, 0, 1) - Vm), Wadv);
                 if (a.out[1]) store_point_t<FILL>(a.out[1], V, p, exact_half(r - adv), a, 0, i, j, k);
                 FVzb = FVz;
             }
@@ -316,7 +316,7 @@ __device__ __forceinline__ void faces_tile(const AdvArgs &a, int tile_x, int til
                 const double r = opaque_negate(((FWz - FWzb) + (yf[2 * Smem::YF + yo] - yf[2 * Smem::YF + ys])) + (xf[2 * Smem::XF + xo] - xf[2 * Smem::XF + xw]));
                 const double Uadv = (sUz + Uw) + LD(U, p, -1, 0, 1);
                 const double Vadv = (sVz + Vs) + LD(V, p, 0, -1, 1);
-                const double adv = (pmul(pmul(c.Bwx, LDA(W, 1, 0, 0) - Ww), Uadv) + pmul(pmul(c.Bwy, LDA(W, 0, 1, 0) - Ws), Vadv)) + pmul(pmul(c.Bwz, LDA(W, 0, 0, 1) - Wm), W0);
+                const double adv = (pmul(pmul(c.Bwx, LDA(W, 1, 0, 0) - Ww), Uadv) + pmul(pmul(c.Bwy, LDA(W, 0, 1, 0) - Ws), Vadv)) + pmul(pmul(c.Bwz, LDA(W, 0, 0, 1) - Wm), Wc);
                 if (a.out[2]) store_point_t<FILL>(a.out[2], W, p, exact_half(r - adv), a, 1, i, j, k);
                 FWzb = FWz;
             }
