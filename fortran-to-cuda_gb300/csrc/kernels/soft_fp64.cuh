@@ -15,6 +15,13 @@
 // common case only: both operands normal, the result normal. Every other case
 // (zeros, subnormals, infinities, NaN, results that overflow or underflow) is
 // handed to the hardware instruction, which is rare in the stencils' fields.
+//
+// The kernels use the product (mul_rn_int). The two additions are kept beside
+// it, checked by the same tests, as the measured alternatives: in the advection
+// kernels, whose integer pipes already carry the products, moving additions
+// off the FP64 pipe made every kernel slower (add_rn_int by about as much time
+// as the DADD it replaces; add_rn_near, about half the integer work, still
+// 4-21 % slower for 6-17 additions per point of the fast-fp kernel).
 #pragma once
 #include <cuda_runtime.h>
 
@@ -66,6 +73,38 @@ __device__ __forceinline__ double add_rn_int(double a, double b) {
     // m carries the hidden bit (or 2^53 after a rounding carry), so adding it to (e - 1) << 52 also
     // carries into the exponent when rounding overflowed the significand
     return __longlong_as_double((long long)((x & kSignBit) | (((unsigned long long)(e - 1) << 52) + m)));
+}
+
+// a + b, rounded to nearest-even, for operands whose exponents differ by at
+// most 9 (the sum of neighbouring values of a smooth field): aligned to the
+// smaller exponent the significands add exactly in 64 bits, so the only
+// rounding is the final one, which needs no sticky bit. About half the
+// integer work of add_rn_int; other operands go to the hardware addition.
+__device__ __forceinline__ double add_rn_near(double a, double b) {
+    const long long ia = __double_as_longlong(a), ib = __double_as_longlong(b);
+    const int ea = (int)((unsigned long long)ia >> 52) & 0x7FF, eb = (int)((unsigned long long)ib >> 52) & 0x7FF;
+    const int d = ea - eb;
+    if ((unsigned)(ea - 1) >= 0x7FCu || (unsigned)(eb - 1) >= 0x7FCu || (unsigned)(d + 9) > 18u) return add_rn_hw(a, b);
+    long long ma = (ia & (long long)kFracMask) | (long long)kHiddenBit;
+    long long mb = (ib & (long long)kFracMask) | (long long)kHiddenBit;
+    ma <<= (d > 0 ? d : 0);  // below 2^62
+    mb <<= (d < 0 ? -d : 0);
+    const int e0 = d > 0 ? eb : ea;
+    const long long s = (ia < 0 ? -ma : ma) + (ib < 0 ? -mb : mb);  // exact, |s| < 2^63
+    const unsigned long long mag = (unsigned long long)(s < 0 ? -s : s);
+    if (mag == 0) return 0.0;  // x + (-x) is +0 when rounding to nearest
+    const int sh = 11 - __clzll((long long)mag);  // bits below the 53 the result keeps
+    unsigned long long m;
+    if (sh > 0) {
+        const unsigned long long half = 1ull << (sh - 1), rest = mag & ((half << 1) - 1);
+        m = (mag + half) >> sh;
+        if (rest == half) m &= ~1ull;  // a tie goes to the even significand
+    } else {
+        m = mag << (-sh);
+    }
+    const int e = e0 + sh;  // biased exponent of the result
+    if (e < 1) return add_rn_hw(a, b);
+    return __longlong_as_double((long long)((s < 0 ? kSignBit : 0ull) | (((unsigned long long)(e - 1) << 52) + m)));
 }
 
 // a * b, rounded to nearest-even.
