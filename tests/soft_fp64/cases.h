@@ -8,6 +8,8 @@
 //   3 cancellation: b is -a moved by up to 1024 units in the last place
 //   4 exponents over the whole normal range (overflow and underflow edges)
 //   5 exponent pairs whose sum lies at the ends of the normal range (products)
+//   6 exponents at most 9 apart (the nearby-exponent addition's own path), full or
+//     short significands, random signs
 #pragma once
 #include <cstdint>
 
@@ -66,6 +68,12 @@ SOFT_CASES_FN void pair(int dist, uint64_t seed, uint64_t i, uint64_t *a, uint64
         *a = make(r0, r1, 1 + (int)(r2 % 2046), false);
         *b = make(r3, r2 ^ r1, 1 + (int)((r2 >> 16) % 2046), false);
         break;
+    case 6: {
+        const int ea = 10 + (int)(r2 % 2028), d = (int)((r2 >> 20) % 19) - 9;  // both exponents in [1, 2046]
+        *a = make(r0, r1, ea, (r3 & 1) != 0);
+        *b = make(r3, r2 ^ r1, ea - d, (r3 & 2) != 0);
+        break;
+    }
     default: {
         const int ea = 1 + (int)(r2 % 2046);
         const int end = ((r2 >> 30) & 1) ? 1023 + 1 : 1023 + 0x7FE;

@@ -28,7 +28,7 @@ int main(int argc, char **argv) {
     const uint64_t n = argc > 1 ? std::strtoull(argv[1], nullptr, 10) : 1000000;
     int failed = 0;
     for (int op = 0; op < 3; ++op)
-        for (int dist = 0; dist < 6; ++dist) {
+        for (int dist = 0; dist < 7; ++dist) {
             uint64_t bad = 0, first_a = 0, first_b = 0;
             const uint64_t seed = 0x5eed0000ull + 131 * (uint64_t)dist + (uint64_t)op;
             for (uint64_t i = 0; i < n; ++i) {

@@ -29,7 +29,7 @@ def test_host_matches_ieee(tmp_path):
                     str(HERE / "soft_fp64_host.cpp"), "-o", str(exe)], check=True)
     run = subprocess.run([str(exe), "1000000"], capture_output=True, text=True, timeout=300)
     lines = [json.loads(line) for line in run.stdout.splitlines()]
-    assert len(lines) == 18
+    assert len(lines) == 21
     assert all(line["mismatches"] == 0 for line in lines), lines
     assert run.returncode == 0
 
@@ -45,6 +45,6 @@ def test_device_matches_dadd_dmul(cuda, tmp_path):
     check.restype = ctypes.c_longlong
     check.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_ulonglong, ctypes.c_ulonglong]
     for op in (0, 1, 2):
-        for dist in range(6):
+        for dist in range(7):
             for seed in (1, 2):
                 assert check(op, dist, 0x5eed0000 + 977 * seed + 31 * dist + op, 1 << 24) == 0, (op, dist, seed)
