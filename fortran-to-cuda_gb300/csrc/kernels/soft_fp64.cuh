@@ -13,8 +13,8 @@
 // a sticky bit jammed into the lowest position, normalise, round to nearest with
 // ties to even; the product's significand as a 106-bit integer), written for the
 // common case only: both operands normal, the result normal. Every other case
-// (zeros, subnormals, infinities, NaN, results that overflow or underflow) is
-// handed to the hardware instruction, which is rare in the stencils' fields.
+// (zeros, subnormals, infinities, NaN, results that overflow or underflow; all
+// rare in the stencils' fields) is handed to the hardware instruction.
 //
 // The kernels use the product (mul_rn_int). The two additions are kept beside
 // it, checked by the same tests, as the measured alternatives: in the advection
